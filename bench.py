@@ -1,0 +1,414 @@
+#!/usr/bin/env python
+"""Benchmark of the plain method's RK4 step on one GB300 (FP64 DOF·stage/s).
+
+Workload: N = 512 (262 144 elements), q_u = q_v = 6, source mode, constant
+coefficients c = 1, α = 1e-6, β = 8, Gaussian source, bottom :absorbing_2beta
+and three :wall sides with κ = 0.5, alternating flux, Chebyshev mass solver,
+dt = h / (10 q²) — the GPU-scale configuration of the reference's plain method.
+The state is synthetic and seeded (the reference measures on no dataset): a
+steepened-wave state whose 1 - 2βv_h spans about [0.42, 1.58] on every element
+(about 30 Chebyshev steps, the regime of data/steepening/nl), and, reported
+beside it, the zero state (one Chebyshev step).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one RK4 step over the whole mesh (4 RHS stages). `value` is
+DOF·stage/s with the state resident in HBM (CUDA events on the library's
+stream); `e2e` is the same metric through the public API (Workspace.rk4_steps)
+with pinned host buffers copied in and out every step. Under torchrun each
+rank runs an independent replica (the path has no exchange step on one mesh).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+Q, NMESH = 6, 512
+KW = dict(mixed=False, mode="source", kappa=0.5, flux="alternating",
+          boundary=dict(bot="absorbing_2beta", top="wall", lft="wall", rgt="wall"))
+COEF = dict(c=1.0, alpha=1e-6, beta=8.0)
+T0 = 0.53
+SAMPLE_N = 64          # CPU sample mesh (same degree, coefficients and sides)
+
+
+def workload_name():
+    return (f"plain method N={NMESH} q_u=q_v={Q} source mode, c=1 alpha=1e-6 beta=8, bottom absorbing_2beta + "
+            f"3 walls kappa=0.5, alternating flux, Chebyshev, RK4 dt=h/(10q^2)")
+
+
+AMP = 0.58 / (2 * COEF["beta"])   # |2βv| ≤ 0.58: 1 - 2βv_h within [0.42, 1.58]
+
+
+def _project(f, N, n):
+    """Modal coefficients (N, N, n, n), column-major, of the L² projection of f(x, y)."""
+    from edg_westervelt_gb300.quadrature import GaussQCofs, JacobiP
+    z, w = GaussQCofs(n + 2)
+    P = np.stack([JacobiP(z, 0, 0, d) for d in range(n)], axis=1)
+    h = 1.0 / N
+    c = (np.arange(N)[:, None] + 0.5 + 0.5 * z[None, :]) * h          # [cell, point]
+    X = c[None, :, None, :]                                           # [j, k, r, s]: x of column k
+    Y = c[:, None, :, None]
+    F = f(np.broadcast_to(X, (N, N, len(z), len(z))), np.broadcast_to(Y, (N, N, len(z), len(z))))
+    return np.asfortranarray(np.einsum("ra,r,jkrs,s,sb->jkab", P, w, F, w, P, optimize=True))
+
+
+def synthetic_state(N, nu, nv, seed, kind="front"):
+    """Seeded smooth states, defined in units of the element size h so that every mesh sees
+    the same per-element variation:
+      front    v = A tanh((r - R)/h) around the source point, r = |x - (0.15, 0.5)|,
+               R seeded in [0.3, 0.4]: a steepened circular front (1 - 2βv_h spans
+               [0.42, 1.58] across the front, about 30 Chebyshev steps there, 1-2 elsewhere);
+      uniform  v = A sin(2πx/h) sin(2π y/h + φ): every element spans the whole range;
+      zero     u = v = 0.
+    u is 1e-4 times a smooth seeded field in all but the zero state."""
+    rng = np.random.default_rng(seed)
+    if kind == "zero":
+        return np.zeros((N, N, nu, nu), order="F"), np.zeros((N, N, nv, nv), order="F")
+    h = 1.0 / N
+    a, b = rng.uniform(1, 3, 2)
+    u = _project(lambda x, y: 1e-4 * np.sin(a * np.pi * x) * np.cos(b * np.pi * y), N, nu)
+    if kind == "front":
+        R = rng.uniform(0.3, 0.4)
+        v = _project(lambda x, y: AMP * np.tanh((np.hypot(x - 0.15, y - 0.5) - R) / h), N, nv)
+    else:
+        ph = rng.uniform(0, 2 * np.pi)
+        v = _project(lambda x, y: AMP * np.sin(2 * np.pi * x / h) * np.sin(2 * np.pi * y / h + ph), N, nv)
+    return u, v
+
+
+def alg_bytes_per_element_stage(nu, nv, qh, one_sided=False, s_mode_nv2=1):
+    """Algorithmic bytes of one element in one RK4 stage (reference data model, FP64)."""
+    nq = nu
+    return 8 * (nu * nu * (nu * nu + 1) / 2 + 2 * nu * nu + qh * qh + 8 * nq + (6 * nq if one_sided else 0)
+                + s_mode_nv2 * nv * nv + 4.25 * (nu * nu + nv * nv))
+
+
+def alg_flops_per_element_stage(nu, nv, qh, n_cheb):
+    nq = nu
+    f = (16 * nu ** 3 + 8 * nu * nv * (nu + nv) + 2 * nu ** 4 + 16 * nu ** 2 + 16 * nv ** 2 + 16 * nu * nv
+         + 4 * (4 * nv * nq + 2 * nu * nq + 4 * nv * nv + 2 * nu * nu) + 60 * nq + 2 * qh * nv * (nv + qh)
+         + 2 * (nu * nu + nv * nv))
+    return f + (n_cheb - 1) * (4 * qh * nv * (nv + qh) + 10 * nv * nv)
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, power, throttle reasons)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["not sampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
+        power = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(power) if power else None, "samples": len(self.rows), "reasons": reasons}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        return {}
+
+
+def fp64_gemm_peak(torch, dev):
+    """cuBLAS DGEMM throughput (TFLOP/s), the FP64 denominator: best of 3, n = 4096."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    return 2 * n ** 3 / best / 1e12
+
+
+def traffic_from_profile():
+    """DRAM bytes per k_stage launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_stage_cfg2_dram.txt")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class CpuPort:
+    """The oracle (C restatement of the reference's RHS and RK4, OpenMP on all host threads)
+    on the same configuration at mesh N."""
+
+    def __init__(self, N, kind="front"):
+        from oracle import coefficients as oc
+        from oracle.precompute import precompute as opre
+        from oracle.rhs import OracleWorkspace, max_threads
+        pre, _ = opre(Q, N, coefficients=oc.constant_coefficients(**COEF), **KW)
+        self.u, self.v = synthetic_state(N, pre["qu1"], pre["qv1"], seed=1, kind=kind)
+        self.ws = OracleWorkspace(pre)
+        self.dt = (1.0 / N) / (10 * Q * Q)
+        self.dof = N * N * (pre["qu1"] ** 2 + pre["qv1"] ** 2)
+        self.cores = max_threads()
+        self.n = 0
+
+    def step(self):
+        t0 = time.perf_counter()
+        self.ws.rk4_step(self.u, self.v, T0 + self.n * self.dt, self.dt)
+        self.n += 1
+        return time.perf_counter() - t0
+
+
+def cpu_baseline(budget_s):
+    port = CpuPort(SAMPLE_N)
+    port.step()
+    n, t = 0, 0.0
+    while (n < 2 or t < budget_s) and n < 200:
+        t += port.step()
+        n += 1
+    return port.dof * 4 * n / t, n, t, port.cores
+
+
+def run_reference(args):
+    """The reference's CPU path on the host cores: the oracle port (Julia is not installed)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    port = CpuPort(SAMPLE_N)
+    for _ in range(args.warmup):
+        port.step()
+    t = sum(port.step() for _ in range(args.steps))
+    value = port.dof * 4 * args.steps / t
+    sample = (f"{args.steps} RK4 steps (after {args.warmup} warm-up) of the same configuration on an "
+              f"N={SAMPLE_N} mesh ({SAMPLE_N ** 2} elements), the same seeded steepened-front state")
+    line = {"impl": "reference", "metric": "FP64 DOF·stage/s on 1 GB300 (plain method, RK4 step)", "value": value,
+            "unit": "DOF·stage/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded state)",
+            "config": {"workload": workload_name(), "sample_mesh": SAMPLE_N},
+            "cpu_baseline": {"value": value, "unit": "DOF·stage/s", "cores": port.cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "DOF·stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "Julia (the reference's toolchain) is not installed here or on the GPU box; the timed CPU path "
+                    "is the oracle's C restatement of src/rhs.jl + src/solver.jl with OpenMP on all host threads"}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import edg_westervelt_gb300 as W
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", init_method="env://")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    pre, _ = W.precompute(Q, NMESH, coefficients=W.constant_coefficients(**COEF), **KW)
+    N, nu, nv, qh = NMESH, pre["qu1"], pre["qv1"], pre["q_high"]
+    E = N * N
+    dof = E * (nu * nu + nv * nv)
+    dt = (1.0 / N) / (10 * Q * Q)
+    ws = W.Workspace(pre, N)
+    stream_ptr = ws.stream
+    ext = torch.cuda.ExternalStream(stream_ptr, device=dev)
+
+    def device_state(kind, seed):
+        u, v = synthetic_state(N, nu, nv, seed, kind)
+        # the reference's column-major bytes, as flat device tensors
+        return (torch.from_numpy(u.reshape(-1, order="F").copy()).to(dev),
+                torch.from_numpy(v.reshape(-1, order="F").copy()).to(dev))
+
+    def timed(kind, steps, warmup):
+        u, v = device_state(kind, seed=0)
+        u0, v0 = u.clone(), v.clone()
+        lib = __import__("edg_westervelt_gb300._lib", fromlist=["lib"]).lib()
+        import ctypes
+        up, vp = ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(v.data_ptr())
+        torch.cuda.synchronize()
+        rc = lib.wedg_rk4_steps_async(ws._h, up, vp, T0, dt, warmup)
+        ws._check(lib.wedg_sync_status(ws._h, None, None) if rc == 0 else rc)
+        u.copy_(u0)
+        v.copy_(v0)
+        lib.wedg_time_kernels(ws._h, 1)
+        lib.wedg_kernel_times(ws._h, None, None, None, None, 1)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            e0.record(ext)
+        rc = lib.wedg_rk4_steps_async(ws._h, up, vp, T0, dt, steps)
+        launches = ws.stats()["kernel_launches"]
+        with torch.cuda.stream(ext):
+            e1.record(ext)
+        done = ctypes.c_int64(0)
+        ws._check(lib.wedg_sync_status(ws._h, ctypes.byref(done), None) if rc == 0 else rc)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+            dist.barrier()
+        pm, pn, sm, sn = (ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64())
+        lib.wedg_kernel_times(ws._h, ctypes.byref(pm), ctypes.byref(pn), ctypes.byref(sm), ctypes.byref(sn), 1)
+        lib.wedg_time_kernels(ws._h, 0)
+        st = ws.stats()
+        return dict(ms=ms, steps=int(done.value), launches=launches, prep_ms=pm.value / max(pn.value, 1),
+                    stage_ms=sm.value / max(sn.value, 1), n_stage=sn.value, cheb=st["cheb_steps_max"])
+
+    with ClockSampler(local) as clocks:
+        main = timed("front", args.steps, args.warmup)
+    zero = timed("zero", max(2, args.steps // 4), args.warmup)
+    unif = timed("uniform", max(2, args.steps // 4), args.warmup)
+    ms_step = main["ms"] / args.steps
+    value = world * dof * 4 * args.steps / (main["ms"] / 1e3)
+
+    # end to end through the public API: pinned host state in, result out, every step
+    e2e = None
+    if rank == 0 or world > 1:
+        tu = torch.empty(E * nu * nu, dtype=torch.float64, pin_memory=True)
+        tv = torch.empty(E * nv * nv, dtype=torch.float64, pin_memory=True)
+        uh = tu.numpy().reshape((N, N, nu, nu), order="F")
+        vh = tv.numpy().reshape((N, N, nv, nv), order="F")
+        us, vs = synthetic_state(N, nu, nv, 0, "front")
+        uh[...] = us
+        vh[...] = vs
+        ws.rk4_steps(uh, vh, T0, dt, 1)               # warm-up
+        uh[...] = us
+        vh[...] = vs
+        ke = max(2, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for i in range(ke):
+            ws.rk4_steps(uh, vh, T0 + i * dt, dt, 1)
+        te = time.perf_counter() - t0
+        e2e = {"value": world * dof * 4 * ke / te, "unit": "DOF·stage/s",
+               "h2d_bytes_per_step": int(uh.nbytes + vh.nbytes), "d2h_bytes_per_step": int(uh.nbytes + vh.nbytes),
+               "steps": ke, "api": "Workspace.rk4_steps (wedg_rk4_steps, WEDG_HOST)"}
+
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    bytes_stage = alg_bytes_per_element_stage(nu, nv, qh) * E
+    achieved_gbs = bytes_stage / (main["stage_ms"] / 1e3) / 1e9
+    fp64_peak = fp64_gemm_peak(torch, dev)
+    flops_stage = alg_flops_per_element_stage(nu, nv, qh, main["cheb"]) * E
+    fp64_achieved = flops_stage / (main["stage_ms"] / 1e3) / 1e12
+    roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                "frac": achieved_gbs / hbm if hbm else None, "traffic": traffic_from_profile(),
+                "kernel": "k_stage", "bytes_per_launch": bytes_stage, "launch_ms": main["stage_ms"],
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm else None,
+                "note": "the path is FP64-pipe bound on GB300 (see roofline_fp64); bytes are the reference data "
+                        "model's algorithmic bytes per element-stage x elements"}
+    roofline_fp64 = {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": fp64_achieved / fp64_peak, "flops_per_launch": flops_stage,
+                     "cheb_steps_max": main["cheb"], "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        r, n, t, cores = cpu_baseline(args.cpu_seconds)
+        cpu = {"value": r, "unit": "DOF·stage/s", "cores": cores, "kind": "port",
+               "sample": f"{n} RK4 steps ({t:.1f} s) of the same configuration and front state on an N={SAMPLE_N} "
+                         f"mesh; the oracle's C restatement with OpenMP"}
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    line = {
+        "metric": "FP64 DOF·stage/s on 1 GB300 (plain method, RK4 step)", "value": value, "unit": "DOF·stage/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded steepened-wave state; the reference measures on no dataset)",
+        "config": {"workload": workload_name(), "elements": E, "dof": dof,
+                   "state": "steepened circular front, 1-2βv_h in [0.42, 1.58] across it (seeded)",
+                   "l2": "inputs larger than L2 (state 206 MB, stage data > 600 MB per stage)",
+                   "cheb_steps": "per element", "t0": T0},
+        "roofline": roofline, "roofline_fp64": roofline_fp64, "cpu_baseline": cpu, "e2e": e2e,
+        "clocks": clocks.summary(), "gpu_launches": main["launches"],
+        "kernel_ms": {"k_prep": main["prep_ms"], "k_stage": main["stage_ms"]},
+        "zero_state": {"value": world * dof * 4 * zero["steps"] / (zero["ms"] / 1e3),
+                       "ms_per_step": zero["ms"] / max(zero["steps"], 1), "cheb_steps_max": zero["cheb"],
+                       "k_stage_ms": zero["stage_ms"]},
+        "uniform_state": {"value": world * dof * 4 * unif["steps"] / (unif["ms"] / 1e3),
+                          "ms_per_step": unif["ms"] / max(unif["steps"], 1), "cheb_steps_max": unif["cheb"],
+                          "k_stage_ms": unif["stage_ms"],
+                          "note": "every element spans 1-2βv in [0.42, 1.58]: no element is cheap"},
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,800 @@
+// Host runtime and C ABI of libwedg (declared in include/wedg.h).
+//
+// wedg_create turns the reference's `pre` (host arrays in Julia layouts,
+// src/solver.jl:428-770) into device arrays in element-fastest layouts,
+// builds the 1D operators the kernels take as parameters, and detects the
+// constant-coefficient fast path. The call functions enqueue the two kernels
+// of each stage (wedg_kernels.cuh) on the workspace stream and report errors
+// with the reference's semantics: boundary-weight errors before mass errors
+// (src/rhs.jl:530-531), the first failing point or element in the order of the
+// serial loops, and the state left untouched by a failing RK4 step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/wedg.h"
+#include "wedg_dispatch.h"
+
+namespace wedg {
+
+__global__ void k_rk4_final(int n_u, int n_v, double *u, double *v, const double *accu, const double *accv,
+                            double c, const unsigned long long *err, unsigned int *nonfinite) {
+  if (*(volatile const unsigned long long *)err != ERR_NONE) return;
+  bool fin = true;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_u + n_v; i += gridDim.x * blockDim.x) {
+    if (i < n_u) {
+      const double x = u[i] + c * accu[i];
+      u[i] = x;
+      fin = fin && isfinite(x);
+    } else {
+      const int l = i - n_u;
+      const double x = v[l] + c * accv[l];
+      v[l] = x;
+      fin = fin && isfinite(x);
+    }
+  }
+  if (!fin) atomicOr(nonfinite, 1u);
+}
+
+__global__ void k_step_done(unsigned long long *err, const unsigned int *nonfinite, int stop_nonfinite,
+                            long long *steps_done) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (*err != ERR_NONE) return;
+  *steps_done += 1;
+  if (stop_nonfinite && *nonfinite) *err = (3ull << ERR_CLASS_SHIFT);
+}
+
+Launchers get_launchers(int nu, int nv, bool fast) {
+  switch (nu) {
+    case 2: return launchers_q1(nv, fast);
+    case 3: return launchers_q2(nv, fast);
+    case 4: return launchers_q3(nv, fast);
+    case 5: return launchers_q4(nv, fast);
+    case 6: return launchers_q5(nv, fast);
+    case 7: return launchers_q6(nv, fast);
+    case 8: return launchers_q7(nv, fast);
+    default: return Launchers();
+  }
+}
+
+}  // namespace wedg
+
+using namespace wedg;
+
+struct wedg_ws {
+  wedg_config cfg;
+  int N = 0, E = 0, nu = 0, nv = 0, nq = 0, qh = 0;
+  bool fast = false;
+  Launchers L;
+  std::vector<char> basis;
+  Fields F{};
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  std::vector<void *> allocs;
+  size_t bytes = 0;
+  // state buffers
+  double *d_u = nullptr, *d_v = nullptr, *d_ut = nullptr, *d_vt = nullptr;
+  double *su = nullptr, *sv = nullptr, *accu = nullptr, *accv = nullptr;
+  long long *steps_done = nullptr;
+  // optional per-launch timing (events recorded around each stage kernel)
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  struct EvTriple { cudaEvent_t a, b, c; };   // prep runs from a to b, stage from b to c
+  std::vector<EvTriple> ev_pending;
+  double t_prep = 0, t_stage = 0;
+  int64_t n_prep = 0, n_stage = 0;
+  // last call
+  int status = WEDG_OK;
+  int64_t key = 0;
+  std::string message;
+  wedg_stats stats{};
+};
+
+namespace {
+
+int cuda_fail(wedg_ws *ws, cudaError_t e, const char *what) {
+  if (ws) {
+    ws->status = WEDG_ERR_CUDA;
+    ws->message = std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e);
+  }
+  return WEDG_ERR_CUDA;
+}
+
+#define CK(ws, call)                                          \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail(ws, e_, #call);   \
+  } while (0)
+
+template <typename T>
+int dalloc(wedg_ws *ws, T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  void *q = nullptr;
+  CK(ws, cudaMalloc(&q, n * sizeof(T)));
+  ws->allocs.push_back(q);
+  ws->bytes += n * sizeof(T);
+  *p = static_cast<T *>(q);
+  return WEDG_OK;
+}
+
+template <typename T>
+int upload(wedg_ws *ws, const T **dst, const std::vector<T> &h) {
+  T *p;
+  int rc = dalloc(ws, &p, h.size());
+  if (rc) return rc;
+  CK(ws, cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  *dst = p;
+  return WEDG_OK;
+}
+
+// Cyclic Jacobi eigen-decomposition of a small symmetric matrix A (n×n, row-major):
+// A = Q diag(lam) Q^T, eigenvalues ascending.
+void sym_eig(int n, std::vector<double> A, std::vector<double> &Q, std::vector<double> &lam) {
+  Q.assign(n * n, 0.0);
+  for (int i = 0; i < n; ++i) Q[i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) off += A[p * n + q] * A[p * n + q];
+    if (off < 1e-40) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A[p * n + q];
+        if (std::fabs(apq) < 1e-300) continue;
+        const double app = A[p * n + p], aqq = A[q * n + q];
+        const double tau = (aqq - app) / (2 * apq);
+        const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1 + tau * tau));
+        const double c = 1 / std::sqrt(1 + t * t), s = t * c;
+        for (int k = 0; k < n; ++k) {
+          const double akp = A[k * n + p], akq = A[k * n + q];
+          A[k * n + p] = c * akp - s * akq;
+          A[k * n + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double apk = A[p * n + k], aqk = A[q * n + k];
+          A[p * n + k] = c * apk - s * aqk;
+          A[q * n + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double qkp = Q[k * n + p], qkq = Q[k * n + q];
+          Q[k * n + p] = c * qkp - s * qkq;
+          Q[k * n + q] = s * qkp + c * qkq;
+        }
+      }
+  }
+  lam.resize(n);
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; ++i) { lam[i] = A[i * n + i]; idx[i] = i; }
+  std::sort(idx.begin(), idx.end(), [&](int a, int b) { return lam[a] < lam[b]; });
+  std::vector<double> Qs(n * n), ls(n);
+  for (int c = 0; c < n; ++c) {
+    ls[c] = lam[idx[c]];
+    for (int r = 0; r < n; ++r) Qs[r * n + c] = Q[r * n + idx[c]];
+  }
+  Q = Qs;
+  lam = ls;
+}
+
+const char *kind_name(int k) {
+  switch (k) {
+    case WEDG_ABSORBING_2BETA: return "absorbing_2beta";
+    case WEDG_ABSORBING: return "absorbing";
+    case WEDG_DIRICHLET: return "dirichlet";
+    case WEDG_WALL: return "wall";
+    default: return "?";
+  }
+}
+
+// Julia's `string(x)` for the tolerance in the CG warning (1.0e-14 style)
+std::string julia_float(double x) {
+  char buf[64];
+  for (int p = 1; p <= 17; ++p) {
+    snprintf(buf, sizeof buf, "%.*e", p - 1, x);
+    if (std::strtod(buf, nullptr) == x) break;
+  }
+  std::string s(buf);
+  const size_t epos = s.find('e');
+  std::string mant = s.substr(0, epos);
+  int ex = std::atoi(s.c_str() + epos + 1);
+  if (ex >= -5 && ex < 16) {
+    snprintf(buf, sizeof buf, "%.17g", x);
+    std::string t;
+    for (int p = 1; p <= 17; ++p) {
+      snprintf(buf, sizeof buf, "%.*g", p, x);
+      if (std::strtod(buf, nullptr) == x) break;
+    }
+    t = buf;
+    if (t.find('.') == std::string::npos && t.find('e') == std::string::npos) t += ".0";
+    return t;
+  }
+  if (mant.find('.') == std::string::npos) mant += ".0";
+  return mant + "e" + std::to_string(ex);
+}
+
+// shape check of src/rhs.jl:500-503
+int check_shapes(wedg_ws *ws, const int64_t *us, const int64_t *vs) {
+  const int N = ws->N;
+  bool ok = us && vs && us[0] == N && us[1] == N && us[2] == ws->nu && us[3] == ws->nu && vs[0] == N &&
+            vs[1] == N && vs[2] == ws->nv && vs[3] == ws->nv;
+  if (ok) return WEDG_OK;
+  ws->status = WEDG_ERR_DIMENSION;
+  ws->message = "state, workspace and pre do not match (N = " + std::to_string(N) +
+                ", q_u + 1 = " + std::to_string(ws->nu) + ", q_v + 1 = " + std::to_string(ws->nv) + ")";
+  return WEDG_ERR_DIMENSION;
+}
+
+void stage_factors(const wedg_ws *ws, double t, StageIO &S) {
+  const wedg_config &c = ws->cfg;
+  const double om = c.omega;
+  S.ct = c.mms_on ? std::cos(om * t) : 0.0;
+  S.st = c.mms_on ? std::sin(om * t) : 0.0;
+  S.srct = 0.0;
+  if (c.src_on && t < c.src_Ts) {
+    const double s = std::sin(M_PI * t / c.src_Ts);
+    S.srct = std::sin(c.src_omega * t) * (s * s);
+  }
+  S.cSP = -(om * om) * S.ct;
+  S.cB = -2.0 * (om * om * om) * S.st * S.ct;
+  S.cC = 1.0 - S.ct;
+  S.cD = om * S.st;
+}
+
+int reset_flags(wedg_ws *ws) {
+  CK(ws, cudaMemsetAsync(ws->F.err, 0xFF, sizeof(unsigned long long), ws->stream));
+  CK(ws, cudaMemsetAsync(ws->F.cg_nfail, 0, sizeof(unsigned int), ws->stream));
+  CK(ws, cudaMemsetAsync(ws->F.nonfinite, 0, sizeof(unsigned int), ws->stream));
+  CK(ws, cudaMemsetAsync(ws->F.nmax, 0, sizeof(int), ws->stream));
+  CK(ws, cudaMemsetAsync(ws->steps_done, 0, sizeof(long long), ws->stream));
+  return WEDG_OK;
+}
+
+cudaEvent_t take_event(wedg_ws *ws) {
+  if (!ws->ev_pool.empty()) {
+    cudaEvent_t e = ws->ev_pool.back();
+    ws->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// fold the recorded launch durations into the totals (after a synchronization)
+void drain_events(wedg_ws *ws) {
+  for (auto &p : ws->ev_pending) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) { ws->t_prep += ms; ws->n_prep += 1; }
+    if (cudaEventElapsedTime(&ms, p.b, p.c) == cudaSuccess) { ws->t_stage += ms; ws->n_stage += 1; }
+    ws->ev_pool.push_back(p.a);
+    ws->ev_pool.push_back(p.b);
+    ws->ev_pool.push_back(p.c);
+  }
+  ws->ev_pending.clear();
+}
+
+// enqueue the two kernels of one stage
+int enqueue_stage(wedg_ws *ws, const StageIO &S) {
+  const int tp = 128, bp = (ws->E + tp - 1) / tp;
+  const int ts = stage_threads(ws->nu, ws->nv), bs = (ws->E + ts - 1) / ts;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  if (ws->timing) {
+    e0 = take_event(ws); e1 = take_event(ws); e2 = take_event(ws);
+    cudaEventRecord(e0, ws->stream);
+  }
+  ws->L.prep(ws->basis.data(), ws->F, S, bp, tp, ws->stream);
+  if (ws->timing) cudaEventRecord(e1, ws->stream);
+  ws->L.stage(ws->basis.data(), ws->F, S, bs, ts, ws->stream);
+  if (ws->timing) {
+    cudaEventRecord(e2, ws->stream);
+    ws->ev_pending.push_back({e0, e1, e2});
+  }
+  ws->stats.kernel_launches += 2;
+  CK(ws, cudaGetLastError());
+  return WEDG_OK;
+}
+
+// one RK4 step on device state u, v (src/solver.jl:289-297)
+int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop_nonfinite) {
+  const double cs[3] = {0.5 * dt, 0.5 * dt, dt};
+  const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
+  const bool cg = ws->cfg.mass_solver == WEDG_CG;
+  for (int s = 0; s < 4; ++s) {
+    StageIO S{};
+    S.xu = s == 0 ? u : ws->su;
+    S.xv = s == 0 ? v : ws->sv;
+    stage_factors(ws, ts[s], S);
+    S.u0 = u; S.v0 = v;
+    S.su = ws->su; S.sv = ws->sv;
+    S.accu = ws->accu; S.accv = ws->accv;
+    S.uo = u; S.vo = v;
+    if (s < 3) {
+      S.mode = OUT_RK4_STAGE;
+      S.first = s == 0;
+      S.c = cs[s];
+    } else {
+      S.mode = cg ? OUT_RK4_LAST_ACC : OUT_RK4_LAST;
+      S.c = dt / 6.0;
+    }
+    int rc = enqueue_stage(ws, S);
+    if (rc) return rc;
+  }
+  if (cg) {
+    const int nU = ws->E * ws->nu * ws->nu, nV = ws->E * ws->nv * ws->nv;
+    const int blocks = std::min((nU + nV + 255) / 256, 152 * 8);
+    k_rk4_final<<<blocks, 256, 0, ws->stream>>>(nU, nV, u, v, ws->accu, ws->accv, dt / 6.0, ws->F.err,
+                                                ws->F.nonfinite);
+    ws->stats.kernel_launches += 1;
+  }
+  k_step_done<<<1, 32, 0, ws->stream>>>(ws->F.err, ws->F.nonfinite, stop_nonfinite, ws->steps_done);
+  ws->stats.kernel_launches += 1;
+  CK(ws, cudaGetLastError());
+  return WEDG_OK;
+}
+
+// read the flags after a synchronized call and turn them into the status
+int collect(wedg_ws *ws) {
+  unsigned long long err;
+  unsigned int cgf, nonf;
+  int nmax;
+  long long done;
+  CK(ws, cudaStreamSynchronize(ws->stream));
+  drain_events(ws);
+  CK(ws, cudaMemcpy(&err, ws->F.err, sizeof err, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(&cgf, ws->F.cg_nfail, sizeof cgf, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(&nonf, ws->F.nonfinite, sizeof nonf, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(&nmax, ws->F.nmax, sizeof nmax, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(&done, ws->steps_done, sizeof done, cudaMemcpyDeviceToHost));
+  ws->stats.cg_not_converged = (int32_t)cgf;
+  ws->stats.finite = nonf ? 0 : 1;
+  ws->stats.cheb_steps_max = nmax;
+  ws->stats.steps_done = done;
+  ws->status = WEDG_OK;
+  ws->key = 0;
+  ws->message.clear();
+  if (err != ERR_NONE) {
+    const unsigned cls = (unsigned)(err >> ERR_CLASS_SHIFT);
+    const int64_t key = (int64_t)(err & ((1ull << ERR_CLASS_SHIFT) - 1));
+    if (cls == 0) {
+      // src/rhs.jl:768-776 and :112-116
+      const int s = (int)((key - 1) / (2 * (int64_t)ws->nq * ws->N));
+      const int check = (key % 2 == 1) ? 1 : 2;
+      const std::string kk = ws->cfg.kb[s] == 2.0 ? "2" : "";
+      const std::string kind = kind_name(ws->cfg.kind[s]);
+      ws->status = WEDG_ERR_BOUNDARY_WEIGHT;
+      ws->key = key;
+      ws->message = check == 1 ? "boundary weight 1 - " + kk + "βv_h ≤ 0 at a face point (" + kind + " side)"
+                               : "boundary weight 1 - " + kk + "βg ≤ 0 for the boundary data g (" + kind + " side)";
+    } else if (cls == 1) {
+      ws->status = WEDG_ERR_MASS_NOT_PD;
+      ws->key = key;
+      if (ws->cfg.mass_solver == WEDG_CG) {
+        const int64_t j = (key - 1) % ws->N + 1, k = (key - 1) / ws->N + 1;
+        ws->message = "mass matrix not positive definite on element (" + std::to_string(j) + ", " +
+                      std::to_string(k) + "): 1 - 2βv_h ≤ 0";
+      } else {
+        ws->message = "mass matrix not positive definite on element " + std::to_string(key) + ": 1 - 2βv_h ≤ 0";
+      }
+    }
+    // class 3: a run stopped after a non-finite step; not an error of the call
+  }
+  if (ws->status == WEDG_OK && cgf > 0 && ws->cfg.mass_solver == WEDG_CG) {
+    ws->status = WEDG_WARN_CG_NOT_CONVERGED;
+    ws->message = "mass solve: " + std::to_string(cgf) + " element systems did not reach the tolerance " +
+                  julia_float(ws->cfg.mass_tol);
+  }
+  return ws->status;
+}
+
+int argument_error(wedg_ws *ws, const std::string &msg) {
+  if (ws) {
+    ws->status = WEDG_ERR_ARGUMENT;
+    ws->message = msg;
+  }
+  return WEDG_ERR_ARGUMENT;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
+  if (!out) return WEDG_ERR_ARGUMENT;
+  *out = nullptr;
+  if (!cfg || !pre) return WEDG_ERR_ARGUMENT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return WEDG_ERR_NO_DEVICE;
+  const int N = cfg->N, nu = cfg->qu1, nv = cfg->qv1;
+  if (N < 1 || nu < 2 || nu > MAXN || !(nv == nu || nv == nu - 1) || cfg->q_high != qhigh(nu, nv))
+    return WEDG_ERR_ARGUMENT;
+  if ((int64_t)N * N > (int64_t)1 << 30) return WEDG_ERR_ARGUMENT;
+  for (int s = 0; s < 4; ++s)
+    if (cfg->kind[s] < 0 || cfg->kind[s] > 3) return WEDG_ERR_ARGUMENT;
+  if (cfg->mass_solver != WEDG_CHEBYSHEV && cfg->mass_solver != WEDG_CG) return WEDG_ERR_ARGUMENT;
+  const double *need[] = {pre->w, pre->P_u, pre->S_u, pre->Ebl_u, pre->Ebr_u, pre->E1bl_u, pre->E1br_u,
+                          pre->P_h_v, pre->W2d_h, pre->Cw, pre->Aw, pre->hc2, pre->haf, pre->hcf, pre->hbf,
+                          pre->vc2, pre->vaf, pre->vcf, pre->vbf, pre->hc2m, pre->hafm, pre->vc2m, pre->vafm,
+                          pre->hJC, pre->vJC, pre->bcB_sp, pre->bcB_spy, pre->bcT_sp, pre->bcT_spy, pre->bcL_sp,
+                          pre->bcL_spx, pre->bcR_sp, pre->bcR_spx, pre->PiSP, pre->PiBSP2, pre->PiCdiv,
+                          pre->PiDdiv, pre->src_projE, pre->beta_hq};
+  for (const double *p : need)
+    if (!p) return WEDG_ERR_ARGUMENT;
+
+  wedg_ws *ws = new wedg_ws();
+  ws->cfg = *cfg;
+  ws->N = N;
+  ws->E = N * N;
+  ws->nu = nu;
+  ws->nv = nv;
+  ws->nq = nu;
+  ws->qh = cfg->q_high;
+  const int E = ws->E, nq = nu, qh = ws->qh;
+  const size_t Es = (size_t)E;
+
+  // ---- 1D operators (Julia column-major inputs)
+  BasisHost bh{};
+  bh.nu = nu; bh.nv = nv; bh.qh = qh;
+  for (int i = 0; i < nq; ++i) {
+    bh.w[i] = pre->w[i];
+    for (int d = 0; d < nu; ++d) { bh.P[i][d] = pre->P_u[i + nq * d]; bh.S[i][d] = pre->S_u[i + nq * d]; }
+  }
+  for (int d = 0; d < nu; ++d) {
+    bh.El[d] = pre->Ebl_u[d]; bh.Er[d] = pre->Ebr_u[d]; bh.E1l[d] = pre->E1bl_u[d]; bh.E1r[d] = pre->E1br_u[d];
+  }
+  for (int r = 0; r < qh; ++r) {
+    for (int d = 0; d < nv; ++d) bh.Ph[r][d] = pre->P_h_v[r + qh * d];
+    for (int s = 0; s < qh; ++s) bh.Wh[r][s] = pre->W2d_h[r + qh * s];
+  }
+  // K1 = S^T diag(w) S; its first row and column vanish (the constant mode has no derivative)
+  for (int a = 0; a < nu; ++a)
+    for (int c = 0; c < nu; ++c) {
+      double s = 0;
+      for (int i = 0; i < nq; ++i) s += bh.S[i][a] * bh.w[i] * bh.S[i][c];
+      bh.K1[a][c] = s;
+    }
+  {
+    // eigen-decomposition of the nonsingular block K1[1:, 1:]; Q = diag(1, Q')
+    const int m = nu - 1;
+    std::vector<double> A(m * m), Qm, lam;
+    for (int a = 0; a < m; ++a)
+      for (int c = 0; c < m; ++c) A[a * m + c] = 0.5 * (bh.K1[a + 1][c + 1] + bh.K1[c + 1][a + 1]);
+    sym_eig(m, A, Qm, lam);
+    std::vector<double> L(nu, 0.0);
+    for (int a = 0; a < nu; ++a)
+      for (int c = 0; c < nu; ++c) bh.Q[a][c] = 0.0;
+    bh.Q[0][0] = 1.0;
+    for (int a = 0; a < m; ++a) {
+      L[a + 1] = lam[a];
+      for (int c = 0; c < m; ++c) bh.Q[a + 1][c + 1] = Qm[a * m + c];
+    }
+    for (int i = 0; i < nu; ++i)
+      for (int j = 0; j < nu; ++j) bh.ilam2[i][j] = (i == 0 && j == 0) ? 1.0 : 1.0 / (L[i] + L[j]);
+  }
+
+  // ---- constant coefficients per element? Cw = c² W and Aw = α W to 1e-14 (relative)
+  std::vector<double> c2e(E), ae(E), ic2e(E);
+  bool fast = !cfg->general_only;
+  for (int e = 0; e < E && fast; ++e) {
+    const double w00 = bh.w[0] * bh.w[0];
+    const double c2 = pre->Cw[0 + nq * ((size_t)e + Es * 0)] / w00;
+    const double al = pre->Aw[0 + nq * ((size_t)e + Es * 0)] / w00;
+    for (int s = 0; s < nq && fast; ++s)
+      for (int r = 0; r < nq; ++r) {
+        const double W = bh.w[r] * bh.w[s];
+        const double cw = pre->Cw[r + nq * ((size_t)e + Es * s)], aw = pre->Aw[r + nq * ((size_t)e + Es * s)];
+        if (std::fabs(cw - c2 * W) > 1e-14 * std::fabs(cw) || std::fabs(aw - al * W) > 1e-14 * std::fabs(aw) ||
+            !(c2 > 0)) {
+          fast = false;
+          break;
+        }
+      }
+    c2e[e] = c2;
+    ae[e] = al;
+    ic2e[e] = 1.0 / c2;
+  }
+  if (!fast && !pre->Ainv_u) {
+    delete ws;
+    return WEDG_ERR_ARGUMENT;
+  }
+  ws->fast = fast;
+  ws->L = get_launchers(nu, nv, fast);
+  if (!ws->L.prep) {
+    delete ws;
+    return WEDG_ERR_ARGUMENT;
+  }
+  ws->basis.resize(ws->L.basis_size);
+  ws->L.pack(bh, ws->basis.data());
+
+  int rc = WEDG_OK;
+#define UP(dst, vec)                     \
+  do {                                   \
+    rc = upload(ws, &(dst), vec);        \
+    if (rc) { wedg_destroy(ws); return rc; } \
+  } while (0)
+  Fields &F = ws->F;
+  F.N = N;
+  F.E = E;
+  // ---- element arrays, element index fastest
+  if (fast) {
+    UP(F.c2e, c2e);
+    UP(F.ae, ae);
+    UP(F.ic2e, ic2e);
+  } else {
+    std::vector<double> cw((size_t)nq * nq * E), aw((size_t)nq * nq * E);
+    for (int s = 0; s < nq; ++s)
+      for (int r = 0; r < nq; ++r)
+        for (int e = 0; e < E; ++e) {
+          cw[(r + nq * s) * Es + e] = pre->Cw[r + nq * ((size_t)e + Es * s)];
+          aw[(r + nq * s) * Es + e] = pre->Aw[r + nq * ((size_t)e + Es * s)];
+        }
+    UP(F.Cw, cw);
+    UP(F.Aw, aw);
+    const size_t nt = (size_t)nu * nu * (nu * nu + 1) / 2;
+    std::vector<double> ai(nt * E);
+    for (int e = 0; e < E; ++e)
+      for (size_t row = 0; row < nt; ++row) ai[row * Es + e] = pre->Ainv_u[row + nt * e];
+    UP(F.Ainv, ai);
+  }
+  // ---- face arrays: (nq, N+1, N) -> [jf + (N+1)(k + N i)], (nq, N, N+1) -> [j + N (kf + (N+1) i)]
+  auto hf = [&](const double *a) {
+    std::vector<double> o((size_t)nq * (N + 1) * N);
+    for (int k = 0; k < N; ++k)
+      for (int jf = 0; jf <= N; ++jf)
+        for (int i = 0; i < nq; ++i) o[jf + (size_t)(N + 1) * (k + (size_t)N * i)] = a[i + nq * (jf + (size_t)(N + 1) * k)];
+    return o;
+  };
+  auto vf = [&](const double *a) {
+    std::vector<double> o((size_t)nq * N * (N + 1));
+    for (int kf = 0; kf <= N; ++kf)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < nq; ++i) o[j + (size_t)N * (kf + (size_t)(N + 1) * i)] = a[i + nq * (j + (size_t)N * kf)];
+    return o;
+  };
+  UP(F.hc2, hf(pre->hc2)); UP(F.haf, hf(pre->haf)); UP(F.hcf, hf(pre->hcf)); UP(F.hbf, hf(pre->hbf));
+  UP(F.hc2m, hf(pre->hc2m)); UP(F.hafm, hf(pre->hafm)); UP(F.hJC, hf(pre->hJC));
+  UP(F.vc2, vf(pre->vc2)); UP(F.vaf, vf(pre->vaf)); UP(F.vcf, vf(pre->vcf)); UP(F.vbf, vf(pre->vbf));
+  UP(F.vc2m, vf(pre->vc2m)); UP(F.vafm, vf(pre->vafm)); UP(F.vJC, vf(pre->vJC));
+  // boundary data (nq, N) -> [m + N i]
+  auto bd = [&](const double *a) {
+    std::vector<double> o((size_t)nq * N);
+    for (int m = 0; m < N; ++m)
+      for (int i = 0; i < nq; ++i) o[m + (size_t)N * i] = a[i + nq * m];
+    return o;
+  };
+  const double *sp[4] = {pre->bcB_sp, pre->bcT_sp, pre->bcL_sp, pre->bcR_sp};
+  const double *spn[4] = {pre->bcB_spy, pre->bcT_spy, pre->bcL_spx, pre->bcR_spx};
+  for (int s = 0; s < 4; ++s) {
+    UP(F.bsp[s], bd(sp[s]));
+    UP(F.bspn[s], bd(spn[s]));
+  }
+  // projections (nv, nv, N, N) -> [(a + nv b) E + e]
+  auto pj = [&](const double *a) {
+    std::vector<double> o((size_t)nv * nv * E);
+    for (int e = 0; e < E; ++e)
+      for (int l = 0; l < nv * nv; ++l) o[l * Es + e] = a[l + (size_t)nv * nv * e];
+    return o;
+  };
+  if (cfg->mms_on) {
+    UP(F.PiSP, pj(pre->PiSP)); UP(F.PiBSP2, pj(pre->PiBSP2)); UP(F.PiDdiv, pj(pre->PiDdiv));
+  }
+  if (!cfg->src_on) UP(F.PiCdiv, pj(pre->PiCdiv));
+  if (cfg->src_on) UP(F.srcP, pj(pre->src_projE));
+  // β at the high-order points (qh, E, qh) -> [(r + qh s) E + e]
+  {
+    std::vector<double> o((size_t)qh * qh * E);
+    for (int s = 0; s < qh; ++s)
+      for (int e = 0; e < E; ++e)
+        for (int r = 0; r < qh; ++r) o[(r + qh * s) * Es + e] = pre->beta_hq[r + qh * ((size_t)e + Es * s)];
+    UP(F.beta, o);
+  }
+#undef UP
+  // ---- scratch
+  const size_t nU = (size_t)nu * nu * E, nV = (size_t)nv * nv * E;
+  if ((rc = dalloc(ws, &F.tr, (size_t)12 * nq * E)) || (rc = dalloc(ws, &F.G, (size_t)qh * qh * E)) ||
+      (rc = dalloc(ws, &F.th, Es)) || (rc = dalloc(ws, &F.de, Es)) || (rc = dalloc(ws, &F.nst, Es)) ||
+      (rc = dalloc(ws, &F.nmax, 1)) || (rc = dalloc(ws, &F.err, 1)) || (rc = dalloc(ws, &F.cg_nfail, 1)) ||
+      (rc = dalloc(ws, &F.nonfinite, 1)) || (rc = dalloc(ws, &ws->steps_done, 1)) ||
+      (rc = dalloc(ws, &ws->d_u, nU)) || (rc = dalloc(ws, &ws->d_v, nV)) || (rc = dalloc(ws, &ws->d_ut, nU)) ||
+      (rc = dalloc(ws, &ws->d_vt, nV)) || (rc = dalloc(ws, &ws->su, nU)) || (rc = dalloc(ws, &ws->sv, nV)) ||
+      (rc = dalloc(ws, &ws->accu, nU)) || (rc = dalloc(ws, &ws->accv, nV))) {
+    wedg_destroy(ws);
+    return rc;
+  }
+  F.theta = cfg->theta; F.tau = cfg->tau; F.lu = cfg->lambda_u; F.lv = cfg->lambda_v;
+  F.omega = cfg->omega;
+  const double h = 1.0 / N;
+  F.two_h = 2.0 / h;
+  F.four_hh = 4.0 / (h * h);
+  F.mass_tol = cfg->mass_tol;
+  F.Lcheb = std::acosh(1.0 / cfg->mass_tol);
+  F.one_sided = cfg->one_sided ? 1 : 0;
+  F.mms_on = cfg->mms_on ? 1 : 0;
+  F.src_on = cfg->src_on ? 1 : 0;
+  F.cg = cfg->mass_solver == WEDG_CG;
+  F.cheb_common = cfg->cheb_steps == WEDG_CHEB_COMMON_MAX;
+  for (int s = 0; s < 4; ++s) {
+    F.kind[s] = cfg->kind[s];
+    F.gam[s] = cfg->gamma_abc[s]; F.eta[s] = cfg->eta_abc[s]; F.sig[s] = cfg->sigma[s];
+    F.kb[s] = cfg->kb[s]; F.kap[s] = cfg->kappa[s];
+  }
+  // sets the shared-memory attribute of k_stage (a launch of zero blocks does nothing else)
+  ws->L.stage(ws->basis.data(), F, StageIO{}, 0, 0, nullptr);
+  cudaError_t ce = cudaStreamCreateWithFlags(&ws->own_stream, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) {
+    int r = cuda_fail(ws, ce, "cudaStreamCreate");
+    wedg_destroy(ws);
+    return r;
+  }
+  ws->stream = ws->own_stream;
+  ws->stats.fast_path = fast ? 1 : 0;
+  ws->stats.device_bytes = (int64_t)ws->bytes;
+  cudaDeviceSynchronize();
+  *out = ws;
+  return WEDG_OK;
+}
+
+void wedg_destroy(wedg_ws *ws) {
+  if (!ws) return;
+  if (ws->own_stream) cudaStreamSynchronize(ws->own_stream);
+  if (ws->stream) cudaStreamSynchronize(ws->stream);
+  drain_events(ws);
+  for (cudaEvent_t e : ws->ev_pool) cudaEventDestroy(e);
+  for (void *p : ws->allocs) cudaFree(p);
+  if (ws->own_stream) cudaStreamDestroy(ws->own_stream);
+  delete ws;
+}
+
+int wedg_rhs(wedg_ws *ws, const double *u, const double *v, double t, double *ut, double *vt,
+             const int64_t u_shape[4], const int64_t v_shape[4], int where) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  ws->stats.kernel_launches = 0;
+  int rc = check_shapes(ws, u_shape, v_shape);
+  if (rc) return rc;
+  if (!u || !v || !ut || !vt) return argument_error(ws, "null state pointer");
+  const size_t bU = sizeof(double) * ws->E * ws->nu * ws->nu, bV = sizeof(double) * ws->E * ws->nv * ws->nv;
+  const double *xu = u, *xv = v;
+  double *ou = ut, *ov = vt;
+  if (where == WEDG_HOST) {
+    CK(ws, cudaMemcpyAsync(ws->d_u, u, bU, cudaMemcpyHostToDevice, ws->stream));
+    CK(ws, cudaMemcpyAsync(ws->d_v, v, bV, cudaMemcpyHostToDevice, ws->stream));
+    xu = ws->d_u; xv = ws->d_v; ou = ws->d_ut; ov = ws->d_vt;
+  }
+  if ((rc = reset_flags(ws))) return rc;
+  StageIO S{};
+  S.xu = xu; S.xv = xv;
+  stage_factors(ws, t, S);
+  S.mode = OUT_RHS;
+  S.ut = ou; S.vt = ov;
+  if ((rc = enqueue_stage(ws, S))) return rc;
+  rc = collect(ws);
+  if ((rc == WEDG_OK || rc == WEDG_WARN_CG_NOT_CONVERGED) && where == WEDG_HOST) {
+    CK(ws, cudaMemcpy(ut, ws->d_ut, bU, cudaMemcpyDeviceToHost));
+    CK(ws, cudaMemcpy(vt, ws->d_vt, bV, cudaMemcpyDeviceToHost));
+  }
+  return rc;
+}
+
+int wedg_rk4_steps(wedg_ws *ws, double *u, double *v, double t0, double dt, int64_t nsteps,
+                   const int64_t u_shape[4], const int64_t v_shape[4], int where, int stop_nonfinite,
+                   int64_t *steps_done, int *finite) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  ws->stats.kernel_launches = 0;
+  int rc = check_shapes(ws, u_shape, v_shape);
+  if (rc) return rc;
+  if (!u || !v) return argument_error(ws, "null state pointer");
+  if (nsteps < 0) return argument_error(ws, "nsteps must be ≥ 0");
+  const size_t bU = sizeof(double) * ws->E * ws->nu * ws->nu, bV = sizeof(double) * ws->E * ws->nv * ws->nv;
+  double *du = u, *dv = v;
+  if (where == WEDG_HOST) {
+    CK(ws, cudaMemcpyAsync(ws->d_u, u, bU, cudaMemcpyHostToDevice, ws->stream));
+    CK(ws, cudaMemcpyAsync(ws->d_v, v, bV, cudaMemcpyHostToDevice, ws->stream));
+    du = ws->d_u; dv = ws->d_v;
+  }
+  if ((rc = reset_flags(ws))) return rc;
+  double t = t0;
+  for (int64_t it = 0; it < nsteps; ++it) {
+    if ((rc = enqueue_rk4(ws, du, dv, t, dt, stop_nonfinite))) return rc;
+    t += dt;
+  }
+  rc = collect(ws);
+  if (steps_done) *steps_done = ws->stats.steps_done;
+  if (finite) *finite = ws->stats.finite;
+  if (where == WEDG_HOST) {
+    CK(ws, cudaMemcpy(u, ws->d_u, bU, cudaMemcpyDeviceToHost));
+    CK(ws, cudaMemcpy(v, ws->d_v, bV, cudaMemcpyDeviceToHost));
+  }
+  return rc;
+}
+
+int wedg_rk4_step(wedg_ws *ws, double *u, double *v, double t, double dt, const int64_t u_shape[4],
+                  const int64_t v_shape[4], int where, int *finite) {
+  return wedg_rk4_steps(ws, u, v, t, dt, 1, u_shape, v_shape, where, 0, nullptr, finite);
+}
+
+int wedg_rk4_steps_async(wedg_ws *ws, double *u_dev, double *v_dev, double t0, double dt, int64_t nsteps) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  ws->stats.kernel_launches = 0;
+  int rc = reset_flags(ws);
+  if (rc) return rc;
+  double t = t0;
+  for (int64_t it = 0; it < nsteps; ++it) {
+    if ((rc = enqueue_rk4(ws, u_dev, v_dev, t, dt, 0))) return rc;
+    t += dt;
+  }
+  return WEDG_OK;
+}
+
+int wedg_sync_status(wedg_ws *ws, int64_t *steps_done, int *finite) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  int rc = collect(ws);
+  if (steps_done) *steps_done = ws->stats.steps_done;
+  if (finite) *finite = ws->stats.finite;
+  return rc;
+}
+
+int wedg_error_message(const wedg_ws *ws, char *buf, size_t len) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  if (buf && len) {
+    std::strncpy(buf, ws->message.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return ws->status;
+}
+
+int64_t wedg_error_key(const wedg_ws *ws) { return ws ? ws->key : 0; }
+
+int wedg_get_stats(const wedg_ws *ws, wedg_stats *out) {
+  if (!ws || !out) return WEDG_ERR_ARGUMENT;
+  *out = ws->stats;
+  return WEDG_OK;
+}
+
+void *wedg_get_stream(const wedg_ws *ws) { return ws ? (void *)ws->stream : nullptr; }
+
+int wedg_set_stream(wedg_ws *ws, void *stream) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  ws->stream = stream ? (cudaStream_t)stream : ws->own_stream;
+  return WEDG_OK;
+}
+
+int wedg_time_kernels(wedg_ws *ws, int enable) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  ws->timing = enable != 0;
+  return WEDG_OK;
+}
+
+int wedg_kernel_times(wedg_ws *ws, double *prep_ms, int64_t *prep_launches, double *stage_ms,
+                      int64_t *stage_launches, int reset) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  CK(ws, cudaStreamSynchronize(ws->stream));
+  drain_events(ws);
+  if (prep_ms) *prep_ms = ws->t_prep;
+  if (prep_launches) *prep_launches = ws->n_prep;
+  if (stage_ms) *stage_ms = ws->t_stage;
+  if (stage_launches) *stage_launches = ws->n_stage;
+  if (reset) { ws->t_prep = ws->t_stage = 0; ws->n_prep = ws->n_stage = 0; }
+  return WEDG_OK;
+}
+
+const char *wedg_status_string(int status) {
+  switch (status) {
+    case WEDG_OK: return "ok";
+    case WEDG_ERR_DIMENSION: return "dimension mismatch";
+    case WEDG_ERR_BOUNDARY_WEIGHT: return "boundary weight not positive";
+    case WEDG_ERR_MASS_NOT_PD: return "mass matrix not positive definite";
+    case WEDG_WARN_CG_NOT_CONVERGED: return "CG did not reach the tolerance";
+    case WEDG_ERR_TIMEOUT: return "device wait timed out";
+    case WEDG_ERR_CUDA: return "CUDA error";
+    case WEDG_ERR_ARGUMENT: return "invalid argument";
+    case WEDG_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char *wedg_version(void) { return "libwedg 0.1 (sm_103a, FP64)"; }
+
+}  // extern "C"

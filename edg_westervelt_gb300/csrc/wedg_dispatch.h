@@ -1,0 +1,90 @@
+// Dispatch of the size-templated kernels of libwedg. Each q_u = NU - 1 is
+// compiled in its own translation unit (wedg_qN.cu) so that the build runs in
+// parallel; this header is the interface between them and wedg_api.cu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "wedg_kernels.cuh"
+
+namespace wedg {
+
+constexpr int MAXN = 8;    // q_u ≤ 7
+constexpr int MAXQH = 12;  // q_high for q_v = 7
+
+// Runtime-sized copy of the 1D operators, packed into Basis<NU, NV> per launch.
+struct BasisHost {
+  int nu, nv, qh;
+  double w[MAXN], P[MAXN][MAXN], S[MAXN][MAXN];
+  double El[MAXN], Er[MAXN], E1l[MAXN], E1r[MAXN];
+  double Ph[MAXQH][MAXN], Wh[MAXQH][MAXQH];
+  double K1[MAXN][MAXN], Q[MAXN][MAXN], ilam2[MAXN][MAXN];
+};
+
+typedef void (*launch_fn)(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads,
+                          cudaStream_t st);
+typedef void (*pack_fn)(const BasisHost &h, void *out);
+
+struct Launchers {
+  launch_fn prep = nullptr, stage = nullptr;
+  pack_fn pack = nullptr;
+  size_t basis_size = 0;
+};
+
+template <int NU, int NV>
+void pack_basis(const BasisHost &h, void *out) {
+  Basis<NU, NV> &b = *static_cast<Basis<NU, NV> *>(out);
+  constexpr int NQ = NU, QH = Basis<NU, NV>::QH;
+  for (int i = 0; i < NQ; ++i) {
+    b.w[i] = h.w[i];
+    for (int d = 0; d < NU; ++d) { b.P[i][d] = h.P[i][d]; b.S[i][d] = h.S[i][d]; }
+  }
+  for (int d = 0; d < NU; ++d) {
+    b.El[d] = h.El[d]; b.Er[d] = h.Er[d]; b.E1l[d] = h.E1l[d]; b.E1r[d] = h.E1r[d];
+    for (int c = 0; c < NU; ++c) { b.K1[d][c] = h.K1[d][c]; b.Q[d][c] = h.Q[d][c]; b.ilam2[d][c] = h.ilam2[d][c]; }
+  }
+  for (int r = 0; r < QH; ++r) {
+    for (int d = 0; d < NV; ++d) b.Ph[r][d] = h.Ph[r][d];
+    for (int s = 0; s < QH; ++s) b.Wh[r][s] = h.Wh[r][s];
+  }
+}
+
+template <int NU, int NV>
+void launch_prep(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads, cudaStream_t st) {
+  k_prep<NU, NV><<<blocks, threads, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S);
+}
+
+// k_stage keeps the element blocks in dynamic shared memory (up to 227 KB per block);
+// `threads` must be stage_threads(NU, NV)
+template <int NU, int NV, bool FAST>
+void launch_stage(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads, cudaStream_t st) {
+  constexpr size_t smem = (size_t)stage_threads(NU, NV) * (2 * NU * NU + 2 * NV * NV) * sizeof(double);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_stage<NU, NV, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  if (blocks <= 0) return;
+  k_stage<NU, NV, FAST><<<blocks, threads, smem, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S);
+}
+
+template <int NU, int NV>
+Launchers make_launchers(bool fast) {
+  Launchers L;
+  L.prep = launch_prep<NU, NV>;
+  L.stage = fast ? launch_stage<NU, NV, true> : launch_stage<NU, NV, false>;
+  L.pack = pack_basis<NU, NV>;
+  L.basis_size = sizeof(Basis<NU, NV>);
+  return L;
+}
+
+// defined in wedg_q1.cu ... wedg_q7.cu (NU = q_u + 1)
+Launchers launchers_q1(int nv, bool fast);
+Launchers launchers_q2(int nv, bool fast);
+Launchers launchers_q3(int nv, bool fast);
+Launchers launchers_q4(int nv, bool fast);
+Launchers launchers_q5(int nv, bool fast);
+Launchers launchers_q6(int nv, bool fast);
+Launchers launchers_q7(int nv, bool fast);
+
+}  // namespace wedg

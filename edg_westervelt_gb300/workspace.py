@@ -1,0 +1,247 @@
+"""GPU ``Workspace``, ``edg_rhs!`` and ``rk4_step!`` behind the reference's API.
+
+Mirrors src/rhs.jl:166-220 (``Workspace``), :475-571 (``edg_rhs!``,
+``edg_rhs``) and src/solver.jl:278-339 (``rk4_step!``, ``rk4_step``) of
+WesterveltEDG.jl. The workspace holds a libwedg handle: the data of ``pre``
+are copied to the GPU once, and every call runs the sm_103a kernels.
+
+State arrays follow the reference's layout: numpy arrays of shape
+(N, N, q+1, q+1) in Fortran (column-major) order, like Julia's
+``Array{Float64,4}``, or CUDA tensors holding the same bytes (any
+contiguous torch tensor with N²(q+1)² doubles, read as that column-major array).
+"""
+import ctypes
+import warnings
+
+import numpy as np
+
+from . import _lib as L
+
+
+class ErrorException(RuntimeError):
+    """The reference's ErrorException (its own error messages, e.g. src/rhs.jl:114-115, 845, 916)."""
+
+
+class DimensionMismatch(ValueError):
+    """The reference's DimensionMismatch (src/rhs.jl:500-503)."""
+
+
+def _f64(a):
+    return np.require(a, dtype=np.float64, requirements=["F_CONTIGUOUS", "ALIGNED"])
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _is_device(x):
+    return hasattr(x, "is_cuda") and x.is_cuda
+
+
+def _dptr(x):
+    if x.dtype.__str__() != "torch.float64" or not x.is_contiguous():
+        raise TypeError("device state must be a contiguous torch.float64 CUDA tensor")
+    return ctypes.cast(ctypes.c_void_p(x.data_ptr()), ctypes.POINTER(ctypes.c_double))
+
+
+def _shape(x, nu, N):
+    """Julia shape of a state array (numpy: its shape; device: from the element count)."""
+    if _is_device(x):
+        n = x.numel()
+        q = int(round((n / (N * N)) ** 0.5)) if N > 0 else 0
+        shp = (N, N, q, q) if N * N * q * q == n else (n, 1, 1, 1)
+    else:
+        shp = tuple(x.shape) + (1,) * (4 - x.ndim) if x.ndim <= 4 else (x.size, 1, 1, 1)
+    return (ctypes.c_int64 * 4)(*shp)
+
+
+def _default_nblocks(pre, N):
+    """src/rhs.jl:139-142 (kept for the `nb` attribute; the GPU grid replaces the blocks)."""
+    import os
+    w = N * N * pre["qu1"] ** 2
+    nt = os.cpu_count() or 1
+    return 1 if w < 5000 else min(4, nt) if w < 20000 else nt
+
+
+class Workspace:
+    """GPU counterpart of ``Workspace(pre, N; nblocks)`` (src/rhs.jl:184-220).
+
+    Holds the device copy of ``pre`` and all scratch. ``nblocks`` is accepted
+    for compatibility (it must be ≥ 1, as in the reference) and only sets the
+    informational ``nb``: one GPU launch covers every element.
+
+    cheb_steps: "per_element" (default; every element takes the Chebyshev step
+    count its own spectral interval needs, each to the same tolerance) or
+    "common_max" (all elements take the largest count, as src/rhs.jl:911-918).
+    """
+
+    def __init__(self, pre, N, nblocks=None, cheb_steps="per_element", fast_path=True):
+        if nblocks is None:
+            nblocks = _default_nblocks(pre, N)
+        if not nblocks >= 1:
+            raise ErrorException(f"nblocks must be ≥ 1 (got {nblocks})")
+        E = N * N
+        self.nb = min(int(nblocks), max(1, E // 4))
+        self.pre = pre
+        self.N = N
+        self.nu, self.nv = pre["qu1"], pre["qv1"]
+        self._h = None
+        cfg = L.Config()
+        cfg.N, cfg.qu1, cfg.qv1, cfg.q_high = N, pre["qu1"], pre["qv1"], pre["q_high"]
+        cfg.theta, cfg.tau, cfg.lambda_u, cfg.lambda_v = pre["theta"], pre["tau"], pre["lambda_u"], pre["lambda_v"]
+        cfg.omega = pre["omega"]
+        cfg.mms_on, cfg.src_on, cfg.one_sided = int(pre["mms_on"]), int(pre["src_on"]), int(pre["one_sided"])
+        cfg.mass_solver = 0 if pre["mass_solver"] == "chebyshev" else 1
+        cfg.mass_tol = pre["mass_tol"]
+        cfg.src_omega, cfg.src_Ts = pre["source"].omega, pre["source"].Ts
+        for i, side in enumerate(("bot", "top", "lft", "rgt")):
+            bs = pre["bc"][side]
+            cfg.kind[i] = L.KINDS[bs["kind"]]
+            cfg.gamma_abc[i], cfg.eta_abc[i], cfg.sigma[i] = bs["gamma_abc"], bs["eta_abc"], bs["sigma"]
+            cfg.kb[i], cfg.kappa[i] = bs["kb"], bs["kappa"]
+        cfg.cheb_steps = {"per_element": 0, "common_max": 1}[cheb_steps]
+        cfg.general_only = 0 if fast_path else 1
+        self._cfg = cfg
+        keep = {}
+        p = L.Pre()
+        for name in L.PRE_FIELDS:
+            a = pre[name]
+            if name == "Ainv_u" and not a.flags.f_contiguous and fast_path:
+                setattr(p, name, ctypes.POINTER(ctypes.c_double)())   # NULL: shared inverse, fast path expected
+                continue
+            a = _f64(np.ascontiguousarray(a) if not a.flags.f_contiguous else a)
+            keep[name] = a
+            setattr(p, name, _ptr(a))
+        h = ctypes.c_void_p()
+        rc = L.lib().wedg_create(ctypes.byref(cfg), ctypes.byref(p), ctypes.byref(h))
+        if rc == L.WEDG_ERR_ARGUMENT and "Ainv_u" not in keep:
+            a = _f64(np.ascontiguousarray(pre["Ainv_u"]))      # the general path needs every inverse
+            keep["Ainv_u"] = a
+            p.Ainv_u = _ptr(a)
+            rc = L.lib().wedg_create(ctypes.byref(cfg), ctypes.byref(p), ctypes.byref(h))
+        if rc == L.WEDG_ERR_NO_DEVICE:
+            raise RuntimeError("libwedg: no CUDA device available")
+        if rc != L.WEDG_OK:
+            raise RuntimeError(f"wedg_create failed: {L.lib().wedg_status_string(rc).decode()}")
+        self._h = h
+        self.ut = np.zeros((N, N, self.nu, self.nu), order="F")
+        self.vt = np.zeros((N, N, self.nv, self.nv), order="F")
+        self.fin = True
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            L.lib().wedg_destroy(self._h)
+            self._h = None
+
+    # ---- status handling
+    def _message(self):
+        buf = ctypes.create_string_buffer(512)
+        L.lib().wedg_error_message(self._h, buf, 512)
+        return buf.value.decode("utf-8")
+
+    def _check(self, rc):
+        if rc == L.WEDG_OK:
+            return
+        if rc == L.WEDG_WARN_CG_NOT_CONVERGED:
+            warnings.warn(self._message())
+            return
+        msg = self._message()
+        if rc == L.WEDG_ERR_DIMENSION:
+            raise DimensionMismatch(msg)
+        if rc in (L.WEDG_ERR_BOUNDARY_WEIGHT, L.WEDG_ERR_MASS_NOT_PD, L.WEDG_ERR_ARGUMENT):
+            raise ErrorException(msg)
+        raise RuntimeError(f"libwedg: {L.lib().wedg_status_string(rc).decode()}: {msg}")
+
+    def stats(self):
+        s = L.Stats()
+        L.lib().wedg_get_stats(self._h, ctypes.byref(s))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    @property
+    def error_key(self):
+        return int(L.lib().wedg_error_key(self._h))
+
+    @property
+    def stream(self):
+        """The cudaStream_t the workspace launches on (an int)."""
+        return L.lib().wedg_get_stream(self._h)
+
+    def set_stream(self, stream_ptr):
+        L.lib().wedg_set_stream(self._h, ctypes.c_void_p(stream_ptr))
+
+    # ---- calls
+    def rhs(self, u, v, t, ut=None, vt=None):
+        """edg_rhs!: the right-hand side at time t into ut, vt (default the workspace's own)."""
+        N, nu, nv = self.N, self.nu, self.nv
+        if _is_device(u):
+            if ut is None or vt is None:
+                raise ValueError("device inputs need device outputs ut, vt")
+            rc = L.lib().wedg_rhs(self._h, _dptr(u), _dptr(v), float(t), _dptr(ut), _dptr(vt),
+                                  _shape(u, nu, N), _shape(v, nv, N), L.WEDG_DEVICE)
+            self._check(rc)
+            return ut, vt
+        u = _f64(u)
+        v = _f64(v)
+        ut = self.ut if ut is None else ut
+        vt = self.vt if vt is None else vt
+        rc = L.lib().wedg_rhs(self._h, _ptr(u), _ptr(v), float(t), _ptr(ut), _ptr(vt),
+                              _shape(u, nu, N), _shape(v, nv, N), L.WEDG_HOST)
+        self._check(rc)
+        return ut, vt
+
+    def rk4_steps(self, u, v, t0, dt, nsteps, stop_nonfinite=False):
+        """nsteps RK4 steps in place from t0 (t advancing by repeated addition of dt).
+        Returns the number of steps completed; sets self.fin."""
+        N = self.N
+        done = ctypes.c_int64(0)
+        fin = ctypes.c_int(1)
+        if _is_device(u):
+            pu, pv, where = _dptr(u), _dptr(v), L.WEDG_DEVICE
+        else:
+            if not (isinstance(u, np.ndarray) and u.dtype == np.float64 and u.flags.f_contiguous
+                    and isinstance(v, np.ndarray) and v.dtype == np.float64 and v.flags.f_contiguous):
+                raise TypeError("rk4_step! updates u, v in place: pass Fortran-ordered float64 arrays")
+            pu, pv, where = _ptr(u), _ptr(v), L.WEDG_HOST
+        rc = L.lib().wedg_rk4_steps(self._h, pu, pv, float(t0), float(dt), int(nsteps), _shape(u, self.nu, N),
+                                    _shape(v, self.nv, N), where, int(stop_nonfinite), ctypes.byref(done),
+                                    ctypes.byref(fin))
+        self.fin = bool(fin.value)
+        self._check(rc)
+        return int(done.value)
+
+
+def edg_rhs_(ws, u, v, t, N, h, pre):
+    """``edg_rhs!(ws, u, v, t, N, h, pre) -> (ws.ut, ws.vt)`` (src/rhs.jl:490-494); the
+    returned arrays are overwritten by the next call."""
+    if ws.pre is not pre and (N != ws.N or pre["qu1"] != ws.nu or pre["qv1"] != ws.nv):
+        raise DimensionMismatch(f"state, workspace and pre do not match (N = {N}, q_u + 1 = {pre['qu1']}, "
+                                f"q_v + 1 = {pre['qv1']})")
+    if N != ws.N:
+        raise DimensionMismatch(f"state, workspace and pre do not match (N = {N}, q_u + 1 = {ws.nu}, "
+                                f"q_v + 1 = {ws.nv})")
+    return ws.rhs(u, v, t)
+
+
+def edg_rhs(u, v, t, N, h, pre, nblocks=None):
+    """Allocating ``edg_rhs`` (src/rhs.jl:560-571): copies of the right-hand side."""
+    ws = Workspace(pre, N, nblocks=nblocks)
+    ut, vt = edg_rhs_(ws, u, v, t, N, h, pre)
+    return ut.copy(order="F"), vt.copy(order="F")
+
+
+def rk4_step_(u, v, t, dt, N, h, pre, ws):
+    """``rk4_step!(u, v, t, dt, N, h, pre, ws) -> (u, v)`` in place (src/solver.jl:289-297);
+    afterwards ``ws.fin`` tells whether all entries are finite."""
+    if N != ws.N:
+        raise DimensionMismatch(f"state, workspace and pre do not match (N = {N}, q_u + 1 = {ws.nu}, "
+                                f"q_v + 1 = {ws.nv})")
+    ws.rk4_steps(u, v, t, dt, 1)
+    return u, v
+
+
+def rk4_step(u, v, t, dt, N, h, pre, nblocks=None):
+    """Allocating ``rk4_step`` (src/solver.jl:331-339): u, v are not modified."""
+    ws = Workspace(pre, N, nblocks=nblocks)
+    u2 = np.array(u, dtype=np.float64, order="F", copy=True)
+    v2 = np.array(v, dtype=np.float64, order="F", copy=True)
+    return rk4_step_(u2, v2, t, dt, N, h, pre, ws)

@@ -1,0 +1,159 @@
+/*
+ * wedg.h -- C ABI of libwedg, the GB300 (sm_103a, FP64) right-hand side and
+ * RK4 step of the energy-based DG scheme of WesterveltEDG.jl (v0.3.0).
+ *
+ * The library is a drop-in for the reference's hot path: a GPU workspace
+ * replaces `Workspace(pre, N)` (src/rhs.jl:184), and the calls below replace
+ * `edg_rhs!` (src/rhs.jl:490-494), `rk4_step!` (src/solver.jl:289-297) and the
+ * step loop of `solve` (src/solver.jl:213-217). `pre` stays the reference's
+ * own host data (`precompute`, src/solver.jl:428-694): `wedg_create` reads its
+ * arrays through host pointers in the reference's (Julia, column-major)
+ * layouts and copies what the device needs.
+ *
+ * Conventions
+ *  - All arithmetic is FP64.
+ *  - Status codes mirror the reference's exceptions (wedg_status); the exact
+ *    message text of the reference is available from wedg_error_message.
+ *  - State arrays u (N,N,q_u+1,q_u+1) and v (N,N,q_v+1,q_v+1) use the
+ *    reference's state layout (column-major, element index j + N*k fastest).
+ *    `where` says whether the pointers are host (WEDG_HOST: the library
+ *    copies in and out) or device (WEDG_DEVICE) memory.
+ *  - Every call is synchronous, like the reference's, and one workspace must
+ *    not be used from two threads at once.
+ */
+#ifndef WEDG_H
+#define WEDG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum wedg_status {
+  WEDG_OK = 0,
+  WEDG_ERR_DIMENSION = 1,          /* DimensionMismatch, src/rhs.jl:500-503 */
+  WEDG_ERR_BOUNDARY_WEIGHT = 2,    /* 1 - kβv ≤ 0 at a face point, src/rhs.jl:112-116, 768-776 */
+  WEDG_ERR_MASS_NOT_PD = 3,        /* 1 - 2βv_h ≤ 0, src/rhs.jl:916 (Chebyshev), :845 (CG) */
+  WEDG_WARN_CG_NOT_CONVERGED = 4,  /* the @warn of src/rhs.jl:855-859; outputs are valid */
+  WEDG_ERR_TIMEOUT = 5,            /* a bounded device wait gave up */
+  WEDG_ERR_CUDA = 6,               /* CUDA runtime error */
+  WEDG_ERR_ARGUMENT = 7,           /* invalid argument (the reference's argument ErrorExceptions) */
+  WEDG_ERR_NO_DEVICE = 8           /* no usable GPU */
+};
+
+enum wedg_kind { WEDG_ABSORBING_2BETA = 0, WEDG_ABSORBING = 1, WEDG_DIRICHLET = 2, WEDG_WALL = 3 };
+enum wedg_where { WEDG_HOST = 0, WEDG_DEVICE = 1 };
+enum wedg_mass_solver { WEDG_CHEBYSHEV = 0, WEDG_CG = 1 };
+enum wedg_cheb_steps { WEDG_CHEB_PER_ELEMENT = 0, WEDG_CHEB_COMMON_MAX = 1 };
+
+/* Scalars of `pre` (src/solver.jl:665-689) and the per-side boundary table
+ * `pre.bc` (src/solver.jl:39-45), sides in the order bot, top, lft, rgt. */
+typedef struct wedg_config {
+  int32_t N, qu1, qv1, q_high;
+  double theta, tau, lambda_u, lambda_v; /* flux parameters, src/solver.jl:16-21 */
+  double omega;                          /* 2π √(kx² + ky²) */
+  int32_t mms_on, src_on, one_sided;     /* mode flags and the face kernel choice */
+  int32_t mass_solver;                   /* wedg_mass_solver */
+  double mass_tol;                       /* 1e-14 in the reference */
+  double src_omega, src_Ts;              /* GaussianSource ω and Ts of src_time (src/solver.jl:662) */
+  int32_t kind[4];                       /* wedg_kind per side */
+  double gamma_abc[4], eta_abc[4], sigma[4], kb[4], kappa[4];
+  int32_t cheb_steps;                    /* wedg_cheb_steps: per-element count (default) or the
+                                            reference's common maximum (src/rhs.jl:911-918) */
+  int32_t general_only;                  /* 1: never use the constant-coefficient kernels */
+} wedg_config;
+
+/* Host pointers to the arrays of `pre`, each in the reference's layout
+ * (src/solver.jl:462-536, 716-770). Ainv_u may be NULL when every element has
+ * constant c² and α (the library then uses the exact fast diagonalization of
+ * the pinned stiffness and never reads Ainv_u). */
+typedef struct wedg_pre {
+  const double *w, *P_u, *S_u, *Ebl_u, *Ebr_u, *E1bl_u, *E1br_u;
+  const double *P_h_v, *W2d_h;
+  const double *Cw, *Aw, *Ainv_u;
+  const double *hc2, *haf, *hcf, *hbf, *vc2, *vaf, *vcf, *vbf;
+  const double *hc2m, *hafm, *vc2m, *vafm, *hJC, *vJC;
+  const double *bcB_sp, *bcB_spy, *bcT_sp, *bcT_spy, *bcL_sp, *bcL_spx, *bcR_sp, *bcR_spx;
+  const double *PiSP, *PiBSP2, *PiCdiv, *PiDdiv, *src_projE;
+  const double *beta_hq;
+} wedg_pre;
+
+/* Per-call statistics of the last call. */
+typedef struct wedg_stats {
+  int32_t cheb_steps_max;      /* largest Chebyshev step count of the last evaluation */
+  int32_t cg_not_converged;    /* element systems above the CG tolerance (summed over stages) */
+  int32_t finite;              /* after an RK4 step: all entries of u and v finite (`all(ws.fin)`) */
+  int32_t fast_path;           /* 1 if the constant-coefficient kernels are in use */
+  int64_t steps_done;          /* RK4 steps completed by the last wedg_rk4_steps */
+  int64_t kernel_launches;     /* kernels launched by the last call */
+  int64_t device_bytes;        /* device memory held by the workspace */
+} wedg_stats;
+
+typedef struct wedg_ws wedg_ws;
+
+/* Workspace(pre, N) of src/rhs.jl:184-220: validates the configuration,
+ * copies pre to the device and allocates all scratch. Replaces the CPU
+ * workspace; there is no nblocks (the GPU grid replaces the element blocks). */
+int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out);
+void wedg_destroy(wedg_ws *ws);
+
+/* edg_rhs!(ws, u, v, t, N, h, pre) of src/rhs.jl:490-550: ut, vt receive the
+ * right-hand side. Shapes are checked as src/rhs.jl:500-503 does. */
+int wedg_rhs(wedg_ws *ws, const double *u, const double *v, double t, double *ut, double *vt,
+             const int64_t u_shape[4], const int64_t v_shape[4], int where);
+
+/* rk4_step!(u, v, t, dt, N, h, pre, ws) of src/solver.jl:289-321: u, v are
+ * updated in place; on an error they are left unchanged. `finite` receives
+ * all(ws.fin). */
+int wedg_rk4_step(wedg_ws *ws, double *u, double *v, double t, double dt, const int64_t u_shape[4],
+                  const int64_t v_shape[4], int where, int *finite);
+
+/* The step loop of solve (src/solver.jl:213-217): nsteps RK4 steps from t0,
+ * t advancing by repeated addition of dt. Stops at the first failing step
+ * (state left as before that step); `steps_done` receives the completed steps.
+ * With stop_nonfinite, it also stops after the first step whose result is not
+ * finite (the blow-up check of src/solver.jl:940); `finite` receives the flag
+ * of the last completed step. */
+int wedg_rk4_steps(wedg_ws *ws, double *u, double *v, double t0, double dt, int64_t nsteps,
+                   const int64_t u_shape[4], const int64_t v_shape[4], int where, int stop_nonfinite,
+                   int64_t *steps_done, int *finite);
+
+/* Message of the last error in the reference's words (src/rhs.jl:114-115,
+ * 845, 916; the DimensionMismatch text of :503). Returns the status. */
+int wedg_error_message(const wedg_ws *ws, char *buf, size_t len);
+
+/* Key of the last error: the boundary key of src/rhs.jl:732 for
+ * WEDG_ERR_BOUNDARY_WEIGHT, the 1-based element for WEDG_ERR_MASS_NOT_PD. */
+int64_t wedg_error_key(const wedg_ws *ws);
+
+int wedg_get_stats(const wedg_ws *ws, wedg_stats *out);
+
+/* Stream used by the workspace (a cudaStream_t). wedg_set_stream makes the
+ * workspace launch on the caller's stream (NULL: the library's own). */
+void *wedg_get_stream(const wedg_ws *ws);
+int wedg_set_stream(wedg_ws *ws, void *stream);
+
+/* Asynchronous form for device-resident runs: enqueue nsteps RK4 steps on
+ * the workspace stream without copies, synchronization or error checks;
+ * wedg_sync_status then waits and reports like wedg_rk4_steps. */
+int wedg_rk4_steps_async(wedg_ws *ws, double *u_dev, double *v_dev, double t0, double dt, int64_t nsteps);
+int wedg_sync_status(wedg_ws *ws, int64_t *steps_done, int *finite);
+
+/* Kernel timing for benchmarks: with enable != 0, every launch of the two stage
+ * kernels is bracketed by CUDA events on the workspace stream and its duration
+ * accumulated; wedg_kernel_times reads (and with reset, clears) the totals in
+ * milliseconds and the number of launches of each. */
+int wedg_time_kernels(wedg_ws *ws, int enable);
+int wedg_kernel_times(wedg_ws *ws, double *prep_ms, int64_t *prep_launches, double *stage_ms,
+                      int64_t *stage_launches, int reset);
+
+const char *wedg_status_string(int status);
+/* Library version and the GPU architecture it was built for. */
+const char *wedg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WEDG_H */

@@ -87,32 +87,28 @@ def side_values(bot, top, lft, rgt, f, xloc, yloc, N, h):
     sv = max(amax(VM[:, :, 1:]), amax(VP[:, :, :N])) if vt else 0.0
     s = JUMP_TOL * max(sh, sv)
 
-    def near(a, b):
-        return abs(a - b) <= JUMP_TOL * max(abs(a), abs(b)) + s
-
     def sides(f0, fm, fp):
-        if math.isfinite(f0) and near(fm, f0) and near(fp, f0):
-            return f0, f0
-        return fm, fp
+        # (f0, f0) where f0 is finite and both shifted values are near it, else (fm, fp)
+        with np.errstate(invalid="ignore"):
+            near_m = np.abs(fm - f0) <= JUMP_TOL * np.maximum(np.abs(fm), np.abs(f0)) + s
+            near_p = np.abs(fp - f0) <= JUMP_TOL * np.maximum(np.abs(fp), np.abs(f0)) + s
+        keep = np.isfinite(f0) & near_m & near_p
+        return np.where(keep, f0, fm), np.where(keep, f0, fp)
 
     if hz:
-        for k in range(N):
-            for jf in range(N + 1):
-                for i in range(nq):
-                    fm, fp = sides(H0[i, jf, k], HM[i, jf, k], HP[i, jf, k])
-                    if jf >= 1:
-                        top[jf - 1, k, i] = fm
-                    if jf <= N - 1:
-                        bot[jf, k, i] = fp
+        fm, fp = sides(H0, HM, HP)
+        for jf in range(N + 1):
+            if jf >= 1:
+                top[jf - 1, :, :] = fm[:, jf, :].T
+            if jf <= N - 1:
+                bot[jf, :, :] = fp[:, jf, :].T
     if vt:
+        fm, fp = sides(V0, VM, VP)
         for kf in range(N + 1):
-            for j in range(N):
-                for i in range(nq):
-                    fm, fp = sides(V0[i, j, kf], VM[i, j, kf], VP[i, j, kf])
-                    if kf >= 1:
-                        rgt[j, kf - 1, i] = fm
-                    if kf <= N - 1:
-                        lft[j, kf, i] = fp
+            if kf >= 1:
+                rgt[:, kf - 1, :] = fm[:, :, kf].T
+            if kf <= N - 1:
+                lft[:, kf, :] = fp[:, :, kf].T
 
 
 def precompute(q, N, mixed=True, flux="upwind", flux_params=None, sigma=0.0,
@@ -203,17 +199,20 @@ def precompute(q, N, mixed=True, flux="upwind", flux_params=None, sigma=0.0,
     for k in range(N):
         for j in range(N):
             e = j + k * N
-            cw_mat = cQ[j, k] ** 2 * W2d
-            aw_mat = aQ[j, k] * W2d
-            Cw[:, e, :] = cw_mat
-            Aw[:, e, :] = aw_mat
-            cw = cw_mat.reshape(-1, order="F")
-            Mj = Phi_xi_u.T @ (cw[:, None] * Phi_xi_u) + Phi_eta_u.T @ (cw[:, None] * Phi_eta_u)
-            Mj[0, 0] += 1.0
-            L = np.linalg.cholesky(Mj)
-            Li = np.linalg.inv(L)
-            Aj = Li.T @ Li
-            Ainv_u[tri_rows, e] = Aj[iu, ju]
+            Cw[:, e, :] = cQ[j, k] ** 2 * W2d
+            Aw[:, e, :] = aQ[j, k] * W2d
+    # M_e = Φ_ξ' diag(c²W) Φ_ξ + Φ_η' diag(c²W) Φ_η, (1,1) += 1; inverse via Cholesky, element by element
+    # (elements stacked in chunks for numpy)
+    for e0 in range(0, E, 1024):
+        es = range(e0, min(E, e0 + 1024))
+        cw = np.stack([Cw[:, e, :].reshape(-1, order="F") for e in es])
+        M = (np.einsum("pi,ep,pj->eij", Phi_xi_u, cw, Phi_xi_u, optimize=True)
+             + np.einsum("pi,ep,pj->eij", Phi_eta_u, cw, Phi_eta_u, optimize=True))
+        M[:, 0, 0] += 1.0
+        L = np.linalg.cholesky(M)
+        Li = np.linalg.inv(L)
+        Aj = np.einsum("eki,ekj->eij", Li, Li, optimize=True)
+        Ainv_u[np.ix_(tri_rows, np.arange(e0, e0 + len(es)))] = Aj[:, iu, ju].T
 
     # one-sided face values of c, alpha, beta (solver.jl:541-552)
     faces = {}

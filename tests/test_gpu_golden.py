@@ -1,0 +1,143 @@
+"""End-to-end runs on the GPU against the reference's stored results (tests/golden/).
+
+* regression pins of test/runtests.jl:207-217 (rtol 1e-9, the reference's own bar);
+* every row of data/convergence/results.csv (756 runs, q = 1..6, three fluxes,
+  both pairings, N = 5..25; the data were computed with mass_solver = :cg, which
+  the runs here use too; rtol 1e-9);
+* data/alpha_limit/order.csv: difference_norms of six initial-value runs
+  (q = 6, N = 20, T = 0.5, compactly supported bump of experiments/alpha_limit/run.jl);
+* data/steepening/{nl,lin,nl_dbc}: the source-mode runs of Section 5.3 (q = 4,
+  N = 64, T = 1.8, 18 432 RK4 steps): receivers, energy / max|v| / min(1-2βv)
+  series and the v_h snapshot at t = 0.8.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import edg_westervelt_gb300 as W
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _load(name):
+    return json.load(open(os.path.join(GOLD, name)))
+
+
+@pytest.mark.parametrize("solver", ["chebyshev", "cg"])
+def test_regression_pins(gpu, solver):
+    for case in _load("regression.json")["cases"]:
+        e = W.solve(case["q"], case["N"], case["T"], mass_solver=solver, **case["kw"])
+        for k in ("erru", "errv", "errgradu", "errE"):
+            assert abs(e[k] / case[k] - 1) < case["rtol"], (k, e[k], case[k])
+
+
+def test_convergence_data_all_rows(gpu):
+    data = _load("convergence.json")
+    worst = 0.0
+    for r in data["rows"]:
+        e = W.solve(r["q"], r["N"], data["T"], flux=r["flux"], mixed=r["mixed"], mass_solver="cg")
+        for k in ("erru", "errv", "errgradu", "errE"):
+            worst = max(worst, abs(e[k] / r[k] - 1))
+    assert len(data["rows"]) == 756
+    assert worst < 1e-9, worst
+
+
+def test_convergence_data_chebyshev(gpu):
+    """The default Chebyshev solver agrees with the :cg data to about 1e-11 (README of the
+    reference); checked on the q = 3 mixed upwind series, which includes the N = 10 case."""
+    data = _load("convergence.json")
+    rows = [r for r in data["rows"] if r["q"] == 3 and r["mixed"] and r["flux"] == "upwind"]
+    worst = 0.0
+    for r in rows:
+        e = W.solve(3, r["N"], data["T"], flux="upwind", mixed=True)
+        for k in ("erru", "errv", "errgradu", "errE"):
+            worst = max(worst, abs(e[k] / r[k] - 1))
+    assert worst < 1e-9, worst
+
+
+# the compactly supported bump of experiments/alpha_limit/run.jl: u0 = g(s), s = |x - x0|²/R²
+_X0, _R = (0.5, 0.5), 0.25
+
+
+def _s(x, y):
+    return ((x - _X0[0]) ** 2 + (y - _X0[1]) ** 2) / _R ** 2
+
+
+def _g(s):
+    return math.exp(1 - 1 / (1 - s)) if s < 1 else 0.0
+
+
+def _g1(s):
+    return -_g(s) / (1 - s) ** 2 if s < 1 else 0.0
+
+
+def _g2(s):
+    return _g(s) * (1 / (1 - s) ** 4 - 2 / (1 - s) ** 3) if s < 1 else 0.0
+
+
+BUMP = dict(u0=lambda x, y: _g(_s(x, y)),
+            u0_x=lambda x, y: _g1(_s(x, y)) * 2 * (x - _X0[0]) / _R ** 2,
+            u0_y=lambda x, y: _g1(_s(x, y)) * 2 * (y - _X0[1]) / _R ** 2,
+            u0_xx=lambda x, y: _g2(_s(x, y)) * (2 * (x - _X0[0]) / _R ** 2) ** 2 + _g1(_s(x, y)) * 2 / _R ** 2,
+            u0_yy=lambda x, y: _g2(_s(x, y)) * (2 * (y - _X0[1]) / _R ** 2) ** 2 + _g1(_s(x, y)) * 2 / _R ** 2)
+
+
+def test_alpha_limit(gpu):
+    data = _load("alpha_limit.json")
+
+    def run(a):
+        return W.solve(6, 20, 0.5, flux="upwind", mixed=True, mode="initial_value",
+                       coefficients=W.replace_coefficients(W.paper_coefficients(), alpha=a),
+                       initial_profile=BUMP, return_state=True)
+
+    ref = run(0.0)
+    worst = {}
+    for r in data["rows"]:
+        d = W.difference_norms(run(r["alpha"]), ref)
+        for k in ("erru", "errv", "errE"):
+            worst[(r["alpha"], k)] = abs(d[k] / r[k] - 1)
+    # the stored values have 11 significant digits; the differences of two runs lose
+    # log10(1/alpha)-ish digits to round-off of the runs themselves
+    for (a, k), x in worst.items():
+        assert x < max(1e-9, 1e-17 / a), (a, k, x)
+
+
+@pytest.mark.parametrize("case,beta,boundary", [("nl", 8.0, "absorbing_2beta"), ("lin", 0.0, "absorbing_2beta"),
+                                                ("nl_dbc", 8.0, "dirichlet")])
+def test_steepening(gpu, case, beta, boundary):
+    data = _load("steepening.json")
+    ref = data["cases"][case]
+    H = W.solve(4, 64, 1.8, flux="upwind", mixed=True, mode="source", boundary=boundary,
+                coefficients=W.constant_coefficients(c=1.0, alpha=1e-6, beta=beta),
+                source=W.GaussianSource(x0=(0.15, 0.5), r0=0.05, omega=16 * math.pi, Ts=1.0),
+                record_every=32, receivers=[(0.45, 0.5), (0.7, 0.5), (0.85, 0.5)], snap_times=[0.5, 0.8, 1.1])
+    assert len(H["recv_t"]) == ref["nsteps"] == 18432
+    rec = np.array(ref["recv"])
+    ours = np.column_stack([H["recv_t"], H["recv"]])[31::32]
+    assert np.max(np.abs(ours[:, 0] - rec[:, 0])) < 1e-12
+    scale = np.max(np.abs(rec[:, 1:]))
+    recv_err = np.max(np.abs(ours[:, 1:] - rec[:, 1:])) / scale
+    ser = np.array(ref["series"])
+    mine = np.column_stack([H["t"], H["energy"], H["vmax"], H["ndmin"]])
+    assert mine.shape == ser.shape
+    e_err = np.max(np.abs(mine[:, 1] - ser[:, 1]) / np.max(np.abs(ser[:, 1])))
+    v_err = np.max(np.abs(mine[:, 2] - ser[:, 2]) / np.max(np.abs(ser[:, 2])))
+    n_err = np.max(np.abs(mine[:, 3] - ser[:, 3]))
+    out = dict(case=case, recv_rel=recv_err, energy_rel=e_err, vmax_rel=v_err, ndmin_abs=n_err)
+    if case == "nl":
+        snap = dict(H["snaps"])
+        t08 = min(snap, key=lambda t: abs(t - 0.8))
+        G = snap[t08][::8, ::8]
+        S = np.array(data["snap_0.80"]["rows"])
+        out["snap_rel"] = float(np.max(np.abs(G - S)) / np.max(np.abs(S)))
+        assert np.allclose(H["grid_x"][::8], data["snap_0.80"]["grid"], rtol=0, atol=1e-15)
+    os.makedirs("gpurun_out", exist_ok=True)
+    with open(os.path.join("gpurun_out", f"steepening_{case}.json"), "w") as f:
+        json.dump(out, f)
+    tol = 1e-8
+    assert recv_err < tol and e_err < tol and v_err < tol and n_err < tol, out
+    assert out.get("snap_rel", 0.0) < tol, out
