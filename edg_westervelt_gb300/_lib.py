@@ -50,7 +50,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("cheb_steps_max", ctypes.c_int32), ("cg_not_converged", ctypes.c_int32),
                 ("finite", ctypes.c_int32), ("fast_path", ctypes.c_int32),
                 ("steps_done", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
-                ("device_bytes", ctypes.c_int64)]
+                ("device_bytes", ctypes.c_int64), ("cheb_steps_sum", ctypes.c_int64),
+                ("element_stages", ctypes.c_int64)]
 
 
 _lib = None

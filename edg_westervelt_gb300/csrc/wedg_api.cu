@@ -249,6 +249,8 @@ int reset_flags(wedg_ws *ws) {
   CK(ws, cudaMemsetAsync(ws->F.cg_nfail, 0, sizeof(unsigned int), ws->stream));
   CK(ws, cudaMemsetAsync(ws->F.nonfinite, 0, sizeof(unsigned int), ws->stream));
   CK(ws, cudaMemsetAsync(ws->F.nmax, 0, sizeof(int), ws->stream));
+  CK(ws, cudaMemsetAsync(ws->F.nsum, 0, sizeof(unsigned long long), ws->stream));
+  ws->stats.element_stages = 0;
   CK(ws, cudaMemsetAsync(ws->steps_done, 0, sizeof(long long), ws->stream));
   return WEDG_OK;
 }
@@ -294,6 +296,7 @@ int enqueue_stage(wedg_ws *ws, const StageIO &S) {
     ws->ev_pending.push_back({e0, e1, e2});
   }
   ws->stats.kernel_launches += 2;
+  ws->stats.element_stages += ws->E;
   CK(ws, cudaGetLastError());
   return WEDG_OK;
 }
@@ -342,8 +345,11 @@ int collect(wedg_ws *ws) {
   unsigned int cgf, nonf;
   int nmax;
   long long done;
+  unsigned long long nsum;
   CK(ws, cudaStreamSynchronize(ws->stream));
   drain_events(ws);
+  CK(ws, cudaMemcpy(&nsum, ws->F.nsum, sizeof nsum, cudaMemcpyDeviceToHost));
+  ws->stats.cheb_steps_sum = (int64_t)nsum;
   CK(ws, cudaMemcpy(&err, ws->F.err, sizeof err, cudaMemcpyDeviceToHost));
   CK(ws, cudaMemcpy(&cgf, ws->F.cg_nfail, sizeof cgf, cudaMemcpyDeviceToHost));
   CK(ws, cudaMemcpy(&nonf, ws->F.nonfinite, sizeof nonf, cudaMemcpyDeviceToHost));
@@ -596,7 +602,8 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
   const size_t nU = (size_t)nu * nu * E, nV = (size_t)nv * nv * E;
   if ((rc = dalloc(ws, &F.tr, (size_t)12 * nq * E)) || (rc = dalloc(ws, &F.G, (size_t)qh * qh * E)) ||
       (rc = dalloc(ws, &F.th, Es)) || (rc = dalloc(ws, &F.de, Es)) || (rc = dalloc(ws, &F.nst, Es)) ||
-      (rc = dalloc(ws, &F.nmax, 1)) || (rc = dalloc(ws, &F.err, 1)) || (rc = dalloc(ws, &F.cg_nfail, 1)) ||
+      (rc = dalloc(ws, &F.nmax, 1)) || (rc = dalloc(ws, &F.nsum, 1)) || (rc = dalloc(ws, &F.err, 1)) ||
+      (rc = dalloc(ws, &F.cg_nfail, 1)) ||
       (rc = dalloc(ws, &F.nonfinite, 1)) || (rc = dalloc(ws, &ws->steps_done, 1)) ||
       (rc = dalloc(ws, &ws->d_u, nU)) || (rc = dalloc(ws, &ws->d_v, nV)) || (rc = dalloc(ws, &ws->d_ut, nU)) ||
       (rc = dalloc(ws, &ws->d_vt, nV)) || (rc = dalloc(ws, &ws->su, nU)) || (rc = dalloc(ws, &ws->sv, nV)) ||

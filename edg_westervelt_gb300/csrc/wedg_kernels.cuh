@@ -78,6 +78,7 @@ struct Fields {
   const double *beta;
   double *tr, *G, *th, *de;
   int *nst, *nmax;
+  unsigned long long *nsum;   // Σ of the per-element Chebyshev step counts
   unsigned long long *err;
   unsigned int *cg_nfail, *nonfinite;
   double theta, tau, lu, lv, omega, two_h, four_hh, mass_tol, Lcheb;
@@ -242,10 +243,14 @@ __global__ void __launch_bounds__(128) k_prep(const __grid_constant__ Basis<NU, 
   F.de[e] = de;
   const int n = (int)ceil(F.Lcheb / acosh(th / de));
   F.nst[e] = n;
-  // largest count: one atomic per warp
+  // largest count and the sum of the counts: one atomic each per warp
   const unsigned mask = __activemask();
   const int nw = __reduce_max_sync(mask, n);
-  if ((threadIdx.x & 31) == __ffs(mask) - 1) atomicMax(F.nmax, nw);
+  const unsigned ns = __reduce_add_sync(mask, (unsigned)n);
+  if ((threadIdx.x & 31) == __ffs(mask) - 1) {
+    atomicMax(F.nmax, nw);
+    atomicAdd(F.nsum, (unsigned long long)ns);
+  }
 }
 
 // ----------------------------------------------------------------------------

@@ -89,6 +89,8 @@ typedef struct wedg_stats {
   int64_t steps_done;          /* RK4 steps completed by the last wedg_rk4_steps */
   int64_t kernel_launches;     /* kernels launched by the last call */
   int64_t device_bytes;        /* device memory held by the workspace */
+  int64_t cheb_steps_sum;      /* Σ over elements and stages of the Chebyshev step counts */
+  int64_t element_stages;      /* elements × stages evaluated by the last call */
 } wedg_stats;
 
 typedef struct wedg_ws wedg_ws;

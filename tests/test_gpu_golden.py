@@ -35,15 +35,21 @@ def test_regression_pins(gpu, solver):
             assert abs(e[k] / case[k] - 1) < case["rtol"], (k, e[k], case[k])
 
 
+def _rows_close(e, r):
+    # relative 1e-9, plus an absolute floor for the error norms that reach round-off level
+    # (q ≥ 4 on fine meshes, e.g. erru = 3.5e-11 at q = 5, N = 25): there the stored values
+    # themselves differ from any re-run by the round-off of the run, about 1e-16 absolute
+    return max(abs(e[k] - r[k]) / (1e-9 * abs(r[k]) + 1e-14) for k in ("erru", "errv", "errgradu", "errE"))
+
+
 def test_convergence_data_all_rows(gpu):
     data = _load("convergence.json")
+    assert len(data["rows"]) == 756
     worst = 0.0
     for r in data["rows"]:
         e = W.solve(r["q"], r["N"], data["T"], flux=r["flux"], mixed=r["mixed"], mass_solver="cg")
-        for k in ("erru", "errv", "errgradu", "errE"):
-            worst = max(worst, abs(e[k] / r[k] - 1))
-    assert len(data["rows"]) == 756
-    assert worst < 1e-9, worst
+        worst = max(worst, _rows_close(e, r))
+    assert worst < 1.0, worst
 
 
 def test_convergence_data_chebyshev(gpu):
