@@ -87,6 +87,8 @@ def lib():
     L.wedg_status_string.argtypes = [ctypes.c_int]
     L.wedg_status_string.restype = ctypes.c_char_p
     L.wedg_version.restype = ctypes.c_char_p
+    L.wedg_time_kernels.argtypes = [vp, ctypes.c_int]
+    L.wedg_kernel_times.argtypes = [vp, _D, _I64, _D, _I64, _D, _I64, ctypes.c_int]
     _lib = L
     return L
 

@@ -80,13 +80,14 @@ struct wedg_ws {
   double *d_u = nullptr, *d_v = nullptr, *d_ut = nullptr, *d_vt = nullptr;
   double *su = nullptr, *sv = nullptr, *accu = nullptr, *accv = nullptr;
   long long *steps_done = nullptr;
+  int parity = 0;   // bin-count buffer of the next stage
   // optional per-launch timing (events recorded around each stage kernel)
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
-  struct EvTriple { cudaEvent_t a, b, c; };   // prep runs from a to b, stage from b to c
-  std::vector<EvTriple> ev_pending;
-  double t_prep = 0, t_stage = 0;
-  int64_t n_prep = 0, n_stage = 0;
+  struct EvQuad { cudaEvent_t a, b, c, d; };   // prep runs from a to b, stage from b to c, mass from c to d
+  std::vector<EvQuad> ev_pending;
+  double t_prep = 0, t_stage = 0, t_mass = 0;
+  int64_t n_prep = 0, n_stage = 0, n_mass = 0;
   // last call
   int status = WEDG_OK;
   int64_t key = 0;
@@ -250,6 +251,8 @@ int reset_flags(wedg_ws *ws) {
   CK(ws, cudaMemsetAsync(ws->F.nonfinite, 0, sizeof(unsigned int), ws->stream));
   CK(ws, cudaMemsetAsync(ws->F.nmax, 0, sizeof(int), ws->stream));
   CK(ws, cudaMemsetAsync(ws->F.nsum, 0, sizeof(unsigned long long), ws->stream));
+  CK(ws, cudaMemsetAsync(ws->F.bin_count, 0, 2 * NBIN * sizeof(int), ws->stream));
+  ws->parity = 0;
   ws->stats.element_stages = 0;
   CK(ws, cudaMemsetAsync(ws->steps_done, 0, sizeof(long long), ws->stream));
   return WEDG_OK;
@@ -272,9 +275,11 @@ void drain_events(wedg_ws *ws) {
     float ms = 0;
     if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) { ws->t_prep += ms; ws->n_prep += 1; }
     if (cudaEventElapsedTime(&ms, p.b, p.c) == cudaSuccess) { ws->t_stage += ms; ws->n_stage += 1; }
+    if (cudaEventElapsedTime(&ms, p.c, p.d) == cudaSuccess) { ws->t_mass += ms; ws->n_mass += 1; }
     ws->ev_pool.push_back(p.a);
     ws->ev_pool.push_back(p.b);
     ws->ev_pool.push_back(p.c);
+    ws->ev_pool.push_back(p.d);
   }
   ws->ev_pending.clear();
 }
@@ -283,19 +288,25 @@ void drain_events(wedg_ws *ws) {
 int enqueue_stage(wedg_ws *ws, const StageIO &S) {
   const int tp = 128, bp = (ws->E + tp - 1) / tp;
   const int ts = stage_threads(ws->nu, ws->nv), bs = (ws->E + ts - 1) / ts;
-  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  const int bm = (ws->E + MASS_THREADS - 1) / MASS_THREADS;
+  StageIO Sp = S;
+  Sp.parity = ws->parity;
+  ws->parity = 1 - ws->parity;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
   if (ws->timing) {
-    e0 = take_event(ws); e1 = take_event(ws); e2 = take_event(ws);
+    e0 = take_event(ws); e1 = take_event(ws); e2 = take_event(ws); e3 = take_event(ws);
     cudaEventRecord(e0, ws->stream);
   }
-  ws->L.prep(ws->basis.data(), ws->F, S, bp, tp, ws->stream);
+  ws->L.prep(ws->basis.data(), ws->F, Sp, bp, tp, ws->stream);
   if (ws->timing) cudaEventRecord(e1, ws->stream);
-  ws->L.stage(ws->basis.data(), ws->F, S, bs, ts, ws->stream);
+  ws->L.stage(ws->basis.data(), ws->F, Sp, bs, ts, ws->stream);
+  if (ws->timing) cudaEventRecord(e2, ws->stream);
+  ws->L.mass(ws->basis.data(), ws->F, Sp, bm, MASS_THREADS, ws->stream);
   if (ws->timing) {
-    cudaEventRecord(e2, ws->stream);
-    ws->ev_pending.push_back({e0, e1, e2});
+    cudaEventRecord(e3, ws->stream);
+    ws->ev_pending.push_back({e0, e1, e2, e3});
   }
-  ws->stats.kernel_launches += 2;
+  ws->stats.kernel_launches += 3;
   ws->stats.element_stages += ws->E;
   CK(ws, cudaGetLastError());
   return WEDG_OK;
@@ -607,7 +618,8 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
       (rc = dalloc(ws, &F.nonfinite, 1)) || (rc = dalloc(ws, &ws->steps_done, 1)) ||
       (rc = dalloc(ws, &ws->d_u, nU)) || (rc = dalloc(ws, &ws->d_v, nV)) || (rc = dalloc(ws, &ws->d_ut, nU)) ||
       (rc = dalloc(ws, &ws->d_vt, nV)) || (rc = dalloc(ws, &ws->su, nU)) || (rc = dalloc(ws, &ws->sv, nV)) ||
-      (rc = dalloc(ws, &ws->accu, nU)) || (rc = dalloc(ws, &ws->accv, nV))) {
+      (rc = dalloc(ws, &ws->accu, nU)) || (rc = dalloc(ws, &ws->accv, nV)) || (rc = dalloc(ws, &F.mrhs, nV)) ||
+      (rc = dalloc(ws, &F.bins, (size_t)NBIN * E)) || (rc = dalloc(ws, &F.bin_count, (size_t)2 * NBIN))) {
     wedg_destroy(ws);
     return rc;
   }
@@ -623,13 +635,16 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
   F.src_on = cfg->src_on ? 1 : 0;
   F.cg = cfg->mass_solver == WEDG_CG;
   F.cheb_common = cfg->cheb_steps == WEDG_CHEB_COMMON_MAX;
+  F.sorted = !F.cg && !F.cheb_common;
   for (int s = 0; s < 4; ++s) {
     F.kind[s] = cfg->kind[s];
     F.gam[s] = cfg->gamma_abc[s]; F.eta[s] = cfg->eta_abc[s]; F.sig[s] = cfg->sigma[s];
     F.kb[s] = cfg->kb[s]; F.kap[s] = cfg->kappa[s];
   }
-  // sets the shared-memory attribute of k_stage (a launch of zero blocks does nothing else)
+  // sets the shared-memory attributes of k_stage and k_mass (a launch of zero blocks does nothing else)
   ws->L.stage(ws->basis.data(), F, StageIO{}, 0, 0, nullptr);
+  ws->L.mass(ws->basis.data(), F, StageIO{}, 0, 0, nullptr);
+  cudaMemset(F.bin_count, 0, 2 * NBIN * sizeof(int));
   cudaError_t ce = cudaStreamCreateWithFlags(&ws->own_stream, cudaStreamNonBlocking);
   if (ce != cudaSuccess) {
     int r = cuda_fail(ws, ce, "cudaStreamCreate");
@@ -775,7 +790,7 @@ int wedg_time_kernels(wedg_ws *ws, int enable) {
 }
 
 int wedg_kernel_times(wedg_ws *ws, double *prep_ms, int64_t *prep_launches, double *stage_ms,
-                      int64_t *stage_launches, int reset) {
+                      int64_t *stage_launches, double *mass_ms, int64_t *mass_launches, int reset) {
   if (!ws) return WEDG_ERR_ARGUMENT;
   CK(ws, cudaStreamSynchronize(ws->stream));
   drain_events(ws);
@@ -783,7 +798,9 @@ int wedg_kernel_times(wedg_ws *ws, double *prep_ms, int64_t *prep_launches, doub
   if (prep_launches) *prep_launches = ws->n_prep;
   if (stage_ms) *stage_ms = ws->t_stage;
   if (stage_launches) *stage_launches = ws->n_stage;
-  if (reset) { ws->t_prep = ws->t_stage = 0; ws->n_prep = ws->n_stage = 0; }
+  if (mass_ms) *mass_ms = ws->t_mass;
+  if (mass_launches) *mass_launches = ws->n_mass;
+  if (reset) { ws->t_prep = ws->t_stage = ws->t_mass = 0; ws->n_prep = ws->n_stage = ws->n_mass = 0; }
   return WEDG_OK;
 }
 

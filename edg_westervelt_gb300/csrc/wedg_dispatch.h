@@ -26,7 +26,7 @@ typedef void (*launch_fn)(const void *basis, const Fields &F, const StageIO &S, 
 typedef void (*pack_fn)(const BasisHost &h, void *out);
 
 struct Launchers {
-  launch_fn prep = nullptr, stage = nullptr;
+  launch_fn prep = nullptr, stage = nullptr, mass = nullptr;
   pack_fn pack = nullptr;
   size_t basis_size = 0;
 };
@@ -68,10 +68,26 @@ void launch_stage(const void *basis, const Fields &F, const StageIO &S, int bloc
   k_stage<NU, NV, FAST><<<blocks, threads, smem, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S);
 }
 
+// k_mass: dynamic shared memory for r and X (Chebyshev) or r, X and A p (CG); `threads` is MASS_THREADS
+template <int NU, int NV>
+void launch_mass(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_mass<NU, NV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mass_smem(NV, false));
+    cudaFuncSetAttribute(k_mass<NU, NV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mass_smem(NV, true));
+    attr = true;
+  }
+  if (blocks <= 0) return;
+  const Basis<NU, NV> &B = *static_cast<const Basis<NU, NV> *>(basis);
+  if (F.cg) k_mass<NU, NV, true><<<blocks, threads, mass_smem(NV, true), st>>>(B, F, S);
+  else k_mass<NU, NV, false><<<blocks, threads, mass_smem(NV, false), st>>>(B, F, S);
+}
+
 template <int NU, int NV>
 Launchers make_launchers(bool fast) {
   Launchers L;
   L.prep = launch_prep<NU, NV>;
+  L.mass = launch_mass<NU, NV>;
   L.stage = fast ? launch_stage<NU, NV, true> : launch_stage<NU, NV, false>;
   L.pack = pack_basis<NU, NV>;
   L.basis_size = sizeof(Basis<NU, NV>);

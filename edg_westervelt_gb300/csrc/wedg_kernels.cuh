@@ -10,7 +10,7 @@
 // registers. Memory is spent freely where it saves arithmetic: traces and
 // Chebyshev weights are computed once per stage and re-read.
 //
-// One RHS evaluation is two kernels:
+// One RHS evaluation is three kernels:
 //   k_prep   traces of the stage state on the four sides of every element
 //            (src/rhs.jl:384-410), the weight check of the boundary points
 //            (src/rhs.jl:105-110, 729-757) and the Chebyshev interval data
@@ -18,9 +18,13 @@
 //            before the second kernel starts;
 //   k_stage  face fluxes of the element's own sides (src/rhs.jl:611-700,
 //            65-103), lifts (:412-473), volume terms (:309-333), source
-//            (:335-350), u-equation (:352-382), the mass solve (Chebyshev
-//            :920-939 or CG :821-853) and the RK4 stage update
-//            (src/solver.jl:299-321).
+//            (:335-350) and u-equation (:352-382) with the u part of the RK4
+//            stage update (src/solver.jl:299-321); it leaves the right-hand
+//            side of the mass system in HBM;
+//   k_mass   the mass solve (Chebyshev :920-939 or CG :821-853) and the v part
+//            of the RK4 update. Elements are visited in the order of their
+//            Chebyshev step counts (k_prep lists them by count), so the lanes
+//            of a warp run the same number of steps.
 // Interior faces are evaluated by both neighbours, each writing only its own
 // slots, so no element writes another element's data.
 //
@@ -34,6 +38,7 @@
 //   bnd data    [m + N i]
 //   Pi, srcP    [(a + NV b) E + e]
 //   beta, G     [(r + QH s) E + e]
+//   mass rhs    [(a + NV b) E + e]
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -42,6 +47,8 @@ namespace wedg {
 
 constexpr unsigned long long ERR_NONE = ~0ull;
 constexpr int ERR_CLASS_SHIFT = 56;   // class 0: boundary weight, 1: mass matrix not PD, 3: stopped (non-finite)
+constexpr int NBIN = 48;              // Chebyshev-count bins of the mass kernel (the last holds n ≥ NBIN)
+constexpr int MASS_THREADS = 64;
 
 __host__ __device__ constexpr int qhigh(int nu, int nv) {
   // q_high = max(ceil(3 q_v / 2) + 1, q_u + 1), src/solver.jl:483
@@ -77,12 +84,14 @@ struct Fields {
   const double *PiSP, *PiBSP2, *PiCdiv, *PiDdiv, *srcP;
   const double *beta;
   double *tr, *G, *th, *de;
+  double *mrhs;               // right-hand side of the mass system, [(a + NV b) E + e]
   int *nst, *nmax;
+  int *bins, *bin_count;      // elements by Chebyshev count: bins[b E + i], two count buffers of NBIN
   unsigned long long *nsum;   // Σ of the per-element Chebyshev step counts
   unsigned long long *err;
   unsigned int *cg_nfail, *nonfinite;
   double theta, tau, lu, lv, omega, two_h, four_hh, mass_tol, Lcheb;
-  int one_sided, mms_on, src_on, cg, cheb_common;
+  int one_sided, mms_on, src_on, cg, cheb_common, sorted;
   int kind[4];
   double gam[4], eta[4], sig[4], kb[4], kap[4];
 };
@@ -94,6 +103,7 @@ struct StageIO {
   double ct, st, srct;       // time factors of the stage (src/rhs.jl:509-511)
   double cSP, cB, cC, cD;    // source weights: -ω²ct, -2ω³ st ct, 1 - ct, ω st
   int mode, first;
+  int parity;                // which bin-count buffer this stage fills (the other is cleared)
   double *ut, *vt;           // OUT_RHS
   const double *u0, *v0;     // RK4 base state
   double *su, *sv;           // next stage state
@@ -171,6 +181,7 @@ __global__ void __launch_bounds__(128) k_prep(const __grid_constant__ Basis<NU, 
   if (e >= E) return;
   if (err_word(F) != ERR_NONE) return;
   const int j = e % N, k = e / N;
+  if (e < NBIN && F.sorted) F.bin_count[(1 - S.parity) * NBIN + e] = 0;   // for the next stage
   {
     double U[NU][NU];
     load_regs<NU>(U, S.xu, E, e);
@@ -247,9 +258,21 @@ __global__ void __launch_bounds__(128) k_prep(const __grid_constant__ Basis<NU, 
   const unsigned mask = __activemask();
   const int nw = __reduce_max_sync(mask, n);
   const unsigned ns = __reduce_add_sync(mask, (unsigned)n);
-  if ((threadIdx.x & 31) == __ffs(mask) - 1) {
+  const int lane = threadIdx.x & 31;
+  if (lane == __ffs(mask) - 1) {
     atomicMax(F.nmax, nw);
     atomicAdd(F.nsum, (unsigned long long)ns);
+  }
+  if (F.sorted) {
+    // append e to the list of its count, one atomic per group of lanes with the same count
+    const int bin = (n < NBIN ? n : NBIN) - 1;
+    const unsigned same = __match_any_sync(mask, bin);
+    const int leader = __ffs(same) - 1;
+    const int rank = __popc(same & ((1u << lane) - 1));
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&F.bin_count[S.parity * NBIN + bin], __popc(same));
+    base = __shfl_sync(same, base, leader);
+    F.bins[(size_t)bin * E + base + rank] = e;
   }
 }
 
@@ -351,55 +374,14 @@ __device__ __forceinline__ void side_point(const Basis<NU, NV> &B, const Fields 
   }
 }
 
-// Kd = P_h^T (G ∘ (P_h d P_h^T)) P_h for one element (K of src/rhs.jl:783)
-template <int NU, int NV, int BT>
-__device__ __forceinline__ void apply_K(const Basis<NU, NV> &B, const double *G, int E, int e, Blk<NV, BT> d,
-                                        Blk<NV, BT> Kd) {
-  constexpr int QH = Basis<NU, NV>::QH;
-#pragma unroll 1
-  for (int a = 0; a < NV; ++a)
-#pragma unroll
-    for (int b = 0; b < NV; ++b) Kd(a, b) = 0.0;
-#pragma unroll 1
-  for (int r = 0; r < QH; ++r) {
-    double T[NV];
-#pragma unroll
-    for (int b = 0; b < NV; ++b) T[b] = 0.0;
-#pragma unroll 1
-    for (int a = 0; a < NV; ++a) {
-      const double p = B.Ph[r][a];
-#pragma unroll
-      for (int b = 0; b < NV; ++b) T[b] = fma(p, d(a, b), T[b]);
-    }
-    double Z[NV];
-#pragma unroll
-    for (int b = 0; b < NV; ++b) Z[b] = 0.0;
-#pragma unroll 2
-    for (int s2 = 0; s2 < QH; ++s2) {
-      double y = 0;
-#pragma unroll
-      for (int b = 0; b < NV; ++b) y = fma(T[b], B.Ph[s2][b], y);
-      y *= G[(r + QH * s2) * (size_t)E + e];
-#pragma unroll
-      for (int b = 0; b < NV; ++b) Z[b] = fma(y, B.Ph[s2][b], Z[b]);
-    }
-#pragma unroll 1
-    for (int a = 0; a < NV; ++a) {
-      const double p = B.Ph[r][a];
-#pragma unroll
-      for (int b = 0; b < NV; ++b) Kd(a, b) = fma(p, Z[b], Kd(a, b));
-    }
-  }
-}
-
 // ----------------------------------------------------------------------------
-// k_stage: fluxes, lifts, volume, source, u-equation, mass solve, RK4 update
+// k_stage: fluxes, lifts, volume, source, u-equation; the mass right-hand side to HBM
 // ----------------------------------------------------------------------------
 template <int NU, int NV, bool FAST>
 __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
     k_stage(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
             const __grid_constant__ StageIO S) {
-  constexpr int NQ = NU, QH = Basis<NU, NV>::QH, BT = stage_threads(NU, NV);
+  constexpr int NQ = NU, BT = stage_threads(NU, NV);
   extern __shared__ double smem[];
   const int tid = threadIdx.x;
   const int E = F.E, N = F.N;
@@ -408,7 +390,6 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
   if (err_word(F) != ERR_NONE) return;
   const int j = e % N, k = e / N;
   const double two_h = F.two_h, four_hh = F.four_hh;
-  (void)QH;
   // thread-private blocks: X1, X2 (NU²), Y1, Y2 (NV²)
   Blk<NU, BT> X1{smem + tid}, X2{smem + NU * NU * BT + tid};
   Blk<NV, BT> Y1{smem + 2 * NU * NU * BT + tid}, Y2{smem + (2 * NU * NU + NV * NV) * BT + tid};
@@ -496,36 +477,51 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
     // 1D stiffness K1 = S^T diag(w) S and the orthonormality of the basis
     //   (c²∇φ_v, ∇u_h) = c² (K1 U + U K1)[v-block],  (α∇φ_v, ∇v_h) = α (K1 V + V K1)
     //   (c²∇φ_u, ∇v_h) = c² (K1[:, v] V + V K1[v, :])
-    // (row and column 0 of K1 vanish: the derivative of the constant mode is 0)
+    // (row and column 0 of K1 vanish: the derivative of the constant mode is 0).
+    // Each output row is built at once, so the FMAs of a row are independent.
     const double c2 = F.c2e[e], al = F.ae[e];
     const double mc2 = -four_hh * c2, mal = -four_hh * al;
 #pragma unroll 1
     for (int a = 0; a < NV; ++a) {
+      double su[NV], sv[NV];
 #pragma unroll
-      for (int b = 0; b < NV; ++b) {
-        double su = 0, sv = 0;
+      for (int b = 0; b < NV; ++b) { su[b] = 0.0; sv[b] = 0.0; }
 #pragma unroll
-        for (int c = 1; c < NU; ++c) su = fma(B.K1[a][c], Ub(c, b), fma(Ub(a, c), B.K1[c][b], su));
+      for (int c = 1; c < NU; ++c) {
+        const double kac = B.K1[a][c], uac = Ub(a, c);
 #pragma unroll
-        for (int c = 1; c < NV; ++c) sv = fma(B.K1[a][c], Vb(c, b), fma(Vb(a, c), B.K1[c][b], sv));
-        Rv(a, b) = fma(mc2, su, fma(mal, sv, Rv(a, b)));
+        for (int b = 0; b < NV; ++b) su[b] = fma(kac, Ub(c, b), fma(uac, B.K1[c][b], su[b]));
       }
+#pragma unroll
+      for (int c = 1; c < NV; ++c) {
+        const double kac = B.K1[a][c], vac = Vb(a, c);
+#pragma unroll
+        for (int b = 0; b < NV; ++b) sv[b] = fma(kac, Vb(c, b), fma(vac, B.K1[c][b], sv[b]));
+      }
+#pragma unroll
+      for (int b = 0; b < NV; ++b) Rv(a, b) = fma(mc2, su[b], fma(mal, sv[b], Rv(a, b)));
     }
 #pragma unroll 1
     for (int a = 0; a < NU; ++a) {
+      double s1[NU];
 #pragma unroll
-      for (int b = 0; b < NU; ++b) {
-        double s1 = 0;
-        if (b < NV) {
+      for (int b = 0; b < NU; ++b) s1[b] = 0.0;
 #pragma unroll
-          for (int c = 1; c < NV; ++c) s1 = fma(B.K1[a][c], Vb(c, b), s1);
-        }
-        if (a < NV) {
+      for (int c = 1; c < NV; ++c) {
+        const double kac = B.K1[a][c];
 #pragma unroll
-          for (int c = 1; c < NV; ++c) s1 = fma(Vb(a, c), B.K1[c][b], s1);
-        }
-        bb(a, b) = fma(c2, s1, bb(a, b));
+        for (int b = 0; b < NV; ++b) s1[b] = fma(kac, Vb(c, b), s1[b]);
       }
+      if (a < NV) {
+#pragma unroll
+        for (int c = 1; c < NV; ++c) {
+          const double vac = Vb(a, c);
+#pragma unroll
+          for (int b = 0; b < NU; ++b) s1[b] = fma(vac, B.K1[c][b], s1[b]);
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < NU; ++b) bb(a, b) = fma(c2, s1[b], bb(a, b));
     }
   } else {
 #pragma unroll 1
@@ -546,22 +542,33 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
           for (int b = 0; b < NV; ++b) { const double x = Vb(a, b); tv1[b] = fma(sa, x, tv1[b]); tv2[b] = fma(pa, x, tv2[b]); }
         }
       }
+      // the row at the points: g1[s] = Σ_b tu1[b] P[s][b], ... (independent over s)
+      double g1[NQ], g2[NQ], gv1[NQ], gv2[NQ];
+#pragma unroll
+      for (int s2 = 0; s2 < NQ; ++s2) { g1[s2] = 0; g2[s2] = 0; gv1[s2] = 0; gv2[s2] = 0; }
+#pragma unroll
+      for (int b = 0; b < NU; ++b) {
+#pragma unroll
+        for (int s2 = 0; s2 < NQ; ++s2) {
+          g1[s2] = fma(tu1[b], B.P[s2][b], g1[s2]);
+          g2[s2] = fma(tu2[b], B.S[s2][b], g2[s2]);
+          if (b < NV) {
+            gv1[s2] = fma(tv1[b], B.P[s2][b], gv1[s2]);
+            gv2[s2] = fma(tv2[b], B.S[s2][b], gv2[s2]);
+          }
+        }
+      }
       double z1[NV], z2[NV], y1[NU], y2[NU];
 #pragma unroll
       for (int b = 0; b < NV; ++b) { z1[b] = 0; z2[b] = 0; }
 #pragma unroll
       for (int b = 0; b < NU; ++b) { y1[b] = 0; y2[b] = 0; }
-#pragma unroll 1
+#pragma unroll
       for (int s2 = 0; s2 < NQ; ++s2) {
-        double g1 = 0, g2 = 0, gv1 = 0, gv2 = 0;
-#pragma unroll
-        for (int b = 0; b < NU; ++b) { g1 = fma(tu1[b], B.P[s2][b], g1); g2 = fma(tu2[b], B.S[s2][b], g2); }
-#pragma unroll
-        for (int b = 0; b < NV; ++b) { gv1 = fma(tv1[b], B.P[s2][b], gv1); gv2 = fma(tv2[b], B.S[s2][b], gv2); }
         const size_t ci = (r + NQ * s2) * Eu + e;
         const double cw = F.Cw[ci], aw = F.Aw[ci];
-        const double h1 = fma(aw, gv1, cw * g1), h2 = fma(aw, gv2, cw * g2);
-        const double b1 = cw * gv1, b2 = cw * gv2;
+        const double h1 = fma(aw, gv1[s2], cw * g1[s2]), h2 = fma(aw, gv2[s2], cw * g2[s2]);
+        const double b1 = cw * gv1[s2], b2 = cw * gv2[s2];
 #pragma unroll
         for (int b = 0; b < NV; ++b) { z1[b] = fma(h1, B.P[s2][b], z1[b]); z2[b] = fma(h2, B.S[s2][b], z2[b]); }
 #pragma unroll
@@ -584,7 +591,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
     }
   }
 
-  // ---- source (src/rhs.jl:340-350)
+  // ---- source (src/rhs.jl:340-350), and the mass right-hand side to HBM
 #pragma unroll 1
   for (int b = 0; b < NV; ++b)
 #pragma unroll
@@ -600,7 +607,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
         x += F.PiCdiv[l];
       }
       if (F.src_on) x = fma(S.srct, F.srcP[l], x);
-      Rv(a, b) = x;
+      F.mrhs[l] = x;
     }
 
   // ---- u-equation (src/rhs.jl:352-382): A_e UT = VB - Fu + e_1 V[0][0]; UT into X1 (U is dead)
@@ -695,7 +702,8 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
     }
   }
 
-  // ---- u outputs (k of the u-equation is final now)
+  // ---- u outputs: RK4 (src/solver.jl:289-321): acc = k1 + 2 k2 + 2 k3 in this order, the next
+  //      stage state u + c k, the last stage u + (dt/6)(acc + k4) with the finite check
   bool fin = true;
 #pragma unroll 1
   for (int b = 0; b < NU; ++b)
@@ -709,7 +717,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
         S.accu[l] = S.first ? kk : S.accu[l] + 2.0 * kk;
         S.su[l] = S.u0[l] + S.c * kk;
       } else if (S.mode == OUT_RK4_LAST) {
-        // Chebyshev mode only: no error can arise in this kernel, so u is updated in place now
+        // Chebyshev mode only: no error can arise after k_prep, so u is updated in place now
         const double x = S.u0[l] + S.c * (S.accu[l] + kk);
         S.uo[l] = x;
         fin = fin && isfinite(x);
@@ -717,71 +725,160 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
         S.accu[l] = S.accu[l] + kk;
       }
     }
+  if (S.mode == OUT_RK4_LAST && !fin) atomicOr(F.nonfinite, 1u);
+}
 
-  // ---- mass system M(v_h) VT = Rv (src/rhs.jl:778-951); blocks: r = Rv (Y2), d (Y1), VT and Kd
-  //      from the start of X1 (UT and b are no longer needed)
-  Blk<NV, BT> VT{smem + tid}, Kd{smem + NV * NV * BT + tid};
-  if (!F.cg) {
+// ----------------------------------------------------------------------------
+// k_mass: M(v_h) VT = R on every element (src/rhs.jl:778-951) and the v part of the outputs
+// ----------------------------------------------------------------------------
+
+// element of thread g: in the order of the Chebyshev step counts, or in mesh order
+__device__ __forceinline__ int mass_element(const Fields &F, const StageIO &S, int g, int *pref) {
+  if (!F.sorted) return g;
+  int lo = 0;
+#pragma unroll 1
+  for (int b = NBIN - 1; b >= 0; --b)
+    if (pref[b] <= g) { lo = b; break; }
+  return F.bins[(size_t)lo * F.E + (g - pref[lo])];
+}
+
+template <int NU, int NV, bool CG>
+__global__ void __launch_bounds__(MASS_THREADS)
+    k_mass(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
+           const __grid_constant__ StageIO S) {
+  constexpr int QH = Basis<NU, NV>::QH, BT = MASS_THREADS;
+  extern __shared__ double smem[];
+  __shared__ int pref[NBIN];
+  const int tid = threadIdx.x;
+  const int E = F.E;
+  const size_t Eu = (size_t)E;
+  if (F.sorted) {
+    // exclusive prefix sum of the counts of this stage's bins
+    if (tid == 0) {
+      int acc = 0;
+      for (int b = 0; b < NBIN; ++b) { pref[b] = acc; acc += F.bin_count[S.parity * NBIN + b]; }
+    }
+    __syncthreads();
+  }
+  const int g = blockIdx.x * BT + tid;
+  if (g >= E) return;
+  if (err_word(F) != ERR_NONE) return;
+  const int e = mass_element(F, S, g, pref);
+  Blk<NV, BT> r{smem + tid}, X{smem + NV * NV * BT + tid};
+  bool fin = true;
+
+  // K P accumulated into O: O += P_h^T (G ∘ (P_h P P_h^T)) P_h, one row r2 of the point grid at a time
+  auto addK = [&](Blk<NV, BT> P, Blk<NV, BT> O) {
+#pragma unroll 1
+    for (int r2 = 0; r2 < QH; ++r2) {
+      double T[NV];
+#pragma unroll
+      for (int b = 0; b < NV; ++b) T[b] = 0.0;
+#pragma unroll
+      for (int a = 0; a < NV; ++a) {
+        const double p = B.Ph[r2][a];
+#pragma unroll
+        for (int b = 0; b < NV; ++b) T[b] = fma(p, P(a, b), T[b]);
+      }
+      double Y[QH];
+#pragma unroll
+      for (int s2 = 0; s2 < QH; ++s2) Y[s2] = 0.0;
+#pragma unroll
+      for (int b = 0; b < NV; ++b)
+#pragma unroll
+        for (int s2 = 0; s2 < QH; ++s2) Y[s2] = fma(T[b], B.Ph[s2][b], Y[s2]);
+#pragma unroll
+      for (int s2 = 0; s2 < QH; ++s2) Y[s2] *= F.G[(r2 + QH * s2) * Eu + e];
+      double Z[NV];
+#pragma unroll
+      for (int b = 0; b < NV; ++b) Z[b] = 0.0;
+#pragma unroll
+      for (int s2 = 0; s2 < QH; ++s2)
+#pragma unroll
+        for (int b = 0; b < NV; ++b) Z[b] = fma(Y[s2], B.Ph[s2][b], Z[b]);
+#pragma unroll
+      for (int a = 0; a < NV; ++a) {
+        const double p = B.Ph[r2][a];
+#pragma unroll
+        for (int b = 0; b < NV; ++b) O(a, b) = fma(p, Z[b], O(a, b));
+      }
+    }
+  };
+
+  if constexpr (!CG) {
+    // Chebyshev iteration (Saad Alg. 12.1, src/rhs.jl:921-939); K d is accumulated straight
+    // into the residual after r -= d
+    Blk<NV, BT> d{smem + 2 * NV * NV * BT + tid};
     const double th = F.th[e], de = F.de[e];
     const double s1 = th / de;
     const int n = F.cheb_common ? *F.nmax : F.nst[e];
     const double ith = 1.0 / th;
-    Blk<NV, BT> r = Rv, d = Vb;
 #pragma unroll 1
     for (int b = 0; b < NV; ++b)
 #pragma unroll
-      for (int a = 0; a < NV; ++a) { d(a, b) = r(a, b) * ith; VT(a, b) = 0.0; }
+      for (int a = 0; a < NV; ++a) {
+        const double x = F.mrhs[(a + NV * b) * Eu + e];
+        r(a, b) = x;
+        d(a, b) = x * ith;
+        X(a, b) = 0.0;
+      }
     double rho = 1.0 / s1;
 #pragma unroll 1
     for (int step = 1; step <= n; ++step) {
 #pragma unroll 1
       for (int b = 0; b < NV; ++b)
 #pragma unroll
-        for (int a = 0; a < NV; ++a) VT(a, b) += d(a, b);
+        for (int a = 0; a < NV; ++a) {
+          const double x = d(a, b);
+          X(a, b) += x;
+          r(a, b) -= x;
+        }
       if (step == n) break;
-      apply_K<NU, NV, BT>(B, F.G, E, e, d, Kd);
+      addK(d, r);
       const double rhon = 1.0 / (2.0 * s1 - rho);
       const double c1 = rhon * rho, c2 = 2.0 * rhon / de;
 #pragma unroll 1
       for (int b = 0; b < NV; ++b)
 #pragma unroll
-        for (int a = 0; a < NV; ++a) {
-          const double rr = r(a, b) - (d(a, b) - Kd(a, b));
-          r(a, b) = rr;
-          d(a, b) = fma(c1, d(a, b), c2 * rr);
-        }
+        for (int a = 0; a < NV; ++a) d(a, b) = fma(c1, d(a, b), c2 * r(a, b));
       rho = rhon;
     }
   } else {
-    // conjugate gradients from X = R (src/rhs.jl:824-853); G = 2βv_q W into the scratch of this element
+    // conjugate gradients from X = R (src/rhs.jl:824-853)
+    Blk<NV, BT> p{smem + 2 * NV * NV * BT + tid}, Ap{smem + 3 * NV * NV * BT + tid};
+    // G = 2βv_q W of this element
 #pragma unroll 1
-    for (int r = 0; r < QH; ++r) {
+    for (int r2 = 0; r2 < QH; ++r2) {
       double T[NV];
 #pragma unroll
       for (int b = 0; b < NV; ++b) T[b] = 0.0;
-#pragma unroll 1
+#pragma unroll
       for (int a = 0; a < NV; ++a) {
-        const double p = B.Ph[r][a];
+        const double pa = B.Ph[r2][a];
 #pragma unroll
-        for (int b = 0; b < NV; ++b) T[b] = fma(p, Vb(a, b), T[b]);
+        for (int b = 0; b < NV; ++b) T[b] = fma(pa, S.xv[e + Eu * (a + NV * b)], T[b]);
       }
-#pragma unroll 1
-      for (int s2 = 0; s2 < QH; ++s2) {
-        double g = 0;
 #pragma unroll
-        for (int b = 0; b < NV; ++b) g = fma(T[b], B.Ph[s2][b], g);
-        const size_t gi = (r + QH * s2) * Eu + e;
-        F.G[gi] = 2.0 * F.beta[gi] * g * B.Wh[r][s2];
+      for (int s2 = 0; s2 < QH; ++s2) {
+        double gq = 0;
+#pragma unroll
+        for (int b = 0; b < NV; ++b) gq = fma(T[b], B.Ph[s2][b], gq);
+        const size_t gi = (r2 + QH * s2) * Eu + e;
+        F.G[gi] = 2.0 * F.beta[gi] * gq * B.Wh[r2][s2];
       }
     }
-    // residual r (Rv block after R is copied into VT), direction p (V block), A p (Kd)
-    Blk<NV, BT> r = Rv, p = Vb, Ap = Kd;
     double r0 = 0;
 #pragma unroll 1
     for (int b = 0; b < NV; ++b)
 #pragma unroll
-      for (int a = 0; a < NV; ++a) { const double x = Rv(a, b); VT(a, b) = x; r0 = fma(x, x, r0); }
-    apply_K<NU, NV, BT>(B, F.G, E, e, VT, r);
+      for (int a = 0; a < NV; ++a) {
+        const double x = F.mrhs[(a + NV * b) * Eu + e];
+        X(a, b) = x;
+        p(a, b) = x;
+        r(a, b) = 0.0;
+        r0 = fma(x, x, r0);
+      }
+    addK(p, r);                                    // r = R - M X = K R for X = R
     double rr = 0;
 #pragma unroll 1
     for (int b = 0; b < NV; ++b)
@@ -793,7 +890,11 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
     bool bad = false;
     while (sqrt(rr) > F.mass_tol * r0 && it < maxit) {
       ++it;
-      apply_K<NU, NV, BT>(B, F.G, E, e, p, Ap);
+#pragma unroll 1
+      for (int b = 0; b < NV; ++b)
+#pragma unroll
+        for (int a = 0; a < NV; ++a) Ap(a, b) = 0.0;
+      addK(p, Ap);
       double pAp = 0;
 #pragma unroll 1
       for (int b = 0; b < NV; ++b)
@@ -806,7 +907,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
       for (int b = 0; b < NV; ++b)
 #pragma unroll
         for (int a = 0; a < NV; ++a) {
-          VT(a, b) = fma(al, p(a, b), VT(a, b));
+          X(a, b) = fma(al, p(a, b), X(a, b));
           const double x = fma(-al, Ap(a, b), r(a, b));
           r(a, b) = x;
           rrn = fma(x, x, rrn);
@@ -825,14 +926,13 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
     if (sqrt(rr) > F.mass_tol * r0) atomicAdd(F.cg_nfail, 1u);
   }
 
-  // ---- v outputs; RK4 (src/solver.jl:289-321): acc = k1 + 2 k2 + 2 k3 in this order, the next
-  //      stage state u + c k, the last stage u + (dt/6)(acc + k4) with the finite check
+  // ---- v outputs (RK4 as in k_stage)
 #pragma unroll 1
   for (int b = 0; b < NV; ++b)
 #pragma unroll
     for (int a = 0; a < NV; ++a) {
       const size_t l = e + Eu * (a + NV * b);
-      const double kk = VT(a, b);
+      const double kk = X(a, b);
       if (S.mode == OUT_RHS) {
         S.vt[l] = kk;
       } else if (S.mode == OUT_RK4_STAGE) {
@@ -849,7 +949,12 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
   if (S.mode == OUT_RK4_LAST && !fin) atomicOr(F.nonfinite, 1u);
 }
 
-// Last RK4 update when the last stage may still raise an error inside k_stage
+// shared memory of k_mass: r, X and d (Chebyshev); r, X, p and A p (CG)
+__host__ __device__ constexpr size_t mass_smem(int nv, bool cg) {
+  return (size_t)MASS_THREADS * (cg ? 4 : 3) * nv * nv * sizeof(double);
+}
+
+// Last RK4 update when the last stage may still raise an error inside k_mass
 // (CG mode): u += (dt/6) acc unless an error was recorded.
 __global__ void k_rk4_final(int n_u, int n_v, double *u, double *v, const double *accu, const double *accv,
                             double c, const unsigned long long *err, unsigned int *nonfinite);

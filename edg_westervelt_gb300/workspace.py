@@ -86,6 +86,14 @@ class Workspace:
         self.N = N
         self.nu, self.nv = pre["qu1"], pre["qv1"]
         self._h = None
+        self.ut = np.zeros((N, N, self.nu, self.nu), order="F")
+        self.vt = np.zeros((N, N, self.nv, self.nv), order="F")
+        self.fin = True
+        # pre of another mesh: the reference's Workspace accepts it and its edg_rhs! refuses it
+        # with a DimensionMismatch (src/rhs.jl:500-503); no device workspace is made from it
+        self._mismatch = pre["Ainv_u"].shape[1] != E or pre["Cw"].shape[1] != E
+        if self._mismatch:
+            return
         cfg = L.Config()
         cfg.N, cfg.qu1, cfg.qv1, cfg.q_high = N, pre["qu1"], pre["qv1"], pre["q_high"]
         cfg.theta, cfg.tau, cfg.lambda_u, cfg.lambda_v = pre["theta"], pre["tau"], pre["lambda_u"], pre["lambda_v"]
@@ -124,9 +132,6 @@ class Workspace:
         if rc != L.WEDG_OK:
             raise RuntimeError(f"wedg_create failed: {L.lib().wedg_status_string(rc).decode()}")
         self._h = h
-        self.ut = np.zeros((N, N, self.nu, self.nu), order="F")
-        self.vt = np.zeros((N, N, self.nv, self.nv), order="F")
-        self.fin = True
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -153,6 +158,7 @@ class Workspace:
         raise RuntimeError(f"libwedg: {L.lib().wedg_status_string(rc).decode()}: {msg}")
 
     def stats(self):
+        self._refuse_mismatch()
         s = L.Stats()
         L.lib().wedg_get_stats(self._h, ctypes.byref(s))
         return {f: getattr(s, f) for f, _ in s._fields_}
@@ -170,8 +176,14 @@ class Workspace:
         L.lib().wedg_set_stream(self._h, ctypes.c_void_p(stream_ptr))
 
     # ---- calls
+    def _refuse_mismatch(self):
+        if self._mismatch:
+            raise DimensionMismatch(f"state, workspace and pre do not match (N = {self.N}, q_u + 1 = {self.nu}, "
+                                    f"q_v + 1 = {self.nv})")
+
     def rhs(self, u, v, t, ut=None, vt=None):
         """edg_rhs!: the right-hand side at time t into ut, vt (default the workspace's own)."""
+        self._refuse_mismatch()
         N, nu, nv = self.N, self.nu, self.nv
         if _is_device(u):
             if ut is None or vt is None:
@@ -192,6 +204,7 @@ class Workspace:
     def rk4_steps(self, u, v, t0, dt, nsteps, stop_nonfinite=False):
         """nsteps RK4 steps in place from t0 (t advancing by repeated addition of dt).
         Returns the number of steps completed; sets self.fin."""
+        self._refuse_mismatch()
         N = self.N
         done = ctypes.c_int64(0)
         fin = ctypes.c_int(1)

@@ -143,13 +143,13 @@ int wedg_set_stream(wedg_ws *ws, void *stream);
 int wedg_rk4_steps_async(wedg_ws *ws, double *u_dev, double *v_dev, double t0, double dt, int64_t nsteps);
 int wedg_sync_status(wedg_ws *ws, int64_t *steps_done, int *finite);
 
-/* Kernel timing for benchmarks: with enable != 0, every launch of the two stage
- * kernels is bracketed by CUDA events on the workspace stream and its duration
- * accumulated; wedg_kernel_times reads (and with reset, clears) the totals in
- * milliseconds and the number of launches of each. */
+/* Kernel timing for benchmarks: with enable != 0, every launch of the three stage
+ * kernels (k_prep, k_stage, k_mass) is bracketed by CUDA events on the workspace
+ * stream and its duration accumulated; wedg_kernel_times reads (and with reset,
+ * clears) the totals in milliseconds and the number of launches of each. */
 int wedg_time_kernels(wedg_ws *ws, int enable);
 int wedg_kernel_times(wedg_ws *ws, double *prep_ms, int64_t *prep_launches, double *stage_ms,
-                      int64_t *stage_launches, int reset);
+                      int64_t *stage_launches, double *mass_ms, int64_t *mass_launches, int reset);
 
 const char *wedg_status_string(int status);
 /* Library version and the GPU architecture it was built for. */
