@@ -87,6 +87,8 @@ def lib():
     L.wedg_status_string.argtypes = [ctypes.c_int]
     L.wedg_status_string.restype = ctypes.c_char_p
     L.wedg_version.restype = ctypes.c_char_p
+    L.wedg_rhs_noalloc.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Pre), vp, vp, ctypes.c_double, vp, vp, vp,
+                                   ctypes.c_char_p, ctypes.c_size_t]
     L.wedg_time_kernels.argtypes = [vp, ctypes.c_int]
     L.wedg_kernel_times.argtypes = [vp, _D, _I64, _D, _I64, _D, _I64, ctypes.c_int]
     _lib = L

@@ -151,6 +151,29 @@ int wedg_time_kernels(wedg_ws *ws, int enable);
 int wedg_kernel_times(wedg_ws *ws, double *prep_ms, int64_t *prep_launches, double *stage_ms,
                       int64_t *stage_launches, double *mass_ms, int64_t *mass_launches, int reset);
 
+/* Size of the static device array used by wedg_rhs_noalloc (16 MiB). */
+#define WEDG_NOALLOC_BYTES ((size_t)16 << 20)
+
+/* One right-hand side evaluation that allocates nothing. It has no counterpart in
+ * the reference: it exists for callers that cannot let a library allocate device
+ * memory, such as programs whose GPU memory belongs to another runtime's pool
+ * allocator or code that must not allocate or free device memory at the point
+ * where it needs a right-hand side. It takes cfg and pre as wedg_create does
+ * (host memory), u and v as device pointers and writes ut, vt (device pointers,
+ * the reference's state layout); no workspace is needed. Its device scratch --
+ * the copy of pre in the kernels' layouts, traces, Chebyshev data and the error
+ * word -- is one static device array of WEDG_NOALLOC_BYTES, which every GPU that
+ * loads the library holds until exit; meshes that need more are rejected with
+ * WEDG_ERR_ARGUMENT and a message. It calls no cudaMalloc, cudaFree or other
+ * allocating routine. The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * Every call shares the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. `stream` is a cudaStream_t (NULL: the default
+ * stream); the call returns after the evaluation has finished. Status and
+ * message (into msg, if not NULL) as wedg_rhs. */
+int wedg_rhs_noalloc(const wedg_config *cfg, const wedg_pre *pre, const double *u, const double *v, double t,
+                     double *ut, double *vt, void *stream, char *msg, size_t msg_len);
+
 const char *wedg_status_string(int status);
 /* Library version and the GPU architecture it was built for. */
 const char *wedg_version(void);
