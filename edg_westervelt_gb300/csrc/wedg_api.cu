@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/wedg.h"
+#include "wedg_basis.h"
 #include "wedg_dispatch.h"
 
 namespace wedg {
@@ -131,54 +132,6 @@ int upload(wedg_ws *ws, const T **dst, const std::vector<T> &h) {
   CK(ws, cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
   *dst = p;
   return WEDG_OK;
-}
-
-// Cyclic Jacobi eigen-decomposition of a small symmetric matrix A (n×n, row-major):
-// A = Q diag(lam) Q^T, eigenvalues ascending.
-void sym_eig(int n, std::vector<double> A, std::vector<double> &Q, std::vector<double> &lam) {
-  Q.assign(n * n, 0.0);
-  for (int i = 0; i < n; ++i) Q[i * n + i] = 1.0;
-  for (int sweep = 0; sweep < 100; ++sweep) {
-    double off = 0;
-    for (int p = 0; p < n; ++p)
-      for (int q = p + 1; q < n; ++q) off += A[p * n + q] * A[p * n + q];
-    if (off < 1e-40) break;
-    for (int p = 0; p < n; ++p)
-      for (int q = p + 1; q < n; ++q) {
-        const double apq = A[p * n + q];
-        if (std::fabs(apq) < 1e-300) continue;
-        const double app = A[p * n + p], aqq = A[q * n + q];
-        const double tau = (aqq - app) / (2 * apq);
-        const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1 + tau * tau));
-        const double c = 1 / std::sqrt(1 + t * t), s = t * c;
-        for (int k = 0; k < n; ++k) {
-          const double akp = A[k * n + p], akq = A[k * n + q];
-          A[k * n + p] = c * akp - s * akq;
-          A[k * n + q] = s * akp + c * akq;
-        }
-        for (int k = 0; k < n; ++k) {
-          const double apk = A[p * n + k], aqk = A[q * n + k];
-          A[p * n + k] = c * apk - s * aqk;
-          A[q * n + k] = s * apk + c * aqk;
-        }
-        for (int k = 0; k < n; ++k) {
-          const double qkp = Q[k * n + p], qkq = Q[k * n + q];
-          Q[k * n + p] = c * qkp - s * qkq;
-          Q[k * n + q] = s * qkp + c * qkq;
-        }
-      }
-  }
-  lam.resize(n);
-  std::vector<int> idx(n);
-  for (int i = 0; i < n; ++i) { lam[i] = A[i * n + i]; idx[i] = i; }
-  std::sort(idx.begin(), idx.end(), [&](int a, int b) { return lam[a] < lam[b]; });
-  std::vector<double> Qs(n * n), ls(n);
-  for (int c = 0; c < n; ++c) {
-    ls[c] = lam[idx[c]];
-    for (int r = 0; r < n; ++r) Qs[r * n + c] = Q[r * n + idx[c]];
-  }
-  Q = Qs;
-  lam = ls;
 }
 
 const char *kind_name(int k) {
@@ -452,44 +405,11 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
   const int E = ws->E, nq = nu, qh = ws->qh;
   const size_t Es = (size_t)E;
 
-  // ---- 1D operators (Julia column-major inputs)
-  BasisHost bh{};
-  bh.nu = nu; bh.nv = nv; bh.qh = qh;
-  for (int i = 0; i < nq; ++i) {
-    bh.w[i] = pre->w[i];
-    for (int d = 0; d < nu; ++d) { bh.P[i][d] = pre->P_u[i + nq * d]; bh.S[i][d] = pre->S_u[i + nq * d]; }
-  }
-  for (int d = 0; d < nu; ++d) {
-    bh.El[d] = pre->Ebl_u[d]; bh.Er[d] = pre->Ebr_u[d]; bh.E1l[d] = pre->E1bl_u[d]; bh.E1r[d] = pre->E1br_u[d];
-  }
-  for (int r = 0; r < qh; ++r) {
-    for (int d = 0; d < nv; ++d) bh.Ph[r][d] = pre->P_h_v[r + qh * d];
-    for (int s = 0; s < qh; ++s) bh.Wh[r][s] = pre->W2d_h[r + qh * s];
-  }
-  // K1 = S^T diag(w) S; its first row and column vanish (the constant mode has no derivative)
-  for (int a = 0; a < nu; ++a)
-    for (int c = 0; c < nu; ++c) {
-      double s = 0;
-      for (int i = 0; i < nq; ++i) s += bh.S[i][a] * bh.w[i] * bh.S[i][c];
-      bh.K1[a][c] = s;
-    }
-  {
-    // eigen-decomposition of the nonsingular block K1[1:, 1:]; Q = diag(1, Q')
-    const int m = nu - 1;
-    std::vector<double> A(m * m), Qm, lam;
-    for (int a = 0; a < m; ++a)
-      for (int c = 0; c < m; ++c) A[a * m + c] = 0.5 * (bh.K1[a + 1][c + 1] + bh.K1[c + 1][a + 1]);
-    sym_eig(m, A, Qm, lam);
-    std::vector<double> L(nu, 0.0);
-    for (int a = 0; a < nu; ++a)
-      for (int c = 0; c < nu; ++c) bh.Q[a][c] = 0.0;
-    bh.Q[0][0] = 1.0;
-    for (int a = 0; a < m; ++a) {
-      L[a + 1] = lam[a];
-      for (int c = 0; c < m; ++c) bh.Q[a + 1][c + 1] = Qm[a * m + c];
-    }
-    for (int i = 0; i < nu; ++i)
-      for (int j = 0; j < nu; ++j) bh.ilam2[i][j] = (i == 0 && j == 0) ? 1.0 : 1.0 / (L[i] + L[j]);
+  // ---- 1D operators (Julia column-major inputs), with their mirror parities made exact
+  BasisHost bh;
+  if (build_basis(cfg, pre, bh)) {
+    delete ws;
+    return WEDG_ERR_ARGUMENT;
   }
 
   // ---- constant coefficients per element? Cw = c² W and Aw = α W to 1e-14 (relative)
@@ -641,7 +561,7 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
     F.gam[s] = cfg->gamma_abc[s]; F.eta[s] = cfg->eta_abc[s]; F.sig[s] = cfg->sigma[s];
     F.kb[s] = cfg->kb[s]; F.kap[s] = cfg->kappa[s];
   }
-  // sets the shared-memory attributes of k_stage and k_mass (a launch of zero blocks does nothing else)
+  // sets the shared-memory attributes of k_stage and k_cg (a launch of zero blocks does nothing else)
   ws->L.stage(ws->basis.data(), F, StageIO{}, 0, 0, nullptr);
   ws->L.mass(ws->basis.data(), F, StageIO{}, 0, 0, nullptr);
   cudaMemset(F.bin_count, 0, 2 * NBIN * sizeof(int));

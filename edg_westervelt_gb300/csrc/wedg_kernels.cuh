@@ -21,10 +21,11 @@
 //            (:335-350) and u-equation (:352-382) with the u part of the RK4
 //            stage update (src/solver.jl:299-321); it leaves the right-hand
 //            side of the mass system in HBM;
-//   k_mass   the mass solve (Chebyshev :920-939 or CG :821-853) and the v part
-//            of the RK4 update. Elements are visited in the order of their
-//            Chebyshev step counts (k_prep lists them by count), so the lanes
-//            of a warp run the same number of steps.
+//   k_cheb   the Chebyshev mass solve (:920-939) and the v part of the RK4
+//            update, a team of threads per element. Elements are visited in
+//            decreasing order of their Chebyshev step counts (k_prep lists them
+//            by count), so the longest solves start first;
+//   k_cg     the same with conjugate gradients (:821-853), one thread per element.
 // Interior faces are evaluated by both neighbours, each writing only its own
 // slots, so no element writes another element's data.
 //
@@ -48,7 +49,8 @@ namespace wedg {
 constexpr unsigned long long ERR_NONE = ~0ull;
 constexpr int ERR_CLASS_SHIFT = 56;   // class 0: boundary weight, 1: mass matrix not PD, 3: stopped (non-finite)
 constexpr int NBIN = 48;              // Chebyshev-count bins of the mass kernel (the last holds n ≥ NBIN)
-constexpr int MASS_THREADS = 64;
+constexpr int MASS_THREADS = 64;     // threads per block of k_cg
+constexpr int CHEB_THREADS = 128;    // threads per block of k_cheb
 
 __host__ __device__ constexpr int qhigh(int nu, int nv) {
   // q_high = max(ceil(3 q_v / 2) + 1, q_u + 1), src/solver.jl:483
@@ -123,43 +125,140 @@ struct Blk {
   __device__ __forceinline__ double &operator()(int a, int b) const { return p[(a + n * b) * BT]; }
 };
 
+// Nonzero pattern of the eigenbasis Q of the 1D stiffness K1 (built so on the host): Q[a][i]
+// vanishes for a + i odd and in row and column 0 outside (0, 0)
+__host__ __device__ constexpr bool qnz(int a, int i) { return ((a + i) & 1) == 0 && ((a == 0) == (i == 0)); }
+
+// ----------------------------------------------------------------------------
+// Mirror-parity contractions. The points of both quadratures are Gauss-Legendre
+// points (mirrored through the element centre) and the basis is the Legendre one,
+// so P[n-1-i][d] = (-1)^d P[i][d] for the values and the opposite sign for the
+// derivatives (the host makes these exact). A contraction over the modes is then
+// done on the first half of the points only -- its even-mode and odd-mode parts give
+// the point and its mirror as a sum and a difference -- and a contraction over the
+// points from the sums (even modes) and differences (odd modes) of mirrored points.
+// ----------------------------------------------------------------------------
+
+// Y[s] = Σ_b T[b] Ph[s][b] at all QH points
+template <int QH, int NV>
+__device__ __forceinline__ void ph_to_points(const double (&Ph)[QH][NV], const double (&T)[NV], double (&Y)[QH]) {
+#pragma unroll
+  for (int s = 0; s < QH / 2; ++s) {
+    double ev = 0.0, od = 0.0;
+#pragma unroll
+    for (int b = 0; b < NV; b += 2) ev = fma(T[b], Ph[s][b], ev);
+#pragma unroll
+    for (int b = 1; b < NV; b += 2) od = fma(T[b], Ph[s][b], od);
+    Y[s] = ev + od;
+    Y[QH - 1 - s] = ev - od;
+  }
+  if constexpr ((QH & 1) != 0) {
+    double ev = 0.0;
+#pragma unroll
+    for (int b = 0; b < NV; b += 2) ev = fma(T[b], Ph[QH / 2][b], ev);
+    Y[QH / 2] = ev;
+  }
+}
+
+// Z[b] = Σ_s Y[s] Ph[s][b]
+template <int QH, int NV>
+__device__ __forceinline__ void ph_from_points(const double (&Ph)[QH][NV], const double (&Y)[QH], double (&Z)[NV]) {
+  double ys[QH / 2 + 1], yd[QH / 2 + 1];
+#pragma unroll
+  for (int s = 0; s < QH / 2; ++s) {
+    ys[s] = Y[s] + Y[QH - 1 - s];
+    yd[s] = Y[s] - Y[QH - 1 - s];
+  }
+#pragma unroll
+  for (int b = 0; b < NV; ++b) {
+    double z = 0.0;
+#pragma unroll
+    for (int s = 0; s < QH / 2; ++s) z = fma((b & 1) ? yd[s] : ys[s], Ph[s][b], z);
+    if constexpr ((QH & 1) != 0) {
+      if (!(b & 1)) z = fma(Y[QH / 2], Ph[QH / 2][b], z);
+    }
+    Z[b] = z;
+  }
+}
+
+// Rows r and QH-1-r (r < QH/2) of Ph X for an NV×NV block x(a, b):
+//   Tp[b] = Σ_a Ph[r][a] x(a, b),  Tm[b] = Σ_a (-1)^a Ph[r][a] x(a, b)
+template <int QH, int NV, class X>
+__device__ __forceinline__ void ph_row_pair(const double (&Ph)[QH][NV], int r, const X &x, double (&Tp)[NV],
+                                            double (&Tm)[NV]) {
+#pragma unroll
+  for (int b = 0; b < NV; ++b) {
+    double ev = 0.0, od = 0.0;
+#pragma unroll
+    for (int a = 0; a < NV; a += 2) ev = fma(Ph[r][a], x(a, b), ev);
+#pragma unroll
+    for (int a = 1; a < NV; a += 2) od = fma(Ph[r][a], x(a, b), od);
+    Tp[b] = ev + od;
+    Tm[b] = ev - od;
+  }
+}
+
+// The middle row QH/2 of Ph X when QH is odd (only the even modes are nonzero there)
+template <int QH, int NV, class X>
+__device__ __forceinline__ void ph_row_mid(const double (&Ph)[QH][NV], const X &x, double (&T)[NV]) {
+#pragma unroll
+  for (int b = 0; b < NV; ++b) {
+    double ev = 0.0;
+#pragma unroll
+    for (int a = 0; a < NV; a += 2) ev = fma(Ph[QH / 2][a], x(a, b), ev);
+    T[b] = ev;
+  }
+}
+
 // ----------------------------------------------------------------------------
 // k_prep: traces, boundary weight check, Chebyshev interval data
 // ----------------------------------------------------------------------------
 
 // Traces of an n×n block X on the four sides (src/rhs.jl:388-410):
 //   oB[i] = Σ_b P[i,b] Σ_a El[a] X[a][b],  oT with Er,
-//   oL[i] = Σ_b P[i,b] Σ_a El[a] X[b][a],  oR with Er.
-template <int NQ, int NU, int n>
+//   oL[i] = Σ_b P[i,b] Σ_a El[a] X[b][a],  oR with Er,
+// where El, Er are the values (DER false) or the derivatives (DER true) of the modes at the
+// two ends: Er[a] = ±(-1)^a El[a], so both ends come from the even and odd parts of one sum.
+template <int NQ, int NU, int n, bool DER>
 __device__ __forceinline__ void trace4(const double (&X)[n][n], const double (&P)[NQ][NU], const double *El,
-                                       const double *Er, double *tr, int fam, int E, int e) {
+                                       double *tr, int fam, int E, int e) {
   double sB[n], sT[n], sL[n], sR[n];
 #pragma unroll
   for (int b = 0; b < n; ++b) {
-    double xb = 0, xt = 0, yl = 0, yr = 0;
+    double xe = 0, xo = 0, ye = 0, yo = 0;
 #pragma unroll
-    for (int a = 0; a < n; ++a) {
-      xb = fma(El[a], X[a][b], xb);
-      xt = fma(Er[a], X[a][b], xt);
-      yl = fma(El[a], X[b][a], yl);
-      yr = fma(Er[a], X[b][a], yr);
-    }
-    sB[b] = xb; sT[b] = xt; sL[b] = yl; sR[b] = yr;
+    for (int a = 0; a < n; a += 2) { xe = fma(El[a], X[a][b], xe); ye = fma(El[a], X[b][a], ye); }
+#pragma unroll
+    for (int a = 1; a < n; a += 2) { xo = fma(El[a], X[a][b], xo); yo = fma(El[a], X[b][a], yo); }
+    sB[b] = xe + xo; sL[b] = ye + yo;
+    sT[b] = DER ? xo - xe : xe - xo;
+    sR[b] = DER ? yo - ye : ye - yo;
   }
-#pragma unroll
-  for (int i = 0; i < NQ; ++i) {
-    double oB = 0, oT = 0, oL = 0, oR = 0;
-#pragma unroll
-    for (int b = 0; b < n; ++b) {
-      oB = fma(P[i][b], sB[b], oB);
-      oT = fma(P[i][b], sT[b], oT);
-      oL = fma(P[i][b], sL[b], oL);
-      oR = fma(P[i][b], sR[b], oR);
-    }
+  auto put = [&](int i, double oB, double oT, double oL, double oR) {
     tr[((fam * 4 + 0) * NQ + i) * (size_t)E + e] = oB;
     tr[((fam * 4 + 1) * NQ + i) * (size_t)E + e] = oT;
     tr[((fam * 4 + 2) * NQ + i) * (size_t)E + e] = oL;
     tr[((fam * 4 + 3) * NQ + i) * (size_t)E + e] = oR;
+  };
+#pragma unroll
+  for (int i = 0; i < (NQ + 1) / 2; ++i) {
+    double eB = 0, eT = 0, eL = 0, eR = 0, oB = 0, oT = 0, oL = 0, oR = 0;
+#pragma unroll
+    for (int b = 0; b < n; b += 2) {
+      eB = fma(P[i][b], sB[b], eB); eT = fma(P[i][b], sT[b], eT);
+      eL = fma(P[i][b], sL[b], eL); eR = fma(P[i][b], sR[b], eR);
+    }
+    if (2 * i + 1 == NQ) {      // the middle point: the odd modes vanish there
+      put(i, eB, eT, eL, eR);
+      continue;
+    }
+#pragma unroll
+    for (int b = 1; b < n; b += 2) {
+      oB = fma(P[i][b], sB[b], oB); oT = fma(P[i][b], sT[b], oT);
+      oL = fma(P[i][b], sL[b], oL); oR = fma(P[i][b], sR[b], oR);
+    }
+    put(i, eB + oB, eT + oT, eL + oL, eR + oR);
+    put(NQ - 1 - i, eB - oB, eT - oT, eL - oL, eR - oR);
   }
 }
 
@@ -185,12 +284,12 @@ __global__ void __launch_bounds__(128) k_prep(const __grid_constant__ Basis<NU, 
   {
     double U[NU][NU];
     load_regs<NU>(U, S.xu, E, e);
-    trace4<NQ, NU, NU>(U, B.P, B.E1l, B.E1r, F.tr, 0, E, e);
+    trace4<NQ, NU, NU, true>(U, B.P, B.E1l, F.tr, 0, E, e);
   }
   double V[NV][NV];
   load_regs<NV>(V, S.xv, E, e);
-  trace4<NQ, NU, NV>(V, B.P, B.El, B.Er, F.tr, 1, E, e);
-  trace4<NQ, NU, NV>(V, B.P, B.E1l, B.E1r, F.tr, 2, E, e);
+  trace4<NQ, NU, NV, false>(V, B.P, B.El, F.tr, 1, E, e);
+  trace4<NQ, NU, NV, true>(V, B.P, B.E1l, F.tr, 2, E, e);
 
   // weight check 1 - kβv > 0 for the trace and the data on physical sides
   // (src/rhs.jl:109-110, 751-757); key of src/rhs.jl:732
@@ -217,31 +316,35 @@ __global__ void __launch_bounds__(128) k_prep(const __grid_constant__ Basis<NU, 
   }
 
   if (F.cg) return;
-  // Chebyshev interval of the element: v_q = P_h V P_h^T, G = 2βv_q, a± = 1 - extrema(G)
+  // Chebyshev interval of the element: v_q = P_h V P_h^T, G = 2βv_q, a± = 1 - extrema(G);
+  // the rows of the point grid in mirrored pairs
   double gmin = 1.0 / 0.0, gmax = -1.0 / 0.0;
   bool nan = false;
-#pragma unroll 1
-  for (int r = 0; r < QH; ++r) {
-    double T[NV];
+  auto vx = [&](int a, int b) { return V[a][b]; };
+  auto points = [&](const double (&T)[NV], int r) {
+    double Y[QH];
+    ph_to_points<QH, NV>(B.Ph, T, Y);
 #pragma unroll
-    for (int b = 0; b < NV; ++b) {
-      double t = 0;
-#pragma unroll
-      for (int a = 0; a < NV; ++a) t = fma(B.Ph[r][a], V[a][b], t);
-      T[b] = t;
-    }
-#pragma unroll 2
     for (int s2 = 0; s2 < QH; ++s2) {
-      double g = 0;
-#pragma unroll
-      for (int b = 0; b < NV; ++b) g = fma(T[b], B.Ph[s2][b], g);
       const size_t gi = (r + QH * s2) * (size_t)E + e;
-      g = g * (2.0 * F.beta[gi]);
+      const double g = Y[s2] * (2.0 * F.beta[gi]);
       nan |= (g != g);
       gmin = fmin(gmin, g);
       gmax = fmax(gmax, g);
       F.G[gi] = g * B.Wh[r][s2];
     }
+  };
+#pragma unroll 1
+  for (int r = 0; r < QH / 2; ++r) {
+    double Tp[NV], Tm[NV];
+    ph_row_pair<QH, NV>(B.Ph, r, vx, Tp, Tm);
+    points(Tp, r);
+    points(Tm, QH - 1 - r);
+  }
+  if constexpr ((QH & 1) != 0) {
+    double T[NV];
+    ph_row_mid<QH, NV>(B.Ph, vx, T);
+    points(T, QH / 2);
   }
   const double amin = 1.0 - gmax, amax = 1.0 - gmin;
   if (nan || !(amin > 0.0)) {
@@ -478,50 +581,71 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
     //   (c²∇φ_v, ∇u_h) = c² (K1 U + U K1)[v-block],  (α∇φ_v, ∇v_h) = α (K1 V + V K1)
     //   (c²∇φ_u, ∇v_h) = c² (K1[:, v] V + V K1[v, :])
     // (row and column 0 of K1 vanish: the derivative of the constant mode is 0).
-    // Each output row is built at once, so the FMAs of a row are independent.
+    // K1 couples only modes of equal parity (K1[a][c] = 0 for a + c odd): the sums run over
+    // c ≡ a and c ≡ b (mod 2). Rows are taken in pairs (a0, a0 + 1), so that the parity of a
+    // is known at compile time; each output row is built at once (independent FMAs).
     const double c2 = F.c2e[e], al = F.ae[e];
     const double mc2 = -four_hh * c2, mal = -four_hh * al;
 #pragma unroll 1
-    for (int a = 0; a < NV; ++a) {
-      double su[NV], sv[NV];
+    for (int a0 = 0; a0 < NV; a0 += 2) {
 #pragma unroll
-      for (int b = 0; b < NV; ++b) { su[b] = 0.0; sv[b] = 0.0; }
+      for (int pa = 0; pa < 2; ++pa) {
+        const int a = a0 + pa;
+        if (a >= NV) break;
+        double su[NV], sv[NV];
 #pragma unroll
-      for (int c = 1; c < NU; ++c) {
-        const double kac = B.K1[a][c], uac = Ub(a, c);
+        for (int b = 0; b < NV; ++b) { su[b] = 0.0; sv[b] = 0.0; }
+        if (a > 0) {                                  // row 0 of K1 vanishes
 #pragma unroll
-        for (int b = 0; b < NV; ++b) su[b] = fma(kac, Ub(c, b), fma(uac, B.K1[c][b], su[b]));
+          for (int c = 2 - pa; c < NU; c += 2) {
+            const double kac = B.K1[a][c];
+#pragma unroll
+            for (int b = 0; b < NV; ++b) su[b] = fma(kac, Ub(c, b), su[b]);
+          }
+#pragma unroll
+          for (int c = 2 - pa; c < NV; c += 2) {
+            const double kac = B.K1[a][c];
+#pragma unroll
+            for (int b = 0; b < NV; ++b) sv[b] = fma(kac, Vb(c, b), sv[b]);
+          }
+        }
+#pragma unroll
+        for (int b = 1; b < NV; ++b) {                // column 0 of K1 vanishes
+#pragma unroll
+          for (int c = 2 - (b & 1); c < NU; c += 2) su[b] = fma(Ub(a, c), B.K1[c][b], su[b]);
+#pragma unroll
+          for (int c = 2 - (b & 1); c < NV; c += 2) sv[b] = fma(Vb(a, c), B.K1[c][b], sv[b]);
+        }
+#pragma unroll
+        for (int b = 0; b < NV; ++b) Rv(a, b) = fma(mc2, su[b], fma(mal, sv[b], Rv(a, b)));
       }
-#pragma unroll
-      for (int c = 1; c < NV; ++c) {
-        const double kac = B.K1[a][c], vac = Vb(a, c);
-#pragma unroll
-        for (int b = 0; b < NV; ++b) sv[b] = fma(kac, Vb(c, b), fma(vac, B.K1[c][b], sv[b]));
-      }
-#pragma unroll
-      for (int b = 0; b < NV; ++b) Rv(a, b) = fma(mc2, su[b], fma(mal, sv[b], Rv(a, b)));
     }
 #pragma unroll 1
-    for (int a = 0; a < NU; ++a) {
-      double s1[NU];
+    for (int a0 = 0; a0 < NU; a0 += 2) {
 #pragma unroll
-      for (int b = 0; b < NU; ++b) s1[b] = 0.0;
+      for (int pa = 0; pa < 2; ++pa) {
+        const int a = a0 + pa;
+        if (a >= NU) break;
+        double s1[NU];
 #pragma unroll
-      for (int c = 1; c < NV; ++c) {
-        const double kac = B.K1[a][c];
+        for (int b = 0; b < NU; ++b) s1[b] = 0.0;
+        if (a > 0) {
 #pragma unroll
-        for (int b = 0; b < NV; ++b) s1[b] = fma(kac, Vb(c, b), s1[b]);
-      }
-      if (a < NV) {
+          for (int c = 2 - pa; c < NV; c += 2) {
+            const double kac = B.K1[a][c];
 #pragma unroll
-        for (int c = 1; c < NV; ++c) {
-          const double vac = Vb(a, c);
-#pragma unroll
-          for (int b = 0; b < NU; ++b) s1[b] = fma(vac, B.K1[c][b], s1[b]);
+            for (int b = 0; b < NV; ++b) s1[b] = fma(kac, Vb(c, b), s1[b]);
+          }
         }
-      }
+        if (a < NV) {
 #pragma unroll
-      for (int b = 0; b < NU; ++b) bb(a, b) = fma(c2, s1[b], bb(a, b));
+          for (int b = 1; b < NU; ++b)
+#pragma unroll
+            for (int c = 2 - (b & 1); c < NV; c += 2) s1[b] = fma(Vb(a, c), B.K1[c][b], s1[b]);
+        }
+#pragma unroll
+        for (int b = 0; b < NU; ++b) bb(a, b) = fma(c2, s1[b], bb(a, b));
+      }
     }
   } else {
 #pragma unroll 1
@@ -615,7 +739,9 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
   Blk<NU, BT> UT = X1;
   if constexpr (FAST) {
     // A_e = c² (K1 ⊗ I + I ⊗ K1) + e_0 e_0^T is diagonal in the eigenbasis Q ⊗ Q of K1 (whose
-    // first eigenvector is e_0 with λ_0 = 0): UT = Q [ (Q^T b Q) ∘ L ] Q^T, L = 1/(c²(λ_i+λ_j)), 1 at (0,0)
+    // first eigenvector is e_0 with λ_0 = 0): UT = Q [ (Q^T b Q) ∘ L ] Q^T, L = 1/(c²(λ_i+λ_j)), 1 at (0,0).
+    // Q[a][i] vanishes for a + i odd and in row and column 0 outside (0, 0): qnz skips those
+    // terms at compile time.
     const double ic2 = F.ic2e[e];
     // T1 = Q^T b into X1
 #pragma unroll 1
@@ -627,7 +753,8 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
       for (int a = 0; a < NU; ++a) {
         const double x = bb(a, c);
 #pragma unroll
-        for (int i = 0; i < NU; ++i) t[i] = fma(B.Q[a][i], x, t[i]);
+        for (int i = 0; i < NU; ++i)
+          if (qnz(a, i)) t[i] = fma(B.Q[a][i], x, t[i]);
       }
 #pragma unroll
       for (int i = 0; i < NU; ++i) X1(i, c) = t[i];
@@ -642,7 +769,8 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
       for (int c = 0; c < NU; ++c) {
         const double x = X1(i, c);
 #pragma unroll
-        for (int jj = 0; jj < NU; ++jj) t[jj] = fma(x, B.Q[c][jj], t[jj]);
+        for (int jj = 0; jj < NU; ++jj)
+          if (qnz(c, jj)) t[jj] = fma(x, B.Q[c][jj], t[jj]);
       }
 #pragma unroll
       for (int jj = 0; jj < NU; ++jj) X2(i, jj) = (i == 0 && jj == 0) ? t[jj] : t[jj] * (B.ilam2[i][jj] * ic2);
@@ -657,7 +785,8 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
       for (int i = 0; i < NU; ++i) {
         const double x = X2(i, jj);
 #pragma unroll
-        for (int a = 0; a < NU; ++a) t[a] = fma(B.Q[a][i], x, t[a]);
+        for (int a = 0; a < NU; ++a)
+          if (qnz(a, i)) t[a] = fma(B.Q[a][i], x, t[a]);
       }
 #pragma unroll
       for (int a = 0; a < NU; ++a) X1(a, jj) = t[a];
@@ -672,7 +801,8 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
       for (int jj = 0; jj < NU; ++jj) {
         const double x = X1(a, jj);
 #pragma unroll
-        for (int c = 0; c < NU; ++c) t[c] = fma(x, B.Q[c][jj], t[c]);
+        for (int c = 0; c < NU; ++c)
+          if (qnz(c, jj)) t[c] = fma(x, B.Q[c][jj], t[c]);
       }
 #pragma unroll
       for (int c = 0; c < NU; ++c) X2(a, c) = t[c];
@@ -729,143 +859,254 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
 }
 
 // ----------------------------------------------------------------------------
-// k_mass: M(v_h) VT = R on every element (src/rhs.jl:778-951) and the v part of the outputs
+// The mass solve M(v_h) VT = R on every element (src/rhs.jl:778-951) and the v part of the outputs
 // ----------------------------------------------------------------------------
 
 // element of thread g: in the order of the Chebyshev step counts, or in mesh order
+// (largest counts first: the blocks with the most work start first, and the short ones fill the
+// SMs behind them). pref[b] = number of elements in the bins above b.
 __device__ __forceinline__ int mass_element(const Fields &F, const StageIO &S, int g, int *pref) {
   if (!F.sorted) return g;
-  int lo = 0;
+  int lo = NBIN - 1;
 #pragma unroll 1
-  for (int b = NBIN - 1; b >= 0; --b)
+  for (int b = 0; b < NBIN; ++b)
     if (pref[b] <= g) { lo = b; break; }
   return F.bins[(size_t)lo * F.E + (g - pref[lo])];
 }
 
-template <int NU, int NV, bool CG>
+// v outputs of modal entry l = e + E (a + NV b): RK4 as in k_stage (src/solver.jl:299-321)
+__device__ __forceinline__ void store_v(const StageIO &S, size_t l, double kk, bool &fin) {
+  if (S.mode == OUT_RHS) {
+    S.vt[l] = kk;
+  } else if (S.mode == OUT_RK4_STAGE) {
+    S.accv[l] = S.first ? kk : S.accv[l] + 2.0 * kk;
+    S.sv[l] = S.v0[l] + S.c * kk;
+  } else if (S.mode == OUT_RK4_LAST) {
+    const double x = S.v0[l] + S.c * (S.accv[l] + kk);
+    S.vo[l] = x;
+    fin = fin && isfinite(x);
+  } else {
+    S.accv[l] = S.accv[l] + kk;
+  }
+}
+
+// k_cheb: the Chebyshev mass solve (Saad Alg. 12.1, src/rhs.jl:920-939) with a team of threads
+// per element. One Chebyshev step costs one application of K = P_h^T diag(G) P_h (G = 2βv W at
+// the high-order points), and its FP64 work is cut across the team by rows of the point grid:
+// unit u of the team takes the mirrored rows u and QH-1-u (the middle row alone when QH is odd),
+// takes them to the points and back (phase 1), and leaves for each mode column b the sum and
+// the difference of the two rows' results in shared memory; then every thread finishes J of the
+// NV² modal entries from the units' rows (phase 2), for which it also keeps the residual, the
+// iterate and the search direction. A team lives in one warp, so its phases are ordered by
+// __syncwarp on the team's lanes. Spreading an element over the team matters because one warp
+// is tied to one SM sub-partition, whose FP64 rate is a small fraction of a lane per clock: with
+// one element per thread, the warps of the elements with the most Chebyshev steps ran for many
+// times the average and left the SMs idle behind them.
+template <int NU, int NV>
+struct ChebTeam {
+  static constexpr int QH = qhigh(NU, NV);
+  static constexpr int U = QH / 2 + (QH & 1);          // team size: row pairs (+ the middle row)
+  static constexpr int TPW = 32 / U;                    // teams per warp
+  static constexpr int TPB = TPW * (CHEB_THREADS / 32); // elements per block
+  static constexpr int NE = NV * NV;
+  static constexpr int J = (NE + U - 1) / U;            // modal entries per thread
+  static constexpr int SLOT = NE + 2 * U * NV;          // d, then the row sums and differences
+};
+
+template <int NU, int NV>
+__global__ void __launch_bounds__(CHEB_THREADS)
+    k_cheb(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
+           const __grid_constant__ StageIO S) {
+  using T = ChebTeam<NU, NV>;
+  constexpr int QH = T::QH, U = T::U, NE = T::NE, J = T::J;
+  __shared__ double sh[T::TPB * T::SLOT];
+  __shared__ double Phs[QH * NV];
+  __shared__ int pref[NBIN];
+  const int tid = threadIdx.x, lane = tid & 31;
+  for (int i = tid; i < QH * NV; i += CHEB_THREADS) Phs[i] = B.Ph[i / NV][i % NV];
+  if (F.sorted && tid == 0) {
+    // exclusive prefix sum of the counts of this stage's bins, from the last bin down
+    int acc = 0;
+    for (int b = NBIN - 1; b >= 0; --b) { pref[b] = acc; acc += F.bin_count[S.parity * NBIN + b]; }
+  }
+  __syncthreads();
+  const int tw = lane / U, u = lane - tw * U;           // team in the warp, unit in the team
+  if (tw >= T::TPW) return;
+  const int slot = (tid >> 5) * T::TPW + tw;
+  const int g = blockIdx.x * T::TPB + slot;
+  if (g >= F.E) return;
+  if (err_word(F) != ERR_NONE) return;
+  const unsigned tmask = ((1u << U) - 1u) << (tw * U);
+  const int e = mass_element(F, S, g, pref);
+  const size_t Eu = (size_t)F.E;
+  double *dsm = sh + slot * T::SLOT, *zs = dsm + NE, *zd = zs + U * NV;
+
+  const double th = F.th[e], de = F.de[e];
+  const double s1 = th / de;
+  const int n = F.cheb_common ? *F.nmax : F.nst[e];
+  const double ith = 1.0 / th;
+  double rr[J], xx[J], dd[J];
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const int k = u + U * j;
+    rr[j] = xx[j] = dd[j] = 0.0;
+    if (k < NE) {
+      const double x = F.mrhs[k * Eu + e];
+      rr[j] = x;
+      dd[j] = x * ith;
+      dsm[k] = dd[j];
+    }
+  }
+  __syncwarp(tmask);
+  const int r1 = u, r2 = QH - 1 - u;                    // the unit's rows (r1 = r2 for the middle row)
+  auto rowZ = [&](const double (&Tv)[NV], int r, double (&Z)[NV]) {
+    double Y[QH];
+    ph_to_points<QH, NV>(B.Ph, Tv, Y);
+#pragma unroll
+    for (int s2 = 0; s2 < QH; ++s2) Y[s2] *= F.G[(r + QH * s2) * Eu + e];
+    ph_from_points<QH, NV>(B.Ph, Y, Z);
+  };
+  double rho = 1.0 / s1;
+#pragma unroll 1
+  for (int step = 1; step <= n; ++step) {
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      xx[j] += dd[j];
+      rr[j] -= dd[j];
+    }
+    if (step == n) break;
+    // phase 1: rows r1, r2 of P_h d, at the points, weighted, back to the modes
+    {
+      double Tp[NV], Tm[NV], Zp[NV], Zm[NV];
+#pragma unroll
+      for (int b = 0; b < NV; ++b) {
+        double ev = 0.0, od = 0.0;
+#pragma unroll
+        for (int a = 0; a < NV; a += 2) ev = fma(Phs[r1 * NV + a], dsm[a + NV * b], ev);
+#pragma unroll
+        for (int a = 1; a < NV; a += 2) od = fma(Phs[r1 * NV + a], dsm[a + NV * b], od);
+        Tp[b] = ev + od;
+        Tm[b] = ev - od;
+      }
+      rowZ(Tp, r1, Zp);
+      rowZ(Tm, r2, Zm);
+#pragma unroll
+      for (int b = 0; b < NV; ++b) {
+        zs[u * NV + b] = r1 == r2 ? Zp[b] : Zp[b] + Zm[b];
+        zd[u * NV + b] = Zp[b] - Zm[b];
+      }
+    }
+    __syncwarp(tmask);
+    // phase 2: r += K d on this thread's entries, then the next direction
+    const double rhon = 1.0 / (2.0 * s1 - rho);
+    const double c1 = rhon * rho, c2 = 2.0 * rhon / de;
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      const int k = u + U * j;
+      if (k < NE) {
+        const int a = k % NV, b = k / NV;
+        const double *z = ((a & 1) ? zd : zs) + b;
+        double acc = rr[j];
+#pragma unroll
+        for (int v = 0; v < U; ++v) acc = fma(Phs[v * NV + a], z[v * NV], acc);
+        rr[j] = acc;
+        dd[j] = fma(c1, dd[j], c2 * acc);
+        dsm[k] = dd[j];
+      }
+    }
+    rho = rhon;
+    __syncwarp(tmask);
+  }
+
+  bool fin = true;
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const int k = u + U * j;
+    if (k < NE) store_v(S, e + Eu * k, xx[j], fin);
+  }
+  if (S.mode == OUT_RK4_LAST && !fin) atomicOr(F.nonfinite, 1u);
+}
+
+// k_cg: the mass solve by conjugate gradients (src/rhs.jl:821-853), one thread per element
+template <int NU, int NV>
 __global__ void __launch_bounds__(MASS_THREADS)
-    k_mass(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
+    k_cg(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
            const __grid_constant__ StageIO S) {
   constexpr int QH = Basis<NU, NV>::QH, BT = MASS_THREADS;
   extern __shared__ double smem[];
-  __shared__ int pref[NBIN];
   const int tid = threadIdx.x;
   const int E = F.E;
   const size_t Eu = (size_t)E;
-  if (F.sorted) {
-    // exclusive prefix sum of the counts of this stage's bins
-    if (tid == 0) {
-      int acc = 0;
-      for (int b = 0; b < NBIN; ++b) { pref[b] = acc; acc += F.bin_count[S.parity * NBIN + b]; }
-    }
-    __syncthreads();
-  }
-  const int g = blockIdx.x * BT + tid;
-  if (g >= E) return;
+  const int e = blockIdx.x * BT + tid;           // mesh order
+  if (e >= E) return;
   if (err_word(F) != ERR_NONE) return;
-  const int e = mass_element(F, S, g, pref);
   Blk<NV, BT> r{smem + tid}, X{smem + NV * NV * BT + tid};
   bool fin = true;
 
-  // K P accumulated into O: O += P_h^T (G ∘ (P_h P P_h^T)) P_h, one row r2 of the point grid at a time
+  // K P accumulated into O: O += P_h^T (G ∘ (P_h P P_h^T)) P_h (G = 2βv W), for a mirrored pair of rows
+  // of the point grid at a time (row QH-1-r of P_h P is the even part minus the odd part of
+  // row r, and both rows go back to the modes through one sum and one difference)
+  auto rowZ = [&](const double (&T)[NV], int r, double (&Z)[NV]) {
+    double Y[QH];
+    ph_to_points<QH, NV>(B.Ph, T, Y);
+#pragma unroll
+    for (int s2 = 0; s2 < QH; ++s2) Y[s2] *= F.G[(r + QH * s2) * Eu + e];
+    ph_from_points<QH, NV>(B.Ph, Y, Z);
+  };
   auto addK = [&](Blk<NV, BT> P, Blk<NV, BT> O) {
+    auto px = [&](int a, int b) { return P(a, b); };
 #pragma unroll 1
-    for (int r2 = 0; r2 < QH; ++r2) {
-      double T[NV];
-#pragma unroll
-      for (int b = 0; b < NV; ++b) T[b] = 0.0;
-#pragma unroll
-      for (int a = 0; a < NV; ++a) {
-        const double p = B.Ph[r2][a];
-#pragma unroll
-        for (int b = 0; b < NV; ++b) T[b] = fma(p, P(a, b), T[b]);
+    for (int r2 = 0; r2 < QH / 2; ++r2) {
+      double Zp[NV], Zm[NV];
+      {
+        double Tp[NV], Tm[NV];
+        ph_row_pair<QH, NV>(B.Ph, r2, px, Tp, Tm);
+        rowZ(Tp, r2, Zp);
+        rowZ(Tm, QH - 1 - r2, Zm);
       }
-      double Y[QH];
 #pragma unroll
-      for (int s2 = 0; s2 < QH; ++s2) Y[s2] = 0.0;
+      for (int b = 0; b < NV; ++b) {
+        const double zs = Zp[b] + Zm[b], zd = Zp[b] - Zm[b];
+#pragma unroll
+        for (int a = 0; a < NV; ++a) O(a, b) = fma(B.Ph[r2][a], (a & 1) ? zd : zs, O(a, b));
+      }
+    }
+    if constexpr ((QH & 1) != 0) {
+      double T[NV], Z[NV];
+      ph_row_mid<QH, NV>(B.Ph, px, T);
+      rowZ(T, QH / 2, Z);
 #pragma unroll
       for (int b = 0; b < NV; ++b)
 #pragma unroll
-        for (int s2 = 0; s2 < QH; ++s2) Y[s2] = fma(T[b], B.Ph[s2][b], Y[s2]);
-#pragma unroll
-      for (int s2 = 0; s2 < QH; ++s2) Y[s2] *= F.G[(r2 + QH * s2) * Eu + e];
-      double Z[NV];
-#pragma unroll
-      for (int b = 0; b < NV; ++b) Z[b] = 0.0;
-#pragma unroll
-      for (int s2 = 0; s2 < QH; ++s2)
-#pragma unroll
-        for (int b = 0; b < NV; ++b) Z[b] = fma(Y[s2], B.Ph[s2][b], Z[b]);
-#pragma unroll
-      for (int a = 0; a < NV; ++a) {
-        const double p = B.Ph[r2][a];
-#pragma unroll
-        for (int b = 0; b < NV; ++b) O(a, b) = fma(p, Z[b], O(a, b));
-      }
+        for (int a = 0; a < NV; a += 2) O(a, b) = fma(B.Ph[QH / 2][a], Z[b], O(a, b));
     }
   };
 
-  if constexpr (!CG) {
-    // Chebyshev iteration (Saad Alg. 12.1, src/rhs.jl:921-939); K d is accumulated straight
-    // into the residual after r -= d
-    Blk<NV, BT> d{smem + 2 * NV * NV * BT + tid};
-    const double th = F.th[e], de = F.de[e];
-    const double s1 = th / de;
-    const int n = F.cheb_common ? *F.nmax : F.nst[e];
-    const double ith = 1.0 / th;
-#pragma unroll 1
-    for (int b = 0; b < NV; ++b)
-#pragma unroll
-      for (int a = 0; a < NV; ++a) {
-        const double x = F.mrhs[(a + NV * b) * Eu + e];
-        r(a, b) = x;
-        d(a, b) = x * ith;
-        X(a, b) = 0.0;
-      }
-    double rho = 1.0 / s1;
-#pragma unroll 1
-    for (int step = 1; step <= n; ++step) {
-#pragma unroll 1
-      for (int b = 0; b < NV; ++b)
-#pragma unroll
-        for (int a = 0; a < NV; ++a) {
-          const double x = d(a, b);
-          X(a, b) += x;
-          r(a, b) -= x;
-        }
-      if (step == n) break;
-      addK(d, r);
-      const double rhon = 1.0 / (2.0 * s1 - rho);
-      const double c1 = rhon * rho, c2 = 2.0 * rhon / de;
-#pragma unroll 1
-      for (int b = 0; b < NV; ++b)
-#pragma unroll
-        for (int a = 0; a < NV; ++a) d(a, b) = fma(c1, d(a, b), c2 * r(a, b));
-      rho = rhon;
-    }
-  } else {
+  {
     // conjugate gradients from X = R (src/rhs.jl:824-853)
     Blk<NV, BT> p{smem + 2 * NV * NV * BT + tid}, Ap{smem + 3 * NV * NV * BT + tid};
-    // G = 2βv_q W of this element
-#pragma unroll 1
-    for (int r2 = 0; r2 < QH; ++r2) {
-      double T[NV];
-#pragma unroll
-      for (int b = 0; b < NV; ++b) T[b] = 0.0;
-#pragma unroll
-      for (int a = 0; a < NV; ++a) {
-        const double pa = B.Ph[r2][a];
-#pragma unroll
-        for (int b = 0; b < NV; ++b) T[b] = fma(pa, S.xv[e + Eu * (a + NV * b)], T[b]);
-      }
+    // G = 2βv_q W of this element, by mirrored pairs of rows
+    auto vx = [&](int a, int b) { return S.xv[e + Eu * (a + NV * b)]; };
+    auto gput = [&](const double (&T)[NV], int r2) {
+      double Y[QH];
+      ph_to_points<QH, NV>(B.Ph, T, Y);
 #pragma unroll
       for (int s2 = 0; s2 < QH; ++s2) {
-        double gq = 0;
-#pragma unroll
-        for (int b = 0; b < NV; ++b) gq = fma(T[b], B.Ph[s2][b], gq);
         const size_t gi = (r2 + QH * s2) * Eu + e;
-        F.G[gi] = 2.0 * F.beta[gi] * gq * B.Wh[r2][s2];
+        F.G[gi] = 2.0 * F.beta[gi] * Y[s2] * B.Wh[r2][s2];
       }
+    };
+#pragma unroll 1
+    for (int r2 = 0; r2 < QH / 2; ++r2) {
+      double Tp[NV], Tm[NV];
+      ph_row_pair<QH, NV>(B.Ph, r2, vx, Tp, Tm);
+      gput(Tp, r2);
+      gput(Tm, QH - 1 - r2);
+    }
+    if constexpr ((QH & 1) != 0) {
+      double T[NV];
+      ph_row_mid<QH, NV>(B.Ph, vx, T);
+      gput(T, QH / 2);
     }
     double r0 = 0;
 #pragma unroll 1
@@ -926,35 +1167,20 @@ __global__ void __launch_bounds__(MASS_THREADS)
     if (sqrt(rr) > F.mass_tol * r0) atomicAdd(F.cg_nfail, 1u);
   }
 
-  // ---- v outputs (RK4 as in k_stage)
+  // ---- v outputs
 #pragma unroll 1
   for (int b = 0; b < NV; ++b)
 #pragma unroll
-    for (int a = 0; a < NV; ++a) {
-      const size_t l = e + Eu * (a + NV * b);
-      const double kk = X(a, b);
-      if (S.mode == OUT_RHS) {
-        S.vt[l] = kk;
-      } else if (S.mode == OUT_RK4_STAGE) {
-        S.accv[l] = S.first ? kk : S.accv[l] + 2.0 * kk;
-        S.sv[l] = S.v0[l] + S.c * kk;
-      } else if (S.mode == OUT_RK4_LAST) {
-        const double x = S.v0[l] + S.c * (S.accv[l] + kk);
-        S.vo[l] = x;
-        fin = fin && isfinite(x);
-      } else {
-        S.accv[l] = S.accv[l] + kk;
-      }
-    }
+    for (int a = 0; a < NV; ++a) store_v(S, e + Eu * (a + NV * b), X(a, b), fin);
   if (S.mode == OUT_RK4_LAST && !fin) atomicOr(F.nonfinite, 1u);
 }
 
-// shared memory of k_mass: r, X and d (Chebyshev); r, X, p and A p (CG)
-__host__ __device__ constexpr size_t mass_smem(int nv, bool cg) {
-  return (size_t)MASS_THREADS * (cg ? 4 : 3) * nv * nv * sizeof(double);
+// shared memory of k_cg: r, X, p and A p
+__host__ __device__ constexpr size_t cg_smem(int nv) {
+  return (size_t)MASS_THREADS * 4 * nv * nv * sizeof(double);
 }
 
-// Last RK4 update when the last stage may still raise an error inside k_mass
+// Last RK4 update when the last stage may still raise an error inside k_cg
 // (CG mode): u += (dt/6) acc unless an error was recorded.
 __global__ void k_rk4_final(int n_u, int n_v, double *u, double *v, const double *accu, const double *accv,
                             double c, const unsigned long long *err, unsigned int *nonfinite);

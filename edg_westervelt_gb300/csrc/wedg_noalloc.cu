@@ -27,6 +27,7 @@
 #include <mutex>
 
 #include "../../include/wedg.h"
+#include "wedg_basis.h"
 #include "wedg_dispatch.h"
 
 namespace wedg {
@@ -69,53 +70,6 @@ __global__ void k_elem_coef(const double *raw, int nq, int E, double w00, double
   }
 }
 
-// Cyclic Jacobi eigen-decomposition of the symmetric m×m block A (m ≤ 7), on the stack.
-void jacobi_eig(int m, double A[MAXN][MAXN], double Q[MAXN][MAXN], double lam[MAXN]) {
-  for (int i = 0; i < m; ++i)
-    for (int j = 0; j < m; ++j) Q[i][j] = i == j;
-  for (int sweep = 0; sweep < 100; ++sweep) {
-    double off = 0;
-    for (int p = 0; p < m; ++p)
-      for (int q = p + 1; q < m; ++q) off += A[p][q] * A[p][q];
-    if (off < 1e-40) break;
-    for (int p = 0; p < m; ++p)
-      for (int q = p + 1; q < m; ++q) {
-        if (std::fabs(A[p][q]) < 1e-300) continue;
-        const double tau = (A[q][q] - A[p][p]) / (2 * A[p][q]);
-        const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1 + tau * tau));
-        const double c = 1 / std::sqrt(1 + t * t), s = t * c;
-        for (int k = 0; k < m; ++k) {
-          const double akp = A[k][p], akq = A[k][q];
-          A[k][p] = c * akp - s * akq;
-          A[k][q] = s * akp + c * akq;
-        }
-        for (int k = 0; k < m; ++k) {
-          const double apk = A[p][k], aqk = A[q][k];
-          A[p][k] = c * apk - s * aqk;
-          A[q][k] = s * apk + c * aqk;
-        }
-        for (int k = 0; k < m; ++k) {
-          const double qkp = Q[k][p], qkq = Q[k][q];
-          Q[k][p] = c * qkp - s * qkq;
-          Q[k][q] = s * qkp + c * qkq;
-        }
-      }
-  }
-  // ascending order
-  int idx[MAXN];
-  for (int i = 0; i < m; ++i) idx[i] = i;
-  for (int i = 0; i < m; ++i)
-    for (int j = i + 1; j < m; ++j)
-      if (A[idx[j]][idx[j]] < A[idx[i]][idx[i]]) { const int t = idx[i]; idx[i] = idx[j]; idx[j] = t; }
-  double Qs[MAXN][MAXN];
-  for (int c = 0; c < m; ++c) {
-    lam[c] = A[idx[c]][idx[c]];
-    for (int r = 0; r < m; ++r) Qs[r][c] = Q[r][idx[c]];
-  }
-  for (int r = 0; r < m; ++r)
-    for (int c = 0; c < m; ++c) Q[r][c] = Qs[r][c];
-}
-
 int fail(char *msg, size_t len, int status, const char *text) {
   if (msg && len) snprintf(msg, len, "%s", text);
   return status;
@@ -155,39 +109,7 @@ extern "C" int wedg_rhs_noalloc(const wedg_config *cfg, const wedg_pre *pre, con
 
   // ---- 1D operators and the constant-coefficient test (host, on the stack)
   BasisHost bh;
-  std::memset(&bh, 0, sizeof bh);
-  bh.nu = nu; bh.nv = nv; bh.qh = qh;
-  for (int i = 0; i < nq; ++i) {
-    bh.w[i] = pre->w[i];
-    for (int d = 0; d < nu; ++d) { bh.P[i][d] = pre->P_u[i + nq * d]; bh.S[i][d] = pre->S_u[i + nq * d]; }
-  }
-  for (int d = 0; d < nu; ++d) {
-    bh.El[d] = pre->Ebl_u[d]; bh.Er[d] = pre->Ebr_u[d]; bh.E1l[d] = pre->E1bl_u[d]; bh.E1r[d] = pre->E1br_u[d];
-  }
-  for (int r = 0; r < qh; ++r) {
-    for (int d = 0; d < nv; ++d) bh.Ph[r][d] = pre->P_h_v[r + qh * d];
-    for (int s = 0; s < qh; ++s) bh.Wh[r][s] = pre->W2d_h[r + qh * s];
-  }
-  for (int a = 0; a < nu; ++a)
-    for (int c = 0; c < nu; ++c) {
-      double s = 0;
-      for (int i = 0; i < nq; ++i) s += bh.S[i][a] * bh.w[i] * bh.S[i][c];
-      bh.K1[a][c] = s;
-    }
-  {
-    const int m = nu - 1;
-    double A[MAXN][MAXN], Qm[MAXN][MAXN], lam[MAXN], L[MAXN] = {0};
-    for (int a = 0; a < m; ++a)
-      for (int c = 0; c < m; ++c) A[a][c] = 0.5 * (bh.K1[a + 1][c + 1] + bh.K1[c + 1][a + 1]);
-    jacobi_eig(m, A, Qm, lam);
-    bh.Q[0][0] = 1.0;
-    for (int a = 0; a < m; ++a) {
-      L[a + 1] = lam[a];
-      for (int c = 0; c < m; ++c) bh.Q[a + 1][c + 1] = Qm[a][c];
-    }
-    for (int i = 0; i < nu; ++i)
-      for (int j = 0; j < nu; ++j) bh.ilam2[i][j] = (i == 0 && j == 0) ? 1.0 : 1.0 / (L[i] + L[j]);
-  }
+  if (const char *why = build_basis(cfg, pre, bh)) return fail(msg, msg_len, WEDG_ERR_ARGUMENT, why);
   const double w00 = bh.w[0] * bh.w[0];
   bool fast = !cfg->general_only;
   for (size_t e = 0; e < E && fast; ++e) {

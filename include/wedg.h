@@ -144,7 +144,7 @@ int wedg_rk4_steps_async(wedg_ws *ws, double *u_dev, double *v_dev, double t0, d
 int wedg_sync_status(wedg_ws *ws, int64_t *steps_done, int *finite);
 
 /* Kernel timing for benchmarks: with enable != 0, every launch of the three stage
- * kernels (k_prep, k_stage, k_mass) is bracketed by CUDA events on the workspace
+ * kernels (k_prep, k_stage, and the mass solve k_cheb or k_cg) is bracketed by CUDA events on the workspace
  * stream and its duration accumulated; wedg_kernel_times reads (and with reset,
  * clears) the totals in milliseconds and the number of launches of each. */
 int wedg_time_kernels(wedg_ws *ws, int enable);
