@@ -173,16 +173,21 @@ def fp64_gemm_peak(torch, dev):
     return 2 * n ** 3 / best / 1e12
 
 
-def traffic_from_profile():
-    """DRAM bytes per RHS stage (its kernels) from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "stage_cfg2_dram.txt")
+def profile_figures():
+    """DRAM bytes per RHS stage and the FP64-pipe utilisation of each stage kernel, from the
+    committed ncu summary of the stage kernels (None where it is missing)."""
+    p = os.path.join(ROOT, "profiles", "stage_dram_N512_q6.txt")
+    out = {"traffic": None, "fp64_pipe_pct": {}}
     try:
         for line in open(p):
             if line.startswith("dram_bytes_per_stage:"):
-                return float(line.split(":")[1])
+                out["traffic"] = float(line.split(":")[1])
+            elif line.startswith("fp64_pipe_pct "):
+                k, v = line[len("fp64_pipe_pct "):].split(":")
+                out["fp64_pipe_pct"][k.strip()] = float(v)
     except OSError:
         pass
-    return None
+    return out
 
 
 class CpuPort:
@@ -360,21 +365,32 @@ def run_ours(args):
     per_step = alg_flops_per_element_stage(nu, nv, qh, 2) - f1
     flops_stage = (f1 + (main["cheb_mean"] - 1) * per_step) * E
     fp64_achieved = flops_stage / (stage_ms / 1e3) / 1e12
+    prof = profile_figures()
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-                "frac": achieved_gbs / hbm if hbm else None, "traffic": traffic_from_profile(),
+                "frac": achieved_gbs / hbm if hbm else None, "traffic": prof["traffic"],
                 "kernel": "RHS stage (k_prep + k_stage + k_cheb)", "dominant_kernel": dominant,
                 "dominant_share": kms[dominant] / stage_ms, "bytes_per_launch": bytes_stage, "launch_ms": stage_ms,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm else None,
-                "note": "the path is FP64-pipe bound on GB300 (see roofline_fp64); bytes are the reference data "
-                        "model's algorithmic bytes per element-stage x elements, over the time of one RHS stage "
-                        "(its three kernels; the formula is defined per stage)"}
-    roofline_fp64 = {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": fp64_achieved / fp64_peak, "flops_per_stage": flops_stage,
+                "note": "the stage is bound by the FP64 pipe, not by HBM (see fp64_pipe); bytes are the "
+                        "reference data model's algorithmic bytes per element-stage x elements, over the time "
+                        "of one RHS stage (its three kernels); traffic is ncu's DRAM bytes of the three kernels "
+                        "per stage (profiles/stage_dram_N512_q6.txt)"}
+    pipe = prof["fp64_pipe_pct"]
+    fp64_pipe = None
+    if pipe and all(k in pipe for k in kms):
+        fp64_pipe = {"unit": "% of the FP64 pipe's peak sustained rate over active cycles (ncu)",
+                     "per_kernel": pipe,
+                     "stage_weighted": sum(pipe[k] * kms[k] for k in kms) / stage_ms,
+                     "source": "profiles/stage_kernels_N256_q6.md"}
+    reference_ops = {"value": fp64_achieved, "unit": "TFLOP/s", "dgemm_peak": fp64_peak,
+                     "flops_per_stage": flops_stage,
                      "cheb_steps_max": main["cheb"], "cheb_steps_mean": main["cheb_mean"],
                      "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
-                     "note": "reference-data-model flop formula with each element's own Chebyshev count, over the "
-                             "k_prep + k_stage + k_cheb time of a stage; the constant-coefficient kernels execute fewer "
-                             "FP64 instructions than the formula counts for the volume and u-equation terms"}
+                     "note": "the reference's FP64 operation count of a stage (each element's own Chebyshev "
+                             "count) over the k_prep + k_stage + k_cheb time; it can exceed the DGEMM rate "
+                             "because the kernels execute fewer FP64 operations than that count (mirror "
+                             "parity of the Gauss-Legendre rules, fast diagonalisation of the u-equation, "
+                             "constant-coefficient volume terms)"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -395,7 +411,8 @@ def run_ours(args):
                    "state": "steepened circular front, 1-2βv_h in [0.42, 1.58] across it (seeded)",
                    "l2": "inputs larger than L2 (state 206 MB, stage data > 600 MB per stage)",
                    "cheb_steps": "per element", "t0": T0, "main_state": args.state},
-        "roofline": roofline, "roofline_fp64": roofline_fp64, "cpu_baseline": cpu, "e2e": e2e,
+        "roofline": roofline, "fp64_pipe": fp64_pipe, "reference_op_rate": reference_ops,
+        "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clocks.summary(), "gpu_launches": main["launches"],
         "kernel_ms": kms,
         "zero_state": {"value": world * dof * 4 * zero["steps"] / (zero["ms"] / 1e3),

@@ -346,6 +346,26 @@ def test_dimension_mismatch_and_arguments(gpu):
     assert W.Workspace(W.precompute(2, 3)[0], 3, nblocks=8).nb == 2
 
 
+def test_mirror_parity_of_the_rules(gpu):
+    """The kernels rely on the mirror symmetry of the Gauss-Legendre rules: arrays that have
+    it to round-off are accepted (and give the oracle's result), a rule without it is refused."""
+    pre, opre_ = _pair(4, 6, flux="upwind", mixed=True)
+    rng = np.random.default_rng(3)
+    u = np.asfortranarray(rng.standard_normal((6, 6, 5, 5)))
+    v = np.asfortranarray(1e-3 * rng.standard_normal((6, 6, 4, 4)))
+    near = dict(pre)
+    for k in ("P_h_v", "P_u", "S_u", "w"):
+        near[k] = np.asfortranarray(pre[k] * (1 + 1e-16 * rng.standard_normal(pre[k].shape)))
+    ours = W.Workspace(near, 6).rhs(u, v, 0.2)
+    ref = OracleWorkspace(opre_).rhs(u, v, 0.2)
+    assert rel_max(ours, ref) < TOL
+    bad = dict(pre)
+    bad["P_h_v"] = np.asfortranarray(pre["P_h_v"].copy())
+    bad["P_h_v"][0, 1] += 1e-6
+    with pytest.raises(RuntimeError, match="wedg_create failed"):
+        W.Workspace(bad, 6)
+
+
 def test_blow_up_flag(gpu):
     """A non-finite state makes ws.fin false after the step (src/solver.jl:311-321, 940). With the
     CG solver the step completes (a NaN residual ends CG at once, src/rhs.jl:841); with Chebyshev
