@@ -240,7 +240,7 @@ void drain_events(wedg_ws *ws) {
 // enqueue the two kernels of one stage
 int enqueue_stage(wedg_ws *ws, const StageIO &S) {
   const int tp = 128, bp = (ws->E + tp - 1) / tp;
-  const int ts = stage_threads(ws->nu, ws->nv), bs = (ws->E + ts - 1) / ts;
+  const int ts = stage_threads(ws->nu, ws->nv, ws->fast), bs = (ws->E + ts - 1) / ts;
   const int bm = (ws->E + MASS_THREADS - 1) / MASS_THREADS;
   StageIO Sp = S;
   Sp.parity = ws->parity;

@@ -55,10 +55,10 @@ void launch_prep(const void *basis, const Fields &F, const StageIO &S, int block
 }
 
 // k_stage keeps the element blocks in dynamic shared memory (up to 227 KB per block);
-// `threads` must be stage_threads(NU, NV)
+// `threads` must be stage_threads(NU, NV, FAST)
 template <int NU, int NV, bool FAST>
 void launch_stage(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads, cudaStream_t st) {
-  constexpr size_t smem = (size_t)stage_threads(NU, NV) * (2 * NU * NU + 2 * NV * NV) * sizeof(double);
+  constexpr size_t smem = stage_smem(NU, NV, FAST);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_stage<NU, NV, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

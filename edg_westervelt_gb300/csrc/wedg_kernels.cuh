@@ -57,10 +57,20 @@ __host__ __device__ constexpr int qhigh(int nu, int nv) {
   return ((3 * (nv - 1) + 1) / 2 + 1) > nu ? ((3 * (nv - 1) + 1) / 2 + 1) : nu;
 }
 
-// threads per block of k_stage: the element arrays (2 NU² + 2 NV² doubles per
-// thread) must fit the 227 KB of shared memory of one block
-__host__ __device__ constexpr int stage_threads(int nu, int nv) {
-  return 128 * (2 * nu * nu + 2 * nv * nv) * 8 <= 232448 ? 128 : 96;
+// Shared memory of k_stage per thread: the general kernels keep U, b, V and R_v (2 NU² + 2 NV²
+// doubles), the constant-coefficient kernels only b and R_v (NU² + NV²).
+__host__ __device__ constexpr int stage_doubles(int nu, int nv, bool fast) {
+  return fast ? nu * nu + nv * nv : 2 * nu * nu + 2 * nv * nv;
+}
+// Threads per block of k_stage: the general kernels fit one block in the 227 KB of one block,
+// the constant-coefficient kernels two blocks per SM (228 KB per SM, 1 KB of it per block
+// reserved).
+__host__ __device__ constexpr int stage_threads(int nu, int nv, bool fast) {
+  return fast ? (2 * (128 * stage_doubles(nu, nv, true) * 8 + 1024) <= 233472 ? 128 : 96)
+              : (128 * stage_doubles(nu, nv, false) * 8 <= 232448 ? 128 : 96);
+}
+__host__ __device__ constexpr size_t stage_smem(int nu, int nv, bool fast) {
+  return (size_t)stage_threads(nu, nv, fast) * stage_doubles(nu, nv, fast) * sizeof(double);
 }
 
 template <int NU, int NV>
@@ -481,10 +491,10 @@ __device__ __forceinline__ void side_point(const Basis<NU, NV> &B, const Fields 
 // k_stage: fluxes, lifts, volume, source, u-equation; the mass right-hand side to HBM
 // ----------------------------------------------------------------------------
 template <int NU, int NV, bool FAST>
-__global__ void __launch_bounds__(stage_threads(NU, NV), 1)
+__global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
     k_stage(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
             const __grid_constant__ StageIO S) {
-  constexpr int NQ = NU, BT = stage_threads(NU, NV);
+  constexpr int NQ = NU, BT = stage_threads(NU, NV, FAST);
   extern __shared__ double smem[];
   const int tid = threadIdx.x;
   const int E = F.E, N = F.N;
@@ -493,11 +503,12 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
   if (err_word(F) != ERR_NONE) return;
   const int j = e % N, k = e / N;
   const double two_h = F.two_h, four_hh = F.four_hh;
-  // thread-private blocks: X1, X2 (NU²), Y1, Y2 (NV²)
-  Blk<NU, BT> X1{smem + tid}, X2{smem + NU * NU * BT + tid};
-  Blk<NV, BT> Y1{smem + 2 * NU * NU * BT + tid}, Y2{smem + (2 * NU * NU + NV * NV) * BT + tid};
-  Blk<NU, BT> Ub = X1, bb = X2;     // U (volume), u-equation right-hand side b
-  Blk<NV, BT> Vb = Y1, Rv = Y2;     // V, v-equation right-hand side
+  // thread-private blocks: b (NU², the u-equation right-hand side, then UT) and R_v (NV², the
+  // v-equation right-hand side); the general kernels also keep U (NU²) and V (NV²)
+  Blk<NU, BT> bb{smem + tid};
+  Blk<NV, BT> Rv{smem + NU * NU * BT + tid};
+  Blk<NU, BT> Ub{smem + (NU * NU + NV * NV) * BT + tid};
+  Blk<NV, BT> Vb{smem + (2 * NU * NU + NV * NV) * BT + tid};
 
   // ---- faces and lifts (src/rhs.jl:421-473): Rv (v-equation), b = -Fu (u-equation)
 #pragma unroll 1
@@ -562,89 +573,88 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
     }
   }
 
-  // ---- state of the stage
+  // ---- state of the stage (the general kernels keep it in shared memory; the
+  //      constant-coefficient kernels read it from HBM, by columns and by rows)
   const size_t Eu = (size_t)E;
+  if constexpr (!FAST) {
 #pragma unroll 1
-  for (int b = 0; b < NV; ++b)
+    for (int b = 0; b < NV; ++b)
 #pragma unroll
-    for (int a = 0; a < NV; ++a) Vb(a, b) = S.xv[e + Eu * (a + NV * b)];
+      for (int a = 0; a < NV; ++a) Vb(a, b) = S.xv[e + Eu * (a + NV * b)];
 #pragma unroll 1
-  for (int b = 0; b < NU; ++b)
+    for (int b = 0; b < NU; ++b)
 #pragma unroll
-    for (int a = 0; a < NU; ++a) Ub(a, b) = S.xu[e + Eu * (a + NU * b)];
+      for (int a = 0; a < NU; ++a) Ub(a, b) = S.xu[e + Eu * (a + NU * b)];
+  }
 
   // ---- volume terms (src/rhs.jl:309-333): Rv += -4/h² [(c²∇φ_v,∇u_h) + (α∇φ_v,∇v_h)],
   //      b += (c²∇φ_u, ∇v_h)
   if constexpr (FAST) {
     // constant c², α on the element: Cw = c² W, Aw = α W, so that with the
     // 1D stiffness K1 = S^T diag(w) S and the orthonormality of the basis
-    //   (c²∇φ_v, ∇u_h) = c² (K1 U + U K1)[v-block],  (α∇φ_v, ∇v_h) = α (K1 V + V K1)
+    //   (c²∇φ_v,∇u_h) + (α∇φ_v,∇v_h) = (K1 W + W K1)[v-block] / (-4/h²),  W = -4/h² (c² U + α V)
     //   (c²∇φ_u, ∇v_h) = c² (K1[:, v] V + V K1[v, :])
-    // (row and column 0 of K1 vanish: the derivative of the constant mode is 0).
-    // K1 couples only modes of equal parity (K1[a][c] = 0 for a + c odd): the sums run over
-    // c ≡ a and c ≡ b (mod 2). Rows are taken in pairs (a0, a0 + 1), so that the parity of a
-    // is known at compile time; each output row is built at once (independent FMAs).
+    // (V padded with zeros to NU × NU; row and column 0 of K1 vanish, and K1 couples only modes
+    // of equal parity). The products with K1 from the left take the columns of U and V, those
+    // from the right their rows: both are read from HBM (L2), so that U and V need no shared
+    // memory.
     const double c2 = F.c2e[e], al = F.ae[e];
     const double mc2 = -four_hh * c2, mal = -four_hh * al;
+    const double *xu = S.xu + e, *xv = S.xv + e;
 #pragma unroll 1
-    for (int a0 = 0; a0 < NV; a0 += 2) {
+    for (int b = 0; b < NV; ++b) {                  // columns: K1 W and K1[:, v] V
+      double w[NU], vc[NV];
 #pragma unroll
-      for (int pa = 0; pa < 2; ++pa) {
-        const int a = a0 + pa;
-        if (a >= NV) break;
-        double su[NV], sv[NV];
-#pragma unroll
-        for (int b = 0; b < NV; ++b) { su[b] = 0.0; sv[b] = 0.0; }
-        if (a > 0) {                                  // row 0 of K1 vanishes
-#pragma unroll
-          for (int c = 2 - pa; c < NU; c += 2) {
-            const double kac = B.K1[a][c];
-#pragma unroll
-            for (int b = 0; b < NV; ++b) su[b] = fma(kac, Ub(c, b), su[b]);
-          }
-#pragma unroll
-          for (int c = 2 - pa; c < NV; c += 2) {
-            const double kac = B.K1[a][c];
-#pragma unroll
-            for (int b = 0; b < NV; ++b) sv[b] = fma(kac, Vb(c, b), sv[b]);
-          }
+      for (int c = 1; c < NU; ++c) {
+        const double uc = xu[Eu * (c + NU * b)];
+        if (c < NV) {
+          const double x = xv[Eu * (c + NV * b)];
+          w[c] = fma(mal, x, mc2 * uc);
+          vc[c] = c2 * x;
+        } else {
+          w[c] = mc2 * uc;
         }
+      }
 #pragma unroll
-        for (int b = 1; b < NV; ++b) {                // column 0 of K1 vanishes
+      for (int a = 1; a < NU; ++a) {
+        if (a < NV) {
+          double acc = Rv(a, b);
 #pragma unroll
-          for (int c = 2 - (b & 1); c < NU; c += 2) su[b] = fma(Ub(a, c), B.K1[c][b], su[b]);
-#pragma unroll
-          for (int c = 2 - (b & 1); c < NV; c += 2) sv[b] = fma(Vb(a, c), B.K1[c][b], sv[b]);
+          for (int c = 2 - (a & 1); c < NU; c += 2) acc = fma(B.K1[a][c], w[c], acc);
+          Rv(a, b) = acc;
         }
+        double acc = bb(a, b);
 #pragma unroll
-        for (int b = 0; b < NV; ++b) Rv(a, b) = fma(mc2, su[b], fma(mal, sv[b], Rv(a, b)));
+        for (int c = 2 - (a & 1); c < NV; c += 2) acc = fma(B.K1[a][c], vc[c], acc);
+        bb(a, b) = acc;
       }
     }
 #pragma unroll 1
-    for (int a0 = 0; a0 < NU; a0 += 2) {
+    for (int a = 0; a < NV; ++a) {                  // rows: W K1 and V K1[v, :]
+      double w[NU], vr[NV];
 #pragma unroll
-      for (int pa = 0; pa < 2; ++pa) {
-        const int a = a0 + pa;
-        if (a >= NU) break;
-        double s1[NU];
-#pragma unroll
-        for (int b = 0; b < NU; ++b) s1[b] = 0.0;
-        if (a > 0) {
-#pragma unroll
-          for (int c = 2 - pa; c < NV; c += 2) {
-            const double kac = B.K1[a][c];
-#pragma unroll
-            for (int b = 0; b < NV; ++b) s1[b] = fma(kac, Vb(c, b), s1[b]);
-          }
+      for (int c = 1; c < NU; ++c) {
+        const double uc = xu[Eu * (a + NU * c)];
+        if (c < NV) {
+          const double x = xv[Eu * (a + NV * c)];
+          w[c] = fma(mal, x, mc2 * uc);
+          vr[c] = c2 * x;
+        } else {
+          w[c] = mc2 * uc;
         }
-        if (a < NV) {
+      }
 #pragma unroll
-          for (int b = 1; b < NU; ++b)
+      for (int b = 1; b < NU; ++b) {
+        if (b < NV) {
+          double acc = Rv(a, b);
 #pragma unroll
-            for (int c = 2 - (b & 1); c < NV; c += 2) s1[b] = fma(Vb(a, c), B.K1[c][b], s1[b]);
+          for (int c = 2 - (b & 1); c < NU; c += 2) acc = fma(w[c], B.K1[c][b], acc);
+          Rv(a, b) = acc;
         }
+        double acc = bb(a, b);
 #pragma unroll
-        for (int b = 0; b < NU; ++b) bb(a, b) = fma(c2, s1[b], bb(a, b));
+        for (int c = 2 - (b & 1); c < NV; c += 2) acc = fma(vr[c], B.K1[c][b], acc);
+        bb(a, b) = acc;
       }
     }
   } else {
@@ -734,18 +744,20 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
       F.mrhs[l] = x;
     }
 
-  // ---- u-equation (src/rhs.jl:352-382): A_e UT = VB - Fu + e_1 V[0][0]; UT into X1 (U is dead)
-  bb(0, 0) += Vb(0, 0);
-  Blk<NU, BT> UT = X1;
+  // ---- u-equation (src/rhs.jl:352-382): A_e UT = VB - Fu + e_1 V[0][0]
+  if constexpr (FAST) bb(0, 0) += S.xv[e];
+  else bb(0, 0) += Vb(0, 0);
+  // UT: in place of b (constant-coefficient kernels), in place of U (general kernels, U is dead)
+  Blk<NU, BT> UT = FAST ? bb : Ub;
   if constexpr (FAST) {
     // A_e = c² (K1 ⊗ I + I ⊗ K1) + e_0 e_0^T is diagonal in the eigenbasis Q ⊗ Q of K1 (whose
     // first eigenvector is e_0 with λ_0 = 0): UT = Q [ (Q^T b Q) ∘ L ] Q^T, L = 1/(c²(λ_i+λ_j)), 1 at (0,0).
     // Q[a][i] vanishes for a + i odd and in row and column 0 outside (0, 0): qnz skips those
-    // terms at compile time.
+    // terms at compile time. The four products run in place: a product with Q from the left
+    // changes each column on its own, one from the right each row.
     const double ic2 = F.ic2e[e];
-    // T1 = Q^T b into X1
 #pragma unroll 1
-    for (int c = 0; c < NU; ++c) {
+    for (int c = 0; c < NU; ++c) {                 // T1 = Q^T b, by columns
       double t[NU];
 #pragma unroll
       for (int i = 0; i < NU; ++i) t[i] = 0;
@@ -757,64 +769,57 @@ __global__ void __launch_bounds__(stage_threads(NU, NV), 1)
           if (qnz(a, i)) t[i] = fma(B.Q[a][i], x, t[i]);
       }
 #pragma unroll
-      for (int i = 0; i < NU; ++i) X1(i, c) = t[i];
+      for (int i = 0; i < NU; ++i) bb(i, c) = t[i];
     }
-    // T2 = (T1 Q) ∘ L into X2
 #pragma unroll 1
-    for (int i = 0; i < NU; ++i) {
+    for (int i = 0; i < NU; ++i) {                 // T2 = (T1 Q) ∘ L, by rows
       double t[NU];
 #pragma unroll
       for (int jj = 0; jj < NU; ++jj) t[jj] = 0;
 #pragma unroll
       for (int c = 0; c < NU; ++c) {
-        const double x = X1(i, c);
+        const double x = bb(i, c);
 #pragma unroll
         for (int jj = 0; jj < NU; ++jj)
           if (qnz(c, jj)) t[jj] = fma(x, B.Q[c][jj], t[jj]);
       }
 #pragma unroll
-      for (int jj = 0; jj < NU; ++jj) X2(i, jj) = (i == 0 && jj == 0) ? t[jj] : t[jj] * (B.ilam2[i][jj] * ic2);
+      for (int jj = 0; jj < NU; ++jj) bb(i, jj) = (i == 0 && jj == 0) ? t[jj] : t[jj] * (B.ilam2[i][jj] * ic2);
     }
-    // T3 = Q T2 into X1
 #pragma unroll 1
-    for (int jj = 0; jj < NU; ++jj) {
+    for (int jj = 0; jj < NU; ++jj) {              // T3 = Q T2, by columns
       double t[NU];
 #pragma unroll
       for (int a = 0; a < NU; ++a) t[a] = 0;
 #pragma unroll
       for (int i = 0; i < NU; ++i) {
-        const double x = X2(i, jj);
+        const double x = bb(i, jj);
 #pragma unroll
         for (int a = 0; a < NU; ++a)
           if (qnz(a, i)) t[a] = fma(B.Q[a][i], x, t[a]);
       }
 #pragma unroll
-      for (int a = 0; a < NU; ++a) X1(a, jj) = t[a];
+      for (int a = 0; a < NU; ++a) bb(a, jj) = t[a];
     }
-    // UT = T3 Q^T into X2, then back to X1
 #pragma unroll 1
-    for (int a = 0; a < NU; ++a) {
+    for (int a = 0; a < NU; ++a) {                 // UT = T3 Q^T, by rows
       double t[NU];
 #pragma unroll
       for (int c = 0; c < NU; ++c) t[c] = 0;
 #pragma unroll
       for (int jj = 0; jj < NU; ++jj) {
-        const double x = X1(a, jj);
+        const double x = bb(a, jj);
 #pragma unroll
         for (int c = 0; c < NU; ++c)
           if (qnz(c, jj)) t[c] = fma(x, B.Q[c][jj], t[c]);
       }
 #pragma unroll
-      for (int c = 0; c < NU; ++c) X2(a, c) = t[c];
+      for (int c = 0; c < NU; ++c) bb(a, c) = t[c];
     }
-#pragma unroll 1
-    for (int a = 0; a < NU; ++a)
-#pragma unroll
-      for (int c = 0; c < NU; ++c) X1(a, c) = X2(a, c);
   } else {
     // packed upper triangle of the symmetric inverse, by columns: entry (i, j), i ≤ j, in row j(j+1)/2 + i
     constexpr int n = NU * NU;
-    double *X = smem + tid, *bv = smem + NU * NU * BT + tid;   // X1 and b (= X2) as vectors a + NU c
+    double *X = &Ub(0, 0), *bv = &bb(0, 0);       // UT and b as vectors a + NU c
 #pragma unroll 1
     for (int i = 0; i < n; ++i) X[i * BT] = 0.0;
 #pragma unroll 1

@@ -298,7 +298,7 @@ extern "C" int wedg_rhs_noalloc(const wedg_config *cfg, const wedg_pre *pre, con
     if (msg && msg_len) snprintf(msg, msg_len, "CUDA error: %s", cudaGetErrorString(ce));
     return WEDG_ERR_CUDA;
   }
-  const int tp = 128, ts = stage_threads(nu, nv);
+  const int tp = 128, ts = stage_threads(nu, nv, fast);
   Lch.prep(basis, F, S, (iE + tp - 1) / tp, tp, st);
   Lch.stage(basis, F, S, (iE + ts - 1) / ts, ts, st);
   Lch.mass(basis, F, S, (iE + MASS_THREADS - 1) / MASS_THREADS, MASS_THREADS, st);
