@@ -525,8 +525,8 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
     std::vector<double> o((size_t)qh * qh * E);
     for (int s = 0; s < qh; ++s)
       for (int e = 0; e < E; ++e)
-        for (int r = 0; r < qh; ++r) o[(r + qh * s) * Es + e] = pre->beta_hq[r + qh * ((size_t)e + Es * s)];
-    UP(F.beta, o);
+        for (int r = 0; r < qh; ++r) o[(r + qh * s) * Es + e] = 2.0 * pre->beta_hq[r + qh * ((size_t)e + Es * s)];
+    UP(F.beta2, o);
   }
 #undef UP
   // ---- scratch

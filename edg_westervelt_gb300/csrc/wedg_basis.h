@@ -2,7 +2,8 @@
 // the reference's `pre` (src/solver.jl:428-520): the u-quadrature (w, P_u, S_u),
 // the face values of the basis (Ebl_u ... E1br_u), the high-order v-quadrature
 // (P_h_v, W2d_h), and, for the constant-coefficient kernels, the 1D stiffness
-// K1 = S^T diag(w) S with its eigenbasis.
+// K1 = S^T diag(w) S with its eigenbasis; some of them with the quadrature
+// weights or the mesh factors 2/h, 4/h² folded in.
 //
 // Both quadratures are Gauss-Legendre rules and the basis is the Legendre one
 // (src/solver.jl:436-486), so every operator has a mirror parity: at the point
@@ -119,6 +120,24 @@ inline const char *build_basis(const wedg_config *cfg, const wedg_pre *pre, Basi
     if (!mirror(&bh.Wh[0][s], qh, MAXQH, 1.0, tWh)) return asym;
   for (int r = 0; r < qh; ++r)
     if (!mirror(&bh.Wh[r][0], qh, 1, 1.0, tWh)) return asym;
+
+  // ---- weights folded into the bases: W2d_h = w_h w_h^T (the kernels weight the point values
+  //      by w_h[s] on the way back to the modes), w P_u, and the lift factors (2/h) El, (4/h²) E1l
+  for (int r = 0; r < qh; ++r) bh.wh[r] = std::sqrt(bh.Wh[r][r]);
+  for (int r = 0; r < qh; ++r)
+    for (int s = 0; s < qh; ++s)
+      if (!(std::fabs(bh.wh[r] * bh.wh[s] - bh.Wh[r][s]) <= 1e-14 * std::fabs(bh.Wh[r][s])))
+        return "W2d_h is not the outer product of one-dimensional weights";
+  for (int r = 0; r < qh; ++r)
+    for (int d = 0; d < nv; ++d) bh.PhW[r][d] = bh.wh[r] * bh.Ph[r][d];
+  for (int i = 0; i < nq; ++i)
+    for (int d = 0; d < nu; ++d) bh.Pw[i][d] = bh.w[i] * bh.P[i][d];
+  const double h = 1.0 / cfg->N, two_h = 2.0 / h, four_hh = 4.0 / (h * h);
+  for (int d = 0; d < nu; ++d) {
+    bh.ElA[d] = two_h * bh.El[d];
+    bh.E1D[d] = four_hh * bh.E1l[d];
+    bh.E1F[d] = -bh.E1l[d];
+  }
 
   // ---- K1 = S^T diag(w) S: zero between modes of unlike parity, and in the first row and
   //      column (the constant mode has no derivative)

@@ -16,8 +16,10 @@ constexpr int MAXQH = 12;  // q_high for q_v = 7
 struct BasisHost {
   int nu, nv, qh;
   double w[MAXN], P[MAXN][MAXN], S[MAXN][MAXN];
+  double Pw[MAXN][MAXN];
   double El[MAXN], Er[MAXN], E1l[MAXN], E1r[MAXN];
-  double Ph[MAXQH][MAXN], Wh[MAXQH][MAXQH];
+  double ElA[MAXN], E1D[MAXN], E1F[MAXN];
+  double Ph[MAXQH][MAXN], Wh[MAXQH][MAXQH], wh[MAXQH], PhW[MAXQH][MAXN];
   double K1[MAXN][MAXN], Q[MAXN][MAXN], ilam2[MAXN][MAXN];
 };
 
@@ -37,16 +39,15 @@ void pack_basis(const BasisHost &h, void *out) {
   constexpr int NQ = NU, QH = Basis<NU, NV>::QH;
   for (int i = 0; i < NQ; ++i) {
     b.w[i] = h.w[i];
-    for (int d = 0; d < NU; ++d) { b.P[i][d] = h.P[i][d]; b.S[i][d] = h.S[i][d]; }
+    for (int d = 0; d < NU; ++d) { b.P[i][d] = h.P[i][d]; b.S[i][d] = h.S[i][d]; b.Pw[i][d] = h.Pw[i][d]; }
   }
   for (int d = 0; d < NU; ++d) {
     b.El[d] = h.El[d]; b.Er[d] = h.Er[d]; b.E1l[d] = h.E1l[d]; b.E1r[d] = h.E1r[d];
+    b.ElA[d] = h.ElA[d]; b.E1D[d] = h.E1D[d]; b.E1F[d] = h.E1F[d];
     for (int c = 0; c < NU; ++c) { b.K1[d][c] = h.K1[d][c]; b.Q[d][c] = h.Q[d][c]; b.ilam2[d][c] = h.ilam2[d][c]; }
   }
-  for (int r = 0; r < QH; ++r) {
-    for (int d = 0; d < NV; ++d) b.Ph[r][d] = h.Ph[r][d];
-    for (int s = 0; s < QH; ++s) b.Wh[r][s] = h.Wh[r][s];
-  }
+  for (int r = 0; r < QH; ++r)
+    for (int d = 0; d < NV; ++d) { b.Ph[r][d] = h.Ph[r][d]; b.PhW[r][d] = h.PhW[r][d]; }
 }
 
 template <int NU, int NV>

@@ -38,10 +38,11 @@
 //   v-faces     [j + N (kf + (N+1) i)]
 //   bnd data    [m + N i]
 //   Pi, srcP    [(a + NV b) E + e]
-//   beta, G     [(r + QH s) E + e]
+//   2β, G       [(r + QH s) E + e]
 //   mass rhs    [(a + NV b) E + e]
 #pragma once
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <stdint.h>
 
 namespace wedg {
@@ -79,9 +80,11 @@ struct Basis {
   static constexpr int QH = qhigh(NU, NV);
   double w[NQ];
   double P[NQ][NU], S[NQ][NU];   // P[i][d] = P_u[i, d], S likewise; the v-basis is d < NV
+  double Pw[NQ][NU];             // w[i] P[i][d]
   double El[NU], Er[NU], E1l[NU], E1r[NU];
+  double ElA[NU], E1D[NU], E1F[NU];  // (2/h) El, (4/h²) E1l, -E1l: the lift factors of a side
   double Ph[QH][NV];             // P_h_v[r, d]
-  double Wh[QH][QH];             // W2d_h[r, s]
+  double PhW[QH][NV];            // w_h[r] P_h_v[r, d], with W2d_h = w_h w_h^T
   double K1[NU][NU];             // 1D stiffness S^T diag(w) S
   double Q[NU][NU];              // its eigenvectors, Q[row][col]; Q[.][0] = e_0
   double ilam2[NU][NU];          // 1 / (λ_i + λ_j), and 1 at (0, 0)
@@ -94,8 +97,8 @@ struct Fields {
   const double *vc2, *vaf, *vcf, *vbf, *vc2m, *vafm, *vJC;
   const double *bsp[4], *bspn[4];
   const double *PiSP, *PiBSP2, *PiCdiv, *PiDdiv, *srcP;
-  const double *beta;
-  double *tr, *G, *th, *de;
+  const double *beta2;        // 2β at the high-order points, [(r + QH s) E + e]
+  double *tr, *G, *th, *de;   // G = 2βv at the high-order points
   double *mrhs;               // right-hand side of the mass system, [(a + NV b) E + e]
   int *nst, *nmax;
   int *bins, *bin_count;      // elements by Chebyshev count: bins[b E + i], two count buffers of NBIN
@@ -327,8 +330,10 @@ __global__ void __launch_bounds__(128) k_prep(const __grid_constant__ Basis<NU, 
 
   if (F.cg) return;
   // Chebyshev interval of the element: v_q = P_h V P_h^T, G = 2βv_q, a± = 1 - extrema(G);
-  // the rows of the point grid in mirrored pairs
-  double gmin = 1.0 / 0.0, gmax = -1.0 / 0.0;
+  // the rows of the point grid in mirrored pairs. The extrema and the NaN test run on the
+  // integer pipe (order-preserving integer keys of the doubles), so that a point costs one
+  // FP64 multiply besides the contractions.
+  long long kmin = LLONG_MAX, kmax = LLONG_MIN;
   bool nan = false;
   auto vx = [&](int a, int b) { return V[a][b]; };
   auto points = [&](const double (&T)[NV], int r) {
@@ -337,11 +342,13 @@ __global__ void __launch_bounds__(128) k_prep(const __grid_constant__ Basis<NU, 
 #pragma unroll
     for (int s2 = 0; s2 < QH; ++s2) {
       const size_t gi = (r + QH * s2) * (size_t)E + e;
-      const double g = Y[s2] * (2.0 * F.beta[gi]);
-      nan |= (g != g);
-      gmin = fmin(gmin, g);
-      gmax = fmax(gmax, g);
-      F.G[gi] = g * B.Wh[r][s2];
+      const double g = Y[s2] * F.beta2[gi];
+      F.G[gi] = g;
+      const long long bits = __double_as_longlong(g);
+      nan |= (bits & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+      const long long key = bits ^ ((bits >> 63) & 0x7fffffffffffffffLL);
+      kmin = min(kmin, key);
+      kmax = max(kmax, key);
     }
   };
 #pragma unroll 1
@@ -356,6 +363,8 @@ __global__ void __launch_bounds__(128) k_prep(const __grid_constant__ Basis<NU, 
     ph_row_mid<QH, NV>(B.Ph, vx, T);
     points(T, QH / 2);
   }
+  const double gmin = __longlong_as_double(kmin ^ ((kmin >> 63) & 0x7fffffffffffffffLL));
+  const double gmax = __longlong_as_double(kmax ^ ((kmax >> 63) & 0x7fffffffffffffffLL));
   const double amin = 1.0 - gmax, amax = 1.0 - gmin;
   if (nan || !(amin > 0.0)) {
     atomicMin(F.err, (1ull << ERR_CLASS_SHIFT) | (unsigned long long)(e + 1));
@@ -510,7 +519,11 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
   Blk<NU, BT> Ub{smem + (NU * NU + NV * NV) * BT + tid};
   Blk<NV, BT> Vb{smem + (2 * NU * NU + NV * NV) * BT + tid};
 
-  // ---- faces and lifts (src/rhs.jl:421-473): Rv (v-equation), b = -Fu (u-equation)
+  // ---- faces and lifts (src/rhs.jl:421-473): Rv (v-equation), b = -Fu (u-equation).
+  //      The numerical flux slots A, D, F of a side are projected on the modes, Y[b] =
+  //      Σ_i w_i P[i][b] (.)_i, from the sums (even b) and differences (odd b) of mirrored points,
+  //      and the two sides of an axis are lifted together: the right-end factors are the
+  //      left-end ones times ±(-1)^a, so both sides need one rank-one update per slot.
 #pragma unroll 1
   for (int a = 0; a < NV; ++a)
 #pragma unroll
@@ -520,55 +533,94 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
 #pragma unroll
     for (int b = 0; b < NU; ++b) bb(a, b) = 0.0;
 #pragma unroll 1
-  for (int s = 0; s < 4; ++s) {
-    const bool boundary = (s == 0 && j == 0) || (s == 1 && j == N - 1) || (s == 2 && k == 0) || (s == 3 && k == N - 1);
+  for (int ax = 0; ax < 2; ++ax) {
+    double A0[NV], D0[NV], F0[NU];          // the projections of the axis' first side (B or L)
     double YA[NV], YD[NV], YF[NU];
-#pragma unroll
-    for (int b = 0; b < NU; ++b) {
-      if (b < NV) { YA[b] = 0.0; YD[b] = 0.0; }
-      YF[b] = 0.0;
-    }
 #pragma unroll 1
-    for (int i = 0; i < NQ; ++i) {
-      double A, D, Fs;
-      side_point<NU, NV>(B, F, S, s, boundary, j, k, e, i, A, D, Fs);
-      const double wa = B.w[i] * A, wd = B.w[i] * D, wf = B.w[i] * Fs;
+    for (int t = 0; t < 2; ++t) {
+      const int s = 2 * ax + t;
+      const bool boundary = (s == 0 && j == 0) || (s == 1 && j == N - 1) || (s == 2 && k == 0) || (s == 3 && k == N - 1);
 #pragma unroll
       for (int b = 0; b < NU; ++b) {
-        if (b < NV) {
-          YA[b] = fma(B.P[i][b], wa, YA[b]);
-          YD[b] = fma(B.P[i][b], wd, YD[b]);
+        if (b < NV) { YA[b] = 0.0; YD[b] = 0.0; }
+        YF[b] = 0.0;
+      }
+#pragma unroll 1
+      for (int i = 0; i < NQ / 2; ++i) {
+        double A1, D1, F1, A2, D2, F2;
+        side_point<NU, NV>(B, F, S, s, boundary, j, k, e, i, A1, D1, F1);
+        side_point<NU, NV>(B, F, S, s, boundary, j, k, e, NQ - 1 - i, A2, D2, F2);
+        const double as = A1 + A2, ad = A1 - A2, ds = D1 + D2, dd = D1 - D2, fs = F1 + F2, fd = F1 - F2;
+#pragma unroll
+        for (int b = 0; b < NU; ++b) {
+          const double p = B.Pw[i][b];
+          if (b < NV) {
+            YA[b] = fma(p, (b & 1) ? ad : as, YA[b]);
+            YD[b] = fma(p, (b & 1) ? dd : ds, YD[b]);
+          }
+          YF[b] = fma(p, (b & 1) ? fd : fs, YF[b]);
         }
-        YF[b] = fma(B.P[i][b], wf, YF[b]);
+      }
+      if constexpr ((NQ & 1) != 0) {         // the middle point: the odd modes vanish there
+        double A1, D1, F1;
+        side_point<NU, NV>(B, F, S, s, boundary, j, k, e, NQ / 2, A1, D1, F1);
+#pragma unroll
+        for (int b = 0; b < NU; b += 2) {
+          const double p = B.Pw[NQ / 2][b];
+          if (b < NV) {
+            YA[b] = fma(p, A1, YA[b]);
+            YD[b] = fma(p, D1, YD[b]);
+          }
+          YF[b] = fma(p, F1, YF[b]);
+        }
+      }
+      if (t == 0) {
+#pragma unroll
+        for (int b = 0; b < NU; ++b) {
+          if (b < NV) { A0[b] = YA[b]; D0[b] = YD[b]; }
+          F0[b] = YF[b];
+        }
       }
     }
-    const double *Ev = (s == 0 || s == 2) ? B.El : B.Er;
-    const double *E1 = (s == 0 || s == 2) ? B.E1l : B.E1r;
-    if (s < 2) {
+    // lifts of both sides: with σ_a = (-1)^a, El = the left-end values, E1l the left-end
+    // derivatives, Rv += (2/h) El ⊗ (A_0 + σ A_1) + (4/h²) E1l ⊗ (D_0 - σ D_1) and
+    // b -= E1l ⊗ (F_0 - σ F_1) (B/T: the row index carries E; L/R: the column index)
+#pragma unroll
+    for (int b = 0; b < NU; ++b) {
+      if (b < NV) {
+        const double ap = A0[b] + YA[b], am = A0[b] - YA[b], dp = D0[b] + YD[b], dm = D0[b] - YD[b];
+        A0[b] = ap; YA[b] = am; D0[b] = dm; YD[b] = dp;       // even-σ and odd-σ combinations
+      }
+      const double fp = F0[b] + YF[b], fm = F0[b] - YF[b];
+      F0[b] = fm; YF[b] = fp;
+    }
+    if (ax == 0) {
 #pragma unroll 1
       for (int a = 0; a < NV; ++a) {
-        const double ca = two_h * Ev[a], cd = four_hh * E1[a];
+        const double ca = B.ElA[a], cd = B.E1D[a];
+        const bool od = a & 1;
 #pragma unroll
-        for (int b = 0; b < NV; ++b) Rv(a, b) = fma(cd, YD[b], fma(ca, YA[b], Rv(a, b)));
+        for (int b = 0; b < NV; ++b)
+          Rv(a, b) = fma(cd, od ? YD[b] : D0[b], fma(ca, od ? YA[b] : A0[b], Rv(a, b)));
       }
 #pragma unroll 1
       for (int a = 0; a < NU; ++a) {
-        const double ce = -E1[a];
+        const double ce = B.E1F[a];
+        const bool od = a & 1;
 #pragma unroll
-        for (int b = 0; b < NU; ++b) bb(a, b) = fma(ce, YF[b], bb(a, b));
+        for (int b = 0; b < NU; ++b) bb(a, b) = fma(ce, od ? YF[b] : F0[b], bb(a, b));
       }
     } else {
 #pragma unroll
       for (int a = 0; a < NV; ++a) {
-        const double ca = two_h * YA[a], cd = four_hh * YD[a];
 #pragma unroll
-        for (int b = 0; b < NV; ++b) Rv(a, b) = fma(cd, E1[b], fma(ca, Ev[b], Rv(a, b)));
+        for (int b = 0; b < NV; ++b)
+          Rv(a, b) = fma(B.E1D[b], (b & 1) ? YD[a] : D0[a], fma(B.ElA[b], (b & 1) ? YA[a] : A0[a], Rv(a, b)));
       }
 #pragma unroll
       for (int a = 0; a < NU; ++a) {
-        const double ce = -YF[a];
 #pragma unroll
-        for (int b = 0; b < NU; ++b) bb(a, b) = fma(ce, E1[b], bb(a, b));
+        for (int b = 0; b < NU; ++b) bb(a, b) = fma(B.E1F[b], (b & 1) ? YF[a] : F0[a], bb(a, b));
       }
     }
   }
@@ -896,8 +948,9 @@ __device__ __forceinline__ void store_v(const StageIO &S, size_t l, double kk, b
 }
 
 // k_cheb: the Chebyshev mass solve (Saad Alg. 12.1, src/rhs.jl:920-939) with a team of threads
-// per element. One Chebyshev step costs one application of K = P_h^T diag(G) P_h (G = 2βv W at
-// the high-order points), and its FP64 work is cut across the team by rows of the point grid:
+// per element. One Chebyshev step costs one application of K = P_h^T diag(G W) P_h (G = 2βv at
+// the high-order points, W = w_h w_h^T their weights, folded into PhW), and its FP64 work is cut
+// across the team by rows of the point grid:
 // unit u of the team takes the mirrored rows u and QH-1-u (the middle row alone when QH is odd),
 // takes them to the points and back (phase 1), and leaves for each mode column b the sum and
 // the difference of the two rows' results in shared memory; then every thread finishes J of the
@@ -925,10 +978,13 @@ __global__ void __launch_bounds__(CHEB_THREADS)
   using T = ChebTeam<NU, NV>;
   constexpr int QH = T::QH, U = T::U, NE = T::NE, J = T::J;
   __shared__ double sh[T::TPB * T::SLOT];
-  __shared__ double Phs[QH * NV];
+  __shared__ double Phs[QH * NV], PhWs[QH * NV];
   __shared__ int pref[NBIN];
   const int tid = threadIdx.x, lane = tid & 31;
-  for (int i = tid; i < QH * NV; i += CHEB_THREADS) Phs[i] = B.Ph[i / NV][i % NV];
+  for (int i = tid; i < QH * NV; i += CHEB_THREADS) {
+    Phs[i] = B.Ph[i / NV][i % NV];
+    PhWs[i] = B.PhW[i / NV][i % NV];
+  }
   if (F.sorted && tid == 0) {
     // exclusive prefix sum of the counts of this stage's bins, from the last bin down
     int acc = 0;
@@ -969,7 +1025,7 @@ __global__ void __launch_bounds__(CHEB_THREADS)
     ph_to_points<QH, NV>(B.Ph, Tv, Y);
 #pragma unroll
     for (int s2 = 0; s2 < QH; ++s2) Y[s2] *= F.G[(r + QH * s2) * Eu + e];
-    ph_from_points<QH, NV>(B.Ph, Y, Z);
+    ph_from_points<QH, NV>(B.PhW, Y, Z);
   };
   double rho = 1.0 / s1;
 #pragma unroll 1
@@ -1013,7 +1069,7 @@ __global__ void __launch_bounds__(CHEB_THREADS)
         const double *z = ((a & 1) ? zd : zs) + b;
         double acc = rr[j];
 #pragma unroll
-        for (int v = 0; v < U; ++v) acc = fma(Phs[v * NV + a], z[v * NV], acc);
+        for (int v = 0; v < U; ++v) acc = fma(PhWs[v * NV + a], z[v * NV], acc);
         rr[j] = acc;
         dd[j] = fma(c1, dd[j], c2 * acc);
         dsm[k] = dd[j];
@@ -1048,7 +1104,8 @@ __global__ void __launch_bounds__(MASS_THREADS)
   Blk<NV, BT> r{smem + tid}, X{smem + NV * NV * BT + tid};
   bool fin = true;
 
-  // K P accumulated into O: O += P_h^T (G ∘ (P_h P P_h^T)) P_h (G = 2βv W), for a mirrored pair of rows
+  // K P accumulated into O: O += P_h^T ((G W) ∘ (P_h P P_h^T)) P_h (G = 2βv, W = w_h w_h^T folded
+  // into PhW), for a mirrored pair of rows
   // of the point grid at a time (row QH-1-r of P_h P is the even part minus the odd part of
   // row r, and both rows go back to the modes through one sum and one difference)
   auto rowZ = [&](const double (&T)[NV], int r, double (&Z)[NV]) {
@@ -1056,7 +1113,7 @@ __global__ void __launch_bounds__(MASS_THREADS)
     ph_to_points<QH, NV>(B.Ph, T, Y);
 #pragma unroll
     for (int s2 = 0; s2 < QH; ++s2) Y[s2] *= F.G[(r + QH * s2) * Eu + e];
-    ph_from_points<QH, NV>(B.Ph, Y, Z);
+    ph_from_points<QH, NV>(B.PhW, Y, Z);
   };
   auto addK = [&](Blk<NV, BT> P, Blk<NV, BT> O) {
     auto px = [&](int a, int b) { return P(a, b); };
@@ -1073,7 +1130,7 @@ __global__ void __launch_bounds__(MASS_THREADS)
       for (int b = 0; b < NV; ++b) {
         const double zs = Zp[b] + Zm[b], zd = Zp[b] - Zm[b];
 #pragma unroll
-        for (int a = 0; a < NV; ++a) O(a, b) = fma(B.Ph[r2][a], (a & 1) ? zd : zs, O(a, b));
+        for (int a = 0; a < NV; ++a) O(a, b) = fma(B.PhW[r2][a], (a & 1) ? zd : zs, O(a, b));
       }
     }
     if constexpr ((QH & 1) != 0) {
@@ -1083,14 +1140,14 @@ __global__ void __launch_bounds__(MASS_THREADS)
 #pragma unroll
       for (int b = 0; b < NV; ++b)
 #pragma unroll
-        for (int a = 0; a < NV; a += 2) O(a, b) = fma(B.Ph[QH / 2][a], Z[b], O(a, b));
+        for (int a = 0; a < NV; a += 2) O(a, b) = fma(B.PhW[QH / 2][a], Z[b], O(a, b));
     }
   };
 
   {
     // conjugate gradients from X = R (src/rhs.jl:824-853)
     Blk<NV, BT> p{smem + 2 * NV * NV * BT + tid}, Ap{smem + 3 * NV * NV * BT + tid};
-    // G = 2βv_q W of this element, by mirrored pairs of rows
+    // G = 2βv_q of this element, by mirrored pairs of rows
     auto vx = [&](int a, int b) { return S.xv[e + Eu * (a + NV * b)]; };
     auto gput = [&](const double (&T)[NV], int r2) {
       double Y[QH];
@@ -1098,7 +1155,7 @@ __global__ void __launch_bounds__(MASS_THREADS)
 #pragma unroll
       for (int s2 = 0; s2 < QH; ++s2) {
         const size_t gi = (r2 + QH * s2) * Eu + e;
-        F.G[gi] = 2.0 * F.beta[gi] * Y[s2] * B.Wh[r2][s2];
+        F.G[gi] = Y[s2] * F.beta2[gi];
       }
     };
 #pragma unroll 1

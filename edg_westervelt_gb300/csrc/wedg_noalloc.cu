@@ -51,13 +51,14 @@ std::once_flag g_setup_once[MAX_DEVICES];
 
 // Reorders a raw copy of one of pre's arrays into the layout the kernels read:
 // mode 0: [a + d0 (b + d1 c)] -> [b + d1 (c + d2 a)]   (the first index becomes the slowest)
-// mode 1: [a + d0 (b + d1 c)] -> [b + d1 (a + d0 c)]   (Cw, Aw, β: the element index b first)
+// mode 1: [a + d0 (b + d1 c)] -> [b + d1 (a + d0 c)]   (Cw, Aw: the element index b first)
+// mode 2: as mode 1, doubled                          (β -> 2β, which the kernels read)
 __global__ void k_relayout(const double *in, double *out, int d0, int d1, int d2, int mode) {
   const size_t n = (size_t)d0 * d1 * d2;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const size_t a = i % d0, bc = i / d0, b = bc % d1, c = bc / d1;
     const size_t o = mode == 0 ? b + (size_t)d1 * (c + (size_t)d2 * a) : b + (size_t)d1 * (a + (size_t)d0 * c);
-    out[o] = in[i];
+    out[o] = mode == 2 ? 2.0 * in[i] : in[i];
   }
 }
 
@@ -219,7 +220,7 @@ extern "C" int wedg_rhs_noalloc(const wedg_config *cfg, const wedg_pre *pre, con
   }
   if (!cfg->src_on) RL(pre->PiCdiv, np, base + o_pic, nv * nv, iE, 1, 0);
   if (cfg->src_on) RL(pre->src_projE, np, base + o_src, nv * nv, iE, 1, 0);
-  RL(pre->beta_hq, (size_t)qh * qh * E, base + o_beta, qh, iE, qh, 1);
+  RL(pre->beta_hq, (size_t)qh * qh * E, base + o_beta, qh, iE, qh, 2);
 #undef RL
 
   // ---- the kernels' view of the array
@@ -237,7 +238,7 @@ extern "C" int wedg_rhs_noalloc(const wedg_config *cfg, const wedg_pre *pre, con
   if (cfg->mms_on) { F.PiSP = base + o_pisp; F.PiBSP2 = base + o_pib; F.PiDdiv = base + o_pid; }
   if (!cfg->src_on) F.PiCdiv = base + o_pic;
   if (cfg->src_on) F.srcP = base + o_src;
-  F.beta = base + o_beta;
+  F.beta2 = base + o_beta;
   F.tr = base + o_tr;
   F.G = base + o_G;
   F.th = base + o_th;
