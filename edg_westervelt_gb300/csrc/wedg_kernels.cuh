@@ -284,7 +284,7 @@ __device__ __forceinline__ void load_regs(double (&X)[n][n], const double *x, in
 }
 
 template <int NU, int NV>
-__global__ void __launch_bounds__(128) k_prep(const __grid_constant__ Basis<NU, NV> B,
+__global__ void __launch_bounds__(128, 3) k_prep(const __grid_constant__ Basis<NU, NV> B,
                                               const __grid_constant__ Fields F,
                                               const __grid_constant__ StageIO S) {
   constexpr int NQ = NU, QH = Basis<NU, NV>::QH;
@@ -972,7 +972,7 @@ struct ChebTeam {
 };
 
 template <int NU, int NV>
-__global__ void __launch_bounds__(CHEB_THREADS)
+__global__ void __launch_bounds__(CHEB_THREADS, 3)
     k_cheb(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
            const __grid_constant__ StageIO S) {
   using T = ChebTeam<NU, NV>;
