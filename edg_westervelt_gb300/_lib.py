@@ -57,6 +57,20 @@ class Stats(ctypes.Structure):
 _lib = None
 
 
+class SourceRun(ctypes.Structure):
+    """wedg_source_run (include/wedg.h)."""
+    _fields_ = [("nsteps", ctypes.c_int64), ("record_every", ctypes.c_int64), ("t0", ctypes.c_double),
+                ("dt", ctypes.c_double), ("nrec", ctypes.c_int), ("rec_j", ctypes.POINTER(ctypes.c_int32)),
+                ("rec_k", ctypes.POINTER(ctypes.c_int32)), ("rec_py", ctypes.POINTER(ctypes.c_double)),
+                ("rec_px", ctypes.POINTER(ctypes.c_double)), ("slice_j", ctypes.c_int),
+                ("slice_py", ctypes.POINTER(ctypes.c_double)), ("nsnap", ctypes.c_int),
+                ("snap_after", ctypes.POINTER(ctypes.c_int64)), ("err_c2", ctypes.POINTER(ctypes.c_double)),
+                ("err_beta", ctypes.POINTER(ctypes.c_double)), ("recv", ctypes.POINTER(ctypes.c_double)),
+                ("energy", ctypes.POINTER(ctypes.c_double)), ("vmax", ctypes.POINTER(ctypes.c_double)),
+                ("ndmin", ctypes.POINTER(ctypes.c_double)), ("slices", ctypes.POINTER(ctypes.c_double)),
+                ("snaps", ctypes.POINTER(ctypes.c_double))]
+
+
 def lib():
     """The loaded libwedg (ctypes.CDLL); raises if the library was not built."""
     global _lib
@@ -90,6 +104,8 @@ def lib():
     L.wedg_rhs_noalloc.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Pre), vp, vp, ctypes.c_double, vp, vp, vp,
                                    ctypes.c_char_p, ctypes.c_size_t]
     L.wedg_time_kernels.argtypes = [vp, ctypes.c_int]
+    L.wedg_run_source.argtypes = [vp, _D, _D, _I64, _I64, ctypes.c_int, ctypes.POINTER(SourceRun), _I64,
+                                  ctypes.POINTER(ctypes.c_int)]
     L.wedg_kernel_times.argtypes = [vp, _D, _I64, _D, _I64, _D, _I64, ctypes.c_int]
     _lib = L
     return L

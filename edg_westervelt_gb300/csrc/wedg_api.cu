@@ -19,6 +19,7 @@
 
 #include "../../include/wedg.h"
 #include "wedg_basis.h"
+#include "wedg_diag.h"
 #include "wedg_dispatch.h"
 
 namespace wedg {
@@ -72,6 +73,7 @@ struct wedg_ws {
   int N = 0, E = 0, nu = 0, nv = 0, nq = 0, qh = 0;
   bool fast = false;
   Launchers L;
+  BasisHost bh;
   std::vector<char> basis;
   Fields F{};
   cudaStream_t own_stream = nullptr, stream = nullptr;
@@ -370,6 +372,28 @@ int argument_error(wedg_ws *ws, const std::string &msg) {
 
 }  // namespace
 
+namespace {
+
+// Device buffers of one wedg_run_source call, freed (after the stream is idle) on every return path.
+struct RunBuffers {
+  cudaStream_t st = nullptr;
+  std::vector<void *> p;
+  template <typename T>
+  cudaError_t get(T **q, size_t n) {
+    *q = nullptr;
+    void *x = nullptr;
+    const cudaError_t e = cudaMalloc(&x, (n ? n : 1) * sizeof(T));
+    if (e == cudaSuccess) { p.push_back(x); *q = static_cast<T *>(x); }
+    return e;
+  }
+  ~RunBuffers() {
+    if (st) cudaStreamSynchronize(st);
+    for (void *x : p) cudaFree(x);
+  }
+};
+
+}  // namespace
+
 extern "C" {
 
 int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
@@ -406,7 +430,7 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
   const size_t Es = (size_t)E;
 
   // ---- 1D operators (Julia column-major inputs), with their mirror parities made exact
-  BasisHost bh;
+  BasisHost &bh = ws->bh;
   if (build_basis(cfg, pre, bh)) {
     delete ws;
     return WEDG_ERR_ARGUMENT;
@@ -645,6 +669,124 @@ int wedg_rk4_steps(wedg_ws *ws, double *u, double *v, double t0, double dt, int6
   rc = collect(ws);
   if (steps_done) *steps_done = ws->stats.steps_done;
   if (finite) *finite = ws->stats.finite;
+  if (where == WEDG_HOST) {
+    CK(ws, cudaMemcpy(u, ws->d_u, bU, cudaMemcpyDeviceToHost));
+    CK(ws, cudaMemcpy(v, ws->d_v, bV, cudaMemcpyDeviceToHost));
+  }
+  return rc;
+}
+
+int wedg_run_source(wedg_ws *ws, double *u, double *v, const int64_t u_shape[4], const int64_t v_shape[4],
+                    int where, const wedg_source_run *run, int64_t *steps_done, int *finite) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  ws->stats.kernel_launches = 0;
+  int rc = check_shapes(ws, u_shape, v_shape);
+  if (rc) return rc;
+  if (!u || !v || !run) return argument_error(ws, "null argument");
+  const int N = ws->N, E = ws->E, nu = ws->nu, nv = ws->nv, nq = ws->nq;
+  if (run->nsteps < 0 || run->record_every < 1) return argument_error(ws, "nsteps must be ≥ 0 and record_every ≥ 1");
+  if (run->nrec < 0 || (run->nrec > 0 && (!run->rec_j || !run->rec_k || !run->rec_py || !run->rec_px)))
+    return argument_error(ws, "invalid receivers");
+  if (run->slice_j < 0 || run->slice_j >= N || !run->slice_py) return argument_error(ws, "invalid slice");
+  if (run->nsnap < 0 || (run->nsnap > 0 && !run->snap_after)) return argument_error(ws, "invalid snapshots");
+  if (!run->err_c2 || !run->err_beta) return argument_error(ws, "err_c2 and err_beta are needed");
+  for (int i = 0; i < run->nrec; ++i)
+    if (run->rec_j[i] < 0 || run->rec_j[i] >= N || run->rec_k[i] < 0 || run->rec_k[i] >= N)
+      return argument_error(ws, "receiver outside the mesh");
+  for (int i = 0; i < run->nsnap; ++i)
+    if (run->snap_after[i] < 1 || run->snap_after[i] > run->nsteps || (i && run->snap_after[i] <= run->snap_after[i - 1]))
+      return argument_error(ws, "snapshot steps must increase within 1..nsteps");
+  const int64_t nsteps = run->nsteps, every = run->record_every;
+  const int64_t nrecord = nsteps / every + (nsteps % every ? 1 : 0);
+  if ((nsteps * run->nrec && !run->recv) || (nrecord && (!run->energy || !run->vmax || !run->ndmin || !run->slices)) ||
+      (run->nsnap && !run->snaps))
+    return argument_error(ws, "null output array");
+
+  // ---- the basis and mesh factors of the diagnostics
+  DiagBasis B{};
+  B.N = N; B.E = E; B.nu = nu; B.nv = nv;
+  const double h = 1.0 / N;
+  B.two_h = 2.0 / h;
+  B.hh4 = h * h / 4;
+  for (int i = 0; i < nq; ++i) {
+    B.w[i] = ws->bh.w[i];
+    for (int d = 0; d < nu; ++d) { B.P[i][d] = ws->bh.P[i][d]; B.S[i][d] = ws->bh.S[i][d]; }
+  }
+
+  // ---- device buffers of the run
+  RunBuffers R;
+  R.st = ws->stream;
+  const size_t M = (size_t)N * nq, nE = (size_t)E * nq * nq;
+  const int nblk = (E + DIAG_THREADS - 1) / DIAG_THREADS;
+  int *d_rec_e;
+  double *d_py, *d_px, *d_spy, *d_recv, *d_rec3, *d_part, *d_slices, *d_snaps, *d_c2, *d_be;
+  CK(ws, R.get(&d_rec_e, run->nrec));
+  CK(ws, R.get(&d_py, (size_t)run->nrec * nv));
+  CK(ws, R.get(&d_px, (size_t)run->nrec * nv));
+  CK(ws, R.get(&d_spy, nv));
+  CK(ws, R.get(&d_recv, (size_t)nsteps * run->nrec));
+  CK(ws, R.get(&d_rec3, 3 * (size_t)nrecord));
+  CK(ws, R.get(&d_part, 3 * (size_t)nblk));
+  CK(ws, R.get(&d_slices, (size_t)nrecord * M));
+  CK(ws, R.get(&d_snaps, (size_t)run->nsnap * M * M));
+  CK(ws, R.get(&d_c2, nE));
+  CK(ws, R.get(&d_be, nE));
+  std::vector<int> rec_e(run->nrec);
+  for (int i = 0; i < run->nrec; ++i) rec_e[i] = run->rec_j[i] + N * run->rec_k[i];
+  CK(ws, cudaMemcpyAsync(d_rec_e, rec_e.data(), sizeof(int) * run->nrec, cudaMemcpyHostToDevice, ws->stream));
+  CK(ws, cudaMemcpyAsync(d_py, run->rec_py, sizeof(double) * run->nrec * nv, cudaMemcpyHostToDevice, ws->stream));
+  CK(ws, cudaMemcpyAsync(d_px, run->rec_px, sizeof(double) * run->nrec * nv, cudaMemcpyHostToDevice, ws->stream));
+  CK(ws, cudaMemcpyAsync(d_spy, run->slice_py, sizeof(double) * nv, cudaMemcpyHostToDevice, ws->stream));
+  CK(ws, cudaMemcpyAsync(d_c2, run->err_c2, sizeof(double) * nE, cudaMemcpyHostToDevice, ws->stream));
+  CK(ws, cudaMemcpyAsync(d_be, run->err_beta, sizeof(double) * nE, cudaMemcpyHostToDevice, ws->stream));
+
+  // ---- the state
+  const size_t bU = sizeof(double) * ws->E * nu * nu, bV = sizeof(double) * ws->E * nv * nv;
+  double *du = u, *dv = v;
+  if (where == WEDG_HOST) {
+    CK(ws, cudaMemcpyAsync(ws->d_u, u, bU, cudaMemcpyHostToDevice, ws->stream));
+    CK(ws, cudaMemcpyAsync(ws->d_v, v, bV, cudaMemcpyHostToDevice, ws->stream));
+    du = ws->d_u; dv = ws->d_v;
+  }
+  if ((rc = reset_flags(ws))) return rc;
+
+  // ---- the loop (src/solver.jl:933-952), all on the workspace stream
+  double t = run->t0;
+  int64_t ir = 0;
+  int is = 0;
+  const int tb = 128;
+  for (int64_t it = 1; it <= nsteps; ++it) {
+    if ((rc = enqueue_rk4(ws, du, dv, t, run->dt, 1))) return rc;
+    t += run->dt;
+    if (run->nrec) {
+      k_receivers<<<(run->nrec + tb - 1) / tb, tb, 0, ws->stream>>>(dv, E, nv, run->nrec, d_rec_e, d_py, d_px,
+                                                                   d_recv + (size_t)(it - 1) * run->nrec);
+      ws->stats.kernel_launches += 1;
+    }
+    if (it % every == 0 || it == nsteps) {
+      k_energy_elems<<<nblk, DIAG_THREADS, 0, ws->stream>>>(du, dv, B, d_c2, d_be, d_part);
+      k_energy_final<<<1, DIAG_THREADS, 0, ws->stream>>>(d_part, nblk, d_rec3 + ir, d_rec3 + nrecord + ir,
+                                                         d_rec3 + 2 * nrecord + ir);
+      k_slice<<<(int)((M + tb - 1) / tb), tb, 0, ws->stream>>>(dv, B, run->slice_j, d_spy, d_slices + ir * M);
+      ws->stats.kernel_launches += 3;
+      ++ir;
+    }
+    if (is < run->nsnap && run->snap_after[is] == it) {
+      k_vgrid<<<(unsigned)((M * M + tb - 1) / tb), tb, 0, ws->stream>>>(dv, B, d_snaps + (size_t)is * M * M);
+      ws->stats.kernel_launches += 1;
+      ++is;
+    }
+    CK(ws, cudaGetLastError());
+  }
+  rc = collect(ws);
+  if (steps_done) *steps_done = ws->stats.steps_done;
+  if (finite) *finite = ws->stats.finite;
+  CK(ws, cudaMemcpy(run->recv, d_recv, sizeof(double) * nsteps * run->nrec, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(run->energy, d_rec3, sizeof(double) * nrecord, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(run->vmax, d_rec3 + nrecord, sizeof(double) * nrecord, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(run->ndmin, d_rec3 + 2 * nrecord, sizeof(double) * nrecord, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(run->slices, d_slices, sizeof(double) * nrecord * M, cudaMemcpyDeviceToHost));
+  if (run->nsnap) CK(ws, cudaMemcpy(run->snaps, d_snaps, sizeof(double) * run->nsnap * M * M, cudaMemcpyDeviceToHost));
   if (where == WEDG_HOST) {
     CK(ws, cudaMemcpy(u, ws->d_u, bU, cudaMemcpyDeviceToHost));
     CK(ws, cudaMemcpy(v, ws->d_v, bV, cudaMemcpyDeviceToHost));

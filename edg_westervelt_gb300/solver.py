@@ -124,38 +124,43 @@ def _vrow(r, qv1):
 
 
 def run_source(u, v, dt, nsteps, N, h, pre, geo, ws, record_every, slice_y, receivers, snap_times):
-    """Source mode: RK4 on the GPU with receivers every step, slices and energy every
-    record_every steps and snapshots (src/solver.jl:892-958)."""
-    qu1, qv1, P_v = pre["qu1"], pre["qv1"], pre["P_v"]
+    """Source mode (src/solver.jl:892-958): the RK4 loop with the receivers after every step,
+    the slice, energy, max|v_h| and min(1 - 2βv_h) every record_every steps and the
+    snapshots, all on the GPU in one call (wedg_run_source). The host computes what the
+    reference computes on the host: receiver elements and basis rows (`locate`, `vrow`),
+    the times (t += dt after every step) and the steps after which snapshots are taken."""
+    qu1, qv1 = pre["qu1"], pre["qv1"]
     j0, eta0 = _locate(slice_y, N)
-    Pveta0 = _vrow(eta0, qv1)
     slice_x = np.concatenate([geo["xloc"][k, :] for k in range(N)])
-    rcv = []
+    rec_jk, rec_py, rec_px = [], [], []
     for xr, yr in receivers:
         kr, xir = _locate(xr, N)
         jr, etar = _locate(yr, N)
-        rcv.append((jr - 1, kr - 1, _vrow(etar, qv1), _vrow(xir, qv1)))
+        rec_jk.append((jr - 1, kr - 1))
+        rec_py.append(_vrow(etar, qv1))
+        rec_px.append(_vrow(xir, qv1))
+    # the times after each step and the snapshot steps, as the reference's loop finds them
+    ts = np.empty(nsteps)
     t = 0.0
-    rec_t, rec_slice, rec_E, rec_vmax, rec_nd, rt_t, rt_v, snaps = [], [], [], [], [], [], [], []
-    snap_left = sorted(snap_times)
+    snap_left, snap_after = sorted(snap_times), []
     for it in range(1, nsteps + 1):
-        ws.rk4_steps(u, v, t, dt, 1)
         t += dt
-        if not ws.fin:
-            raise ErrorException(f"blow-up at t={t}")
-        rt_t.append(t)
-        rt_v.append([float(r[2] @ v[r[0], r[1]] @ r[3]) for r in rcv])
-        if it % record_every == 0 or it == nsteps:
-            E, vmax, nd = energy_diag(u, v, pre, geo, N, h)
-            rec_t.append(t)
-            rec_slice.append(np.concatenate([P_v @ (Pveta0 @ v[j0 - 1, k]) for k in range(N)]))
-            rec_E.append(E)
-            rec_vmax.append(vmax)
-            rec_nd.append(nd)
+        ts[it - 1] = t
         if snap_left and t >= snap_left[0]:
-            G = np.einsum("ra,jkab,sb->jrks", P_v, _elem(v), P_v, optimize=True).reshape(N * qu1, N * qu1)
-            snaps.append((t, G))
+            snap_after.append(it)
             snap_left.pop(0)
+    done, recv, E, vmax, nd, slices, snaps_g = ws.run_source(
+        u, v, 0.0, dt, nsteps, record_every, rec_jk, np.array(rec_py).reshape(len(rec_jk), qv1),
+        np.array(rec_px).reshape(len(rec_jk), qv1), j0 - 1, _vrow(eta0, qv1), snap_after,
+        geo["err_c2"], geo["err_beta"])
+    if done < nsteps or not ws.fin:
+        raise ErrorException(f"blow-up at t={ts[done - 1] if done else dt}")
+    rec_steps = [it for it in range(1, nsteps + 1) if it % record_every == 0 or it == nsteps]
+    rec_t = [ts[it - 1] for it in rec_steps]
+    snaps = [(ts[it - 1], G) for it, G in zip(snap_after, snaps_g)]
+    rt_t = ts
+    rt_v = recv
+    rec_slice, rec_E, rec_vmax, rec_nd = list(slices), E, vmax, nd
     grid = np.concatenate([geo["xloc"][k, :] for k in range(N)])
     return dict(t=np.array(rec_t), slice_x=slice_x, slices=np.array(rec_slice).T, energy=np.array(rec_E),
                 vmax=np.array(rec_vmax), ndmin=np.array(rec_nd), recv_t=np.array(rt_t), recv=np.array(rt_v),

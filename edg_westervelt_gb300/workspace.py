@@ -223,6 +223,50 @@ class Workspace:
         return int(done.value)
 
 
+    def run_source(self, u, v, t0, dt, nsteps, record_every, rec_jk, rec_py, rec_px, slice_j, slice_py,
+                   snap_after, err_c2, err_beta):
+        """The source-mode loop with its diagnostics on the device (wedg_run_source): u, v
+        advance in place; returns (steps_done, recv (nsteps × nrec), energy, vmax, ndmin,
+        slices (records × N q_u1), snapshots (nsnap × (N q_u1)², column-major))."""
+        self._refuse_mismatch()
+        N, nq = self.N, self.nu
+        if not (isinstance(u, np.ndarray) and u.flags.f_contiguous and isinstance(v, np.ndarray)
+                and v.flags.f_contiguous and u.dtype == np.float64 and v.dtype == np.float64):
+            raise TypeError("run_source advances u, v in place: pass Fortran-ordered float64 arrays")
+        nrec = len(rec_jk)
+        nrecord = nsteps // record_every + (1 if nsteps % record_every else 0)
+        keep = []
+
+        def arr(a, dtype=np.float64):
+            a = np.ascontiguousarray(a, dtype=dtype)
+            keep.append(a)
+            return a.ctypes.data_as(ctypes.POINTER(np.ctypeslib.as_ctypes_type(dtype)))
+
+        out = dict(recv=np.zeros((max(nsteps, 0), nrec)), energy=np.zeros(nrecord), vmax=np.zeros(nrecord),
+                   ndmin=np.zeros(nrecord), slices=np.zeros((nrecord, N * nq)),
+                   snaps=np.zeros((len(snap_after), N * nq * N * nq)))
+        r = L.SourceRun()
+        r.nsteps, r.record_every, r.t0, r.dt = int(nsteps), int(record_every), float(t0), float(dt)
+        r.nrec = nrec
+        jk = np.array(rec_jk, dtype=np.int32).reshape(nrec, 2)
+        r.rec_j, r.rec_k = arr(jk[:, 0], np.int32), arr(jk[:, 1], np.int32)
+        r.rec_py, r.rec_px = arr(np.reshape(rec_py, (nrec, self.nv))), arr(np.reshape(rec_px, (nrec, self.nv)))
+        r.slice_j, r.slice_py = int(slice_j), arr(slice_py)
+        r.nsnap, r.snap_after = len(snap_after), arr(np.array(snap_after, dtype=np.int64), np.int64)
+        r.err_c2 = arr(np.asarray(err_c2, dtype=np.float64).reshape(-1, order="F"))
+        r.err_beta = arr(np.asarray(err_beta, dtype=np.float64).reshape(-1, order="F"))
+        for k in ("recv", "energy", "vmax", "ndmin", "slices", "snaps"):
+            setattr(r, k, out[k].ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        done = ctypes.c_int64(0)
+        fin = ctypes.c_int(1)
+        rc = L.lib().wedg_run_source(self._h, _ptr(u), _ptr(v), _shape(u, self.nu, N), _shape(v, self.nv, N),
+                                     L.WEDG_HOST, ctypes.byref(r), ctypes.byref(done), ctypes.byref(fin))
+        self.fin = bool(fin.value)
+        self._check(rc)
+        snaps = [s.reshape((N * nq, N * nq), order="F") for s in out["snaps"]]
+        return int(done.value), out["recv"], out["energy"], out["vmax"], out["ndmin"], out["slices"], snaps
+
+
 def edg_rhs_(ws, u, v, t, N, h, pre):
     """``edg_rhs!(ws, u, v, t, N, h, pre) -> (ws.ut, ws.vt)`` (src/rhs.jl:490-494); the
     returned arrays are overwritten by the next call."""

@@ -151,6 +151,37 @@ int wedg_time_kernels(wedg_ws *ws, int enable);
 int wedg_kernel_times(wedg_ws *ws, double *prep_ms, int64_t *prep_launches, double *stage_ms,
                       int64_t *stage_launches, double *mass_ms, int64_t *mass_launches, int reset);
 
+/* Source-mode run with its diagnostics on the device: the loop of `_run_source`
+ * (src/solver.jl:892-958). It replaces the per-step host work of that loop -- the
+ * receiver values after every step, and after every record_every-th step (and the
+ * last) the Westervelt energy, max|v_h|, min(1 - 2βv_h) (src/solver.jl:864-888) and
+ * the slice of v_h along y = slice_y -- with kernels on the workspace stream, and
+ * takes the snapshots of v_h on the (N q_u1)² point grid after the listed steps.
+ * The time t advances by t += dt after every step, as in the reference. The run
+ * stops at the first step with a non-finite state (the reference's "blow-up"),
+ * reported through steps_done and finite; errors of the RHS as wedg_rk4_steps.
+ * Receiver and slice positions are given as the element and the Legendre values
+ * at the local coordinate, which the host computes as the reference does
+ * (`locate`, `vrow`, src/solver.jl:898-899). Outputs are host arrays. */
+typedef struct wedg_source_run {
+  int64_t nsteps, record_every;
+  double t0, dt;
+  int nrec;                        /* receivers */
+  const int32_t *rec_j, *rec_k;    /* 0-based element row j (y) and column k (x) of each receiver */
+  const double *rec_py, *rec_px;   /* nrec × q_v1 (receiver-major): P_d at the local y and at the local x */
+  int slice_j;                     /* 0-based element row of the slice */
+  const double *slice_py;          /* q_v1: P_d at the slice's local y */
+  int nsnap;                       /* snapshots, after these step counts (1-based, increasing) */
+  const int64_t *snap_after;
+  const double *err_c2, *err_beta; /* c² and β at the u-quadrature points, (N, N, q_u1, q_u1) column-major */
+  double *recv;                    /* out: nsteps × nrec, step-major */
+  double *energy, *vmax, *ndmin;   /* out: one per record, ceil(nsteps / record_every) records */
+  double *slices;                  /* out: records × N q_u1 */
+  double *snaps;                   /* out: nsnap × (N q_u1)², each column-major */
+} wedg_source_run;
+int wedg_run_source(wedg_ws *ws, double *u, double *v, const int64_t u_shape[4], const int64_t v_shape[4],
+                    int where, const wedg_source_run *run, int64_t *steps_done, int *finite);
+
 /* Size of the static device array used by wedg_rhs_noalloc (16 MiB). */
 #define WEDG_NOALLOC_BYTES ((size_t)16 << 20)
 

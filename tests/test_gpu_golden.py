@@ -151,3 +151,38 @@ def test_steepening(gpu, case, beta, boundary):
     tol = 1e-8
     assert recv_err < tol and e_err < tol and v_err < tol and n_err < tol, out
     assert out.get("snap_rel", 0.0) < tol, out
+
+
+def test_source_run_diagnostics_against_oracle(gpu):
+    """The on-device source-mode loop (wedg_run_source) against the oracle's host loop on a
+    small case: receivers after every step, slices, energy, max|v_h|, min(1 - 2βv_h) at
+    every record (record_every not dividing nsteps, so the last step records too), and
+    snapshots, one of them with two snapshot times passed in the same step."""
+    from oracle.solver import solve as osolve
+    kw = dict(flux="alternating", mixed=False, mode="source", boundary=dict(bot="absorbing_2beta", top="wall",
+              lft="dirichlet", rgt="absorbing"), kappa=0.5,
+              coefficients=W.constant_coefficients(c=1.0, alpha=1e-4, beta=4.0),
+              source=W.GaussianSource(x0=(0.4, 0.55), r0=0.1, omega=12 * math.pi, Ts=0.5),
+              record_every=7, slice_y=0.37, receivers=[(0.45, 0.5), (0.71, 0.23), (0.05, 0.95)],
+              snap_times=[0.02, 0.0201, 0.05])
+    okw = dict(kw)
+    from oracle import coefficients as oc
+    okw["coefficients"] = oc.constant_coefficients(c=1.0, alpha=1e-4, beta=4.0)
+    okw["source"] = oc.GaussianSource(x0=(0.4, 0.55), r0=0.1, omega=12 * math.pi, Ts=0.5)
+    H = W.solve(3, 8, 0.06, **kw)
+    O = osolve(3, 8, 0.06, **okw)
+    n = len(O["recv_t"])
+    assert n % 7 != 0 and len(H["recv_t"]) == n
+    assert np.array_equal(np.asarray(H["recv_t"]), np.asarray(O["recv_t"]))
+    assert np.array_equal(np.asarray(H["t"]), np.asarray(O["t"]))
+
+    def rel(a, b):
+        a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
+        return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+    assert rel(H["recv"], O["recv"]) < 1e-12
+    assert rel(H["slices"], O["slices"]) < 1e-12
+    for k in ("energy", "vmax", "ndmin"):
+        assert rel(H[k], O[k]) < 1e-12, k
+    assert [t for t, _ in H["snaps"]] == [t for t, _ in O["snaps"]] and len(H["snaps"]) == 3
+    for (_, a), (_, b) in zip(H["snaps"], O["snaps"]):
+        assert rel(a, b) < 1e-12
