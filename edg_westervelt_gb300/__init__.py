@@ -12,9 +12,9 @@ from .coefficients import (Coefficients, GaussianSource, constant_coefficients, 
 from .precompute import precompute
 from .quadrature import GaussQCofs, GradJacobiP, JacobiP
 from .solver import difference_norms, solve
-from .workspace import DimensionMismatch, ErrorException, Workspace, edg_rhs, edg_rhs_, rk4_step, rk4_step_
+from .workspace import Batch, DimensionMismatch, ErrorException, Workspace, edg_rhs, edg_rhs_, rk4_step, rk4_step_
 
-__all__ = ["solve", "precompute", "edg_rhs", "edg_rhs_", "rk4_step", "rk4_step_", "Workspace",
+__all__ = ["solve", "precompute", "edg_rhs", "edg_rhs_", "rk4_step", "rk4_step_", "Workspace", "Batch",
            "difference_norms", "flux_parameters", "GaussianSource", "Coefficients", "paper_coefficients",
            "replace_coefficients", "constant_coefficients", "JacobiP", "GradJacobiP", "GaussQCofs",
            "ErrorException", "DimensionMismatch"]

@@ -104,6 +104,11 @@ def lib():
     L.wedg_rhs_noalloc.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Pre), vp, vp, ctypes.c_double, vp, vp, vp,
                                    ctypes.c_char_p, ctypes.c_size_t]
     L.wedg_time_kernels.argtypes = [vp, ctypes.c_int]
+    L.wedg_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    L.wedg_batch_destroy.argtypes = [vp]
+    L.wedg_batch_destroy.restype = None
+    L.wedg_batch_rk4_steps.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), _D, _D, ctypes.c_int64,
+                                       ctypes.c_int, _I64, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.wedg_run_source.argtypes = [vp, _D, _D, _I64, _I64, ctypes.c_int, ctypes.POINTER(SourceRun), _I64,
                                   ctypes.POINTER(ctypes.c_int)]
     L.wedg_kernel_times.argtypes = [vp, _D, _I64, _D, _I64, _D, _I64, ctypes.c_int]

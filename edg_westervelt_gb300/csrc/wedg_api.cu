@@ -243,7 +243,7 @@ void drain_events(wedg_ws *ws) {
 int enqueue_stage(wedg_ws *ws, const StageIO &S) {
   const int tp = 128, bp = (ws->E + tp - 1) / tp;
   const int ts = stage_threads(ws->nu, ws->nv, ws->fast), bs = (ws->E + ts - 1) / ts;
-  const int bm = (ws->E + MASS_THREADS - 1) / MASS_THREADS;
+  const int bm = 1;   // the mass kernels size their own grid
   StageIO Sp = S;
   Sp.parity = ws->parity;
   ws->parity = 1 - ws->parity;
@@ -256,7 +256,7 @@ int enqueue_stage(wedg_ws *ws, const StageIO &S) {
   if (ws->timing) cudaEventRecord(e1, ws->stream);
   ws->L.stage(ws->basis.data(), ws->F, Sp, bs, ts, ws->stream);
   if (ws->timing) cudaEventRecord(e2, ws->stream);
-  ws->L.mass(ws->basis.data(), ws->F, Sp, bm, MASS_THREADS, ws->stream);
+  ws->L.mass(ws->basis.data(), ws->F, Sp, bm, CHEB_THREADS, ws->stream);
   if (ws->timing) {
     cudaEventRecord(e3, ws->stream);
     ws->ev_pending.push_back({e0, e1, e2, e3});
@@ -268,7 +268,26 @@ int enqueue_stage(wedg_ws *ws, const StageIO &S) {
 }
 
 // one RK4 step on device state u, v (src/solver.jl:289-297)
-int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop_nonfinite) {
+// Time factors of the four stages of `count` steps from the step at time t (t advancing by
+// t += dt), 8 doubles per stage (the seven of StageIO and a pad), for graph replays.
+void factor_table(const wedg_ws *ws, double t, double dt, int64_t count, double *out) {
+  for (int64_t it = 0; it < count; ++it) {
+    const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
+    for (int s = 0; s < 4; ++s) {
+      StageIO S{};
+      stage_factors(ws, ts[s], S);
+      double *f = out + (it * 4 + s) * 8;
+      f[0] = S.ct; f[1] = S.st; f[2] = S.srct; f[3] = S.cSP; f[4] = S.cB; f[5] = S.cC; f[6] = S.cD; f[7] = 0.0;
+    }
+    t += dt;
+  }
+}
+
+// One RK4 step on the workspace stream. With tf != nullptr the stage kernels take their time
+// factors from the device table tf (tf_n steps, indexed by the device step counter), so that the
+// launches can be captured once into a CUDA graph and replayed for every step.
+int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop_nonfinite,
+                const double *tf = nullptr, long long tf_n = 0) {
   const double cs[3] = {0.5 * dt, 0.5 * dt, dt};
   const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
   const bool cg = ws->cfg.mass_solver == WEDG_CG;
@@ -276,7 +295,14 @@ int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop
     StageIO S{};
     S.xu = s == 0 ? u : ws->su;
     S.xv = s == 0 ? v : ws->sv;
-    stage_factors(ws, ts[s], S);
+    if (tf) {
+      S.tf = tf;
+      S.tf_n = tf_n;
+      S.step = ws->steps_done;
+      S.stage = s;
+    } else {
+      stage_factors(ws, ts[s], S);
+    }
     S.u0 = u; S.v0 = v;
     S.su = ws->su; S.sv = ws->sv;
     S.accu = ws->accu; S.accv = ws->accv;
@@ -393,6 +419,36 @@ struct RunBuffers {
 };
 
 }  // namespace
+
+// A batch of workspaces advanced by one replayed CUDA graph per step (wedg_batch_*)
+struct wedg_batch {
+  std::vector<wedg_ws *> ws;
+  cudaStream_t main = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaEvent_t half_done[2] = {nullptr, nullptr};   // the host half of the tables may be refilled
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  // what the captured graph was made for
+  std::vector<double *> gu, gv;
+  std::vector<double> gdt;
+  int gstop = -1;
+  // per instance: device factor table of 2 chunks (the kernels index it by step mod 2 chunks)
+  std::vector<double *> d_tf;
+  double *h_tf = nullptr;                           // pinned: 2 halves × instances × one chunk
+  ~wedg_batch() {
+    if (main) cudaStreamSynchronize(main);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (double *p : d_tf) cudaFree(p);
+    if (h_tf) cudaFreeHost(h_tf);
+    for (cudaEvent_t e : join) cudaEventDestroy(e);
+    for (cudaEvent_t e : half_done)
+      if (e) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (main) cudaStreamDestroy(main);
+  }
+};
 
 extern "C" {
 
@@ -674,6 +730,135 @@ int wedg_rk4_steps(wedg_ws *ws, double *u, double *v, double t0, double dt, int6
     CK(ws, cudaMemcpy(v, ws->d_v, bV, cudaMemcpyDeviceToHost));
   }
   return rc;
+}
+
+int wedg_batch_create(int n, wedg_ws *const *instances, wedg_batch **out) {
+  if (!out) return WEDG_ERR_ARGUMENT;
+  *out = nullptr;
+  if (n < 1 || !instances) return WEDG_ERR_ARGUMENT;
+  for (int i = 0; i < n; ++i)
+    if (!instances[i]) return WEDG_ERR_ARGUMENT;
+  wedg_batch *b = new wedg_batch();
+  b->ws.assign(instances, instances + n);
+  const size_t per = (size_t)2 * WEDG_BATCH_CHUNK * 4 * 8;    // doubles of one instance's table
+  bool ok = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->half_done[0], cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->half_done[1], cudaEventDisableTiming) == cudaSuccess &&
+            cudaMallocHost(&b->h_tf, sizeof(double) * per * n) == cudaSuccess;
+  for (int i = 0; i < n && ok; ++i) {
+    cudaEvent_t e = nullptr;
+    double *d = nullptr;
+    ok = cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    if (ok) b->join.push_back(e);
+    ok = ok && cudaMalloc(&d, sizeof(double) * per) == cudaSuccess;
+    if (ok) b->d_tf.push_back(d);
+  }
+  if (!ok) {
+    cudaGetLastError();
+    delete b;
+    return WEDG_ERR_CUDA;
+  }
+  *out = b;
+  return WEDG_OK;
+}
+
+void wedg_batch_destroy(wedg_batch *b) { delete b; }
+
+int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_dev, const double *t0,
+                         const double *dt, int64_t nsteps, int stop_nonfinite, int64_t *steps_done, int *finite,
+                         int *status) {
+  if (!b || !u_dev || !v_dev || !t0 || !dt || nsteps < 0) return WEDG_ERR_ARGUMENT;
+  const int n = (int)b->ws.size();
+  const int64_t C = WEDG_BATCH_CHUNK;
+  for (int i = 0; i < n; ++i)
+    if (!u_dev[i] || !v_dev[i]) return WEDG_ERR_ARGUMENT;
+  auto cuda_err = [&](cudaError_t e) {
+    for (wedg_ws *w : b->ws) cuda_fail(w, e, "wedg_batch_rk4_steps");
+    return WEDG_ERR_CUDA;
+  };
+#define BK(call)                                  \
+  do {                                            \
+    cudaError_t e_ = (call);                      \
+    if (e_ != cudaSuccess) return cuda_err(e_);   \
+  } while (0)
+  // ---- flags of every instance reset on its stream, before anything of the batch's stream
+  for (int i = 0; i < n; ++i) {
+    wedg_ws *w = b->ws[i];
+    w->stats.kernel_launches = 0;
+    int rc = reset_flags(w);
+    if (rc) return rc;
+    BK(cudaEventRecord(b->join[i], w->stream));
+    BK(cudaStreamWaitEvent(b->main, b->join[i], 0));
+  }
+  // ---- the graph of one step of every instance, captured again when its key changed
+  bool same = b->exec && b->gstop == (stop_nonfinite ? 1 : 0);
+  for (int i = 0; i < n && same; ++i) same = b->gu[i] == u_dev[i] && b->gv[i] == v_dev[i] && b->gdt[i] == dt[i];
+  if (!same) {
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    BK(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = cudaEventRecord(b->fork, b->main);
+    int rc = WEDG_OK;
+    for (int i = 0; i < n && ce == cudaSuccess && rc == WEDG_OK; ++i) {
+      wedg_ws *w = b->ws[i];
+      ce = cudaStreamWaitEvent(w->stream, b->fork, 0);
+      if (ce != cudaSuccess) break;
+      const bool timing = w->timing;
+      w->timing = false;
+      rc = enqueue_rk4(w, u_dev[i], v_dev[i], 0.0, dt[i], stop_nonfinite ? 1 : 0, b->d_tf[i], 2 * C);
+      w->timing = timing;
+      if (rc == WEDG_OK) ce = cudaEventRecord(b->join[i], w->stream);
+      if (ce == cudaSuccess && rc == WEDG_OK) ce = cudaStreamWaitEvent(b->main, b->join[i], 0);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce2 = cudaStreamEndCapture(b->main, &g);
+    if (rc != WEDG_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ce != cudaSuccess || ce2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return cuda_err(ce != cudaSuccess ? ce : ce2);
+    }
+    b->graph = g;
+    BK(cudaGraphInstantiate(&b->exec, g, 0));
+    b->gu.assign(u_dev, u_dev + n);
+    b->gv.assign(v_dev, v_dev + n);
+    b->gdt.assign(dt, dt + n);
+    b->gstop = stop_nonfinite ? 1 : 0;
+  }
+  // ---- the steps, one chunk of factor tables at a time (double-buffered, host and device)
+  const size_t chunk = (size_t)C * 4 * 8;
+  std::vector<double> t(t0, t0 + n);
+  for (int64_t c = 0; c * C < nsteps; ++c) {
+    const int half = (int)(c & 1);
+    const int64_t cnt = std::min<int64_t>(C, nsteps - c * C);
+    if (c >= 2) BK(cudaEventSynchronize(b->half_done[half]));   // its last upload has been read
+    double *h = b->h_tf + (size_t)half * n * chunk;
+    for (int i = 0; i < n; ++i) {
+      factor_table(b->ws[i], t[i], dt[i], cnt, h + (size_t)i * chunk);
+      for (int64_t it = 0; it < cnt; ++it) t[i] += dt[i];
+    }
+    for (int i = 0; i < n; ++i)
+      BK(cudaMemcpyAsync(b->d_tf[i] + (size_t)half * chunk, h + (size_t)i * chunk, sizeof(double) * cnt * 32,
+                         cudaMemcpyHostToDevice, b->main));
+    BK(cudaEventRecord(b->half_done[half], b->main));
+    for (int64_t it = 0; it < cnt; ++it) BK(cudaGraphLaunch(b->exec, b->main));
+  }
+  BK(cudaStreamSynchronize(b->main));
+#undef BK
+  int first = WEDG_OK;
+  for (int i = 0; i < n; ++i) {
+    wedg_ws *w = b->ws[i];
+    w->stats.kernel_launches = 0;
+    const int rc = collect(w);
+    if (steps_done) steps_done[i] = w->stats.steps_done;
+    if (finite) finite[i] = w->stats.finite;
+    if (status) status[i] = rc;
+    if (rc != WEDG_OK && first == WEDG_OK) first = rc;
+  }
+  return first;
 }
 
 int wedg_run_source(wedg_ws *ws, double *u, double *v, const int64_t u_shape[4], const int64_t v_shape[4],

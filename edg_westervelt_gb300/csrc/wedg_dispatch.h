@@ -69,24 +69,17 @@ void launch_stage(const void *basis, const Fields &F, const StageIO &S, int bloc
   k_stage<NU, NV, FAST><<<blocks, threads, smem, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S);
 }
 
-// The mass solve: k_cheb (a team of threads per element, static shared memory; `blocks` only
-// says whether to launch) or k_cg (one thread per element, r, X, p and A p in dynamic shared memory)
+// The mass solve: k_cheb or k_cg, a team of threads per element (static shared memory; the
+// grid follows from F.E, `blocks` only says whether to launch)
 template <int NU, int NV>
 void launch_mass(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_cg<NU, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cg_smem(NV));
-    attr = true;
-  }
   if (blocks <= 0) return;
   (void)threads;
   const Basis<NU, NV> &B = *static_cast<const Basis<NU, NV> *>(basis);
-  if (F.cg) {
-    k_cg<NU, NV><<<(F.E + MASS_THREADS - 1) / MASS_THREADS, MASS_THREADS, cg_smem(NV), st>>>(B, F, S);
-  } else {
-    constexpr int tpb = ChebTeam<NU, NV>::TPB;
-    k_cheb<NU, NV><<<(F.E + tpb - 1) / tpb, CHEB_THREADS, 0, st>>>(B, F, S);
-  }
+  constexpr int tpb = ChebTeam<NU, NV>::TPB;
+  const int grid = (F.E + tpb - 1) / tpb;
+  if (F.cg) k_cg<NU, NV><<<grid, CHEB_THREADS, 0, st>>>(B, F, S);
+  else k_cheb<NU, NV><<<grid, CHEB_THREADS, 0, st>>>(B, F, S);
 }
 
 template <int NU, int NV>

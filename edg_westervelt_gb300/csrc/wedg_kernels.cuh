@@ -25,7 +25,7 @@
 //            update, a team of threads per element. Elements are visited in
 //            decreasing order of their Chebyshev step counts (k_prep lists them
 //            by count), so the longest solves start first;
-//   k_cg     the same with conjugate gradients (:821-853), one thread per element.
+//   k_cg     the same with conjugate gradients (:821-853), also a team per element.
 // Interior faces are evaluated by both neighbours, each writing only its own
 // slots, so no element writes another element's data.
 //
@@ -50,8 +50,7 @@ namespace wedg {
 constexpr unsigned long long ERR_NONE = ~0ull;
 constexpr int ERR_CLASS_SHIFT = 56;   // class 0: boundary weight, 1: mass matrix not PD, 3: stopped (non-finite)
 constexpr int NBIN = 48;              // Chebyshev-count bins of the mass kernel (the last holds n ≥ NBIN)
-constexpr int MASS_THREADS = 64;     // threads per block of k_cg
-constexpr int CHEB_THREADS = 128;    // threads per block of k_cheb
+constexpr int CHEB_THREADS = 128;    // threads per block of the mass-solve kernels
 
 __host__ __device__ constexpr int qhigh(int nu, int nv) {
   // q_high = max(ceil(3 q_v / 2) + 1, q_u + 1), src/solver.jl:483
@@ -117,6 +116,13 @@ struct StageIO {
   const double *xu, *xv;     // stage state
   double ct, st, srct;       // time factors of the stage (src/rhs.jl:509-511)
   double cSP, cB, cC, cD;    // source weights: -ω²ct, -2ω³ st ct, 1 - ct, ω st
+  // or, for launches replayed from a CUDA graph, the same seven factors (and one pad) from a
+  // host-computed table of tf_n steps: tf[((step mod tf_n)·4 + stage)·8 + f], step = *step (the
+  // workspace's device step counter); the host refills the table every tf_n steps
+  const double *tf;
+  const long long *step;
+  long long tf_n;
+  int stage;
   int mode, first;
   int parity;                // which bin-count buffer this stage fills (the other is cleared)
   double *ut, *vt;           // OUT_RHS
@@ -126,6 +132,18 @@ struct StageIO {
   double *uo, *vo;           // in-place target of the last stage
   double c;                  // next-stage factor, or dt/6 on the last stage
 };
+
+// The time factors of a stage: from the launch parameters, or from the table of a graph replay
+struct TimeF {
+  double ct, st, srct, cSP, cB, cC, cD;
+};
+__device__ __forceinline__ TimeF time_factors(const StageIO &S) {
+  if (!S.tf) return TimeF{S.ct, S.st, S.srct, S.cSP, S.cB, S.cC, S.cD};
+  long long it = *(volatile const long long *)S.step;
+  it = it < 0 ? 0 : it % S.tf_n;
+  const double *f = S.tf + (it * 4 + S.stage) * 8;
+  return TimeF{f[0], f[1], f[2], f[3], f[4], f[5], f[6]};
+}
 
 __device__ __forceinline__ unsigned long long err_word(const Fields &F) {
   return *(volatile unsigned long long *)F.err;
@@ -304,6 +322,7 @@ __global__ void __launch_bounds__(128, 3) k_prep(const __grid_constant__ Basis<N
   trace4<NQ, NU, NV, false>(V, B.P, B.El, F.tr, 1, E, e);
   trace4<NQ, NU, NV, true>(V, B.P, B.E1l, F.tr, 2, E, e);
 
+  const TimeF tf = time_factors(S);
   // weight check 1 - kβv > 0 for the trace and the data on physical sides
   // (src/rhs.jl:109-110, 751-757); key of src/rhs.jl:732
   const bool onb[4] = {j == 0, j == N - 1, k == 0, k == N - 1};
@@ -317,7 +336,7 @@ __global__ void __launch_bounds__(128, 3) k_prep(const __grid_constant__ Basis<N
       const double bf = s < 2 ? F.hbf[(s == 0 ? 0 : N) + (size_t)(N + 1) * (k + (size_t)N * i)]
                               : F.vbf[j + (size_t)N * ((s == 2 ? 0 : N) + (size_t)(N + 1) * i)];
       const double v_fp = F.tr[((1 * 4 + s) * NQ + i) * (size_t)E + e];
-      const double v_ex = -F.omega * S.st * F.bsp[s][m + (size_t)N * i];
+      const double v_ex = -F.omega * tf.st * F.bsp[s][m + (size_t)N * i];
       const int check = (1.0 - F.kb[s] * bf * v_fp <= 0.0) ? 1 : (1.0 - F.kb[s] * bf * v_ex <= 0.0) ? 2 : 0;
       if (check) {
         const unsigned long long kk =
@@ -405,7 +424,7 @@ __global__ void __launch_bounds__(128, 3) k_prep(const __grid_constant__ Basis<N
 // Numerical flux slots A, D, F at point i of side s of the element
 // (src/rhs.jl:620-700 for interior faces, :65-103 and :738-763 for physical sides).
 template <int NU, int NV>
-__device__ __forceinline__ void side_point(const Basis<NU, NV> &B, const Fields &F, const StageIO &S, int s,
+__device__ __forceinline__ void side_point(const Basis<NU, NV> &B, const Fields &F, const TimeF &S, int s,
                                            bool boundary, int j, int k, int e, int i, double &A, double &D,
                                            double &Fs) {
   constexpr int NQ = NU;
@@ -512,6 +531,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
   if (err_word(F) != ERR_NONE) return;
   const int j = e % N, k = e / N;
   const double two_h = F.two_h, four_hh = F.four_hh;
+  const TimeF tf = time_factors(S);
   // thread-private blocks: b (NU², the u-equation right-hand side, then UT) and R_v (NV², the
   // v-equation right-hand side); the general kernels also keep U (NU²) and V (NV²)
   Blk<NU, BT> bb{smem + tid};
@@ -548,8 +568,8 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
 #pragma unroll 1
       for (int i = 0; i < NQ / 2; ++i) {
         double A1, D1, F1, A2, D2, F2;
-        side_point<NU, NV>(B, F, S, s, boundary, j, k, e, i, A1, D1, F1);
-        side_point<NU, NV>(B, F, S, s, boundary, j, k, e, NQ - 1 - i, A2, D2, F2);
+        side_point<NU, NV>(B, F, tf, s, boundary, j, k, e, i, A1, D1, F1);
+        side_point<NU, NV>(B, F, tf, s, boundary, j, k, e, NQ - 1 - i, A2, D2, F2);
         const double as = A1 + A2, ad = A1 - A2, ds = D1 + D2, dd = D1 - D2, fs = F1 + F2, fd = F1 - F2;
 #pragma unroll
         for (int b = 0; b < NU; ++b) {
@@ -563,7 +583,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
       }
       if constexpr ((NQ & 1) != 0) {         // the middle point: the odd modes vanish there
         double A1, D1, F1;
-        side_point<NU, NV>(B, F, S, s, boundary, j, k, e, NQ / 2, A1, D1, F1);
+        side_point<NU, NV>(B, F, tf, s, boundary, j, k, e, NQ / 2, A1, D1, F1);
 #pragma unroll
         for (int b = 0; b < NU; b += 2) {
           const double p = B.Pw[NQ / 2][b];
@@ -785,14 +805,14 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
       const size_t l = (a + NV * b) * Eu + e;
       double x = Rv(a, b);
       if (F.mms_on) {
-        x = fma(S.cSP, F.PiSP[l], x);
-        x = fma(S.cB, F.PiBSP2[l], x);
-        x = fma(S.cC, F.PiCdiv[l], x);
-        x = fma(S.cD, F.PiDdiv[l], x);
+        x = fma(tf.cSP, F.PiSP[l], x);
+        x = fma(tf.cB, F.PiBSP2[l], x);
+        x = fma(tf.cC, F.PiCdiv[l], x);
+        x = fma(tf.cD, F.PiDdiv[l], x);
       } else if (!F.src_on) {
         x += F.PiCdiv[l];
       }
-      if (F.src_on) x = fma(S.srct, F.srcP[l], x);
+      if (F.src_on) x = fma(tf.srct, F.srcP[l], x);
       F.mrhs[l] = x;
     }
 
@@ -947,19 +967,18 @@ __device__ __forceinline__ void store_v(const StageIO &S, size_t l, double kk, b
   }
 }
 
-// k_cheb: the Chebyshev mass solve (Saad Alg. 12.1, src/rhs.jl:920-939) with a team of threads
-// per element. One Chebyshev step costs one application of K = P_h^T diag(G W) P_h (G = 2βv at
-// the high-order points, W = w_h w_h^T their weights, folded into PhW), and its FP64 work is cut
-// across the team by rows of the point grid:
-// unit u of the team takes the mirrored rows u and QH-1-u (the middle row alone when QH is odd),
-// takes them to the points and back (phase 1), and leaves for each mode column b the sum and
-// the difference of the two rows' results in shared memory; then every thread finishes J of the
-// NV² modal entries from the units' rows (phase 2), for which it also keeps the residual, the
-// iterate and the search direction. A team lives in one warp, so its phases are ordered by
-// __syncwarp on the team's lanes. Spreading an element over the team matters because one warp
-// is tied to one SM sub-partition, whose FP64 rate is a small fraction of a lane per clock: with
-// one element per thread, the warps of the elements with the most Chebyshev steps ran for many
-// times the average and left the SMs idle behind them.
+// The mass solves run on a team of threads per element. One step of either solver costs one
+// application of K = P_h^T diag(G W) P_h (G = 2βv at the high-order points, W = w_h w_h^T their
+// weights, folded into PhW) to a vector of NV² modal entries, and its FP64 work is cut across
+// the team by rows of the point grid: unit u of the team takes the mirrored rows u and QH-1-u
+// (the middle row alone when QH is odd), takes them to the points and back (phase 1), and leaves
+// for each mode column b the sum and the difference of the two rows' results in shared memory;
+// then every thread finishes J of the NV² modal entries from the units' rows (phase 2), for
+// which it also keeps the solver's vectors. A team lives in one warp, so its phases are ordered
+// by __syncwarp on the team's lanes. Spreading an element over the team matters because one
+// warp is tied to one SM sub-partition, whose FP64 rate is a small fraction of a lane per clock:
+// with one element per thread, the warps of the elements with the most steps ran for many times
+// the average and left the SMs idle behind them.
 template <int NU, int NV>
 struct ChebTeam {
   static constexpr int QH = qhigh(NU, NV);
@@ -968,40 +987,127 @@ struct ChebTeam {
   static constexpr int TPB = TPW * (CHEB_THREADS / 32); // elements per block
   static constexpr int NE = NV * NV;
   static constexpr int J = (NE + U - 1) / U;            // modal entries per thread
-  static constexpr int SLOT = NE + 2 * U * NV;          // d, then the row sums and differences
+  static constexpr int SLOT = NE + 2 * U * NV;          // x, then the row sums and differences
 };
 
+// The shared setup of a team kernel: Ph and PhW in shared memory, the team of this thread, its
+// unit, its lanes. Returns false for lanes without a team.
+struct TeamPos {
+  int slot, u;
+  unsigned mask;
+};
+template <int NU, int NV>
+__device__ __forceinline__ bool team_pos(TeamPos &P) {
+  using T = ChebTeam<NU, NV>;
+  const int lane = threadIdx.x & 31, tw = lane / T::U;
+  if (tw >= T::TPW) return false;
+  P.u = lane - tw * T::U;
+  P.slot = (threadIdx.x >> 5) * T::TPW + tw;
+  P.mask = ((1u << T::U) - 1u) << (tw * T::U);
+  return true;
+}
+
+// Σ over the team's lanes of x, in the order of the units, on every lane of the team
+template <int U>
+__device__ __forceinline__ double team_sum(double x, unsigned mask) {
+  const int base = __ffs(mask) - 1;
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < U; ++i) s += __shfl_sync(mask, x, base + i);
+  return s;
+}
+
+// acc[j] ± (K x)[k_j] on the thread's entries k_j = u + U j (+ with SIGN = 1, - with -1), for x in
+// the team's shared slot xs (complete, after a __syncwarp). zs, zd hold the units' row results
+// until the next __syncwarp of the caller.
+template <int NU, int NV, int SIGN>
+__device__ __forceinline__ void team_K(const Basis<NU, NV> &B, const Fields &F, size_t Eu, int e, int u,
+                                       unsigned mask, const double *Phs, const double *PhWs, const double *xs,
+                                       double *zs, double *zd, double (&acc)[ChebTeam<NU, NV>::J]) {
+  using T = ChebTeam<NU, NV>;
+  constexpr int QH = T::QH, U = T::U, NE = T::NE, J = T::J;
+  const int r1 = u, r2 = QH - 1 - u;                    // the unit's rows (r1 = r2 for the middle row)
+  auto rowZ = [&](const double (&Tv)[NV], int r, double (&Z)[NV]) {
+    double Y[QH];
+    ph_to_points<QH, NV>(B.Ph, Tv, Y);
+#pragma unroll
+    for (int s2 = 0; s2 < QH; ++s2) Y[s2] *= F.G[(r + QH * s2) * Eu + e];
+    ph_from_points<QH, NV>(B.PhW, Y, Z);
+  };
+  // phase 1: rows r1, r2 of P_h x, at the points, weighted, back to the modes
+  {
+    double Tp[NV], Tm[NV], Zp[NV], Zm[NV];
+#pragma unroll
+    for (int b = 0; b < NV; ++b) {
+      double ev = 0.0, od = 0.0;
+#pragma unroll
+      for (int a = 0; a < NV; a += 2) ev = fma(Phs[r1 * NV + a], xs[a + NV * b], ev);
+#pragma unroll
+      for (int a = 1; a < NV; a += 2) od = fma(Phs[r1 * NV + a], xs[a + NV * b], od);
+      Tp[b] = ev + od;
+      Tm[b] = ev - od;
+    }
+    rowZ(Tp, r1, Zp);
+    rowZ(Tm, r2, Zm);
+#pragma unroll
+    for (int b = 0; b < NV; ++b) {
+      zs[u * NV + b] = r1 == r2 ? Zp[b] : Zp[b] + Zm[b];
+      zd[u * NV + b] = Zp[b] - Zm[b];
+    }
+  }
+  __syncwarp(mask);
+  // phase 2: the thread's entries
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const int k = u + U * j;
+    if (k < NE) {
+      const int a = k % NV, b = k / NV;
+      const double *z = ((a & 1) ? zd : zs) + b;
+      double x = acc[j];
+#pragma unroll
+      for (int v = 0; v < U; ++v) x = fma(SIGN * PhWs[v * NV + a], z[v * NV], x);
+      acc[j] = x;
+    }
+  }
+}
+
+// Shared memory of a team kernel and its setup: the bin prefix (sorted order) and the bases
+#define WEDG_TEAM_SETUP()                                                                       \
+  using T = ChebTeam<NU, NV>;                                                                   \
+  constexpr int U = T::U, NE = T::NE, J = T::J;                                                 \
+  __shared__ double sh[T::TPB * T::SLOT];                                                       \
+  __shared__ double Phs[T::QH * NV], PhWs[T::QH * NV];                                          \
+  __shared__ int pref[NBIN];                                                                    \
+  for (int i = threadIdx.x; i < T::QH * NV; i += CHEB_THREADS) {                               \
+    Phs[i] = B.Ph[i / NV][i % NV];                                                              \
+    PhWs[i] = B.PhW[i / NV][i % NV];                                                            \
+  }                                                                                             \
+  if (F.sorted && threadIdx.x == 0) {                                                           \
+    int acc_ = 0;                                                                               \
+    for (int b = NBIN - 1; b >= 0; --b) { pref[b] = acc_; acc_ += F.bin_count[S.parity * NBIN + b]; } \
+  }                                                                                             \
+  __syncthreads();                                                                              \
+  TeamPos tp;                                                                                   \
+  if (!team_pos<NU, NV>(tp)) return;                                                            \
+  const int g = blockIdx.x * T::TPB + tp.slot;                                                  \
+  if (g >= F.E) return;                                                                         \
+  if (err_word(F) != ERR_NONE) return;                                                          \
+  const int u = tp.u;                                                                           \
+  const unsigned tmask = tp.mask;                                                               \
+  const size_t Eu = (size_t)F.E;                                                                \
+  double *xs = sh + tp.slot * T::SLOT, *zs = xs + NE, *zd = zs + U * NV;                        \
+  (void)Eu;
+
+// k_cheb: the Chebyshev mass solve (Saad Alg. 12.1, src/rhs.jl:920-939). Elements are visited in
+// decreasing order of their step counts (k_prep lists them by count), so the longest solves start
+// first. The team keeps the residual r, the iterate X and the direction d of its entries in
+// registers and d in its shared slot.
 template <int NU, int NV>
 __global__ void __launch_bounds__(CHEB_THREADS, 3)
     k_cheb(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
            const __grid_constant__ StageIO S) {
-  using T = ChebTeam<NU, NV>;
-  constexpr int QH = T::QH, U = T::U, NE = T::NE, J = T::J;
-  __shared__ double sh[T::TPB * T::SLOT];
-  __shared__ double Phs[QH * NV], PhWs[QH * NV];
-  __shared__ int pref[NBIN];
-  const int tid = threadIdx.x, lane = tid & 31;
-  for (int i = tid; i < QH * NV; i += CHEB_THREADS) {
-    Phs[i] = B.Ph[i / NV][i % NV];
-    PhWs[i] = B.PhW[i / NV][i % NV];
-  }
-  if (F.sorted && tid == 0) {
-    // exclusive prefix sum of the counts of this stage's bins, from the last bin down
-    int acc = 0;
-    for (int b = NBIN - 1; b >= 0; --b) { pref[b] = acc; acc += F.bin_count[S.parity * NBIN + b]; }
-  }
-  __syncthreads();
-  const int tw = lane / U, u = lane - tw * U;           // team in the warp, unit in the team
-  if (tw >= T::TPW) return;
-  const int slot = (tid >> 5) * T::TPW + tw;
-  const int g = blockIdx.x * T::TPB + slot;
-  if (g >= F.E) return;
-  if (err_word(F) != ERR_NONE) return;
-  const unsigned tmask = ((1u << U) - 1u) << (tw * U);
+  WEDG_TEAM_SETUP();
   const int e = mass_element(F, S, g, pref);
-  const size_t Eu = (size_t)F.E;
-  double *dsm = sh + slot * T::SLOT, *zs = dsm + NE, *zd = zs + U * NV;
-
   const double th = F.th[e], de = F.de[e];
   const double s1 = th / de;
   const int n = F.cheb_common ? *F.nmax : F.nst[e];
@@ -1015,18 +1121,10 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
       const double x = F.mrhs[k * Eu + e];
       rr[j] = x;
       dd[j] = x * ith;
-      dsm[k] = dd[j];
+      xs[k] = dd[j];
     }
   }
   __syncwarp(tmask);
-  const int r1 = u, r2 = QH - 1 - u;                    // the unit's rows (r1 = r2 for the middle row)
-  auto rowZ = [&](const double (&Tv)[NV], int r, double (&Z)[NV]) {
-    double Y[QH];
-    ph_to_points<QH, NV>(B.Ph, Tv, Y);
-#pragma unroll
-    for (int s2 = 0; s2 < QH; ++s2) Y[s2] *= F.G[(r + QH * s2) * Eu + e];
-    ph_from_points<QH, NV>(B.PhW, Y, Z);
-  };
   double rho = 1.0 / s1;
 #pragma unroll 1
   for (int step = 1; step <= n; ++step) {
@@ -1036,43 +1134,15 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
       rr[j] -= dd[j];
     }
     if (step == n) break;
-    // phase 1: rows r1, r2 of P_h d, at the points, weighted, back to the modes
-    {
-      double Tp[NV], Tm[NV], Zp[NV], Zm[NV];
-#pragma unroll
-      for (int b = 0; b < NV; ++b) {
-        double ev = 0.0, od = 0.0;
-#pragma unroll
-        for (int a = 0; a < NV; a += 2) ev = fma(Phs[r1 * NV + a], dsm[a + NV * b], ev);
-#pragma unroll
-        for (int a = 1; a < NV; a += 2) od = fma(Phs[r1 * NV + a], dsm[a + NV * b], od);
-        Tp[b] = ev + od;
-        Tm[b] = ev - od;
-      }
-      rowZ(Tp, r1, Zp);
-      rowZ(Tm, r2, Zm);
-#pragma unroll
-      for (int b = 0; b < NV; ++b) {
-        zs[u * NV + b] = r1 == r2 ? Zp[b] : Zp[b] + Zm[b];
-        zd[u * NV + b] = Zp[b] - Zm[b];
-      }
-    }
-    __syncwarp(tmask);
-    // phase 2: r += K d on this thread's entries, then the next direction
+    team_K<NU, NV, 1>(B, F, Eu, e, u, tmask, Phs, PhWs, xs, zs, zd, rr);   // r += K d
     const double rhon = 1.0 / (2.0 * s1 - rho);
     const double c1 = rhon * rho, c2 = 2.0 * rhon / de;
 #pragma unroll
     for (int j = 0; j < J; ++j) {
       const int k = u + U * j;
       if (k < NE) {
-        const int a = k % NV, b = k / NV;
-        const double *z = ((a & 1) ? zd : zs) + b;
-        double acc = rr[j];
-#pragma unroll
-        for (int v = 0; v < U; ++v) acc = fma(PhWs[v * NV + a], z[v * NV], acc);
-        rr[j] = acc;
-        dd[j] = fma(c1, dd[j], c2 * acc);
-        dsm[k] = dd[j];
+        dd[j] = fma(c1, dd[j], c2 * rr[j]);
+        xs[k] = dd[j];
       }
     }
     rho = rhon;
@@ -1088,159 +1158,108 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
   if (S.mode == OUT_RK4_LAST && !fin) atomicOr(F.nonfinite, 1u);
 }
 
-// k_cg: the mass solve by conjugate gradients (src/rhs.jl:821-853), one thread per element
+// k_cg: the mass solve by conjugate gradients from X = R (src/rhs.jl:821-853), elements in mesh
+// order. The team first forms G = 2βv at the high-order points of its rows (each unit reads only
+// the rows it wrote), then iterates with p in its shared slot and the inner products summed over
+// the team's lanes in a fixed order, so that every lane takes the same decisions.
 template <int NU, int NV>
-__global__ void __launch_bounds__(MASS_THREADS)
+__global__ void __launch_bounds__(CHEB_THREADS, 3)
     k_cg(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
-           const __grid_constant__ StageIO S) {
-  constexpr int QH = Basis<NU, NV>::QH, BT = MASS_THREADS;
-  extern __shared__ double smem[];
-  const int tid = threadIdx.x;
-  const int E = F.E;
-  const size_t Eu = (size_t)E;
-  const int e = blockIdx.x * BT + tid;           // mesh order
-  if (e >= E) return;
-  if (err_word(F) != ERR_NONE) return;
-  Blk<NV, BT> r{smem + tid}, X{smem + NV * NV * BT + tid};
-  bool fin = true;
-
-  // K P accumulated into O: O += P_h^T ((G W) ∘ (P_h P P_h^T)) P_h (G = 2βv, W = w_h w_h^T folded
-  // into PhW), for a mirrored pair of rows
-  // of the point grid at a time (row QH-1-r of P_h P is the even part minus the odd part of
-  // row r, and both rows go back to the modes through one sum and one difference)
-  auto rowZ = [&](const double (&T)[NV], int r, double (&Z)[NV]) {
-    double Y[QH];
-    ph_to_points<QH, NV>(B.Ph, T, Y);
-#pragma unroll
-    for (int s2 = 0; s2 < QH; ++s2) Y[s2] *= F.G[(r + QH * s2) * Eu + e];
-    ph_from_points<QH, NV>(B.PhW, Y, Z);
-  };
-  auto addK = [&](Blk<NV, BT> P, Blk<NV, BT> O) {
-    auto px = [&](int a, int b) { return P(a, b); };
-#pragma unroll 1
-    for (int r2 = 0; r2 < QH / 2; ++r2) {
-      double Zp[NV], Zm[NV];
-      {
-        double Tp[NV], Tm[NV];
-        ph_row_pair<QH, NV>(B.Ph, r2, px, Tp, Tm);
-        rowZ(Tp, r2, Zp);
-        rowZ(Tm, QH - 1 - r2, Zm);
-      }
-#pragma unroll
-      for (int b = 0; b < NV; ++b) {
-        const double zs = Zp[b] + Zm[b], zd = Zp[b] - Zm[b];
-#pragma unroll
-        for (int a = 0; a < NV; ++a) O(a, b) = fma(B.PhW[r2][a], (a & 1) ? zd : zs, O(a, b));
-      }
-    }
-    if constexpr ((QH & 1) != 0) {
-      double T[NV], Z[NV];
-      ph_row_mid<QH, NV>(B.Ph, px, T);
-      rowZ(T, QH / 2, Z);
-#pragma unroll
-      for (int b = 0; b < NV; ++b)
-#pragma unroll
-        for (int a = 0; a < NV; a += 2) O(a, b) = fma(B.PhW[QH / 2][a], Z[b], O(a, b));
-    }
-  };
-
+         const __grid_constant__ StageIO S) {
+  WEDG_TEAM_SETUP();
+  constexpr int QH = T::QH;
+  const int e = g;
   {
-    // conjugate gradients from X = R (src/rhs.jl:824-853)
-    Blk<NV, BT> p{smem + 2 * NV * NV * BT + tid}, Ap{smem + 3 * NV * NV * BT + tid};
-    // G = 2βv_q of this element, by mirrored pairs of rows
+    // G rows u and QH-1-u of this element
+    const int r1 = u, r2 = QH - 1 - u;
     auto vx = [&](int a, int b) { return S.xv[e + Eu * (a + NV * b)]; };
-    auto gput = [&](const double (&T)[NV], int r2) {
+    double Tp[NV], Tm[NV];
+    ph_row_pair<QH, NV>(B.Ph, r1, vx, Tp, Tm);
+    auto gput = [&](const double (&Tv)[NV], int r) {
       double Y[QH];
-      ph_to_points<QH, NV>(B.Ph, T, Y);
+      ph_to_points<QH, NV>(B.Ph, Tv, Y);
 #pragma unroll
       for (int s2 = 0; s2 < QH; ++s2) {
-        const size_t gi = (r2 + QH * s2) * Eu + e;
+        const size_t gi = (r + QH * s2) * Eu + e;
         F.G[gi] = Y[s2] * F.beta2[gi];
       }
     };
-#pragma unroll 1
-    for (int r2 = 0; r2 < QH / 2; ++r2) {
-      double Tp[NV], Tm[NV];
-      ph_row_pair<QH, NV>(B.Ph, r2, vx, Tp, Tm);
-      gput(Tp, r2);
-      gput(Tm, QH - 1 - r2);
-    }
-    if constexpr ((QH & 1) != 0) {
-      double T[NV];
-      ph_row_mid<QH, NV>(B.Ph, vx, T);
-      gput(T, QH / 2);
-    }
-    double r0 = 0;
-#pragma unroll 1
-    for (int b = 0; b < NV; ++b)
-#pragma unroll
-      for (int a = 0; a < NV; ++a) {
-        const double x = F.mrhs[(a + NV * b) * Eu + e];
-        X(a, b) = x;
-        p(a, b) = x;
-        r(a, b) = 0.0;
-        r0 = fma(x, x, r0);
-      }
-    addK(p, r);                                    // r = R - M X = K R for X = R
-    double rr = 0;
-#pragma unroll 1
-    for (int b = 0; b < NV; ++b)
-#pragma unroll
-      for (int a = 0; a < NV; ++a) { const double x = r(a, b); p(a, b) = x; rr = fma(x, x, rr); }
-    r0 = sqrt(r0);
-    const int maxit = NV * NV + 10;
-    int it = 0;
-    bool bad = false;
-    while (sqrt(rr) > F.mass_tol * r0 && it < maxit) {
-      ++it;
-#pragma unroll 1
-      for (int b = 0; b < NV; ++b)
-#pragma unroll
-        for (int a = 0; a < NV; ++a) Ap(a, b) = 0.0;
-      addK(p, Ap);
-      double pAp = 0;
-#pragma unroll 1
-      for (int b = 0; b < NV; ++b)
-#pragma unroll
-        for (int a = 0; a < NV; ++a) { const double x = p(a, b) - Ap(a, b); Ap(a, b) = x; pAp = fma(p(a, b), x, pAp); }
-      if (!(pAp > 0.0)) { bad = true; break; }
-      const double al = rr / pAp;
-      double rrn = 0;
-#pragma unroll 1
-      for (int b = 0; b < NV; ++b)
-#pragma unroll
-        for (int a = 0; a < NV; ++a) {
-          X(a, b) = fma(al, p(a, b), X(a, b));
-          const double x = fma(-al, Ap(a, b), r(a, b));
-          r(a, b) = x;
-          rrn = fma(x, x, rrn);
-        }
-      const double bt = rrn / rr;
-#pragma unroll 1
-      for (int b = 0; b < NV; ++b)
-#pragma unroll
-        for (int a = 0; a < NV; ++a) p(a, b) = fma(bt, p(a, b), r(a, b));
-      rr = rrn;
-    }
-    if (bad) {
-      atomicMin(F.err, (1ull << ERR_CLASS_SHIFT) | (unsigned long long)(e + 1));
-      return;
-    }
-    if (sqrt(rr) > F.mass_tol * r0) atomicAdd(F.cg_nfail, 1u);
+    gput(Tp, r1);
+    if (r2 != r1) gput(Tm, r2);
   }
-
-  // ---- v outputs
-#pragma unroll 1
-  for (int b = 0; b < NV; ++b)
+  double X[J], r[J], p[J], Ap[J];
+  double r0 = 0;
 #pragma unroll
-    for (int a = 0; a < NV; ++a) store_v(S, e + Eu * (a + NV * b), X(a, b), fin);
+  for (int j = 0; j < J; ++j) {
+    const int k = u + U * j;
+    X[j] = r[j] = p[j] = 0.0;
+    if (k < NE) {
+      const double x = F.mrhs[k * Eu + e];
+      X[j] = x;
+      xs[k] = x;
+      r0 = fma(x, x, r0);
+    }
+  }
+  r0 = sqrt(team_sum<U>(r0, tmask));
+  __syncwarp(tmask);
+  team_K<NU, NV, 1>(B, F, Eu, e, u, tmask, Phs, PhWs, xs, zs, zd, r);    // r = R - M X = K R for X = R
+  double rr = 0;
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    p[j] = r[j];
+    rr = fma(r[j], r[j], rr);
+  }
+  rr = team_sum<U>(rr, tmask);
+  const int maxit = NV * NV + 10;
+  int it = 0;
+  bool bad = false;
+  while (sqrt(rr) > F.mass_tol * r0 && it < maxit) {
+    ++it;
+    __syncwarp(tmask);                              // the last phase 2 has read zs, zd
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      const int k = u + U * j;
+      if (k < NE) xs[k] = p[j];
+    }
+    __syncwarp(tmask);
+#pragma unroll
+    for (int j = 0; j < J; ++j) Ap[j] = p[j];
+    team_K<NU, NV, -1>(B, F, Eu, e, u, tmask, Phs, PhWs, xs, zs, zd, Ap);  // A p = p - K p
+    double pAp = 0;
+#pragma unroll
+    for (int j = 0; j < J; ++j) pAp = fma(p[j], Ap[j], pAp);
+    pAp = team_sum<U>(pAp, tmask);
+    if (!(pAp > 0.0)) { bad = true; break; }
+    const double al = rr / pAp;
+    double rrn = 0;
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      X[j] = fma(al, p[j], X[j]);
+      r[j] = fma(-al, Ap[j], r[j]);
+      rrn = fma(r[j], r[j], rrn);
+    }
+    rrn = team_sum<U>(rrn, tmask);
+    const double bt = rrn / rr;
+#pragma unroll
+    for (int j = 0; j < J; ++j) p[j] = fma(bt, p[j], r[j]);
+    rr = rrn;
+  }
+  if (bad) {
+    if (u == 0) atomicMin(F.err, (1ull << ERR_CLASS_SHIFT) | (unsigned long long)(e + 1));
+    return;
+  }
+  if (u == 0 && sqrt(rr) > F.mass_tol * r0) atomicAdd(F.cg_nfail, 1u);
+
+  bool fin = true;
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const int k = u + U * j;
+    if (k < NE) store_v(S, e + Eu * k, X[j], fin);
+  }
   if (S.mode == OUT_RK4_LAST && !fin) atomicOr(F.nonfinite, 1u);
 }
 
-// shared memory of k_cg: r, X, p and A p
-__host__ __device__ constexpr size_t cg_smem(int nv) {
-  return (size_t)MASS_THREADS * 4 * nv * nv * sizeof(double);
-}
+#undef WEDG_TEAM_SETUP
 
 // Last RK4 update when the last stage may still raise an error inside k_cg
 // (CG mode): u += (dt/6) acc unless an error was recorded.

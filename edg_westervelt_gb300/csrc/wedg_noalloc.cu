@@ -302,7 +302,7 @@ extern "C" int wedg_rhs_noalloc(const wedg_config *cfg, const wedg_pre *pre, con
   const int tp = 128, ts = stage_threads(nu, nv, fast);
   Lch.prep(basis, F, S, (iE + tp - 1) / tp, tp, st);
   Lch.stage(basis, F, S, (iE + ts - 1) / ts, ts, st);
-  Lch.mass(basis, F, S, (iE + MASS_THREADS - 1) / MASS_THREADS, MASS_THREADS, st);
+  Lch.mass(basis, F, S, 1, CHEB_THREADS, st);
   unsigned long long err = 0;
   unsigned int cgf = 0;
   if ((ce = cudaGetLastError()) != cudaSuccess ||

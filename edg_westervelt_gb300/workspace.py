@@ -267,6 +267,55 @@ class Workspace:
         return int(done.value), out["recv"], out["energy"], out["vmax"], out["ndmin"], out["slices"], snaps
 
 
+class Batch:
+    """Many independent instances advanced together (wedg_batch_*): each a Workspace of its own
+    N, degrees, flux, boundary kinds and coefficients; one RK4 step of all of them is one replay
+    of a CUDA graph. No counterpart in the reference (there, batching is a loop over solves)."""
+
+    def __init__(self, workspaces):
+        self.ws = list(workspaces)
+        n = len(self.ws)
+        arr = (ctypes.c_void_p * n)(*[w._h for w in self.ws])
+        h = ctypes.c_void_p()
+        rc = L.lib().wedg_batch_create(n, arr, ctypes.byref(h))
+        if rc != L.WEDG_OK:
+            raise RuntimeError(f"wedg_batch_create failed: {L.lib().wedg_status_string(rc).decode()}")
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            L.lib().wedg_batch_destroy(self._h)
+            self._h = None
+
+    def rk4_steps(self, us, vs, t0s, dts, nsteps, stop_nonfinite=True):
+        """nsteps RK4 steps of every instance in place on its CUDA state tensors (contiguous
+        float64, the reference's layout). Returns (steps_done, finite, status) per instance and
+        raises the first instance error like Workspace.rk4_steps."""
+        n = len(self.ws)
+        if not (len(us) == len(vs) == len(t0s) == len(dts) == n):
+            raise ValueError("one state, t0 and dt per instance")
+        for w, u, v in zip(self.ws, us, vs):
+            if not (_is_device(u) and _is_device(v)):
+                raise TypeError("batched steps take CUDA tensors")
+            if u.numel() != w.N * w.N * w.nu * w.nu or v.numel() != w.N * w.N * w.nv * w.nv:
+                raise DimensionMismatch(f"state, workspace and pre do not match (N = {w.N}, q_u + 1 = {w.nu}, "
+                                        f"q_v + 1 = {w.nv})")
+        pu = (ctypes.c_void_p * n)(*[u.data_ptr() for u in us])
+        pv = (ctypes.c_void_p * n)(*[v.data_ptr() for v in vs])
+        t0 = np.array(t0s, dtype=np.float64)
+        dt = np.array(dts, dtype=np.float64)
+        done = np.zeros(n, dtype=np.int64)
+        fin = (ctypes.c_int * n)()
+        st = (ctypes.c_int * n)()
+        L.lib().wedg_batch_rk4_steps(self._h, pu, pv, _ptr(t0), _ptr(dt), int(nsteps), int(stop_nonfinite),
+                                     done.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), fin, st)
+        for i, w in enumerate(self.ws):
+            w.fin = bool(fin[i])
+        for i, w in enumerate(self.ws):
+            w._check(st[i])
+        return [int(x) for x in done], [bool(x) for x in fin], [int(x) for x in st]
+
+
 def edg_rhs_(ws, u, v, t, N, h, pre):
     """``edg_rhs!(ws, u, v, t, N, h, pre) -> (ws.ut, ws.vt)`` (src/rhs.jl:490-494); the
     returned arrays are overwritten by the next call."""

@@ -182,6 +182,29 @@ typedef struct wedg_source_run {
 int wedg_run_source(wedg_ws *ws, double *u, double *v, const int64_t u_shape[4], const int64_t v_shape[4],
                     int where, const wedg_source_run *run, int64_t *steps_done, int *finite);
 
+/* Batched form: many independent instances -- workspaces made by wedg_create, each with its
+ * own N, degrees, flux, boundary kinds and coefficients -- advanced together. No counterpart in
+ * the reference, whose batching is the caller's loop over instances. One RK4 step of every
+ * instance is captured once into a CUDA graph (each instance's kernels on its own stream,
+ * forked from and joined to the batch's stream) and replayed for every step: a step of the
+ * whole batch is one graph launch, and small instances run side by side on the GPU. The stage
+ * kernels of a replay take their time factors from per-instance tables that the host refills
+ * every WEDG_BATCH_CHUNK steps (the factors are the ones the single-instance calls compute).
+ * The graph is captured again when the state pointers, the steps dt or stop_nonfinite change. */
+#define WEDG_BATCH_CHUNK 256
+typedef struct wedg_batch wedg_batch;
+int wedg_batch_create(int n, wedg_ws *const *instances, wedg_batch **out);
+void wedg_batch_destroy(wedg_batch *b);
+/* nsteps RK4 steps of every instance i, in place on its device state u_dev[i], v_dev[i] (the
+ * reference's layout), from t0[i] with step dt[i] (t advancing by t += dt). With
+ * stop_nonfinite, an instance stops after its first step with a non-finite state. Per
+ * instance: steps_done[i], finite[i] and status[i] (a status of wedg_rk4_steps; the message
+ * through wedg_error_message on that instance); any of the three may be NULL. Returns WEDG_OK
+ * or the first nonzero instance status. */
+int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_dev, const double *t0,
+                         const double *dt, int64_t nsteps, int stop_nonfinite, int64_t *steps_done, int *finite,
+                         int *status);
+
 /* Size of the static device array used by wedg_rhs_noalloc (16 MiB). */
 #define WEDG_NOALLOC_BYTES ((size_t)16 << 20)
 
