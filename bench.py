@@ -262,6 +262,9 @@ def run_ours(args):
         dist.init_process_group("nccl", init_method="env://")
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    if args.batched_only:
+        print(json.dumps({"batched": run_batched(torch, dev, args.steps, args.warmup)}), flush=True)
+        return
 
     pre, _ = W.precompute(Q, NMESH, coefficients=W.constant_coefficients(**COEF), **KW)
     N, nu, nv, qh = NMESH, pre["qu1"], pre["qv1"], pre["q_high"]
@@ -327,6 +330,7 @@ def run_ours(args):
         return
     zero = timed("zero", max(2, args.steps // 4), args.warmup)
     unif = timed("uniform", max(2, args.steps // 4), args.warmup)
+
     ms_step = main["ms"] / args.steps
     value = world * dof * 4 * args.steps / (main["ms"] / 1e3)
 
@@ -351,6 +355,10 @@ def run_ours(args):
         e2e = {"value": world * dof * 4 * ke / te, "unit": "DOF·stage/s",
                "h2d_bytes_per_step": int(uh.nbytes + vh.nbytes), "d2h_bytes_per_step": int(uh.nbytes + vh.nbytes),
                "steps": ke, "api": "Workspace.rk4_steps (wedg_rk4_steps, WEDG_HOST)"}
+
+    batched = None
+    if world == 1 and not args.no_batched:
+        batched = run_batched(torch, dev, max(4, 2 * args.steps), args.warmup)
 
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
@@ -415,6 +423,7 @@ def run_ours(args):
         "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clocks.summary(), "gpu_launches": main["launches"],
         "kernel_ms": kms,
+        "batched": batched,
         "zero_state": {"value": world * dof * 4 * zero["steps"] / (zero["ms"] / 1e3),
                        "ms_per_step": zero["ms"] / max(zero["steps"], 1), "cheb_steps_max": zero["cheb"],
                        "stage_ms": zero["prep_ms"] + zero["stage_ms"] + zero["mass_ms"]},
@@ -426,6 +435,94 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+BATCH_SIZES = (16, 24, 32, 48, 64, 96, 128)
+
+
+def batch_instances(n=256, seed=4):
+    """The mixed batch: n instances drawn from default_rng(seed): N from BATCH_SIZES, q_u from
+    2..7, q_v in {q_u - 1, q_u}, flux and the four boundary kinds uniformly, and c ~ U[0.5, 2],
+    α log-uniform on [1e-6, 1e-3], β ~ U[0, 10] constant on each of 4 × 4 mesh-aligned
+    subsquares; source mode (Gaussian source) from the zero state, dt = h / (dt_fac q_u²) with
+    dt_fac = 10 max c. Yields (q_u, N, precompute keywords, dt)."""
+    import edg_westervelt_gb300 as W
+    rng = np.random.default_rng(seed)
+
+    def piecewise(tab):
+        def f(x, y):
+            x = np.asarray(x, dtype=float)
+            y = np.asarray(y, dtype=float)
+            return tab[np.clip(np.floor(4 * y).astype(int), 0, 3), np.clip(np.floor(4 * x).astype(int), 0, 3)]
+        return f
+
+    def zero(x, y):
+        return np.zeros(np.broadcast(np.asarray(x), np.asarray(y)).shape)
+
+    for _ in range(n):
+        N = int(rng.choice(BATCH_SIZES))
+        qu = int(rng.integers(2, 8))
+        qv = int(rng.choice([qu - 1, qu]))
+        flux = str(rng.choice(["upwind", "central", "alternating"]))
+        kinds = [str(k) for k in rng.choice(["absorbing_2beta", "absorbing", "dirichlet", "wall"], 4)]
+        c = rng.uniform(0.5, 2.0, (4, 4))
+        al = 10.0 ** rng.uniform(-6, -3, (4, 4))
+        be = rng.uniform(0.0, 10.0, (4, 4))
+        co = W.Coefficients(piecewise(c), zero, zero, piecewise(al), zero, zero, piecewise(be))
+        kw = dict(mixed=(qv == qu - 1), flux=flux, mode="source", coefficients=co, kappa=0.5,
+                  boundary=dict(bot=kinds[0], top=kinds[1], lft=kinds[2], rgt=kinds[3]))
+        yield qu, N, kw, (1.0 / N) / (10.0 * float(c.max()) * qu * qu)
+
+
+def run_batched(torch, dev, steps, warmup):
+    """The batched form against the plain per-instance loop on the same instances: aggregate
+    DOF·stage/s of Batch.rk4_steps (one CUDA-graph replay per step of all instances) and of
+    Workspace.rk4_steps called instance after instance, both on device-resident states."""
+    import edg_westervelt_gb300 as W
+    t_setup = time.perf_counter()
+    wss, us, vs, dts, dof = [], [], [], [], 0
+    for qu, N, kw, dt in batch_instances():
+        pre, _ = W.precompute(qu, N, **kw)
+        ws = W.Workspace(pre, N)
+        wss.append(ws)
+        us.append(torch.zeros(N * N * pre["qu1"] ** 2, dtype=torch.float64, device=dev))
+        vs.append(torch.zeros(N * N * pre["qv1"] ** 2, dtype=torch.float64, device=dev))
+        dts.append(dt)
+        dof += N * N * (pre["qu1"] ** 2 + pre["qv1"] ** 2)
+    t_setup = time.perf_counter() - t_setup
+    batch = W.Batch(wss)
+    n = len(wss)
+    t = [0.0] * n
+
+    def advance(k):
+        for i in range(n):
+            t[i] += k * dts[i]
+    batch.rk4_steps(us, vs, t, dts, warmup)                       # captures the graph
+    advance(warmup)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    done, fin, _ = batch.rk4_steps(us, vs, t, dts, steps)
+    tb = time.perf_counter() - t0
+    advance(steps)
+    assert all(d == steps for d in done) and all(fin)
+    for i, ws in enumerate(wss):                                  # warm the single-instance path
+        ws.rk4_steps(us[i], vs[i], t[i], dts[i], 1)
+    advance(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i, ws in enumerate(wss):
+        assert ws.rk4_steps(us[i], vs[i], t[i], dts[i], steps) == steps
+    tp = time.perf_counter() - t0
+    vb, vp = dof * 4 * steps / tb, dof * 4 * steps / tp
+    return {"workload": "256 instances, N in {16..128}, q_u 2-7, q_v in {q_u-1, q_u}, random flux and boundary "
+                        "kinds, piecewise-constant c, alpha, beta on 4x4 subsquares (default_rng(4)), source mode",
+            "instances": n, "elements": int(sum(w.N * w.N for w in wss)), "dof": int(dof), "steps": steps,
+            "value": vb, "unit": "DOF·stage/s", "ms_per_step": tb / steps * 1e3,
+            "plain_loop_value": vp, "plain_loop_ms_per_step": tp / steps * 1e3, "speedup_vs_plain_loop": vb / vp,
+            "setup_s": t_setup,
+            "timing": "host clock around each call (each call returns synchronised); states resident on the GPU",
+            "batched": "Batch.rk4_steps: one CUDA graph of one RK4 step of every instance, replayed per step",
+            "plain_loop": "Workspace.rk4_steps for each instance in turn"}
 
 
 def main():
@@ -440,6 +537,8 @@ def main():
     ap.add_argument("--mesh", type=int, default=512, help="mesh size N (profiling runs on smaller cases)")
     ap.add_argument("--state", default="front", choices=["front", "uniform", "zero"])
     ap.add_argument("--profile-only", action="store_true", help="only the main timed run (for ncu)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
+    ap.add_argument("--batched-only", action="store_true", help="only the batched-form measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
