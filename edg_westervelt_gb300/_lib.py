@@ -71,6 +71,16 @@ class SourceRun(ctypes.Structure):
                 ("snaps", ctypes.POINTER(ctypes.c_double))]
 
 
+class NormArgs(ctypes.Structure):
+    """wedg_norm_args (include/wedg.h)."""
+    _D = ctypes.POINTER(ctypes.c_double)
+    _fields_ = [("N", ctypes.c_int), ("qu1", ctypes.c_int), ("qv1", ctypes.c_int), ("w", _D), ("P_u", _D),
+                ("S_u", _D), ("err_c2", _D), ("uA", _D), ("vA", _D), ("uB", _D), ("vB", _D), ("where", ctypes.c_int),
+                ("omega", ctypes.c_double), ("ctT", ctypes.c_double), ("stT", ctypes.c_double),
+                ("kx", ctypes.c_int), ("ky", ctypes.c_int), ("px", ctypes.c_double), ("py", ctypes.c_double),
+                ("xloc", _D), ("yloc", _D)]
+
+
 def lib():
     """The loaded libwedg (ctypes.CDLL); raises if the library was not built."""
     global _lib
@@ -109,6 +119,7 @@ def lib():
     L.wedg_batch_destroy.restype = None
     L.wedg_batch_rk4_steps.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), _D, _D, ctypes.c_int64,
                                        ctypes.c_int, _I64, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.wedg_norms.argtypes = [ctypes.POINTER(NormArgs), _D]
     L.wedg_run_source.argtypes = [vp, _D, _D, _I64, _I64, ctypes.c_int, ctypes.POINTER(SourceRun), _I64,
                                   ctypes.POINTER(ctypes.c_int)]
     L.wedg_kernel_times.argtypes = [vp, _D, _I64, _D, _I64, _D, _I64, ctypes.c_int]

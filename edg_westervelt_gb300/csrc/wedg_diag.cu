@@ -1,13 +1,18 @@
-// Diagnostics of the source-mode run on the device (src/solver.jl:839-958):
+// Diagnostics on the device: of the source-mode run (src/solver.jl:839-958) the
 // receiver values of v_h, the Westervelt energy with max|v_h| and min(1 - 2βv_h),
-// the slice of v_h along a mesh line, and snapshots of v_h on the point grid.
+// the slice of v_h along a mesh line and snapshots of v_h on the point grid; and
+// the error norms of src/solver.jl:774-836 (wedg_norms).
 //
-// They run once per step (receivers) or once per record, so they use runtime
-// sizes (n ≤ 8) and one thread per element or per output value; the energy is
-// summed in a fixed order (per block a fixed tree, then the blocks in order), so
-// a run gives the same values every time.
+// They run once per step (receivers), once per record or once per run, so they
+// use runtime sizes (n ≤ 8) and one thread per element or per output value; sums
+// are taken in a fixed order (per block a fixed tree, then the blocks in order),
+// so a run gives the same values every time.
 #include <cuda_runtime.h>
 
+#include <cmath>
+#include <vector>
+
+#include "../../include/wedg.h"
 #include "wedg_diag.h"
 
 namespace wedg {
@@ -159,3 +164,178 @@ __global__ void k_vgrid(const double *v, DiagBasis B, double *out) {
 }
 
 }  // namespace wedg
+
+namespace wedg {
+
+// Error norms (src/solver.jl:774-836): per element the four sums Σ W du², Σ W dv²,
+// Σ W (dux² + duy²), Σ W (½c²(dux² + duy²) + ½dv²) at the u-quadrature points, with du, dv,
+// dux, duy the modal differences A - B taken to the points (difference_norms) or the
+// manufactured solution minus the state (_mms_errors); a fixed-order block reduction.
+__global__ void __launch_bounds__(DIAG_THREADS) k_norms(NormArgs A, double *part) {
+  __shared__ double sm[4][DIAG_THREADS];
+  const DiagBasis &B = A.B;
+  const int E = B.E, N = B.N, nu = B.nu, nv = B.nv, nq = B.nu;
+  const int e = blockIdx.x * DIAG_THREADS + threadIdx.x;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  if (e < E) {
+    const int j = e % N, k = e / N;
+    double U[8][8], V[8][8];
+    for (int b = 0; b < nu; ++b)
+      for (int a = 0; a < nu; ++a) {
+        const size_t l = e + (size_t)E * (a + nu * b);
+        U[a][b] = A.uB ? A.uA[l] - A.uB[l] : A.uA[l];
+      }
+    for (int b = 0; b < nv; ++b)
+      for (int a = 0; a < nv; ++a) {
+        const size_t l = e + (size_t)E * (a + nv * b);
+        V[a][b] = A.vB ? A.vA[l] - A.vB[l] : A.vA[l];
+      }
+    double US[8][8], UP[8][8], VP[8][8];
+    for (int a = 0; a < nu; ++a)
+      for (int s = 0; s < nq; ++s) {
+        double x = 0, y = 0;
+        for (int b = 0; b < nu; ++b) { x = fma(U[a][b], B.S[s][b], x); y = fma(U[a][b], B.P[s][b], y); }
+        US[a][s] = x;
+        UP[a][s] = y;
+      }
+    for (int a = 0; a < nv; ++a)
+      for (int s = 0; s < nq; ++s) {
+        double x = 0;
+        for (int b = 0; b < nv; ++b) x = fma(V[a][b], B.P[s][b], x);
+        VP[a][s] = x;
+      }
+    const double kxa = 2.0 * M_PI * A.kx, kya = 2.0 * M_PI * A.ky, cm = A.ctT - 1.0, vs = -A.omega * A.stT;
+    for (int s = 0; s < nq; ++s)
+      for (int r = 0; r < nq; ++r) {
+        double uh = 0, ux = 0, uy = 0, vh = 0;
+        for (int a = 0; a < nu; ++a) {
+          uh = fma(B.P[r][a], UP[a][s], uh);
+          ux = fma(B.P[r][a], US[a][s], ux);
+          uy = fma(B.S[r][a], UP[a][s], uy);
+        }
+        for (int a = 0; a < nv; ++a) vh = fma(B.P[r][a], VP[a][s], vh);
+        ux *= B.two_h;
+        uy *= B.two_h;
+        double du, dv, dux, duy;
+        if (A.mms) {
+          const double X = A.xloc[k + (size_t)N * s], Y = A.yloc[j + (size_t)N * r];
+          const double cx = cos(kxa * X + A.px), sx = sin(kxa * X + A.px);
+          const double cy = cos(kya * Y + A.py), sy = sin(kya * Y + A.py);
+          const double sp = cx * sy, sp_x = -kxa * sx * sy, sp_y = kya * cx * cy;
+          du = cm * sp - uh;
+          dv = vs * sp - vh;
+          dux = cm * sp_x - ux;
+          duy = cm * sp_y - uy;
+        } else {
+          du = uh; dv = vh; dux = ux; duy = uy;
+        }
+        const double W = B.w[r] * B.w[s];
+        const double g = dux * dux + duy * duy;
+        acc[0] += W * (du * du);
+        acc[1] += W * (dv * dv);
+        acc[2] += W * g;
+        acc[3] += W * (0.5 * A.c2q[e + (size_t)E * (r + nq * s)] * g + 0.5 * (dv * dv));
+      }
+  }
+  for (int q = 0; q < 4; ++q) sm[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = DIAG_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int q = 0; q < 4; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 4; ++q) part[q * gridDim.x + blockIdx.x] = sm[q][0];
+}
+
+// The four sums over all blocks, in a fixed order
+__global__ void __launch_bounds__(DIAG_THREADS) k_norms_final(const double *part, int nblk, double *out) {
+  __shared__ double sm[4][DIAG_THREADS];
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < nblk; i += DIAG_THREADS)
+    for (int q = 0; q < 4; ++q) acc[q] += part[q * nblk + i];
+  for (int q = 0; q < 4; ++q) sm[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = DIAG_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int q = 0; q < 4; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) out[threadIdx.x] = sm[threadIdx.x][0];
+}
+
+}  // namespace wedg
+
+namespace {
+
+// Device buffers of one wedg_norms call, freed on every return path
+struct NormBuffers {
+  std::vector<void *> p;
+  cudaError_t get(double **q, size_t n) {
+    void *x = nullptr;
+    const cudaError_t e = cudaMalloc(&x, (n ? n : 1) * sizeof(double));
+    if (e == cudaSuccess) p.push_back(x);
+    *q = static_cast<double *>(x);
+    return e;
+  }
+  ~NormBuffers() {
+    for (void *x : p) cudaFree(x);
+  }
+};
+
+}  // namespace
+
+extern "C" int wedg_norms(const wedg_norm_args *a, double out[4]) {
+  using namespace wedg;
+  if (!a || !out) return WEDG_ERR_ARGUMENT;
+  const int N = a->N, nu = a->qu1, nv = a->qv1, nq = nu;
+  if (N < 1 || nu < 2 || nu > 8 || !(nv == nu || nv == nu - 1) || !a->w || !a->P_u || !a->S_u || !a->err_c2 ||
+      !a->uA || !a->vA || (!a->uB) != (!a->vB) || (!a->uB && (!a->xloc || !a->yloc)))
+    return WEDG_ERR_ARGUMENT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return WEDG_ERR_NO_DEVICE;
+  const size_t E = (size_t)N * N, nU = E * nu * nu, nV = E * nv * nv, nC = E * nq * nq;
+  NormArgs A{};
+  A.B.N = N; A.B.E = (int)E; A.B.nu = nu; A.B.nv = nv;
+  const double h = 1.0 / N;
+  A.B.two_h = 2.0 / h;
+  A.B.hh4 = h * h / 4;
+  for (int i = 0; i < nq; ++i) {
+    A.B.w[i] = a->w[i];
+    for (int d = 0; d < nu; ++d) { A.B.P[i][d] = a->P_u[i + nq * d]; A.B.S[i][d] = a->S_u[i + nq * d]; }
+  }
+  A.mms = a->uB ? 0 : 1;
+  A.kx = a->kx; A.ky = a->ky;
+  A.omega = a->omega; A.ctT = a->ctT; A.stT = a->stT; A.px = a->px; A.py = a->py;
+  NormBuffers R;
+  cudaError_t ce = cudaSuccess;
+  auto put = [&](const double *src, size_t n, bool state, const double **dst) {
+    if (ce != cudaSuccess || !src) { *dst = nullptr; return; }
+    if (state && a->where == WEDG_DEVICE) { *dst = src; return; }
+    double *d = nullptr;
+    ce = R.get(&d, n);
+    if (ce == cudaSuccess) ce = cudaMemcpy(d, src, n * sizeof(double), cudaMemcpyHostToDevice);
+    *dst = d;
+  };
+  put(a->uA, nU, true, &A.uA);
+  put(a->vA, nV, true, &A.vA);
+  put(a->uB, nU, true, &A.uB);
+  put(a->vB, nV, true, &A.vB);
+  put(a->err_c2, nC, false, &A.c2q);
+  put(a->xloc, (size_t)N * nq, false, &A.xloc);
+  put(a->yloc, (size_t)N * nq, false, &A.yloc);
+  const int nblk = (int)((E + DIAG_THREADS - 1) / DIAG_THREADS);
+  double *part = nullptr, *sums = nullptr;
+  if (ce == cudaSuccess) ce = R.get(&part, 4 * (size_t)nblk);
+  if (ce == cudaSuccess) ce = R.get(&sums, 4);
+  if (ce == cudaSuccess) {
+    k_norms<<<nblk, DIAG_THREADS>>>(A, part);
+    k_norms_final<<<1, DIAG_THREADS>>>(part, nblk, sums);
+    ce = cudaGetLastError();
+  }
+  double s4[4] = {0, 0, 0, 0};
+  if (ce == cudaSuccess) ce = cudaMemcpy(s4, sums, sizeof s4, cudaMemcpyDeviceToHost);
+  if (ce != cudaSuccess) return WEDG_ERR_CUDA;
+  for (int q = 0; q < 4; ++q) out[q] = (h / 2) * std::sqrt(s4[q]);
+  return WEDG_OK;
+}

@@ -47,71 +47,56 @@ def solve(q, N, T, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, bo
     ws.rk4_steps(u, v, 0.0, dt, nsteps)
     if return_state:
         return dict(u=u, v=v, N=N, h=h, P_u=pre["P_u"], P_v=pre["P_v"], S_u=geo["S_u"], W2d=geo["W2d"],
-                    err_c2=geo["err_c2"])
+                    err_c2=geo["err_c2"], w=pre["w"])
     if mode != "mms":
         raise ErrorException("errors are only available in :mms mode; use return_state = true")
     return mms_errors(u, v, T, N, h, pre, geo, kx, ky, phase)
 
 
-def _elem(x):
-    """(N, N, n, n) -> (N, N, n, n) C-ordered view for einsum over the element blocks."""
-    return np.ascontiguousarray(x)
+def _norms(N, qu1, qv1, w, P_u, S_u, err_c2, uA, vA, uB=None, vB=None, omega=0.0, T=0.0, kx=1, ky=1,
+           phase=(0.0, 0.0), xloc=None, yloc=None):
+    """wedg_norms: the error norms of src/solver.jl:774-836 on the GPU."""
+    import ctypes
+    from . import _lib as L
+    keep = []
+
+    def ptr(x):
+        if x is None:
+            return None
+        x = np.asfortranarray(x, dtype=np.float64)
+        keep.append(x)
+        return x.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    a = L.NormArgs()
+    a.N, a.qu1, a.qv1 = int(N), int(qu1), int(qv1)
+    a.w, a.P_u, a.S_u, a.err_c2 = ptr(w), ptr(P_u), ptr(S_u), ptr(err_c2)
+    a.uA, a.vA, a.uB, a.vB = ptr(uA), ptr(vA), ptr(uB), ptr(vB)
+    a.where = L.WEDG_HOST
+    a.omega, a.ctT, a.stT = float(omega), math.cos(omega * T), math.sin(omega * T)
+    a.kx, a.ky, a.px, a.py = int(kx), int(ky), float(phase[0]), float(phase[1])
+    a.xloc, a.yloc = ptr(xloc), ptr(yloc)
+    out = (ctypes.c_double * 4)()
+    rc = L.lib().wedg_norms(ctypes.byref(a), out)
+    if rc != L.WEDG_OK:
+        raise RuntimeError(f"wedg_norms failed: {L.lib().wedg_status_string(rc).decode()}")
+    return list(out)
 
 
 def mms_errors(u, v, T, N, h, pre, geo, kx, ky, phase=(0.0, 0.0)):
-    """L² errors of u, v, ∇u and the energy error against u = cos(ωT) Φ (src/solver.jl:774-810)."""
-    px, py = phase
-    P_u, P_v, S_u, W2d = pre["P_u"], pre["P_v"], geo["S_u"], geo["W2d"]
-    om = pre["omega"]
-    ctT, stT = math.cos(om * T), math.sin(om * T)
-    pi = math.pi
-    X = geo["xloc"][None, :, None, :]
-    Y = geo["yloc"][:, None, :, None]
-    sp = np.cos(2 * pi * kx * X + px) * np.sin(2 * pi * ky * Y + py)
-    sp_x = -2 * pi * kx * np.sin(2 * pi * kx * X + px) * np.sin(2 * pi * ky * Y + py)
-    sp_y = 2 * pi * ky * np.cos(2 * pi * kx * X + px) * np.cos(2 * pi * ky * Y + py)
-    U, V = _elem(u), _elem(v)
-    u_h = np.einsum("ra,jkab,sb->jkrs", P_u, U, P_u, optimize=True)
-    v_h = np.einsum("ra,jkab,sb->jkrs", P_v, V, P_v, optimize=True)
-    ux_h = (2 / h) * np.einsum("ra,jkab,sb->jkrs", P_u, U, S_u, optimize=True)
-    uy_h = (2 / h) * np.einsum("ra,jkab,sb->jkrs", S_u, U, P_u, optimize=True)
-    g = ((ctT - 1.0) * sp_x - ux_h) ** 2 + ((ctT - 1.0) * sp_y - uy_h) ** 2
-    ev = (-om * stT * sp - v_h) ** 2
-    s = h / 2
-    return dict(erru=s * math.sqrt(np.sum(W2d * ((ctT - 1.0) * sp - u_h) ** 2)),
-                errv=s * math.sqrt(np.sum(W2d * ev)),
-                errgradu=s * math.sqrt(np.sum(W2d * g)),
-                errE=s * math.sqrt(np.sum(W2d * (0.5 * geo["err_c2"] * g + 0.5 * ev))))
+    """L² errors of u, v, ∇u and the energy error against u = cos(ωT) Φ (src/solver.jl:774-810),
+    summed on the GPU (wedg_norms)."""
+    eu, ev, eg, eE = _norms(N, pre["qu1"], pre["qv1"], pre["w"], pre["P_u"], geo["S_u"], geo["err_c2"], u, v,
+                            omega=pre["omega"], T=T, kx=kx, ky=ky, phase=phase, xloc=geo["xloc"], yloc=geo["yloc"])
+    return dict(erru=eu, errv=ev, errgradu=eg, errE=eE)
 
 
 def difference_norms(A, B):
     """L² norms of u_A - u_B, v_A - v_B and the energy norm of the difference of two final
-    states of ``solve(...; return_state=True)`` (src/solver.jl:819-836)."""
-    h = B["h"]
-    P_u, P_v, S_u, W2d = B["P_u"], B["P_v"], B["S_u"], B["W2d"]
-    eu = _elem(A["u"] - B["u"])
-    ev = _elem(A["v"] - B["v"])
-    du = np.einsum("ra,jkab,sb->jkrs", P_u, eu, P_u, optimize=True)
-    dux = (2 / h) * np.einsum("ra,jkab,sb->jkrs", P_u, eu, S_u, optimize=True)
-    duy = (2 / h) * np.einsum("ra,jkab,sb->jkrs", S_u, eu, P_u, optimize=True)
-    dv = np.einsum("ra,jkab,sb->jkrs", P_v, ev, P_v, optimize=True)
-    s = h / 2
-    return dict(erru=s * math.sqrt(np.sum(W2d * du ** 2)), errv=s * math.sqrt(np.sum(W2d * dv ** 2)),
-                errE=s * math.sqrt(np.sum(W2d * (0.5 * B["err_c2"] * (dux ** 2 + duy ** 2) + 0.5 * dv ** 2))))
-
-
-def energy_diag(u, v, pre, geo, N, h):
-    """Westervelt energy Σ (h²/4) Σ W (½c²|∇u_h|² + (½ - ⅔βv_h) v_h²), max|v_h| and
-    min(1 - 2βv_h) (src/solver.jl:864-888, 914-926)."""
-    P_u, P_v, S_u, W2d = pre["P_u"], pre["P_v"], geo["S_u"], geo["W2d"]
-    U, V = _elem(u), _elem(v)
-    ux = (2 / h) * np.einsum("ra,jkab,sb->jkrs", P_u, U, S_u, optimize=True)
-    uy = (2 / h) * np.einsum("ra,jkab,sb->jkrs", S_u, U, P_u, optimize=True)
-    vh = np.einsum("ra,jkab,sb->jkrs", P_v, V, P_v, optimize=True)
-    c2q, bq = geo["err_c2"], geo["err_beta"]
-    Z = W2d * (0.5 * c2q * (ux ** 2 + uy ** 2) + (0.5 - (2 / 3) * bq * vh) * vh ** 2)
-    Ee = (h ** 2 / 4) * Z.sum(axis=(2, 3))
-    return float(np.sum(Ee)), float(np.max(np.abs(vh))), float(np.min(1 - 2 * bq * vh))
+    states of ``solve(...; return_state=True)`` (src/solver.jl:819-836), summed on the GPU."""
+    N = B["N"]
+    nu, nv = B["u"].shape[2], B["v"].shape[2]
+    w = B["w"] if "w" in B else np.sqrt(np.diag(B["W2d"]))
+    eu, ev, _, eE = _norms(N, nu, nv, w, B["P_u"], B["S_u"], B["err_c2"], A["u"], A["v"], B["u"], B["v"])
+    return dict(erru=eu, errv=ev, errE=eE)
 
 
 def _locate(s, N):

@@ -205,6 +205,27 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
                          const double *dt, int64_t nsteps, int stop_nonfinite, int64_t *steps_done, int *finite,
                          int *status);
 
+/* Error norms on the device (src/solver.jl:774-836). With uB = vB = NULL: `_mms_errors`, the
+ * L² errors of the state A against the manufactured solution u = cos(ωT)Φ (the solver stores
+ * u - Φ, so A is compared with (cos(ωT) - 1)Φ), Φ = cos(2πkx x + px) sin(2πky y + py) at the
+ * points (xloc, yloc); otherwise `difference_norms`, the norms of A - B. out = {erru, errv,
+ * errgradu, errE}, each (h/2)·sqrt(Σ over elements and points of W2d times the squared
+ * difference), errE with ½c²|∇e_u|² + ½e_v². States in the reference's layout, host or device
+ * memory (where); the other arrays host memory. */
+typedef struct wedg_norm_args {
+  int N, qu1, qv1;
+  const double *w;                  /* q_u1 weights of the u-quadrature */
+  const double *P_u, *S_u;          /* (q_u1, q_u1) column-major: P_u[i + q_u1 d] */
+  const double *err_c2;             /* c² at the u-quadrature points, (N, N, q_u1, q_u1) column-major */
+  const double *uA, *vA, *uB, *vB;  /* states; uB = vB = NULL for the manufactured-solution errors */
+  int where;
+  double omega, ctT, stT;           /* ω, cos(ωT), sin(ωT) */
+  int kx, ky;
+  double px, py;
+  const double *xloc, *yloc;        /* (N, q_u1) column-major: x of column k, y of row j at point i */
+} wedg_norm_args;
+int wedg_norms(const wedg_norm_args *a, double out[4]);
+
 /* Size of the static device array used by wedg_rhs_noalloc (16 MiB). */
 #define WEDG_NOALLOC_BYTES ((size_t)16 << 20)
 

@@ -186,3 +186,32 @@ def test_source_run_diagnostics_against_oracle(gpu):
     assert [t for t, _ in H["snaps"]] == [t for t, _ in O["snaps"]] and len(H["snaps"]) == 3
     for (_, a), (_, b) in zip(H["snaps"], O["snaps"]):
         assert rel(a, b) < 1e-12
+
+
+def test_error_norms_on_device_against_oracle(gpu):
+    """wedg_norms against the oracle's restatement of _mms_errors and difference_norms
+    (src/solver.jl:774-836) on seeded states, mixed and matched pairings, phase and wave numbers."""
+    from oracle.precompute import precompute as opre
+    from oracle.solver import difference_norms as odiff, mms_errors as omms
+    from edg_westervelt_gb300.solver import mms_errors
+    rng = np.random.default_rng(21)
+    for q, N, mixed in ((1, 3, False), (3, 7, True), (6, 5, False)):
+        kw = dict(mixed=mixed, kx=2, ky=1, phase=(0.3, 0.7))
+        pre, geo = W.precompute(q, N, **kw)
+        po, go = opre(q, N, **kw)
+        nu, nv = pre["qu1"], pre["qv1"]
+        u = np.asfortranarray(rng.standard_normal((N, N, nu, nu)))
+        v = np.asfortranarray(rng.standard_normal((N, N, nv, nv)))
+        a = mms_errors(u, v, 0.37, N, 1.0 / N, pre, geo, 2, 1, (0.3, 0.7))
+        b = omms(u, v, 0.37, N, 1.0 / N, po, go, 2, 1, (0.3, 0.7))
+        for k in ("erru", "errv", "errgradu", "errE"):
+            assert abs(a[k] / b[k] - 1) < 1e-12, (q, N, k, a[k], b[k])
+        u2 = np.asfortranarray(u + 1e-3 * rng.standard_normal(u.shape))
+        v2 = np.asfortranarray(v + 1e-3 * rng.standard_normal(v.shape))
+        A = dict(u=u2, v=v2)
+        B = dict(u=u, v=v, N=N, h=1.0 / N, P_u=pre["P_u"], P_v=pre["P_v"], S_u=geo["S_u"], W2d=geo["W2d"],
+                 err_c2=geo["err_c2"], w=pre["w"])
+        Bo = dict(B, P_u=po["P_u"], P_v=po["P_v"], S_u=go["S_u"], W2d=go["W2d"], err_c2=go["err_c2"])
+        da, db = W.difference_norms(A, B), odiff(A, Bo)
+        for k in ("erru", "errv", "errE"):
+            assert abs(da[k] / db[k] - 1) < 1e-12, (q, N, k, da[k], db[k])
