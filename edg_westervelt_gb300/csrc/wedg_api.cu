@@ -20,6 +20,7 @@
 #include "../../include/wedg.h"
 #include "wedg_basis.h"
 #include "wedg_diag.h"
+#include "wedg_setup.h"
 #include "wedg_dispatch.h"
 
 namespace wedg {
@@ -513,10 +514,6 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
     ae[e] = al;
     ic2e[e] = 1.0 / c2;
   }
-  if (!fast && !pre->Ainv_u) {
-    delete ws;
-    return WEDG_ERR_ARGUMENT;
-  }
   ws->fast = fast;
   ws->L = get_launchers(nu, nv, fast);
   if (!ws->L.prep) {
@@ -551,10 +548,37 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
     UP(F.Cw, cw);
     UP(F.Aw, aw);
     const size_t nt = (size_t)nu * nu * (nu * nu + 1) / 2;
-    std::vector<double> ai(nt * E);
-    for (int e = 0; e < E; ++e)
-      for (size_t row = 0; row < nt; ++row) ai[row * Es + e] = pre->Ainv_u[row + nt * e];
-    UP(F.Ainv, ai);
+    if (pre->Ainv_u) {
+      std::vector<double> ai(nt * E);
+      for (int e = 0; e < E; ++e)
+        for (size_t row = 0; row < nt; ++row) ai[row * Es + e] = pre->Ainv_u[row + nt * e];
+      UP(F.Ainv, ai);
+    } else {
+      // the packed inverses of src/solver.jl:528-535, computed on the device from Cw
+      const double *Pu = nullptr, *Su = nullptr;
+      UP(Pu, std::vector<double>(pre->P_u, pre->P_u + (size_t)nq * nu));
+      UP(Su, std::vector<double>(pre->S_u, pre->S_u + (size_t)nq * nu));
+      double *ainv = nullptr;
+      unsigned int *bad = nullptr;
+      if ((rc = dalloc(ws, &ainv, nt * E)) || (rc = dalloc(ws, &bad, 1))) {
+        wedg_destroy(ws);
+        return rc;
+      }
+      const size_t sm = ainv_smem(nu);
+      unsigned int nbad = 0;
+      cudaError_t ce = cudaMemset(bad, 0, sizeof(unsigned int));
+      if (ce == cudaSuccess) ce = cudaFuncSetAttribute(k_ainv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (ce == cudaSuccess) {
+        k_ainv<<<E, 128, sm>>>(F.Cw, E, nu, Pu, Su, ainv, bad);
+        ce = cudaGetLastError();
+      }
+      if (ce == cudaSuccess) ce = cudaMemcpy(&nbad, bad, sizeof nbad, cudaMemcpyDeviceToHost);
+      if (ce != cudaSuccess || nbad) {
+        wedg_destroy(ws);
+        return ce != cudaSuccess ? WEDG_ERR_CUDA : WEDG_ERR_ARGUMENT;
+      }
+      F.Ainv = ainv;
+    }
   }
   // ---- face arrays: (nq, N+1, N) -> [jf + (N+1)(k + N i)], (nq, N, N+1) -> [j + N (kf + (N+1) i)]
   auto hf = [&](const double *a) {

@@ -7,6 +7,9 @@ Fortran order, indices 0-based), so that ``pre["Cw"][r, e, s]`` is Julia's
 ``pre.Cw[r+1, e+1, s+1]`` at the same memory offset. The work is vectorised
 over the mesh; the inverse pinned stiffness ``Ainv_u`` is computed once per
 distinct element matrix (all elements share one for constant coefficients).
+With ``inverses="device"`` (the default) and more than 64 distinct element
+matrices, ``Ainv_u`` is left to the GPU workspace (``pre["Ainv_u"]`` is None and
+wedg_create computes the inverses on the device from ``Cw``).
 """
 import math
 
@@ -116,7 +119,7 @@ def _packed_inverses(Cw_blocks, Phi_xi, Phi_eta, chunk=2048):
 
 def precompute(q, N, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, boundary="absorbing_2beta",
                sigma_dirichlet=None, kappa=0.0, phase=(0.0, 0.0), coefficients=None, mode="mms", kx=1, ky=1,
-               source=None, mass_solver="chebyshev", initial_profile=None):
+               source=None, mass_solver="chebyshev", initial_profile=None, inverses="device"):
     """Element operators, face coefficients and data arrays of the RHS (``pre``) and the
     quadrature geometry for errors and diagnostics (``geo``); src/solver.jl:428-694.
 
@@ -190,13 +193,18 @@ def precompute(q, N, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, 
     Cw = _F(np.transpose(cw_e, (1, 0, 2)))
     Aw = _F(np.transpose(aw_e, (1, 0, 2)))
     cw_cols = np.transpose(cw_e, (0, 2, 1)).reshape(E, qu1 * qu1)      # vec in column-major (r fastest)
+    if inverses not in ("device", "host"):
+        raise ValueError(f"inverses must be \"device\" or \"host\", not {inverses!r}")
     uniq, inv = np.unique(cw_cols, axis=0, return_inverse=True)
-    packed = _packed_inverses(uniq, Phi_xi_u, Phi_eta_u)
-    if packed.shape[0] == 1 and E > 1:
-        # one matrix for all elements (constant coefficients): a read-only broadcast view
-        Ainv_u = np.broadcast_to(packed[0][:, None], (packed.shape[1], E))
+    if inverses == "device" and uniq.shape[0] > 64:
+        Ainv_u = None                         # computed by the GPU workspace from Cw
     else:
-        Ainv_u = _F(packed[inv.reshape(-1)].T)
+        packed = _packed_inverses(uniq, Phi_xi_u, Phi_eta_u)
+        if packed.shape[0] == 1 and E > 1:
+            # one matrix for all elements (constant coefficients): a read-only broadcast view
+            Ainv_u = np.broadcast_to(packed[0][:, None], (packed.shape[1], E))
+        else:
+            Ainv_u = _F(packed[inv.reshape(-1)].T)
 
     # ---- one-sided face values of c, α, β (solver.jl:538-552)
     faces = {s: {} for s in ("bot", "top", "lft", "rgt")}

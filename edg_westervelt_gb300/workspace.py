@@ -91,7 +91,7 @@ class Workspace:
         self.fin = True
         # pre of another mesh: the reference's Workspace accepts it and its edg_rhs! refuses it
         # with a DimensionMismatch (src/rhs.jl:500-503); no device workspace is made from it
-        self._mismatch = pre["Ainv_u"].shape[1] != E or pre["Cw"].shape[1] != E
+        self._mismatch = pre["Cw"].shape[1] != E
         if self._mismatch:
             return
         cfg = L.Config()
@@ -114,19 +114,15 @@ class Workspace:
         p = L.Pre()
         for name in L.PRE_FIELDS:
             a = pre[name]
-            if name == "Ainv_u" and not a.flags.f_contiguous and fast_path:
-                setattr(p, name, ctypes.POINTER(ctypes.c_double)())   # NULL: shared inverse, fast path expected
+            if name == "Ainv_u" and (a is None or not a.flags.f_contiguous):
+                # NULL: not needed by the constant-coefficient kernels, else computed on the device
+                setattr(p, name, ctypes.POINTER(ctypes.c_double)())
                 continue
             a = _f64(np.ascontiguousarray(a) if not a.flags.f_contiguous else a)
             keep[name] = a
             setattr(p, name, _ptr(a))
         h = ctypes.c_void_p()
         rc = L.lib().wedg_create(ctypes.byref(cfg), ctypes.byref(p), ctypes.byref(h))
-        if rc == L.WEDG_ERR_ARGUMENT and "Ainv_u" not in keep:
-            a = _f64(np.ascontiguousarray(pre["Ainv_u"]))      # the general path needs every inverse
-            keep["Ainv_u"] = a
-            p.Ainv_u = _ptr(a)
-            rc = L.lib().wedg_create(ctypes.byref(cfg), ctypes.byref(p), ctypes.byref(h))
         if rc == L.WEDG_ERR_NO_DEVICE:
             raise RuntimeError("libwedg: no CUDA device available")
         if rc != L.WEDG_OK:

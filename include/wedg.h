@@ -66,9 +66,12 @@ typedef struct wedg_config {
 } wedg_config;
 
 /* Host pointers to the arrays of `pre`, each in the reference's layout
- * (src/solver.jl:462-536, 716-770). Ainv_u may be NULL when every element has
- * constant c² and α (the library then uses the exact fast diagonalization of
- * the pinned stiffness and never reads Ainv_u). */
+ * (src/solver.jl:462-536, 716-770). Ainv_u may be NULL: when every element has
+ * constant c² and α the library uses the exact fast diagonalization of the
+ * pinned stiffness and never needs it; otherwise wedg_create computes the packed
+ * inverses of src/solver.jl:528-535 on the device from Cw (and fails with
+ * WEDG_ERR_ARGUMENT if a stiffness matrix is not positive definite).
+ * wedg_rhs_noalloc needs Ainv_u for coefficients that vary inside elements. */
 typedef struct wedg_pre {
   const double *w, *P_u, *S_u, *Ebl_u, *Ebr_u, *E1bl_u, *E1br_u;
   const double *P_h_v, *W2d_h;

@@ -407,3 +407,20 @@ def test_full_size_rhs_against_oracle(gpu):
     assert ws.stats()["fast_path"] == 1
     b = ws.rhs(u, v, 0.3)
     assert rel_max(a, b) < TOL
+
+
+def test_inverses_computed_on_the_device(gpu):
+    """Coefficients that vary inside the elements need the packed inverse stiffnesses of
+    src/solver.jl:528-535; without them in pre, wedg_create computes them on the device. The
+    RHS then matches the one from the host-computed inverses, and the oracle."""
+    rng = np.random.default_rng(31)
+    for q, N, mixed in ((2, 9, True), (5, 9, False), (7, 9, True)):
+        pd, po = _pair(q, N, mixed=mixed, mode="mms", phase=(0.4, 0.3))
+        ph = W.precompute(q, N, mixed=mixed, mode="mms", phase=(0.4, 0.3), inverses="host")[0]
+        assert pd["Ainv_u"] is None and ph["Ainv_u"] is not None
+        u, v = _state(rng, pd, N)
+        a = W.Workspace(pd, N).rhs(u, v, 0.037)
+        a = tuple(x.copy() for x in a)
+        b = W.Workspace(ph, N).rhs(u, v, 0.037)
+        assert rel_max(a, b) < 1e-13
+        assert rel_max(OracleWorkspace(po).rhs(u, v, 0.037), a) < TOL

@@ -187,3 +187,16 @@ def test_oracle_library_builds():
     from oracle import rhs
     assert os.path.exists(rhs.build())
     assert rhs.max_threads() >= 1
+
+
+def test_precompute_leaves_many_distinct_inverses_to_the_device():
+    """inverses="device" (default): more than 64 distinct element stiffnesses are not inverted
+    on the host (the GPU workspace does it); "host" inverts them as the reference does."""
+    pre, _ = W.precompute(2, 9, mode="mms")                  # paper coefficients: 81 distinct matrices
+    assert pre["Ainv_u"] is None
+    pre_h, _ = W.precompute(2, 9, mode="mms", inverses="host")
+    assert pre_h["Ainv_u"].shape == (9 * 10 // 2, 81)
+    pre_c, _ = W.precompute(2, 9, mode="mms", coefficients=W.constant_coefficients(c=1.0, alpha=1e-4, beta=1.0))
+    assert pre_c["Ainv_u"] is not None                        # one shared matrix: inverted on the host
+    with pytest.raises(ValueError):
+        W.precompute(2, 3, inverses="gpu")

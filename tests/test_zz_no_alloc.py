@@ -64,7 +64,7 @@ def test_noalloc_matches_workspace_twice(case):
     import torch
     assert torch.cuda.is_available()
     q, N, kw = CASES[case]
-    pre, _ = W.precompute(q, N, **kw)
+    pre, _ = W.precompute(q, N, inverses="host", **kw)     # wedg_rhs_noalloc reads Ainv_u from pre
     nu, nv = pre["qu1"], pre["qv1"]
     cfg, p, keep = _abi_structs(pre, N)
     ws = W.Workspace(pre, N)
