@@ -223,6 +223,20 @@ def cpu_baseline(budget_s):
     return port.dof * 4 * n / t, n, t, port.cores
 
 
+def max_over_ranks(x, dist, device):
+    """The largest of the ranks' values of x (the slowest replica sets the whole job's time)."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(dof_per_rank, world, steps, ms_max):
+    """Whole-job DOF·stage/s of `world` replicas, each advancing dof_per_rank DOF by `steps` RK4
+    steps, over the slowest rank's time in milliseconds."""
+    return world * dof_per_rank * 4 * steps / (ms_max / 1e3)
+
+
 def run_reference(args):
     """The reference's CPU path on the host cores: the oracle port (Julia is not installed)."""
     rank = int(os.environ.get("RANK", "0"))
@@ -309,9 +323,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         if dist:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+            ms = max_over_ranks(ms, dist, dev)
             dist.barrier()
         pm, pn, sm, sn = (ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64())
         mm, mn = ctypes.c_double(), ctypes.c_int64()
@@ -332,7 +344,7 @@ def run_ours(args):
     unif = timed("uniform", max(2, args.steps // 4), args.warmup)
 
     ms_step = main["ms"] / args.steps
-    value = world * dof * 4 * args.steps / (main["ms"] / 1e3)
+    value = replica_value(dof, world, args.steps, main["ms"])
 
     # end to end through the public API: pinned host state in, result out, every step
     e2e = None

@@ -1,0 +1,61 @@
+"""The multi-GPU path of the bench is replicas only: every rank runs its own copy of the
+workload and the job's time is the slowest rank's. These CPU tests run that host logic with
+the gloo backend on two ranks (the GPU launch itself is exercised by the bench on the GPU):
+the max-over-ranks reduction and the whole-job value, and the torchrun launch of the
+reference arm, which prints one line from rank 0 while the other rank exits without work."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, q):
+    import torch
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    import bench
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    ms = bench.max_over_ranks(10.0 + 5.0 * rank, dist, torch.device("cpu"))
+    q.put((rank, ms, bench.replica_value(1000, world, 4, ms)))
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_and_job_value_gloo():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    # both ranks see the slower rank's 15 ms; 2 replicas × 1000 DOF × 4 stages × 4 steps / 15 ms
+    assert [o[1] for o in out] == [15.0, 15.0]
+    assert out[0][2] == pytest.approx(2 * 1000 * 4 * 4 / 0.015)
+
+
+def test_reference_arm_under_torchrun_two_ranks():
+    port = _free_port()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
+           "--gpus", "2", "--steps", "1", "--warmup", "3"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
