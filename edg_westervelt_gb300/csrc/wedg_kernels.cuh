@@ -110,7 +110,12 @@ struct Fields {
   double gam[4], eta[4], sig[4], kb[4], kap[4];
 };
 
-enum StageMode { OUT_RHS = 0, OUT_RK4_STAGE = 1, OUT_RK4_LAST = 2, OUT_RK4_LAST_ACC = 3 };
+enum StageMode {
+  OUT_RHS = 0, OUT_RK4_STAGE = 1, OUT_RK4_LAST = 2, OUT_RK4_LAST_ACC = 3,
+  // adjoint parts of k_stage (both forms are symmetric, so the forward code is its own transpose):
+  OUT_ADJ_USOLVE = 4,   // ut = A_e⁻¹ xu (the u-solve alone)
+  OUT_ADJ_VOLUME = 5    // vt = R_v, ut = b of the volume terms alone, for the state (xu, xv)
+};
 
 struct StageIO {
   const double *xu, *xv;     // stage state
@@ -308,10 +313,12 @@ __global__ void __launch_bounds__(128, 3) k_prep(const __grid_constant__ Basis<N
   constexpr int NQ = NU, QH = Basis<NU, NV>::QH;
   const int E = F.E, N = F.N;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  // the bin counts of the next stage start at zero: all NBIN of them, whatever the element count
+  if (blockIdx.x == 0 && F.sorted)
+    for (int b = threadIdx.x; b < NBIN; b += blockDim.x) F.bin_count[(1 - S.parity) * NBIN + b] = 0;
   if (e >= E) return;
   if (err_word(F) != ERR_NONE) return;
   const int j = e % N, k = e / N;
-  if (e < NBIN && F.sorted) F.bin_count[(1 - S.parity) * NBIN + e] = 0;   // for the next stage
   {
     double U[NU][NU];
     load_regs<NU>(U, S.xu, E, e);
@@ -421,6 +428,54 @@ __global__ void __launch_bounds__(128, 3) k_prep(const __grid_constant__ Basis<N
 // k_stage helpers
 // ----------------------------------------------------------------------------
 
+// Coefficients of an interior face point: the one-sided values of c² and α on the "-" and "+"
+// sides and the jump term K (one-sided faces), or the face values c², α (continuous faces)
+struct FaceCoef {
+  double c2m, c2p, afm, afp, K;
+};
+__device__ __forceinline__ FaceCoef face_coef(const Fields &F, const double *c2p_a, const double *afp_a,
+                                              const double *c2m_a, const double *afm_a, const double *jc_a,
+                                              size_t fi) {
+  if (F.one_sided) return FaceCoef{c2m_a[fi], c2p_a[fi], afm_a[fi], afp_a[fi], jc_a[fi]};
+  return FaceCoef{0.0, c2p_a[fi], 0.0, afp_a[fi], 0.0};
+}
+
+// The flux slots of the "+" (plus) or "-" element at an interior face point from the traces of
+// both elements (src/rhs.jl:620-700): affine in (dum, dup, vm, vp, dvm, dvp)
+__device__ __forceinline__ void interior_flux(const Fields &F, const FaceCoef &cf, bool plus, double dum,
+                                              double dup, double vm, double vp, double dvm, double dvp,
+                                              double &A, double &D, double &Fs) {
+  const double th = F.theta, tau = F.tau, two_h = F.two_h;
+  if (F.one_sided) {
+    const double c2m = cf.c2m, c2p = cf.c2p, afm = cf.afm, afp = cf.afp, K = cf.K;
+    const double J = two_h * (c2m * dum - c2p * dup + afm * dvm - afp * dvp) + K;
+    const double G = two_h * ((1 - th) * (c2m * dum + afm * dvm) + th * (c2p * dup + afp * dvp));
+    const double pen = (0.5 * (c2m + c2p)) * F.lu + (0.5 * (afm + afp)) * F.lv;
+    const double sj = vm - vp;
+    if (plus) {
+      const double dvsp = th * sj - tau * J;
+      A = pen * sj - G - (1 - th) * K; D = -afp * dvsp; Fs = c2p * dvsp;
+    } else {
+      const double dvsm = (1 - th) * (vp - vm) - tau * J;
+      A = G - pen * sj - th * K; D = afm * dvsm; Fs = -c2m * dvsm;
+    }
+  } else {
+    const double c2 = cf.c2p, af = cf.afp;
+    const double gs = two_h * (c2 * (th * dup + (1 - th) * dum) + af * (th * dvp + (1 - th) * dvm));
+    const double Jt = c2 * (two_h * (dum - dup)) + af * (two_h * (dvm - dvp));
+    const double pen = c2 * F.lu + af * F.lv;
+    if (plus) {
+      A = pen * (vm - vp) - gs;
+      D = -af * (th * (vm - vp) - tau * Jt);
+      Fs = c2 * (th * (vm - vp) - tau * Jt);
+    } else {
+      A = gs - pen * (vm - vp);
+      D = af * ((1 - th) * (vp - vm) - tau * Jt);
+      Fs = -c2 * ((1 - th) * (vp - vm) - tau * Jt);
+    }
+  }
+}
+
 // Numerical flux slots A, D, F at point i of side s of the element
 // (src/rhs.jl:620-700 for interior faces, :65-103 and :738-763 for physical sides).
 template <int NU, int NV>
@@ -472,7 +527,6 @@ __device__ __forceinline__ void side_point(const Basis<NU, NV> &B, const Fields 
   const int nb = s == 0 ? e - 1 : s == 1 ? e + 1 : s == 2 ? e - N : e + N;
   const int sm = s < 2 ? 1 : 3, spp = s < 2 ? 0 : 2;      // trace sides of the "-" and "+" elements
   const int em = plus ? nb : e, ep = plus ? e : nb;
-  const double th = F.theta, tau = F.tau, two_h = F.two_h;
   size_t fi;
   const double *c2p_a, *afp_a, *c2m_a, *afm_a, *jc_a;
   if (s < 2) {
@@ -485,34 +539,8 @@ __device__ __forceinline__ void side_point(const Basis<NU, NV> &B, const Fields 
   const double vm = T(1, sm, em), vp = T(1, spp, ep);
   const double dum = T(0, sm, em), dup = T(0, spp, ep);
   const double dvm = T(2, sm, em), dvp = T(2, spp, ep);
-  if (F.one_sided) {
-    const double c2m = c2m_a[fi], c2p = c2p_a[fi], afm = afm_a[fi], afp = afp_a[fi], K = jc_a[fi];
-    const double J = two_h * (c2m * dum - c2p * dup + afm * dvm - afp * dvp) + K;
-    const double G = two_h * ((1 - th) * (c2m * dum + afm * dvm) + th * (c2p * dup + afp * dvp));
-    const double pen = (0.5 * (c2m + c2p)) * F.lu + (0.5 * (afm + afp)) * F.lv;
-    const double sj = vm - vp;
-    if (plus) {
-      const double dvsp = th * sj - tau * J;
-      A = pen * sj - G - (1 - th) * K; D = -afp * dvsp; Fs = c2p * dvsp;
-    } else {
-      const double dvsm = (1 - th) * (vp - vm) - tau * J;
-      A = G - pen * sj - th * K; D = afm * dvsm; Fs = -c2m * dvsm;
-    }
-  } else {
-    const double c2 = c2p_a[fi], af = afp_a[fi];
-    const double gs = two_h * (c2 * (th * dup + (1 - th) * dum) + af * (th * dvp + (1 - th) * dvm));
-    const double Jt = c2 * (two_h * (dum - dup)) + af * (two_h * (dvm - dvp));
-    const double pen = c2 * F.lu + af * F.lv;
-    if (plus) {
-      A = pen * (vm - vp) - gs;
-      D = -af * (th * (vm - vp) - tau * Jt);
-      Fs = c2 * (th * (vm - vp) - tau * Jt);
-    } else {
-      A = gs - pen * (vm - vp);
-      D = af * ((1 - th) * (vp - vm) - tau * Jt);
-      Fs = -c2 * ((1 - th) * (vp - vm) - tau * Jt);
-    }
-  }
+  const FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);
+  interior_flux(F, cf, plus, dum, dup, vm, vp, dvm, dvp, A, D, Fs);
 }
 
 // ----------------------------------------------------------------------------
@@ -551,9 +579,10 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
 #pragma unroll 1
   for (int a = 0; a < NU; ++a)
 #pragma unroll
-    for (int b = 0; b < NU; ++b) bb(a, b) = 0.0;
+    for (int b = 0; b < NU; ++b) bb(a, b) = S.mode == OUT_ADJ_USOLVE ? S.xu[e + (size_t)E * (a + NU * b)] : 0.0;
+  const bool adjoint = S.mode >= OUT_ADJ_USOLVE;
 #pragma unroll 1
-  for (int ax = 0; ax < 2; ++ax) {
+  for (int ax = 0; ax < 2 && !adjoint; ++ax) {
     double A0[NV], D0[NV], F0[NU];          // the projections of the axis' first side (B or L)
     double YA[NV], YD[NV], YF[NU];
 #pragma unroll 1
@@ -648,6 +677,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
   // ---- state of the stage (the general kernels keep it in shared memory; the
   //      constant-coefficient kernels read it from HBM, by columns and by rows)
   const size_t Eu = (size_t)E;
+  if (S.mode != OUT_ADJ_USOLVE) {
   if constexpr (!FAST) {
 #pragma unroll 1
     for (int b = 0; b < NV; ++b)
@@ -797,9 +827,23 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
     }
   }
 
+  }   // volume terms
+
+  if (S.mode == OUT_ADJ_VOLUME) {
+#pragma unroll 1
+    for (int b = 0; b < NV; ++b)
+#pragma unroll
+      for (int a = 0; a < NV; ++a) S.vt[e + Eu * (a + NV * b)] = Rv(a, b);
+#pragma unroll 1
+    for (int b = 0; b < NU; ++b)
+#pragma unroll
+      for (int a = 0; a < NU; ++a) S.ut[e + Eu * (a + NU * b)] = bb(a, b);
+    return;
+  }
+
   // ---- source (src/rhs.jl:340-350), and the mass right-hand side to HBM
 #pragma unroll 1
-  for (int b = 0; b < NV; ++b)
+  for (int b = 0; b < NV && !adjoint; ++b)
 #pragma unroll
     for (int a = 0; a < NV; ++a) {
       const size_t l = (a + NV * b) * Eu + e;
@@ -817,8 +861,10 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
     }
 
   // ---- u-equation (src/rhs.jl:352-382): A_e UT = VB - Fu + e_1 V[0][0]
-  if constexpr (FAST) bb(0, 0) += S.xv[e];
-  else bb(0, 0) += Vb(0, 0);
+  if (!adjoint) {
+    if constexpr (FAST) bb(0, 0) += S.xv[e];
+    else bb(0, 0) += Vb(0, 0);
+  }
   // UT: in place of b (constant-coefficient kernels), in place of U (general kernels, U is dead)
   Blk<NU, BT> UT = FAST ? bb : Ub;
   if constexpr (FAST) {
@@ -918,7 +964,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
     for (int a = 0; a < NU; ++a) {
       const size_t l = e + Eu * (a + NU * b);
       const double kk = UT(a, b);
-      if (S.mode == OUT_RHS) {
+      if (S.mode == OUT_RHS || S.mode == OUT_ADJ_USOLVE) {
         S.ut[l] = kk;
       } else if (S.mode == OUT_RK4_STAGE) {
         S.accu[l] = S.first ? kk : S.accu[l] + 2.0 * kk;
@@ -1272,3 +1318,6 @@ __global__ void k_step_done(unsigned long long *err, const unsigned int *nonfini
                             long long *steps_done);
 
 }  // namespace wedg
+
+#include "wedg_adjoint.cuh"
+

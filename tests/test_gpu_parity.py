@@ -424,3 +424,25 @@ def test_inverses_computed_on_the_device(gpu):
         b = W.Workspace(ph, N).rhs(u, v, 0.037)
         assert rel_max(a, b) < 1e-13
         assert rel_max(OracleWorkspace(po).rhs(u, v, 0.037), a) < TOL
+
+
+def test_rk4_many_steps_on_a_mesh_with_fewer_elements_than_bins(gpu):
+    """Twenty RK4 steps on a 4 × 4 mesh (16 elements, fewer than the 48 Chebyshev-count bins of
+    the mass kernel) while the step counts climb past 16: every stage must start from empty
+    bins, whatever the element count (a stale bin once dropped an element from the solve)."""
+    rng = np.random.default_rng(5)
+    q, N = 3, 4
+    kw = dict(mode="source", flux="upwind", boundary="absorbing_2beta")
+    pp = W.precompute(q, N, coefficients=W.constant_coefficients(c=1.1, alpha=1e-3, beta=3.0), **kw)[0]
+    po = opre(q, N, coefficients=oc.constant_coefficients(c=1.1, alpha=1e-3, beta=3.0), **kw)[0]
+    nu, nv = pp["qu1"], pp["qv1"]
+    d = lambda n: 1.0 / (1.0 + np.add.outer(np.arange(n), np.arange(n))) ** 2
+    u = np.asfortranarray(0.01 * rng.standard_normal((N, N, nu, nu)) * d(nu))
+    v = np.asfortranarray(0.001 * rng.standard_normal((N, N, nv, nv)) * d(nv))
+    dt = (1.0 / N) / (10 * q * q)
+    uo, vo = u.copy(order="F"), v.copy(order="F")
+    OracleWorkspace(po).rk4_steps(uo, vo, 0.02, dt, 20)
+    ws = W.Workspace(pp, N)
+    assert ws.rk4_steps(u, v, 0.02, dt, 20) == 20
+    assert ws.stats()["cheb_steps_max"] > N * N       # counts beyond the element count
+    assert rel_max((u, v), (uo, vo)) < TOL, rel_max((u, v), (uo, vo))
