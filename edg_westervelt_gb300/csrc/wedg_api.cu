@@ -52,6 +52,17 @@ __global__ void k_step_done(unsigned long long *err, const unsigned int *nonfini
   if (stop_nonfinite && *nonfinite) *err = (3ull << ERR_CLASS_SHIFT);
 }
 
+// out = a x + b y (+ z), elementwise; y, z may be null
+__global__ void k_lincomb(size_t n, double *out, double a, const double *x, double b, const double *y,
+                          const double *z) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double r = a * x[i];
+    if (y) r = fma(b, y[i], r);
+    if (z) r += z[i];
+    out[i] = r;
+  }
+}
+
 Launchers get_launchers(int nu, int nv, bool fast) {
   switch (nu) {
     case 2: return launchers_q1(nv, fast);
@@ -85,6 +96,14 @@ struct wedg_ws {
   double *su = nullptr, *sv = nullptr, *accu = nullptr, *accv = nullptr;
   long long *steps_done = nullptr;
   int parity = 0;   // bin-count buffer of the next stage
+  // adjoint scratch (allocated on first use): μ, ν, -(h²/4)ν, forward ut and vt, slot weights
+  double *adj_mu = nullptr, *adj_nu = nullptr, *adj_nus = nullptr, *adj_ut = nullptr, *adj_vt = nullptr;
+  double *adj_hat = nullptr;
+  double *adj_in[4] = {nullptr, nullptr, nullptr, nullptr};   // host-call copies of u, v, λ_u, λ_v
+  // reverse RK4: checkpoints, the stage states of one segment, λ, its update, K̄ and Jᵀ K̄
+  std::vector<double *> rk_chk, rk_seg;
+  int64_t rk_chk_n = 0, rk_seg_n = 0;
+  double *rk_lam = nullptr, *rk_acc = nullptr, *rk_kbar = nullptr, *rk_g = nullptr, *rk_y = nullptr;
   // optional per-launch timing (events recorded around each stage kernel)
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -288,14 +307,21 @@ void factor_table(const wedg_ws *ws, double t, double dt, int64_t count, double 
 // factors from the device table tf (tf_n steps, indexed by the device step counter), so that the
 // launches can be captured once into a CUDA graph and replayed for every step.
 int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop_nonfinite,
-                const double *tf = nullptr, long long tf_n = 0) {
+                const double *tf = nullptr, long long tf_n = 0, double *const *stage_u = nullptr,
+                double *const *stage_v = nullptr) {
+  // with stage_u, stage_v (four buffers each) the stage states Y1..Y4 of the step are kept there
   const double cs[3] = {0.5 * dt, 0.5 * dt, dt};
   const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
   const bool cg = ws->cfg.mass_solver == WEDG_CG;
+  if (stage_u) {
+    const size_t bU = sizeof(double) * ws->E * ws->nu * ws->nu, bV = sizeof(double) * ws->E * ws->nv * ws->nv;
+    CK(ws, cudaMemcpyAsync(stage_u[0], u, bU, cudaMemcpyDeviceToDevice, ws->stream));
+    CK(ws, cudaMemcpyAsync(stage_v[0], v, bV, cudaMemcpyDeviceToDevice, ws->stream));
+  }
   for (int s = 0; s < 4; ++s) {
     StageIO S{};
-    S.xu = s == 0 ? u : ws->su;
-    S.xv = s == 0 ? v : ws->sv;
+    S.xu = s == 0 ? u : (stage_u ? stage_u[s] : ws->su);
+    S.xv = s == 0 ? v : (stage_v ? stage_v[s] : ws->sv);
     if (tf) {
       S.tf = tf;
       S.tf_n = tf_n;
@@ -305,7 +331,8 @@ int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop
       stage_factors(ws, ts[s], S);
     }
     S.u0 = u; S.v0 = v;
-    S.su = ws->su; S.sv = ws->sv;
+    S.su = stage_u && s < 3 ? stage_u[s + 1] : ws->su;
+    S.sv = stage_v && s < 3 ? stage_v[s + 1] : ws->sv;
     S.accu = ws->accu; S.accv = ws->accv;
     S.uo = u; S.vo = v;
     if (s < 3) {
@@ -333,6 +360,65 @@ int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop
 }
 
 // read the flags after a synchronized call and turn them into the status
+int adjoint_buffers(wedg_ws *ws) {
+  if (ws->adj_mu) return WEDG_OK;
+  const size_t nU = (size_t)ws->E * ws->nu * ws->nu, nV = (size_t)ws->E * ws->nv * ws->nv;
+  int rc;
+  if ((rc = dalloc(ws, &ws->adj_nu, nU)) || (rc = dalloc(ws, &ws->adj_nus, nU)) || (rc = dalloc(ws, &ws->adj_ut, nU)) ||
+      (rc = dalloc(ws, &ws->adj_vt, nV)) || (rc = dalloc(ws, &ws->adj_hat, (size_t)3 * 4 * ws->nq * ws->E)) ||
+      (rc = dalloc(ws, &ws->adj_in[0], nU)) || (rc = dalloc(ws, &ws->adj_in[1], nV)) ||
+      (rc = dalloc(ws, &ws->adj_in[2], nU)) || (rc = dalloc(ws, &ws->adj_in[3], nV)) ||
+      (rc = dalloc(ws, &ws->adj_mu, nV)))
+    return rc;
+  return WEDG_OK;
+}
+
+// Jᵀ(λ_u, λ_v) of the RHS at the state (u, v), time t, into (gu, gv); device pointers, on the
+// workspace stream (see wedg_adjoint.cuh for the steps). The forward RHS at the state runs first:
+// its traces, Chebyshev data and vt are inputs of the transpose.
+int enqueue_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t, const double *lam_u,
+                        const double *lam_v, double *gu, double *gv) {
+  int rc = adjoint_buffers(ws);
+  if (rc) return rc;
+  StageIO S{};
+  S.xu = u; S.xv = v;
+  stage_factors(ws, t, S);
+  S.mode = OUT_RHS;
+  S.ut = ws->adj_ut;
+  S.vt = ws->adj_vt;
+  const int par = ws->parity;
+  if ((rc = enqueue_stage(ws, S))) return rc;
+  S.parity = par;
+  const int ts = stage_threads(ws->nu, ws->nv, ws->fast), bs = (ws->E + ts - 1) / ts;
+  // μ = M(v)⁻¹ λ_v, on the Chebyshev data of the state
+  Fields Fm = ws->F;
+  Fm.mrhs = const_cast<double *>(lam_v);
+  StageIO Sm = S;
+  Sm.vt = ws->adj_mu;
+  ws->L.mass(ws->basis.data(), Fm, Sm, 1, CHEB_THREADS, ws->stream);
+  // ν = A_e⁻¹ λ_u
+  StageIO Su = S;
+  Su.mode = OUT_ADJ_USOLVE;
+  Su.xu = lam_u;
+  Su.ut = ws->adj_nu;
+  ws->L.stage(ws->basis.data(), ws->F, Su, bs, ts, ws->stream);
+  const AdjIO A{ws->adj_mu, ws->adj_nu, ws->adj_nus, ws->adj_vt, ws->adj_hat, gu, gv};
+  ws->L.adj_hats(ws->basis.data(), ws->F, S, A, ws->stream);
+  // the volume transposes: the volume terms of the state (-(h²/4) ν, μ)
+  StageIO Sv = S;
+  Sv.mode = OUT_ADJ_VOLUME;
+  Sv.xu = ws->adj_nus;
+  Sv.xv = ws->adj_mu;
+  Sv.vt = gv;
+  Sv.ut = gu;
+  ws->L.stage(ws->basis.data(), ws->F, Sv, bs, ts, ws->stream);
+  ws->L.adj_mass(ws->basis.data(), ws->F, S, A, ws->stream);
+  ws->L.adj_face(ws->basis.data(), ws->F, S, A, ws->stream);
+  ws->stats.kernel_launches += 6;
+  CK(ws, cudaGetLastError());
+  return WEDG_OK;
+}
+
 int collect(wedg_ws *ws) {
   unsigned long long err;
   unsigned int cgf, nonf;
@@ -1000,6 +1086,124 @@ int wedg_run_source(wedg_ws *ws, double *u, double *v, const int64_t u_shape[4],
     CK(ws, cudaMemcpy(u, ws->d_u, bU, cudaMemcpyDeviceToHost));
     CK(ws, cudaMemcpy(v, ws->d_v, bV, cudaMemcpyDeviceToHost));
   }
+  return rc;
+}
+
+int wedg_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t, const double *lam_u,
+                     const double *lam_v, double *gu, double *gv, const int64_t u_shape[4], const int64_t v_shape[4],
+                     int where) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  ws->stats.kernel_launches = 0;
+  int rc = check_shapes(ws, u_shape, v_shape);
+  if (rc) return rc;
+  if (!u || !v || !lam_u || !lam_v || !gu || !gv) return argument_error(ws, "null pointer");
+  if ((rc = adjoint_buffers(ws))) return rc;
+  const size_t bU = sizeof(double) * ws->E * ws->nu * ws->nu, bV = sizeof(double) * ws->E * ws->nv * ws->nv;
+  const double *du = u, *dv = v, *dlu = lam_u, *dlv = lam_v;
+  double *dgu = gu, *dgv = gv;
+  if (where == WEDG_HOST) {
+    CK(ws, cudaMemcpyAsync(ws->adj_in[0], u, bU, cudaMemcpyHostToDevice, ws->stream));
+    CK(ws, cudaMemcpyAsync(ws->adj_in[1], v, bV, cudaMemcpyHostToDevice, ws->stream));
+    CK(ws, cudaMemcpyAsync(ws->adj_in[2], lam_u, bU, cudaMemcpyHostToDevice, ws->stream));
+    CK(ws, cudaMemcpyAsync(ws->adj_in[3], lam_v, bV, cudaMemcpyHostToDevice, ws->stream));
+    du = ws->adj_in[0]; dv = ws->adj_in[1]; dlu = ws->adj_in[2]; dlv = ws->adj_in[3];
+    dgu = ws->d_ut; dgv = ws->d_vt;
+  }
+  if ((rc = reset_flags(ws))) return rc;
+  if ((rc = enqueue_rhs_adjoint(ws, du, dv, t, dlu, dlv, dgu, dgv))) return rc;
+  rc = collect(ws);
+  if (where == WEDG_HOST) {
+    CK(ws, cudaMemcpy(gu, ws->d_ut, bU, cudaMemcpyDeviceToHost));
+    CK(ws, cudaMemcpy(gv, ws->d_vt, bV, cudaMemcpyDeviceToHost));
+  }
+  return rc;
+}
+
+int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0, double dt, int64_t nsteps,
+                     int64_t every, const double *lam_u, const double *lam_v, double *gu, double *gv,
+                     const int64_t u_shape[4], const int64_t v_shape[4], int where) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  ws->stats.kernel_launches = 0;
+  int rc = check_shapes(ws, u_shape, v_shape);
+  if (rc) return rc;
+  if (!u0 || !v0 || !lam_u || !lam_v || !gu || !gv) return argument_error(ws, "null pointer");
+  if (nsteps < 0 || every < 1) return argument_error(ws, "nsteps must be ≥ 0 and the checkpoint interval ≥ 1");
+  if ((rc = adjoint_buffers(ws))) return rc;
+  const size_t nU = (size_t)ws->E * ws->nu * ws->nu, nV = (size_t)ws->E * ws->nv * ws->nv, n = nU + nV;
+  const int64_t nchk = nsteps ? (nsteps + every - 1) / every : 0;
+  const int64_t seg = std::min<int64_t>(every, std::max<int64_t>(nsteps, 1));
+  // buffers: a state is u followed by v (n doubles)
+  if (!ws->rk_lam) {
+    if ((rc = dalloc(ws, &ws->rk_lam, n)) || (rc = dalloc(ws, &ws->rk_acc, n)) || (rc = dalloc(ws, &ws->rk_kbar, n)) ||
+        (rc = dalloc(ws, &ws->rk_g, n)) || (rc = dalloc(ws, &ws->rk_y, n)))
+      return rc;
+  }
+  while (ws->rk_chk_n < nchk) {
+    double *p;
+    if ((rc = dalloc(ws, &p, n))) return rc;
+    ws->rk_chk.push_back(p);
+    ++ws->rk_chk_n;
+  }
+  while (ws->rk_seg_n < 4 * seg) {
+    double *p;
+    if ((rc = dalloc(ws, &p, n))) return rc;
+    ws->rk_seg.push_back(p);
+    ++ws->rk_seg_n;
+  }
+  cudaStream_t st = ws->stream;
+  const cudaMemcpyKind in = where == WEDG_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  double *yu = ws->rk_y, *yv = ws->rk_y + nU;
+  CK(ws, cudaMemcpyAsync(yu, u0, sizeof(double) * nU, in, st));
+  CK(ws, cudaMemcpyAsync(yv, v0, sizeof(double) * nV, in, st));
+  CK(ws, cudaMemcpyAsync(ws->rk_lam, lam_u, sizeof(double) * nU, in, st));
+  CK(ws, cudaMemcpyAsync(ws->rk_lam + nU, lam_v, sizeof(double) * nV, in, st));
+  std::vector<double> t(nsteps + 1);
+  t[0] = t0;
+  for (int64_t k = 0; k < nsteps; ++k) t[k + 1] = t[k] + dt;
+  if ((rc = reset_flags(ws))) return rc;
+  // ---- forward pass: the checkpoints
+  for (int64_t k = 0; k < nsteps; ++k) {
+    if (k % every == 0) CK(ws, cudaMemcpyAsync(ws->rk_chk[k / every], ws->rk_y, sizeof(double) * n,
+                                               cudaMemcpyDeviceToDevice, st));
+    if ((rc = enqueue_rk4(ws, yu, yv, t[k], dt, 1))) return rc;
+  }
+  const int lb = 256, lg = (int)std::min<size_t>((n + lb - 1) / lb, 152 * 16);
+  auto lin = [&](double *out, double a, const double *x, double b, const double *y, const double *z) {
+    k_lincomb<<<lg, lb, 0, st>>>(n, out, a, x, b, y, z);
+  };
+  // ---- reverse pass, segment by segment
+  for (int64_t c = nchk - 1; c >= 0; --c) {
+    const int64_t k0 = c * every, k1 = std::min(nsteps, k0 + every);
+    CK(ws, cudaMemcpyAsync(ws->rk_y, ws->rk_chk[c], sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    for (int64_t k = k0; k < k1; ++k) {
+      double *su[4], *sv[4];
+      for (int s = 0; s < 4; ++s) {
+        su[s] = ws->rk_seg[4 * (k - k0) + s];
+        sv[s] = su[s] + nU;
+      }
+      if ((rc = enqueue_rk4(ws, yu, yv, t[k], dt, 1, nullptr, 0, su, sv))) return rc;
+    }
+    for (int64_t k = k1 - 1; k >= k0; --k) {
+      const double ts[4] = {t[k], t[k] + 0.5 * dt, t[k] + 0.5 * dt, t[k] + dt};
+      // K̄_s = ca[s] λ + cb[s] Ȳ_{s+1}, Ȳ = Jᵀ K̄ at the stage state: y_{n+1} = y + dt/6 (K1 + 2K2 +
+      // 2K3 + K4), Y2 = y + dt/2 K1, Y3 = y + dt/2 K2, Y4 = y + dt K3
+      const double ca[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};
+      const double cb[4] = {0.5 * dt, 0.5 * dt, dt, 0.0};
+      for (int s = 3; s >= 0; --s) {
+        lin(ws->rk_kbar, ca[s], ws->rk_lam, cb[s], s == 3 ? nullptr : ws->rk_g, nullptr);
+        const double *Y = ws->rk_seg[4 * (k - k0) + s];
+        if ((rc = enqueue_rhs_adjoint(ws, Y, Y + nU, ts[s], ws->rk_kbar, ws->rk_kbar + nU, ws->rk_g, ws->rk_g + nU)))
+          return rc;
+        lin(ws->rk_acc, 1.0, s == 3 ? ws->rk_lam : ws->rk_acc, 1.0, ws->rk_g, nullptr);
+      }
+      std::swap(ws->rk_lam, ws->rk_acc);
+    }
+  }
+  CK(ws, cudaGetLastError());
+  rc = collect(ws);
+  const cudaMemcpyKind out = where == WEDG_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  CK(ws, cudaMemcpy(gu, ws->rk_lam, sizeof(double) * nU, out));
+  CK(ws, cudaMemcpy(gv, ws->rk_lam + nU, sizeof(double) * nV, out));
   return rc;
 }
 

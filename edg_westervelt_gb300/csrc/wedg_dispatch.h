@@ -27,8 +27,11 @@ typedef void (*launch_fn)(const void *basis, const Fields &F, const StageIO &S, 
                           cudaStream_t st);
 typedef void (*pack_fn)(const BasisHost &h, void *out);
 
+typedef void (*adj_fn)(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, cudaStream_t st);
+
 struct Launchers {
   launch_fn prep = nullptr, stage = nullptr, mass = nullptr;
+  adj_fn adj_hats = nullptr, adj_mass = nullptr, adj_face = nullptr;
   pack_fn pack = nullptr;
   size_t basis_size = 0;
 };
@@ -82,9 +85,28 @@ void launch_mass(const void *basis, const Fields &F, const StageIO &S, int block
   else k_cheb<NU, NV><<<grid, CHEB_THREADS, 0, st>>>(B, F, S);
 }
 
+// The adjoint kernels (wedg_adjoint.cuh): element grids of 128 threads, the mass term on the team grid
+template <int NU, int NV>
+void launch_adj_hats(const void *basis, const Fields &F, const StageIO &, const AdjIO &A, cudaStream_t st) {
+  k_adj_hats<NU, NV><<<(F.E + 127) / 128, 128, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, A);
+}
+template <int NU, int NV>
+void launch_adj_mass(const void *basis, const Fields &F, const StageIO &, const AdjIO &A, cudaStream_t st) {
+  constexpr int tpb = ChebTeam<NU, NV>::TPB;
+  k_adj_mass<NU, NV><<<(F.E + tpb - 1) / tpb, CHEB_THREADS, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F,
+                                                                     A);
+}
+template <int NU, int NV>
+void launch_adj_face(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, cudaStream_t st) {
+  k_adj_face<NU, NV><<<(F.E + 127) / 128, 128, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S, A);
+}
+
 template <int NU, int NV>
 Launchers make_launchers(bool fast) {
   Launchers L;
+  L.adj_hats = launch_adj_hats<NU, NV>;
+  L.adj_mass = launch_adj_mass<NU, NV>;
+  L.adj_face = launch_adj_face<NU, NV>;
   L.prep = launch_prep<NU, NV>;
   L.mass = launch_mass<NU, NV>;
   L.stage = fast ? launch_stage<NU, NV, true> : launch_stage<NU, NV, false>;

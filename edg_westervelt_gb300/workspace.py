@@ -197,6 +197,34 @@ class Workspace:
         self._check(rc)
         return ut, vt
 
+    def rhs_adjoint(self, u, v, t, lam_u, lam_v):
+        """wedg_rhs_adjoint: Jᵀ(λ_u, λ_v), the gradient of λ_u·ut + λ_v·vt with respect to u and
+        v, where (ut, vt) is the right-hand side at (u, v, t). Host arrays in, new arrays out."""
+        self._refuse_mismatch()
+        N, nu, nv = self.N, self.nu, self.nv
+        u, v, lam_u, lam_v = _f64(u), _f64(v), _f64(lam_u), _f64(lam_v)
+        gu = np.zeros((N, N, nu, nu), order="F")
+        gv = np.zeros((N, N, nv, nv), order="F")
+        rc = L.lib().wedg_rhs_adjoint(self._h, _ptr(u), _ptr(v), float(t), _ptr(lam_u), _ptr(lam_v), _ptr(gu),
+                                      _ptr(gv), _shape(u, nu, N), _shape(v, nv, N), L.WEDG_HOST)
+        self._check(rc)
+        return gu, gv
+
+    def rk4_adjoint(self, u0, v0, t0, dt, nsteps, lam_u, lam_v, every=32):
+        """wedg_rk4_adjoint: the gradient with respect to the initial state (u0, v0) of
+        λ_u·u(T) + λ_v·v(T) after nsteps RK4 steps (the adjoint state at t0 for the final-time
+        adjoint (λ_u, λ_v)); checkpoints every `every` steps. Host arrays in, new arrays out."""
+        self._refuse_mismatch()
+        N, nu, nv = self.N, self.nu, self.nv
+        u0, v0, lam_u, lam_v = _f64(u0), _f64(v0), _f64(lam_u), _f64(lam_v)
+        gu = np.zeros((N, N, nu, nu), order="F")
+        gv = np.zeros((N, N, nv, nv), order="F")
+        rc = L.lib().wedg_rk4_adjoint(self._h, _ptr(u0), _ptr(v0), float(t0), float(dt), int(nsteps), int(every),
+                                      _ptr(lam_u), _ptr(lam_v), _ptr(gu), _ptr(gv), _shape(u0, nu, N),
+                                      _shape(v0, nv, N), L.WEDG_HOST)
+        self._check(rc)
+        return gu, gv
+
     def rk4_steps(self, u, v, t0, dt, nsteps, stop_nonfinite=False):
         """nsteps RK4 steps in place from t0 (t advancing by repeated addition of dt).
         Returns the number of steps completed; sets self.fin."""

@@ -185,6 +185,25 @@ typedef struct wedg_source_run {
 int wedg_run_source(wedg_ws *ws, double *u, double *v, const int64_t u_shape[4], const int64_t v_shape[4],
                     int where, const wedg_source_run *run, int64_t *steps_done, int *finite);
 
+/* Discrete adjoint of edg_rhs! (no counterpart in the reference): at the state (u, v) and time
+ * t, gu and gv receive Jᵀ(λ_u, λ_v), the gradient of λ_u·ut + λ_v·vt with respect to u and v,
+ * where (ut, vt) is the right-hand side of src/rhs.jl:490-550. Layouts, `where` and errors as
+ * wedg_rhs (the forward RHS at the state is evaluated first and checked). */
+int wedg_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t, const double *lam_u,
+                     const double *lam_v, double *gu, double *gv, const int64_t u_shape[4], const int64_t v_shape[4],
+                     int where);
+
+/* Discrete adjoint of the RK4 time stepping (no counterpart in the reference): for nsteps RK4
+ * steps from (u0, v0) at t0 (t advancing by t += dt, as wedg_rk4_steps), gu and gv receive the
+ * gradient with respect to (u0, v0) of λ_u·u(T) + λ_v·v(T), i.e. the adjoint state at t0 for the
+ * final-time adjoint (λ_u, λ_v) -- for a misfit J(u(T), v(T)), pass ∂J/∂u(T), ∂J/∂v(T). The
+ * forward states are kept every `every` steps (checkpoints); each segment is run again with its
+ * RK4 stage states kept, and the steps are reversed through wedg_rhs_adjoint's transposes at the
+ * stage states. Device memory: (nsteps / every + 4 every) states besides the workspace. */
+int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0, double dt, int64_t nsteps,
+                     int64_t every, const double *lam_u, const double *lam_v, double *gu, double *gv,
+                     const int64_t u_shape[4], const int64_t v_shape[4], int where);
+
 /* Batched form: many independent instances -- workspaces made by wedg_create, each with its
  * own N, degrees, flux, boundary kinds and coefficients -- advanced together. No counterpart in
  * the reference, whose batching is the caller's loop over instances. One RK4 step of every

@@ -1,0 +1,109 @@
+"""The discrete adjoint (no counterpart in the reference): wedg_rhs_adjoint against central
+finite differences of the forward right-hand side (wedg_rhs) -- the dot-product test
+⟨λ, (F(x + εw) - F(x - εw)) / 2ε⟩ = ⟨Jᵀλ, w⟩ on seeded x, w, λ -- over both pairings, every
+boundary kind (the absorbing families are nonlinear through √(1 - kβv)), the three fluxes,
+one-sided faces with jumping coefficients, both mass solvers and the constant-coefficient and
+general kernels."""
+import math
+
+import numpy as np
+import pytest
+
+import edg_westervelt_gb300 as W
+from oracle import coefficients as oc
+from test_oracle import quadrant_coefficients
+
+pytestmark = pytest.mark.gpu
+
+
+def _dot(a, b):
+    return float(np.sum(a[0] * b[0]) + np.sum(a[1] * b[1]))
+
+
+def _check(pre, N, t, rng, amp_v=0.004, eps=1e-6, fast_path=True):
+    nu, nv = pre["qu1"], pre["qv1"]
+    ws = W.Workspace(pre, N, fast_path=fast_path)
+    x = (np.asfortranarray(0.3 * rng.standard_normal((N, N, nu, nu))),
+         np.asfortranarray(amp_v * rng.standard_normal((N, N, nv, nv))))
+    w = (np.asfortranarray(rng.standard_normal((N, N, nu, nu))),
+         np.asfortranarray(amp_v * rng.standard_normal((N, N, nv, nv))))
+    lam = (np.asfortranarray(rng.standard_normal((N, N, nu, nu))),
+           np.asfortranarray(rng.standard_normal((N, N, nv, nv))))
+    fp = [y.copy() for y in ws.rhs(x[0] + eps * w[0], x[1] + eps * w[1], t)]
+    fm = [y.copy() for y in ws.rhs(x[0] - eps * w[0], x[1] - eps * w[1], t)]
+    jvp = ((fp[0] - fm[0]) / (2 * eps), (fp[1] - fm[1]) / (2 * eps))
+    g = ws.rhs_adjoint(x[0], x[1], t, lam[0], lam[1])
+    a, b = _dot(lam, jvp), _dot(g, w)
+    scale = abs(_dot(lam, (np.abs(jvp[0]), np.abs(jvp[1])))) + 1e-300
+    return abs(a - b) / max(abs(a), 1e-12 * scale)
+
+
+@pytest.mark.parametrize("solver", ["chebyshev", "cg"])
+def test_rhs_adjoint_dot_product(gpu, solver):
+    rng = np.random.default_rng(41)
+    worst = 0.0
+    for q, N, mixed, flux, boundary, mode in (
+            (1, 3, True, "upwind", "absorbing_2beta", "mms"),
+            (2, 4, False, "central", "absorbing", "source"),
+            (3, 4, True, "alternating", "dirichlet", "initial_value"),
+            (4, 3, False, "upwind", "wall", "source"),
+            (3, 5, True, "upwind", dict(bot="absorbing_2beta", top="wall", lft="dirichlet", rgt="absorbing"), "mms")):
+        co = oc.constant_coefficients(c=1.2, alpha=1e-3, beta=4.0) if mode != "mms" else None
+        kw = dict(mixed=mixed, flux=flux, boundary=boundary, mode=mode, mass_solver=solver, kappa=0.6, sigma=0.3,
+                  sigma_dirichlet=0.5, phase=(0.4, 0.3))
+        if co is not None:
+            kw["coefficients"] = W.constant_coefficients(c=1.2, alpha=1e-3, beta=4.0)
+        pre, _ = W.precompute(q, N, **kw)
+        for fast in (True, False):
+            worst = max(worst, _check(pre, N, 0.037, rng, fast_path=fast))
+    assert worst < 1e-6, worst
+
+
+def test_rhs_adjoint_one_sided_faces(gpu):
+    """Jumping coefficients: the one-sided face kernel (src/rhs.jl:660-700) and its jump terms."""
+    rng = np.random.default_rng(42)
+    co = quadrant_coefficients(0.5, 0.5, smooth=False)
+    worst = 0.0
+    for q, N in ((2, 4), (4, 4)):
+        pre, _ = W.precompute(q, N, mode="source", coefficients=co, flux_params=dict(theta=0.3, tau=0.7, lambda_u=0.4,
+                                                                                        lambda_v=0.9),
+                              boundary="absorbing_2beta")
+        assert pre["one_sided"]
+        worst = max(worst, _check(pre, N, 0.2, rng))
+    assert worst < 1e-6, worst
+
+
+@pytest.mark.parametrize("solver", ["chebyshev", "cg"])
+def test_rk4_adjoint_against_finite_differences(gpu, solver):
+    """The reverse RK4 with checkpoints: the gradient of J = λ·y(T) with respect to the initial
+    state against central differences of forward runs (wedg_rk4_steps) along seeded directions;
+    37 steps with a checkpoint every 8, so the last segment is partial."""
+    rng = np.random.default_rng(43)
+    for q, N, kw in ((3, 4, dict(mode="source", flux="upwind", boundary="absorbing_2beta",
+                                 coefficients=W.constant_coefficients(c=1.1, alpha=1e-3, beta=3.0))),
+                     (2, 5, dict(mode="mms", flux="alternating", mixed=False,
+                                 boundary=dict(bot="wall", top="absorbing", lft="dirichlet", rgt="absorbing_2beta"),
+                                 kappa=0.5))):
+        pre, _ = W.precompute(q, N, mass_solver=solver, **kw)
+        nu, nv = pre["qu1"], pre["qv1"]
+        ws = W.Workspace(pre, N)
+        dt = (1.0 / N) / (10 * q * q)
+        nsteps, t0 = 37, 0.02
+        def smooth(n, amp):                      # modal coefficients decaying with the degree
+            d = 1.0 / (1.0 + np.add.outer(np.arange(n), np.arange(n))) ** 2
+            return np.asfortranarray(amp * rng.standard_normal((N, N, n, n)) * d)
+        y0 = (smooth(nu, 0.01), smooth(nv, 0.001))
+        lam = (np.asfortranarray(rng.standard_normal((N, N, nu, nu))),
+               np.asfortranarray(rng.standard_normal((N, N, nv, nv))))
+
+        def J(u, v):
+            u, v = u.copy(order="F"), v.copy(order="F")
+            assert ws.rk4_steps(u, v, t0, dt, nsteps) == nsteps
+            return float(np.sum(lam[0] * u) + np.sum(lam[1] * v))
+        gu, gv = ws.rk4_adjoint(y0[0], y0[1], t0, dt, nsteps, lam[0], lam[1], every=8)
+        for _ in range(3):
+            w = (smooth(nu, 1.0), smooth(nv, 0.1))
+            eps = 1e-5
+            fd = (J(y0[0] + eps * w[0], y0[1] + eps * w[1]) - J(y0[0] - eps * w[0], y0[1] - eps * w[1])) / (2 * eps)
+            ad = float(np.sum(gu * w[0]) + np.sum(gv * w[1]))
+            assert abs(fd - ad) <= 1e-6 * abs(fd), (q, N, fd, ad)
