@@ -292,4 +292,185 @@ __global__ void __launch_bounds__(128) k_adj_face(const __grid_constant__ Basis<
     for (int a = 0; a < NV; ++a) A.gv[e + Eu * (a + NV * b)] = gV[a][b];
 }
 
+// The slots of a physical side point as functions of the coefficients there (side_point's
+// formulas with c², α, c, β as arguments), for their derivatives in k_adj_param
+__device__ __forceinline__ void boundary_slots(const Fields &F, int s, double c2f, double af, double cf, double bf,
+                                               double v_fp, double gun, double gvn, double gu_ex, double gv_ex,
+                                               double v_ex, double sgn, double (&q)[3]) {
+  double F1, dv;
+  if (F.kind[s] == 3) {
+    const double g2 = c2f * gu_ex + af * gv_ex;
+    const double rho_w = c2f * gun + af * gvn - g2;
+    dv = -(F.kap[s] / cf) * rho_w;
+    F1 = g2;
+  } else {
+    const double g = F.gam[s], et = F.eta[s], sg = F.sig[s], kb = F.kb[s];
+    const double sqf = sqrt(1.0 - kb * bf * v_fp);
+    const double rho_num = et * (c2f * gun + af * gvn) + g * cf * sqf * v_fp;
+    const double rho_ex = et * (c2f * gu_ex + af * gv_ex) + g * cf * sqrt(1.0 - kb * bf * v_ex) * v_ex;
+    const double rho = rho_num - rho_ex;
+    F1 = c2f * gun + af * gvn - (et + sg * g) * rho;
+    dv = -(g - sg * et) / (cf * sqf) * rho;
+  }
+  q[0] = F1;
+  q[1] = sgn * (af * dv);
+  q[2] = -sgn * (c2f * dv);
+}
+
+// k_adj_param: for the constant-coefficient kernels (c², α, β constant on each element), the
+// derivative of the stage's weighted output K̄·F(Y) with respect to the element's c², α and β,
+// added to gc2[e], gal[e], gbe[e]. With μ = M⁻¹K̄_v, ν = A_e⁻¹K̄_u and the forward outputs ut, vt
+// at Y (all from the adjoint evaluation just made at Y):
+//   volume   μ·∂R/∂p + ν·∂b/∂p   (R ∋ -(4/h²)(c²(K1U + UK1) + α(K1V + VK1)), b ∋ c²(K1V + VK1))
+//   u-solve  -ν·(∂A_e/∂c²) ut = -ν·(K1 ut + ut K1)
+//   mass     μ·(∂K/∂β) vt = Σ_points 2 W v_q vt_q μ_q
+//   faces    the slots' derivatives times their weights (the hats): at an interior point of a
+//            one-sided face, the element's own coefficient enters its own slots and the
+//            neighbour's (each slot is quadratic in one coefficient, so a central difference
+//            of step |c| is exact); at a continuous face the shared face value enters the own
+//            slots (the neighbour adds its own); on a physical side c², α, c = √c², β enter the
+//            own slots (central differences of relative step 1e-6).
+template <int NU, int NV>
+__global__ void __launch_bounds__(128) k_adj_param(const __grid_constant__ Basis<NU, NV> B,
+                                                    const __grid_constant__ Fields F,
+                                                    const __grid_constant__ StageIO S, const AdjIO A,
+                                                    double *gc2, double *gal, double *gbe) {
+  constexpr int NQ = NU, QH = Basis<NU, NV>::QH;
+  const int E = F.E, N = F.N;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  if (err_word(F) != ERR_NONE) return;
+  const int j = e % N, k = e / N;
+  const size_t Eu = (size_t)E;
+  const TimeF tf = time_factors(S);
+  auto U = [&](int a, int b) { return S.xu[e + Eu * (a + NU * b)]; };
+  auto V = [&](int a, int b) { return (a < NV && b < NV) ? S.xv[e + Eu * (a + NV * b)] : 0.0; };
+  auto MU = [&](int a, int b) { return (a < NV && b < NV) ? A.mu[e + Eu * (a + NV * b)] : 0.0; };
+  auto NUv = [&](int a, int b) { return A.nu[e + Eu * (a + NU * b)]; };
+  auto UT = [&](int a, int b) { return S.ut[e + Eu * (a + NU * b)]; };
+  double dc2 = 0.0, dal = 0.0, dbe = 0.0;
+  // ---- volume and u-solve
+  for (int a = 0; a < NU; ++a)
+    for (int b = 0; b < NU; ++b) {
+      double ku = 0, kv = 0, kt = 0;
+      for (int c = 0; c < NU; ++c) {
+        ku += B.K1[a][c] * U(c, b) + U(a, c) * B.K1[c][b];
+        kv += B.K1[a][c] * V(c, b) + V(a, c) * B.K1[c][b];
+        kt += B.K1[a][c] * UT(c, b) + UT(a, c) * B.K1[c][b];
+      }
+      const double m = MU(a, b), n = NUv(a, b);
+      dc2 += -F.four_hh * m * ku - n * kt + n * kv;   // R (v-block: μ is zero outside), u-solve, b
+      dal += -F.four_hh * m * kv;
+    }
+  // ---- mass: Σ_points 2 W v_q vt_q μ_q (β constant on the element)
+  {
+    double Tv[QH][NV], Tt[QH][NV], Tm[QH][NV];
+    for (int r = 0; r < QH; ++r)
+      for (int b = 0; b < NV; ++b) {
+        double x = 0, y = 0, z = 0;
+        for (int a = 0; a < NV; ++a) {
+          x += B.Ph[r][a] * S.xv[e + Eu * (a + NV * b)];
+          y += B.Ph[r][a] * S.vt[e + Eu * (a + NV * b)];
+          z += B.Ph[r][a] * A.mu[e + Eu * (a + NV * b)];
+        }
+        Tv[r][b] = x; Tt[r][b] = y; Tm[r][b] = z;
+      }
+    for (int r = 0; r < QH; ++r)
+      for (int s2 = 0; s2 < QH; ++s2) {
+        double x = 0, y = 0, z = 0;
+        for (int b = 0; b < NV; ++b) { x += Tv[r][b] * B.Ph[s2][b]; y += Tt[r][b] * B.Ph[s2][b]; z += Tm[r][b] * B.Ph[s2][b]; }
+        dbe += 2.0 * (B.PhW[r][0] / B.Ph[r][0]) * (B.PhW[s2][0] / B.Ph[s2][0]) * x * y * z;
+      }
+  }
+  // ---- faces
+  const double *tr = F.tr;
+  auto T = [&](int fam, int side, int i, int el) { return tr[((fam * 4 + side) * NQ + i) * Eu + el]; };
+  auto hat = [&](int fam, int side, int i, int el) {
+    const double h = A.hat[((fam * 4 + side) * NQ + i) * Eu + el];
+    const double w = B.w[i];
+    return fam == 0 ? F.two_h * w * h : fam == 1 ? F.four_hh * w * h : -w * h;
+  };
+  for (int s = 0; s < 4; ++s) {
+    const bool boundary = (s == 0 && j == 0) || (s == 1 && j == N - 1) || (s == 2 && k == 0) || (s == 3 && k == N - 1);
+    for (int i = 0; i < NQ; ++i) {
+      const double ho[3] = {hat(0, s, i, e), hat(1, s, i, e), hat(2, s, i, e)};
+      if (boundary) {
+        const int m = s < 2 ? k : j;
+        const double sgn = (s == 0 || s == 2) ? -1.0 : 1.0;
+        size_t fi;
+        const double *c2a, *afa, *cfa, *bfa;
+        if (s < 2) { fi = (s == 0 ? 0 : N) + (size_t)(N + 1) * (k + (size_t)N * i); c2a = F.hc2; afa = F.haf; cfa = F.hcf; bfa = F.hbf; }
+        else { fi = j + (size_t)N * ((s == 2 ? 0 : N) + (size_t)(N + 1) * i); c2a = F.vc2; afa = F.vaf; cfa = F.vcf; bfa = F.vbf; }
+        const double c2f = c2a[fi], af = afa[fi], cf = cfa[fi], bf = bfa[fi];
+        const double v_fp = T(1, s, i, e);
+        const double gun = sgn * (F.two_h * T(0, s, i, e)), gvn = sgn * (F.two_h * T(2, s, i, e));
+        const double spn = F.bspn[s][m + (size_t)N * i], sp = F.bsp[s][m + (size_t)N * i];
+        const double gu_ex = sgn * (tf.ct * spn - spn), gv_ex = sgn * (-F.omega * tf.st * spn);
+        const double v_ex = -F.omega * tf.st * sp;
+        double x[4] = {c2f, af, cf, bf}, d[4];
+        for (int p = 0; p < 4; ++p) {
+          const double hstep = 1e-6 * (fabs(x[p]) > 1e-300 ? fabs(x[p]) : 1.0);
+          double qp[3], qm[3], y[4] = {x[0], x[1], x[2], x[3]};
+          y[p] = x[p] + hstep;
+          boundary_slots(F, s, y[0], y[1], y[2], y[3], v_fp, gun, gvn, gu_ex, gv_ex, v_ex, sgn, qp);
+          y[p] = x[p] - hstep;
+          boundary_slots(F, s, y[0], y[1], y[2], y[3], v_fp, gun, gvn, gu_ex, gv_ex, v_ex, sgn, qm);
+          d[p] = ((qp[0] - qm[0]) * ho[0] + (qp[1] - qm[1]) * ho[1] + (qp[2] - qm[2]) * ho[2]) / (2.0 * hstep);
+        }
+        dc2 += d[0] + d[2] / (2.0 * cf);        // c = √c²
+        dal += d[1];
+        dbe += d[3];
+      } else {
+        const bool plus = (s == 0 || s == 2);
+        const int nb = s == 0 ? e - 1 : s == 1 ? e + 1 : s == 2 ? e - N : e + N;
+        const int sn = s ^ 1;
+        const int sm = s < 2 ? 1 : 3, spp = s < 2 ? 0 : 2;
+        const int em = plus ? nb : e, ep = plus ? e : nb;
+        size_t fi;
+        const double *c2p_a, *afp_a, *c2m_a, *afm_a, *jc_a;
+        if (s < 2) {
+          fi = (s == 0 ? j : j + 1) + (size_t)(N + 1) * (k + (size_t)N * i);
+          c2p_a = F.hc2; afp_a = F.haf; c2m_a = F.hc2m; afm_a = F.hafm; jc_a = F.hJC;
+        } else {
+          fi = j + (size_t)N * ((s == 2 ? k : k + 1) + (size_t)(N + 1) * i);
+          c2p_a = F.vc2; afp_a = F.vaf; c2m_a = F.vc2m; afm_a = F.vafm; jc_a = F.vJC;
+        }
+        const FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);
+        const double vm = T(1, sm, i, em), vp = T(1, spp, i, ep);
+        const double dum = T(0, sm, i, em), dup = T(0, spp, i, ep);
+        const double dvm = T(2, sm, i, em), dvp = T(2, spp, i, ep);
+        const double hn[3] = {hat(0, sn, i, nb), hat(1, sn, i, nb), hat(2, sn, i, nb)};
+        // weighted slots (own, and with the neighbour's role and weights on one-sided faces)
+        auto wslots = [&](const FaceCoef &c) {
+          double Ao, Do, Fo;
+          interior_flux(F, c, plus, dum, dup, vm, vp, dvm, dvp, Ao, Do, Fo);
+          double r = Ao * ho[0] + Do * ho[1] + Fo * ho[2];
+          if (F.one_sided) {
+            double An, Dn, Fn;
+            interior_flux(F, c, !plus, dum, dup, vm, vp, dvm, dvp, An, Dn, Fn);
+            r += An * hn[0] + Dn * hn[1] + Fn * hn[2];
+          }
+          return r;
+        };
+        // the element's own coefficient: its side's values on one-sided faces, the face value else
+        for (int p = 0; p < 2; ++p) {
+          FaceCoef cp = cf, cm = cf;
+          double *xp, *xm, x;
+          if (F.one_sided && !plus) { xp = p ? &cp.afm : &cp.c2m; xm = p ? &cm.afm : &cm.c2m; x = p ? cf.afm : cf.c2m; }
+          else { xp = p ? &cp.afp : &cp.c2p; xm = p ? &cm.afp : &cm.c2p; x = p ? cf.afp : cf.c2p; }
+          const double hstep = fabs(x) > 1e-300 ? fabs(x) : 1.0;
+          *xp = x + hstep;
+          *xm = x - hstep;
+          const double d = (wslots(cp) - wslots(cm)) / (2.0 * hstep);
+          if (p == 0) dc2 += d;
+          else dal += d;
+        }
+      }
+    }
+  }
+  gc2[e] += dc2;
+  gal[e] += dal;
+  gbe[e] += dbe;
+}
+
 }  // namespace wedg

@@ -104,6 +104,7 @@ struct wedg_ws {
   std::vector<double *> rk_chk, rk_seg;
   int64_t rk_chk_n = 0, rk_seg_n = 0;
   double *rk_lam = nullptr, *rk_acc = nullptr, *rk_kbar = nullptr, *rk_g = nullptr, *rk_y = nullptr;
+  double *rk_par = nullptr;   // per-element gradients with respect to c², α, β
   // optional per-launch timing (events recorded around each stage kernel)
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -1121,12 +1122,17 @@ int wedg_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t, co
 
 int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0, double dt, int64_t nsteps,
                      int64_t every, const double *lam_u, const double *lam_v, double *gu, double *gv,
-                     const int64_t u_shape[4], const int64_t v_shape[4], int where) {
+                     double *g_c2, double *g_alpha, double *g_beta, const int64_t u_shape[4],
+                     const int64_t v_shape[4], int where) {
   if (!ws) return WEDG_ERR_ARGUMENT;
   ws->stats.kernel_launches = 0;
   int rc = check_shapes(ws, u_shape, v_shape);
   if (rc) return rc;
   if (!u0 || !v0 || !lam_u || !lam_v || !gu || !gv) return argument_error(ws, "null pointer");
+  const bool params = g_c2 || g_alpha || g_beta;
+  if (params && !(g_c2 && g_alpha && g_beta)) return argument_error(ws, "give all three parameter gradients or none");
+  if (params && (!ws->fast || !ws->cfg.src_on || ws->cfg.mms_on))
+    return argument_error(ws, "parameter gradients need source mode and c², α, β constant on each element");
   if (nsteps < 0 || every < 1) return argument_error(ws, "nsteps must be ≥ 0 and the checkpoint interval ≥ 1");
   if ((rc = adjoint_buffers(ws))) return rc;
   const size_t nU = (size_t)ws->E * ws->nu * ws->nu, nV = (size_t)ws->E * ws->nv * ws->nv, n = nU + nV;
@@ -1135,9 +1141,11 @@ int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0,
   // buffers: a state is u followed by v (n doubles)
   if (!ws->rk_lam) {
     if ((rc = dalloc(ws, &ws->rk_lam, n)) || (rc = dalloc(ws, &ws->rk_acc, n)) || (rc = dalloc(ws, &ws->rk_kbar, n)) ||
-        (rc = dalloc(ws, &ws->rk_g, n)) || (rc = dalloc(ws, &ws->rk_y, n)))
+        (rc = dalloc(ws, &ws->rk_g, n)) || (rc = dalloc(ws, &ws->rk_y, n)) ||
+        (rc = dalloc(ws, &ws->rk_par, 3 * (size_t)ws->E)))
       return rc;
   }
+  if (params) CK(ws, cudaMemsetAsync(ws->rk_par, 0, sizeof(double) * 3 * ws->E, ws->stream));
   while (ws->rk_chk_n < nchk) {
     double *p;
     if ((rc = dalloc(ws, &p, n))) return rc;
@@ -1194,6 +1202,15 @@ int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0,
         const double *Y = ws->rk_seg[4 * (k - k0) + s];
         if ((rc = enqueue_rhs_adjoint(ws, Y, Y + nU, ts[s], ws->rk_kbar, ws->rk_kbar + nU, ws->rk_g, ws->rk_g + nU)))
           return rc;
+        if (params) {
+          // K̄_s · ∂F/∂p at Y_s, from the adjoint evaluation just made (μ, ν, the slot weights, ut, vt)
+          StageIO Sp{};
+          Sp.xu = Y; Sp.xv = Y + nU;
+          stage_factors(ws, ts[s], Sp);
+          Sp.ut = ws->adj_ut; Sp.vt = ws->adj_vt;
+          const AdjIO A{ws->adj_mu, ws->adj_nu, ws->adj_nus, ws->adj_vt, ws->adj_hat, ws->rk_g, ws->rk_g + nU};
+          ws->L.adj_param(ws->basis.data(), ws->F, Sp, A, ws->rk_par, ws->rk_par + ws->E, ws->rk_par + 2 * ws->E, st);
+        }
         lin(ws->rk_acc, 1.0, s == 3 ? ws->rk_lam : ws->rk_acc, 1.0, ws->rk_g, nullptr);
       }
       std::swap(ws->rk_lam, ws->rk_acc);
@@ -1204,6 +1221,11 @@ int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0,
   const cudaMemcpyKind out = where == WEDG_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   CK(ws, cudaMemcpy(gu, ws->rk_lam, sizeof(double) * nU, out));
   CK(ws, cudaMemcpy(gv, ws->rk_lam + nU, sizeof(double) * nV, out));
+  if (params) {
+    CK(ws, cudaMemcpy(g_c2, ws->rk_par, sizeof(double) * ws->E, out));
+    CK(ws, cudaMemcpy(g_alpha, ws->rk_par + ws->E, sizeof(double) * ws->E, out));
+    CK(ws, cudaMemcpy(g_beta, ws->rk_par + 2 * ws->E, sizeof(double) * ws->E, out));
+  }
   return rc;
 }
 

@@ -29,9 +29,13 @@ typedef void (*pack_fn)(const BasisHost &h, void *out);
 
 typedef void (*adj_fn)(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, cudaStream_t st);
 
+typedef void (*adj_param_fn)(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, double *gc2,
+                             double *gal, double *gbe, cudaStream_t st);
+
 struct Launchers {
   launch_fn prep = nullptr, stage = nullptr, mass = nullptr;
   adj_fn adj_hats = nullptr, adj_mass = nullptr, adj_face = nullptr;
+  adj_param_fn adj_param = nullptr;
   pack_fn pack = nullptr;
   size_t basis_size = 0;
 };
@@ -102,8 +106,16 @@ void launch_adj_face(const void *basis, const Fields &F, const StageIO &S, const
 }
 
 template <int NU, int NV>
+void launch_adj_param(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, double *gc2, double *gal,
+                      double *gbe, cudaStream_t st) {
+  k_adj_param<NU, NV><<<(F.E + 127) / 128, 128, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S, A, gc2,
+                                                         gal, gbe);
+}
+
+template <int NU, int NV>
 Launchers make_launchers(bool fast) {
   Launchers L;
+  L.adj_param = launch_adj_param<NU, NV>;
   L.adj_hats = launch_adj_hats<NU, NV>;
   L.adj_mass = launch_adj_mass<NU, NV>;
   L.adj_face = launch_adj_face<NU, NV>;

@@ -150,3 +150,60 @@ def run_source(u, v, dt, nsteps, N, h, pre, geo, ws, record_every, slice_y, rece
     return dict(t=np.array(rec_t), slice_x=slice_x, slices=np.array(rec_slice).T, energy=np.array(rec_E),
                 vmax=np.array(rec_vmax), ndmin=np.array(rec_nd), recv_t=np.array(rt_t), recv=np.array(rt_v),
                 receivers=list(receivers), snaps=snaps, grid_x=grid, grid_y=grid.copy(), dt=dt)
+
+
+def piecewise_coefficients(c2, alpha, beta):
+    """Coefficients constant on the cells of an m × n grid of (0,1)²: c2, alpha, beta are (m, n)
+    arrays indexed [row (y), column (x)] of c², α and β (the parameter fields of the misfit
+    gradient). The derivatives of c and α vanish inside the cells."""
+    from .coefficients import Coefficients
+    c2, alpha, beta = (np.asarray(a, dtype=np.float64) for a in (c2, alpha, beta))
+    m, n = c2.shape
+
+    def cell(tab):
+        def f(x, y):
+            x = np.asarray(x, dtype=np.float64)
+            y = np.asarray(y, dtype=np.float64)
+            return tab[np.clip(np.floor(m * y).astype(int), 0, m - 1), np.clip(np.floor(n * x).astype(int), 0, n - 1)]
+        return f
+
+    def zero(x, y):
+        return np.zeros(np.broadcast(np.asarray(x), np.asarray(y)).shape)
+    return Coefficients(cell(np.sqrt(c2)), zero, zero, cell(alpha), zero, zero, cell(beta))
+
+
+def misfit_gradient(q, N, T, c2, alpha, beta, receivers, u_obs, *, dt_fac=10, every=32, **kw):
+    """The discrete adjoint's gradient of the final-time misfit J = ½ Σ_r (u_h(x_r, T) - u_obs_r)²
+    of a source-mode run from the zero state with respect to c², α and β constant on the cells
+    of the grid of the (m, n) arrays c2, alpha, beta (every cell a block of N/m × N/n elements).
+    Returns (J, dict(c2=..., alpha=..., beta=...)) with gradients of the cells' shape. The forward
+    run, the misfit and the final-time adjoint λ_u = Σ_r (u_h(x_r) - u_obs_r) ∂u_h(x_r)/∂U are
+    computed here, the reverse sweep by wedg_rk4_adjoint (checkpoints every `every` steps)."""
+    c2 = np.asarray(c2, dtype=np.float64)
+    m, n = c2.shape
+    if N % m or N % n:
+        raise ErrorException(f"the {m} × {n} parameter cells must be unions of elements (N = {N})")
+    pre, geo = precompute(q, N, mode="source", coefficients=piecewise_coefficients(c2, alpha, beta), **kw)
+    nu, nv = pre["qu1"], pre["qv1"]
+    h = 1.0 / N
+    dt = h / (dt_fac * q ** 2)
+    nsteps = int(round(T / dt))
+    dt = T / nsteps
+    ws = Workspace(pre, N)
+    u = np.zeros((N, N, nu, nu), order="F")
+    v = np.zeros((N, N, nv, nv), order="F")
+    ws.rk4_steps(u, v, 0.0, dt, nsteps)
+    lam_u = np.zeros_like(u)
+    J = 0.0
+    for (xr, yr), obs in zip(receivers, u_obs):
+        kr, xi = _locate(xr, N)
+        jr, eta = _locate(yr, N)
+        py, px = _vrow(eta, nu), _vrow(xi, nu)
+        res = float(py @ u[jr - 1, kr - 1] @ px) - obs
+        J += 0.5 * res * res
+        lam_u[jr - 1, kr - 1] += res * np.outer(py, px)
+    zu, zv = np.zeros_like(u), np.zeros_like(v)
+    _, _, gc2, gal, gbe = ws.rk4_adjoint(zu, zv, 0.0, dt, nsteps, lam_u, np.zeros_like(v), every=every, params=True)
+    # element (j, k) lies in cell (j // (N/m), k // (N/n))
+    cells = lambda g: g.reshape(m, N // m, n, N // n).sum(axis=(1, 3))
+    return J, dict(c2=cells(gc2), alpha=cells(gal), beta=cells(gbe))

@@ -210,20 +210,25 @@ class Workspace:
         self._check(rc)
         return gu, gv
 
-    def rk4_adjoint(self, u0, v0, t0, dt, nsteps, lam_u, lam_v, every=32):
+    def rk4_adjoint(self, u0, v0, t0, dt, nsteps, lam_u, lam_v, every=32, params=False):
         """wedg_rk4_adjoint: the gradient with respect to the initial state (u0, v0) of
         λ_u·u(T) + λ_v·v(T) after nsteps RK4 steps (the adjoint state at t0 for the final-time
-        adjoint (λ_u, λ_v)); checkpoints every `every` steps. Host arrays in, new arrays out."""
+        adjoint (λ_u, λ_v)); checkpoints every `every` steps. With params, also the gradients with
+        respect to every element's c², α and β (source mode, coefficients constant per element),
+        as (N, N) arrays. Host arrays in, new arrays out."""
         self._refuse_mismatch()
         N, nu, nv = self.N, self.nu, self.nv
         u0, v0, lam_u, lam_v = _f64(u0), _f64(v0), _f64(lam_u), _f64(lam_v)
         gu = np.zeros((N, N, nu, nu), order="F")
         gv = np.zeros((N, N, nv, nv), order="F")
+        gp = [np.zeros((N, N), order="F") for _ in range(3)] if params else None
+        null = ctypes.POINTER(ctypes.c_double)()
+        pc = [_ptr(g) for g in gp] if params else [null, null, null]
         rc = L.lib().wedg_rk4_adjoint(self._h, _ptr(u0), _ptr(v0), float(t0), float(dt), int(nsteps), int(every),
-                                      _ptr(lam_u), _ptr(lam_v), _ptr(gu), _ptr(gv), _shape(u0, nu, N),
-                                      _shape(v0, nv, N), L.WEDG_HOST)
+                                      _ptr(lam_u), _ptr(lam_v), _ptr(gu), _ptr(gv), pc[0], pc[1], pc[2],
+                                      _shape(u0, nu, N), _shape(v0, nv, N), L.WEDG_HOST)
         self._check(rc)
-        return gu, gv
+        return (gu, gv, *gp) if params else (gu, gv)
 
     def rk4_steps(self, u, v, t0, dt, nsteps, stop_nonfinite=False):
         """nsteps RK4 steps in place from t0 (t advancing by repeated addition of dt).

@@ -199,10 +199,15 @@ int wedg_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t, co
  * final-time adjoint (λ_u, λ_v) -- for a misfit J(u(T), v(T)), pass ∂J/∂u(T), ∂J/∂v(T). The
  * forward states are kept every `every` steps (checkpoints); each segment is run again with its
  * RK4 stage states kept, and the steps are reversed through wedg_rhs_adjoint's transposes at the
- * stage states. Device memory: (nsteps / every + 4 every) states besides the workspace. */
+ * stage states. Device memory: (nsteps / every + 4 every) states besides the workspace.
+ * With g_c2, g_alpha, g_beta (E each, or all NULL) it also returns the gradient with respect to
+ * each element's c², α and β, for source-mode runs whose coefficients are constant on every
+ * element (the constant-coefficient kernels); a parameter constant on a union of elements has
+ * the sum of their entries as its gradient. */
 int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0, double dt, int64_t nsteps,
                      int64_t every, const double *lam_u, const double *lam_v, double *gu, double *gv,
-                     const int64_t u_shape[4], const int64_t v_shape[4], int where);
+                     double *g_c2, double *g_alpha, double *g_beta, const int64_t u_shape[4],
+                     const int64_t v_shape[4], int where);
 
 /* Batched form: many independent instances -- workspaces made by wedg_create, each with its
  * own N, degrees, flux, boundary kinds and coefficients -- advanced together. No counterpart in

@@ -107,3 +107,32 @@ def test_rk4_adjoint_against_finite_differences(gpu, solver):
             fd = (J(y0[0] + eps * w[0], y0[1] + eps * w[1]) - J(y0[0] - eps * w[0], y0[1] - eps * w[1])) / (2 * eps)
             ad = float(np.sum(gu * w[0]) + np.sum(gv * w[1]))
             assert abs(fd - ad) <= 1e-6 * abs(fd), (q, N, fd, ad)
+
+
+def test_misfit_gradient_against_finite_differences(gpu):
+    """The gradient of a receiver misfit with respect to c², α, β constant on 2 × 2 cells (the
+    parameter fields of the adjoint form) against central differences of the misfit along
+    seeded directions: forward runs with perturbed cell values."""
+    rng = np.random.default_rng(44)
+    q, N, T = 2, 8, 0.06
+    c2 = rng.uniform(0.8, 1.5, (2, 2))
+    al = 10 ** rng.uniform(-4, -3, (2, 2))
+    be = rng.uniform(0.5, 3.0, (2, 2))
+    g = (np.arange(4) + 0.5) / 4
+    receivers = [(x, y) for y in g for x in g]
+    u_obs = 1e-4 * rng.standard_normal(len(receivers))
+    src = W.GaussianSource(x0=(0.4, 0.55), r0=0.15, omega=12 * math.pi, Ts=0.5)
+    kw = dict(flux="upwind", mixed=False, boundary="absorbing_2beta", source=src)
+    J0, grad = W.misfit_gradient(q, N, T, c2, al, be, receivers, u_obs, every=7, **kw)
+    assert J0 > 0
+    for _ in range(3):
+        d = {"c2": rng.standard_normal((2, 2)) * c2, "alpha": rng.standard_normal((2, 2)) * al,
+             "beta": rng.standard_normal((2, 2)) * be}
+        eps = 1e-6
+        Jp = W.misfit_gradient(q, N, T, c2 + eps * d["c2"], al + eps * d["alpha"], be + eps * d["beta"],
+                               receivers, u_obs, every=7, **kw)[0]
+        Jm = W.misfit_gradient(q, N, T, c2 - eps * d["c2"], al - eps * d["alpha"], be - eps * d["beta"],
+                               receivers, u_obs, every=7, **kw)[0]
+        fd = (Jp - Jm) / (2 * eps)
+        ad = sum(float(np.sum(grad[k] * d[k])) for k in d)
+        assert abs(fd - ad) <= 1e-5 * abs(fd), (fd, ad)
