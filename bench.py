@@ -279,6 +279,9 @@ def run_ours(args):
     if args.batched_only:
         print(json.dumps({"batched": run_batched(torch, dev, args.steps, args.warmup)}), flush=True)
         return
+    if args.adjoint:
+        print(json.dumps({"adjoint": run_adjoint(torch, args.adjoint_T)}), flush=True)
+        return
 
     pre, _ = W.precompute(Q, NMESH, coefficients=W.constant_coefficients(**COEF), **KW)
     N, nu, nv, qh = NMESH, pre["qu1"], pre["qv1"], pre["q_high"]
@@ -537,6 +540,62 @@ def run_batched(torch, dev, steps, warmup):
             "plain_loop": "Workspace.rk4_steps for each instance in turn"}
 
 
+def run_adjoint(torch, T, every=32):
+    """The adjoint form: one gradient of J = ½ Σ_r (u_h(x_r, T) - u_obs_r)² over a 32 × 32 receiver
+    grid (cell centres) with respect to c², α, β constant on 16 × 16 cells (c ~ U[0.8, 1.25],
+    α log-uniform on [1e-6, 1e-5] -- larger α makes the explicit RK4 step unstable at this dt --
+    β ~ U[0, 4]), forward N = 128,
+    q_u = q_v = 4, absorbing_2beta sides, Gaussian source, checkpoints every 32 steps; u_obs from
+    the forward solver on the field perturbed by ±10 % (default_rng(5)). Timed: one forward solve
+    (the misfit) and one gradient (misfit_gradient: forward, reverse sweep, parameter sums)."""
+    import edg_westervelt_gb300 as W
+    from edg_westervelt_gb300.solver import _locate, _vrow
+    rng = np.random.default_rng(5)
+    q, N, m = 4, 128, 16
+    c2 = rng.uniform(0.8, 1.25, (m, m)) ** 2
+    al = 10.0 ** rng.uniform(-6, -5, (m, m))
+    be = rng.uniform(0.0, 4.0, (m, m))
+    g = (np.arange(32) + 0.5) / 32
+    receivers = [(x, y) for y in g for x in g]
+    kw = dict(flux="upwind", mixed=False, boundary="absorbing_2beta")
+    # observations: the forward solver on the perturbed field
+    pert = lambda a: a * (1.0 + 0.1 * rng.uniform(-1, 1, a.shape))
+    pre, _ = W.precompute(q, N, mode="source", coefficients=W.piecewise_coefficients(pert(c2), pert(al), pert(be)),
+                          **kw)
+    dt = (1.0 / N) / (10 * q * q)
+    nsteps = int(round(T / dt))
+    dt = T / nsteps
+    ws = W.Workspace(pre, N)
+    u = np.zeros((N, N, 5, 5), order="F")
+    v = np.zeros((N, N, 5, 5), order="F")
+    ws.rk4_steps(u, v, 0.0, dt, nsteps)
+    u_obs = []
+    for xr, yr in receivers:
+        kr, xi = _locate(xr, N)
+        jr, eta = _locate(yr, N)
+        u_obs.append(float(_vrow(eta, 5) @ u[jr - 1, kr - 1] @ _vrow(xi, 5)))
+    del ws
+    # one forward solve of the unperturbed field (device time of the step loop, host clock)
+    pre, _ = W.precompute(q, N, mode="source", coefficients=W.piecewise_coefficients(c2, al, be), **kw)
+    ws = W.Workspace(pre, N)
+    u[...] = 0.0
+    v[...] = 0.0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ws.rk4_steps(u, v, 0.0, dt, nsteps)
+    t_fwd = time.perf_counter() - t0
+    del ws
+    t0 = time.perf_counter()
+    J, grad = W.misfit_gradient(q, N, T, c2, al, be, receivers, u_obs, every=every, **kw)
+    t_grad = time.perf_counter() - t0
+    return {"workload": f"misfit gradient, N={N} q_u=q_v={q}, 16x16 cells of c2, alpha, beta, 32x32 receivers, "
+                        f"absorbing_2beta, Gaussian source, T={T} ({nsteps} RK4 steps), checkpoints every {every}",
+            "value": t_grad, "unit": "s/grad", "forward_s": t_fwd, "grad_over_forward": t_grad / t_fwd,
+            "misfit": J, "grad_norms": {k: float(np.linalg.norm(vv)) for k, vv in grad.items()},
+            "timing": "host clock around misfit_gradient (forward solve, misfit, reverse sweep with the parameter "
+                      "sensitivities, cell sums) and around one forward solve (Workspace.rk4_steps, host state)"}
+
+
 def main():
     global NMESH
     ap = argparse.ArgumentParser()
@@ -551,6 +610,8 @@ def main():
     ap.add_argument("--profile-only", action="store_true", help="only the main timed run (for ncu)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
     ap.add_argument("--batched-only", action="store_true", help="only the batched-form measurement")
+    ap.add_argument("--adjoint", action="store_true", help="only the adjoint-form measurement (one gradient)")
+    ap.add_argument("--adjoint-T", type=float, default=0.5, help="final time of the adjoint-form workload")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -18,6 +18,10 @@
 
 namespace wedg {
 
+// Threads per block of the per-element adjoint kernels: long serial work per thread, so small
+// blocks spread the elements of mid-size meshes over all SMs
+constexpr int ADJ_THREADS = 32;
+
 // Buffers of the adjoint kernels; every array in the state layout [e + E k] unless noted
 struct AdjIO {
   const double *mu;      // μ = M⁻¹ λ_v (NV²)
@@ -32,7 +36,7 @@ struct AdjIO {
 // whose scaled values are the weights of the slots A, D and F (src/rhs.jl:412-473 transposed:
 // Â = (2/h) w_i tr_v(μ), D̂ = (4/h²) w_i tr_dv(μ), F̂ = -w_i tr_du(ν)); and nus.
 template <int NU, int NV>
-__global__ void __launch_bounds__(128) k_adj_hats(const __grid_constant__ Basis<NU, NV> B,
+__global__ void __launch_bounds__(ADJ_THREADS) k_adj_hats(const __grid_constant__ Basis<NU, NV> B,
                                                    const __grid_constant__ Fields F, const AdjIO A) {
   constexpr int NQ = NU;
   const int E = F.E;
@@ -177,7 +181,7 @@ __device__ __forceinline__ void boundary_partials(const Fields &F, const TimeF &
 // derivatives are read off exactly from the values at zero and at unit traces.
 // On entry gu holds the volume transpose's b; on exit gu, gv hold Jᵀλ.
 template <int NU, int NV>
-__global__ void __launch_bounds__(128) k_adj_face(const __grid_constant__ Basis<NU, NV> B,
+__global__ void __launch_bounds__(ADJ_THREADS) k_adj_face(const __grid_constant__ Basis<NU, NV> B,
                                                    const __grid_constant__ Fields F,
                                                    const __grid_constant__ StageIO S, const AdjIO A) {
   constexpr int NQ = NU;
@@ -331,7 +335,7 @@ __device__ __forceinline__ void boundary_slots(const Fields &F, int s, double c2
 //            slots (the neighbour adds its own); on a physical side c², α, c = √c², β enter the
 //            own slots (central differences of relative step 1e-6).
 template <int NU, int NV>
-__global__ void __launch_bounds__(128) k_adj_param(const __grid_constant__ Basis<NU, NV> B,
+__global__ void __launch_bounds__(ADJ_THREADS) k_adj_param(const __grid_constant__ Basis<NU, NV> B,
                                                     const __grid_constant__ Fields F,
                                                     const __grid_constant__ StageIO S, const AdjIO A,
                                                     double *gc2, double *gal, double *gbe) {
@@ -343,25 +347,39 @@ __global__ void __launch_bounds__(128) k_adj_param(const __grid_constant__ Basis
   const int j = e % N, k = e / N;
   const size_t Eu = (size_t)E;
   const TimeF tf = time_factors(S);
-  auto U = [&](int a, int b) { return S.xu[e + Eu * (a + NU * b)]; };
-  auto V = [&](int a, int b) { return (a < NV && b < NV) ? S.xv[e + Eu * (a + NV * b)] : 0.0; };
-  auto MU = [&](int a, int b) { return (a < NV && b < NV) ? A.mu[e + Eu * (a + NV * b)] : 0.0; };
-  auto NUv = [&](int a, int b) { return A.nu[e + Eu * (a + NU * b)]; };
-  auto UT = [&](int a, int b) { return S.ut[e + Eu * (a + NU * b)]; };
   double dc2 = 0.0, dal = 0.0, dbe = 0.0;
-  // ---- volume and u-solve
-  for (int a = 0; a < NU; ++a)
-    for (int b = 0; b < NU; ++b) {
-      double ku = 0, kv = 0, kt = 0;
-      for (int c = 0; c < NU; ++c) {
-        ku += B.K1[a][c] * U(c, b) + U(a, c) * B.K1[c][b];
-        kv += B.K1[a][c] * V(c, b) + V(a, c) * B.K1[c][b];
-        kt += B.K1[a][c] * UT(c, b) + UT(a, c) * B.K1[c][b];
+  // ---- volume and u-solve: the element's blocks loaded once (V and μ padded to NU × NU)
+  {
+    double Ul[NU][NU], Vl[NU][NU], Ml[NU][NU], Nl[NU][NU], Tl[NU][NU];
+#pragma unroll
+    for (int b = 0; b < NU; ++b)
+#pragma unroll
+      for (int a = 0; a < NU; ++a) {
+        const size_t lu = e + Eu * (a + NU * b), lv = e + Eu * (a + NV * b);
+        const bool inv = a < NV && b < NV;
+        Ul[a][b] = S.xu[lu];
+        Nl[a][b] = A.nu[lu];
+        Tl[a][b] = S.ut[lu];
+        Vl[a][b] = inv ? S.xv[lv] : 0.0;
+        Ml[a][b] = inv ? A.mu[lv] : 0.0;
       }
-      const double m = MU(a, b), n = NUv(a, b);
-      dc2 += -F.four_hh * m * ku - n * kt + n * kv;   // R (v-block: μ is zero outside), u-solve, b
-      dal += -F.four_hh * m * kv;
-    }
+#pragma unroll 1
+    for (int a = 0; a < NU; ++a)
+#pragma unroll
+      for (int b = 0; b < NU; ++b) {
+        double ku = 0, kv = 0, kt = 0;
+#pragma unroll
+        for (int c = 0; c < NU; ++c) {
+          const double l = B.K1[a][c], r = B.K1[c][b];
+          ku = fma(l, Ul[c][b], fma(Ul[a][c], r, ku));
+          kv = fma(l, Vl[c][b], fma(Vl[a][c], r, kv));
+          kt = fma(l, Tl[c][b], fma(Tl[a][c], r, kt));
+        }
+        const double m = Ml[a][b], n = Nl[a][b];
+        dc2 += -F.four_hh * m * ku - n * kt + n * kv;   // R (v-block: μ is zero outside), u-solve, b
+        dal += -F.four_hh * m * kv;
+      }
+  }
   // ---- mass: Σ_points 2 W v_q vt_q μ_q (β constant on the element)
   {
     double Tv[QH][NV], Tt[QH][NV], Tm[QH][NV];

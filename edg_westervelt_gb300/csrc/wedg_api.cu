@@ -105,6 +105,11 @@ struct wedg_ws {
   int64_t rk_chk_n = 0, rk_seg_n = 0;
   double *rk_lam = nullptr, *rk_acc = nullptr, *rk_kbar = nullptr, *rk_g = nullptr, *rk_y = nullptr;
   double *rk_par = nullptr;   // per-element gradients with respect to c², α, β
+  // the forward run the next reverse sweep differentiates
+  bool rk_ready = false;
+  double rk_dt = 0;
+  int64_t rk_nsteps = 0, rk_every = 1;
+  std::vector<double> rk_t;
   // optional per-launch timing (events recorded around each stage kernel)
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -1120,19 +1125,15 @@ int wedg_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t, co
   return rc;
 }
 
-int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0, double dt, int64_t nsteps,
-                     int64_t every, const double *lam_u, const double *lam_v, double *gu, double *gv,
-                     double *g_c2, double *g_alpha, double *g_beta, const int64_t u_shape[4],
-                     const int64_t v_shape[4], int where) {
+int wedg_rk4_adjoint_forward(wedg_ws *ws, const double *u0, const double *v0, double t0, double dt, int64_t nsteps,
+                             int64_t every, double *uT, double *vT, const int64_t u_shape[4],
+                             const int64_t v_shape[4], int where) {
   if (!ws) return WEDG_ERR_ARGUMENT;
   ws->stats.kernel_launches = 0;
+  ws->rk_ready = false;
   int rc = check_shapes(ws, u_shape, v_shape);
   if (rc) return rc;
-  if (!u0 || !v0 || !lam_u || !lam_v || !gu || !gv) return argument_error(ws, "null pointer");
-  const bool params = g_c2 || g_alpha || g_beta;
-  if (params && !(g_c2 && g_alpha && g_beta)) return argument_error(ws, "give all three parameter gradients or none");
-  if (params && (!ws->fast || !ws->cfg.src_on || ws->cfg.mms_on))
-    return argument_error(ws, "parameter gradients need source mode and c², α, β constant on each element");
+  if (!u0 || !v0) return argument_error(ws, "null pointer");
   if (nsteps < 0 || every < 1) return argument_error(ws, "nsteps must be ≥ 0 and the checkpoint interval ≥ 1");
   if ((rc = adjoint_buffers(ws))) return rc;
   const size_t nU = (size_t)ws->E * ws->nu * ws->nu, nV = (size_t)ws->E * ws->nv * ws->nv, n = nU + nV;
@@ -1145,7 +1146,6 @@ int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0,
         (rc = dalloc(ws, &ws->rk_par, 3 * (size_t)ws->E)))
       return rc;
   }
-  if (params) CK(ws, cudaMemsetAsync(ws->rk_par, 0, sizeof(double) * 3 * ws->E, ws->stream));
   while (ws->rk_chk_n < nchk) {
     double *p;
     if ((rc = dalloc(ws, &p, n))) return rc;
@@ -1163,18 +1163,51 @@ int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0,
   double *yu = ws->rk_y, *yv = ws->rk_y + nU;
   CK(ws, cudaMemcpyAsync(yu, u0, sizeof(double) * nU, in, st));
   CK(ws, cudaMemcpyAsync(yv, v0, sizeof(double) * nV, in, st));
-  CK(ws, cudaMemcpyAsync(ws->rk_lam, lam_u, sizeof(double) * nU, in, st));
-  CK(ws, cudaMemcpyAsync(ws->rk_lam + nU, lam_v, sizeof(double) * nV, in, st));
-  std::vector<double> t(nsteps + 1);
-  t[0] = t0;
-  for (int64_t k = 0; k < nsteps; ++k) t[k + 1] = t[k] + dt;
+  ws->rk_t.assign(nsteps + 1, t0);
+  for (int64_t k = 0; k < nsteps; ++k) ws->rk_t[k + 1] = ws->rk_t[k] + dt;
   if ((rc = reset_flags(ws))) return rc;
-  // ---- forward pass: the checkpoints
   for (int64_t k = 0; k < nsteps; ++k) {
     if (k % every == 0) CK(ws, cudaMemcpyAsync(ws->rk_chk[k / every], ws->rk_y, sizeof(double) * n,
                                                cudaMemcpyDeviceToDevice, st));
-    if ((rc = enqueue_rk4(ws, yu, yv, t[k], dt, 1))) return rc;
+    if ((rc = enqueue_rk4(ws, yu, yv, ws->rk_t[k], dt, 1))) return rc;
   }
+  CK(ws, cudaGetLastError());
+  rc = collect(ws);
+  if (rc != WEDG_OK && rc != WEDG_WARN_CG_NOT_CONVERGED) return rc;
+  if (!ws->stats.finite) return argument_error(ws, "the forward run is not finite");
+  const cudaMemcpyKind out = where == WEDG_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if (uT) CK(ws, cudaMemcpy(uT, yu, sizeof(double) * nU, out));
+  if (vT) CK(ws, cudaMemcpy(vT, yv, sizeof(double) * nV, out));
+  ws->rk_dt = dt;
+  ws->rk_nsteps = nsteps;
+  ws->rk_every = every;
+  ws->rk_ready = true;
+  return rc;
+}
+
+int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam_v, double *gu, double *gv,
+                             double *g_c2, double *g_alpha, double *g_beta, int where) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  ws->stats.kernel_launches = 0;
+  if (!ws->rk_ready) return argument_error(ws, "no forward run with checkpoints (wedg_rk4_adjoint_forward) to reverse");
+  if (!lam_u || !lam_v || !gu || !gv) return argument_error(ws, "null pointer");
+  const bool params = g_c2 || g_alpha || g_beta;
+  if (params && !(g_c2 && g_alpha && g_beta)) return argument_error(ws, "give all three parameter gradients or none");
+  if (params && (!ws->fast || !ws->cfg.src_on || ws->cfg.mms_on))
+    return argument_error(ws, "parameter gradients need source mode and c², α, β constant on each element");
+  int rc;
+  const size_t nU = (size_t)ws->E * ws->nu * ws->nu, nV = (size_t)ws->E * ws->nv * ws->nv, n = nU + nV;
+  const int64_t nsteps = ws->rk_nsteps, every = ws->rk_every;
+  const int64_t nchk = nsteps ? (nsteps + every - 1) / every : 0;
+  const double dt = ws->rk_dt;
+  const std::vector<double> &t = ws->rk_t;
+  cudaStream_t st = ws->stream;
+  double *yu = ws->rk_y, *yv = ws->rk_y + nU;
+  const cudaMemcpyKind in = where == WEDG_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  CK(ws, cudaMemcpyAsync(ws->rk_lam, lam_u, sizeof(double) * nU, in, st));
+  CK(ws, cudaMemcpyAsync(ws->rk_lam + nU, lam_v, sizeof(double) * nV, in, st));
+  if (params) CK(ws, cudaMemsetAsync(ws->rk_par, 0, sizeof(double) * 3 * ws->E, st));
+  if ((rc = reset_flags(ws))) return rc;
   const int lb = 256, lg = (int)std::min<size_t>((n + lb - 1) / lb, 152 * 16);
   auto lin = [&](double *out, double a, const double *x, double b, const double *y, const double *z) {
     k_lincomb<<<lg, lb, 0, st>>>(n, out, a, x, b, y, z);
@@ -1227,6 +1260,17 @@ int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0,
     CK(ws, cudaMemcpy(g_beta, ws->rk_par + 2 * ws->E, sizeof(double) * ws->E, out));
   }
   return rc;
+}
+
+int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0, double dt, int64_t nsteps,
+                     int64_t every, const double *lam_u, const double *lam_v, double *gu, double *gv,
+                     double *g_c2, double *g_alpha, double *g_beta, const int64_t u_shape[4],
+                     const int64_t v_shape[4], int where) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  if (!lam_u || !lam_v || !gu || !gv) return argument_error(ws, "null pointer");
+  int rc = wedg_rk4_adjoint_forward(ws, u0, v0, t0, dt, nsteps, every, nullptr, nullptr, u_shape, v_shape, where);
+  if (rc != WEDG_OK && rc != WEDG_WARN_CG_NOT_CONVERGED) return rc;
+  return wedg_rk4_adjoint_reverse(ws, lam_u, lam_v, gu, gv, g_c2, g_alpha, g_beta, where);
 }
 
 int wedg_rk4_step(wedg_ws *ws, double *u, double *v, double t, double dt, const int64_t u_shape[4],

@@ -92,7 +92,8 @@ void launch_mass(const void *basis, const Fields &F, const StageIO &S, int block
 // The adjoint kernels (wedg_adjoint.cuh): element grids of 128 threads, the mass term on the team grid
 template <int NU, int NV>
 void launch_adj_hats(const void *basis, const Fields &F, const StageIO &, const AdjIO &A, cudaStream_t st) {
-  k_adj_hats<NU, NV><<<(F.E + 127) / 128, 128, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, A);
+  k_adj_hats<NU, NV><<<(F.E + ADJ_THREADS - 1) / ADJ_THREADS, ADJ_THREADS, 0, st>>>(
+      *static_cast<const Basis<NU, NV> *>(basis), F, A);
 }
 template <int NU, int NV>
 void launch_adj_mass(const void *basis, const Fields &F, const StageIO &, const AdjIO &A, cudaStream_t st) {
@@ -102,14 +103,15 @@ void launch_adj_mass(const void *basis, const Fields &F, const StageIO &, const 
 }
 template <int NU, int NV>
 void launch_adj_face(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, cudaStream_t st) {
-  k_adj_face<NU, NV><<<(F.E + 127) / 128, 128, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S, A);
+  k_adj_face<NU, NV><<<(F.E + ADJ_THREADS - 1) / ADJ_THREADS, ADJ_THREADS, 0, st>>>(
+      *static_cast<const Basis<NU, NV> *>(basis), F, S, A);
 }
 
 template <int NU, int NV>
 void launch_adj_param(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, double *gc2, double *gal,
                       double *gbe, cudaStream_t st) {
-  k_adj_param<NU, NV><<<(F.E + 127) / 128, 128, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S, A, gc2,
-                                                         gal, gbe);
+  k_adj_param<NU, NV><<<(F.E + ADJ_THREADS - 1) / ADJ_THREADS, ADJ_THREADS, 0, st>>>(
+      *static_cast<const Basis<NU, NV> *>(basis), F, S, A, gc2, gal, gbe);
 }
 
 template <int NU, int NV>

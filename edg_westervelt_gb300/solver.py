@@ -178,7 +178,8 @@ def misfit_gradient(q, N, T, c2, alpha, beta, receivers, u_obs, *, dt_fac=10, ev
     of the grid of the (m, n) arrays c2, alpha, beta (every cell a block of N/m × N/n elements).
     Returns (J, dict(c2=..., alpha=..., beta=...)) with gradients of the cells' shape. The forward
     run, the misfit and the final-time adjoint λ_u = Σ_r (u_h(x_r) - u_obs_r) ∂u_h(x_r)/∂U are
-    computed here, the reverse sweep by wedg_rk4_adjoint (checkpoints every `every` steps)."""
+    computed here; the forward run (keeping checkpoints every `every` steps) and the reverse
+    sweep are wedg_rk4_adjoint_forward and wedg_rk4_adjoint_reverse."""
     c2 = np.asarray(c2, dtype=np.float64)
     m, n = c2.shape
     if N % m or N % n:
@@ -190,9 +191,9 @@ def misfit_gradient(q, N, T, c2, alpha, beta, receivers, u_obs, *, dt_fac=10, ev
     nsteps = int(round(T / dt))
     dt = T / nsteps
     ws = Workspace(pre, N)
-    u = np.zeros((N, N, nu, nu), order="F")
-    v = np.zeros((N, N, nv, nv), order="F")
-    ws.rk4_steps(u, v, 0.0, dt, nsteps)
+    u0 = np.zeros((N, N, nu, nu), order="F")
+    v0 = np.zeros((N, N, nv, nv), order="F")
+    u, v = ws.rk4_adjoint_forward(u0, v0, 0.0, dt, nsteps, every=every)
     lam_u = np.zeros_like(u)
     J = 0.0
     for (xr, yr), obs in zip(receivers, u_obs):
@@ -202,8 +203,7 @@ def misfit_gradient(q, N, T, c2, alpha, beta, receivers, u_obs, *, dt_fac=10, ev
         res = float(py @ u[jr - 1, kr - 1] @ px) - obs
         J += 0.5 * res * res
         lam_u[jr - 1, kr - 1] += res * np.outer(py, px)
-    zu, zv = np.zeros_like(u), np.zeros_like(v)
-    _, _, gc2, gal, gbe = ws.rk4_adjoint(zu, zv, 0.0, dt, nsteps, lam_u, np.zeros_like(v), every=every, params=True)
+    _, _, gc2, gal, gbe = ws.rk4_adjoint_reverse(lam_u, np.zeros_like(v), params=True)
     # element (j, k) lies in cell (j // (N/m), k // (N/n))
     cells = lambda g: g.reshape(m, N // m, n, N // n).sum(axis=(1, 3))
     return J, dict(c2=cells(gc2), alpha=cells(gal), beta=cells(gbe))

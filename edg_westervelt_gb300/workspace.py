@@ -230,6 +230,36 @@ class Workspace:
         self._check(rc)
         return (gu, gv, *gp) if params else (gu, gv)
 
+    def rk4_adjoint_forward(self, u0, v0, t0, dt, nsteps, every=32):
+        """wedg_rk4_adjoint_forward: the forward run of a reverse sweep, checkpoints kept in the
+        workspace; returns the final state (new arrays)."""
+        self._refuse_mismatch()
+        N, nu, nv = self.N, self.nu, self.nv
+        u0, v0 = _f64(u0), _f64(v0)
+        uT = np.zeros((N, N, nu, nu), order="F")
+        vT = np.zeros((N, N, nv, nv), order="F")
+        rc = L.lib().wedg_rk4_adjoint_forward(self._h, _ptr(u0), _ptr(v0), float(t0), float(dt), int(nsteps),
+                                              int(every), _ptr(uT), _ptr(vT), _shape(u0, nu, N), _shape(v0, nv, N),
+                                              L.WEDG_HOST)
+        self._check(rc)
+        return uT, vT
+
+    def rk4_adjoint_reverse(self, lam_u, lam_v, params=False):
+        """wedg_rk4_adjoint_reverse: the reverse sweep of the last rk4_adjoint_forward for the
+        final-time adjoint (λ_u, λ_v); returns (gu, gv) and, with params, the per-element
+        gradients with respect to c², α, β."""
+        N, nu, nv = self.N, self.nu, self.nv
+        lam_u, lam_v = _f64(lam_u), _f64(lam_v)
+        gu = np.zeros((N, N, nu, nu), order="F")
+        gv = np.zeros((N, N, nv, nv), order="F")
+        gp = [np.zeros((N, N), order="F") for _ in range(3)] if params else None
+        null = ctypes.POINTER(ctypes.c_double)()
+        pc = [_ptr(g) for g in gp] if params else [null, null, null]
+        rc = L.lib().wedg_rk4_adjoint_reverse(self._h, _ptr(lam_u), _ptr(lam_v), _ptr(gu), _ptr(gv), pc[0], pc[1],
+                                              pc[2], L.WEDG_HOST)
+        self._check(rc)
+        return (gu, gv, *gp) if params else (gu, gv)
+
     def rk4_steps(self, u, v, t0, dt, nsteps, stop_nonfinite=False):
         """nsteps RK4 steps in place from t0 (t advancing by repeated addition of dt).
         Returns the number of steps completed; sets self.fin."""

@@ -209,6 +209,17 @@ int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0,
                      double *g_c2, double *g_alpha, double *g_beta, const int64_t u_shape[4],
                      const int64_t v_shape[4], int where);
 
+/* The two halves of wedg_rk4_adjoint, for a final-time adjoint that depends on the final
+ * state (a misfit): wedg_rk4_adjoint_forward runs the nsteps steps from (u0, v0), keeps the
+ * checkpoints in the workspace and returns the final state (uT, vT; either may be NULL);
+ * wedg_rk4_adjoint_reverse then takes (λ_u, λ_v) at T and returns the gradients as
+ * wedg_rk4_adjoint does. A reverse sweep needs a preceding forward run on the same workspace. */
+int wedg_rk4_adjoint_forward(wedg_ws *ws, const double *u0, const double *v0, double t0, double dt, int64_t nsteps,
+                             int64_t every, double *uT, double *vT, const int64_t u_shape[4],
+                             const int64_t v_shape[4], int where);
+int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam_v, double *gu, double *gv,
+                             double *g_c2, double *g_alpha, double *g_beta, int where);
+
 /* Batched form: many independent instances -- workspaces made by wedg_create, each with its
  * own N, degrees, flux, boundary kinds and coefficients -- advanced together. No counterpart in
  * the reference, whose batching is the caller's loop over instances. One RK4 step of every
