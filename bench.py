@@ -371,9 +371,10 @@ def run_ours(args):
                "h2d_bytes_per_step": int(uh.nbytes + vh.nbytes), "d2h_bytes_per_step": int(uh.nbytes + vh.nbytes),
                "steps": ke, "api": "Workspace.rk4_steps (wedg_rk4_steps, WEDG_HOST)"}
 
-    batched = None
+    batched = config3 = None
     if world == 1 and not args.no_batched:
         batched = run_batched(torch, dev, max(4, 2 * args.steps), args.warmup)
+        config3 = run_config3(torch, dev, args.steps, args.warmup)
 
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
@@ -439,6 +440,7 @@ def run_ours(args):
         "clocks": clocks.summary(), "gpu_launches": main["launches"],
         "kernel_ms": kms,
         "batched": batched,
+        "config3": config3,
         "zero_state": {"value": world * dof * 4 * zero["steps"] / (zero["ms"] / 1e3),
                        "ms_per_step": zero["ms"] / max(zero["steps"], 1), "cheb_steps_max": zero["cheb"],
                        "stage_ms": zero["prep_ms"] + zero["stage_ms"] + zero["mass_ms"]},
@@ -538,6 +540,75 @@ def run_batched(torch, dev, steps, warmup):
             "timing": "host clock around each call (each call returns synchronised); states resident on the GPU",
             "batched": "Batch.rk4_steps: one CUDA graph of one RK4 step of every instance, replayed per step",
             "plain_loop": "Workspace.rk4_steps for each instance in turn"}
+
+
+def device_steps_ms(torch, ws, u, v, t0, dt, steps, warmup):
+    """Milliseconds of `steps` RK4 steps on device-resident states after `warmup` untimed ones (CUDA
+    events on the workspace's stream around wedg_rk4_steps_async)."""
+    import ctypes
+    from edg_westervelt_gb300 import _lib as L
+    lib = L.lib()
+    up, vp = ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(v.data_ptr())
+    ext = torch.cuda.ExternalStream(ws.stream, device=u.device)
+    rc = lib.wedg_rk4_steps_async(ws._h, up, vp, t0, dt, warmup)
+    ws._check(lib.wedg_sync_status(ws._h, None, None) if rc == 0 else rc)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(ext):
+        e0.record(ext)
+    rc = lib.wedg_rk4_steps_async(ws._h, up, vp, t0 + warmup * dt, dt, steps)
+    with torch.cuda.stream(ext):
+        e1.record(ext)
+    ws._check(lib.wedg_sync_status(ws._h, None, None) if rc == 0 else rc)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_config3(torch, dev, steps, warmup):
+    """Plain method with jumping coefficients, initial-value mode: N = 256, q_u = 5, q_v = 4, c, α, β
+    constant on 4 × 4 subsquares from default_rng(3) (c ~ U[0.5, 2], α log-uniform on [1e-6, 1e-3],
+    β ~ U[0, 10]), initial displacement a sum of 3 seeded Gaussians (centres U[0.2, 0.8]², widths
+    U[0.03, 0.08], amplitudes U[-1, 1] scaled to 1e-3 so that 1 - 2βv stays positive), sides
+    dirichlet / absorbing / absorbing_2beta / wall (bot, top, lft, rgt), central flux, one-sided faces,
+    dt = h / (10 max c q_u²). From the reference's zero start; DOF·stage/s over the timed steps."""
+    import edg_westervelt_gb300 as W
+    rng = np.random.default_rng(3)
+    q, N = 5, 256
+    c = rng.uniform(0.5, 2.0, (4, 4))
+    al = 10.0 ** rng.uniform(-6, -3, (4, 4))
+    be = rng.uniform(0.0, 10.0, (4, 4))
+    cen = rng.uniform(0.2, 0.8, (3, 2))
+    wid = rng.uniform(0.03, 0.08, 3)
+    amp = 1e-3 * rng.uniform(-1.0, 1.0, 3)
+
+    def gauss(d):
+        def f(x, y):
+            x = np.asarray(x, dtype=float)
+            y = np.asarray(y, dtype=float)
+            out = np.zeros(np.broadcast(x, y).shape)
+            for (x0, y0), w, a in zip(cen, wid, amp):
+                X, Y = x - x0, y - y0
+                gv = a * np.exp(-(X * X + Y * Y) / (w * w))
+                out = out + {"": gv, "x": -2 * X / w ** 2 * gv, "y": -2 * Y / w ** 2 * gv,
+                             "xx": (4 * X * X / w ** 4 - 2 / w ** 2) * gv, "yy": (4 * Y * Y / w ** 4 - 2 / w ** 2) * gv}[d]
+            return out
+        return f
+    prof = dict(u0=gauss(""), u0_x=gauss("x"), u0_y=gauss("y"), u0_xx=gauss("xx"), u0_yy=gauss("yy"))
+    co = W.piecewise_coefficients(c ** 2, al, be)
+    pre, _ = W.precompute(q, N, mixed=True, mode="initial_value", flux="central", coefficients=co,
+                          initial_profile=prof, kappa=0.5,
+                          boundary=dict(bot="dirichlet", top="absorbing", lft="absorbing_2beta", rgt="wall"))
+    ws = W.Workspace(pre, N)
+    nu, nv = pre["qu1"], pre["qv1"]
+    u = torch.zeros(N * N * nu * nu, dtype=torch.float64, device=dev)
+    v = torch.zeros(N * N * nv * nv, dtype=torch.float64, device=dev)
+    dt = (1.0 / N) / (10.0 * float(c.max()) * q * q)
+    ms = device_steps_ms(torch, ws, u, v, 0.0, dt, steps, warmup)
+    dof = N * N * (nu * nu + nv * nv)
+    return {"workload": "plain method, jumping coefficients: N=256 q_u=5 q_v=4, initial-value mode, central flux, "
+                        "4x4 subsquares of c, alpha, beta (default_rng(3)), mixed boundary kinds",
+            "value": dof * 4 * steps / (ms / 1e3), "unit": "DOF·stage/s", "ms_per_step": ms / steps, "steps": steps,
+            "dof": dof, "one_sided": bool(pre["one_sided"]), "fast_path": bool(ws.stats()["fast_path"])}
 
 
 def run_adjoint(torch, T, every=32):
