@@ -14,6 +14,9 @@
 //   k_adj_mass   + P_hᵀ (2βW ∘ vt_q ∘ μ_q) P_h, the derivative of M(v) acting on vt
 //   k_adj_face   the slots' derivatives with respect to the element's own traces (its own slots
 //                and the neighbour's on the shared face), then the trace transposes.
+// The slots of an interior face point are affine in its six traces and, on one-sided faces, the
+// jump of the traces enters through the four one-sided coefficients only: their derivatives
+// are closed forms in the face coefficients and the slot weights (face_weights below).
 #pragma once
 
 namespace wedg {
@@ -30,7 +33,30 @@ struct AdjIO {
   const double *vt;      // the forward vt at this state
   double *hat;           // slot weights, [((fam·4 + side)·NQ + i) E + e], fam A, D, F (unscaled)
   double *gu, *gv;       // the gradient; gu holds the volume's b on entry to k_adj_face
+  const double *xv;      // the state's V (for the β-derivative of the mass matrix)
+  double *gbe;           // per-element β-gradient that k_adj_mass adds to, or null
 };
+
+// The weighted slot sums of an interior face point, from the scaled slot weights of the "+"
+// element (hP: A, D, F) and of the "-" element (hM), with c² and α of both sides (a continuous
+// face has c2m = c2p, afm = afp). With J, G, pen, sj of interior_flux,
+//   Σ slots·weights = (pen sj - G)(hP_A - hM_A) + dvsp wP + dvsm wM,
+//   wP = c2p hP_F - afp hP_D,  wM = afm hM_D - c2m hM_F,
+//   dvsp = θ sj - τ J,  dvsm = -(1 - θ) sj - τ J,
+// so a derivative of the sum is ∂(pen sj - G) wA - ∂J τ (wP + wM) plus the coefficients'
+// direct terms.
+struct FaceWeights {
+  double wA, wP, wM, wS;  // wS = τ (wP + wM)
+};
+__device__ __forceinline__ FaceWeights face_weights(const Fields &F, const FaceCoef &c, double hPA, double hPD,
+                                                    double hPF, double hMA, double hMD, double hMF) {
+  FaceWeights w;
+  w.wA = hPA - hMA;
+  w.wP = c.c2p * hPF - c.afp * hPD;
+  w.wM = c.afm * hMD - c.c2m * hMF;
+  w.wS = F.tau * (w.wP + w.wM);
+  return w;
+}
 
 // k_adj_hats: the traces of μ (values and derivatives) and of ν (derivatives) on the four sides,
 // whose scaled values are the weights of the slots A, D and F (src/rhs.jl:412-473 transposed:
@@ -61,7 +87,8 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_hats(const __grid_constant_
 
 // k_adj_mass: gv += P_hᵀ (2βW ∘ vt_q ∘ μ_q) P_h on every element, by the team layout of the mass
 // solves: each unit forms the weights 2β vt_q of its two point rows (into G, which the forward
-// solve of this state no longer needs) and applies them to μ with team_K.
+// solve of this state no longer needs) and applies them to μ with team_K. With A.gbe, also the
+// β-derivative of μ·M(v) vt for β constant on the element, gbe[e] += Σ_q 2 W_q v_q vt_q μ_q.
 template <int NU, int NV>
 __global__ void __launch_bounds__(CHEB_THREADS, 3)
     k_adj_mass(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F, const AdjIO A) {
@@ -83,13 +110,13 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
   const unsigned tmask = tp.mask;
   const size_t Eu = (size_t)F.E;
   double *xs = sh + tp.slot * T::SLOT, *zs = xs + NE, *zd = zs + U * NV;
+  double db = 0.0;                                      // Σ over the unit's points of w v_q vt_q μ_q
   {
     const int r1 = u, r2 = QH - 1 - u;
-    auto vx = [&](int a, int b) { return A.vt[e + Eu * (a + NV * b)]; };
+    auto tx = [&](int a, int b) { return A.vt[e + Eu * (a + NV * b)]; };
     double Tp[NV], Tm[NV];
-    ph_row_pair<QH, NV>(B.Ph, r1, vx, Tp, Tm);
-    auto gput = [&](const double (&Tv)[NV], int r) {
-      double Y[QH];
+    ph_row_pair<QH, NV>(B.Ph, r1, tx, Tp, Tm);
+    auto gput = [&](const double (&Tv)[NV], int r, double (&Y)[QH]) {
       ph_to_points<QH, NV>(B.Ph, Tv, Y);
 #pragma unroll
       for (int s2 = 0; s2 < QH; ++s2) {
@@ -97,8 +124,31 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
         F.G[gi] = Y[s2] * F.beta2[gi];
       }
     };
-    gput(Tp, r1);
-    if (r2 != r1) gput(Tm, r2);
+    double Yp[QH], Ym[QH];
+    gput(Tp, r1, Yp);
+    if (r2 != r1) gput(Tm, r2, Ym);
+    if (A.gbe) {
+      auto vx = [&](int a, int b) { return A.xv[e + Eu * (a + NV * b)]; };
+      auto mx = [&](int a, int b) { return A.mu[e + Eu * (a + NV * b)]; };
+      double Vp[NV], Vm[NV], Mp[NV], Mm[NV];
+      ph_row_pair<QH, NV>(B.Ph, r1, vx, Vp, Vm);
+      ph_row_pair<QH, NV>(B.Ph, r1, mx, Mp, Mm);
+      auto row = [&](const double (&Y)[QH], const double (&Tv)[NV], const double (&Tmu)[NV]) {
+        double Yv[QH], Yu[QH];
+        ph_to_points<QH, NV>(B.Ph, Tv, Yv);
+        ph_to_points<QH, NV>(B.Ph, Tmu, Yu);
+        double r = 0.0;
+#pragma unroll
+        for (int s2 = 0; s2 < QH; ++s2) r = fma(B.wh[s2], Y[s2] * Yv[s2] * Yu[s2], r);
+        return r;
+      };
+      db = B.wh[r1] * row(Yp, Vp, Mp);
+      if (r2 != r1) db = fma(B.wh[r2], row(Ym, Vm, Mm), db);
+    }
+  }
+  if (A.gbe) {
+    db = team_sum<U>(db, tmask);
+    if (u == 0) A.gbe[e] += 2.0 * db;
   }
   double acc[J];
 #pragma unroll
@@ -177,8 +227,8 @@ __device__ __forceinline__ void boundary_partials(const Fields &F, const TimeF &
 // k_adj_face: the trace weights of the element, t̂_x(s, i) = Σ_slots ∂slot/∂x · ŝlot over the
 // element's own slots and (interior faces) the neighbour's slots of the shared point, for its
 // traces x = du, v, dv; then the trace transposes (k_prep's trace4 transposed) into gu, gv.
-// The interior slots are affine in the six traces of the face point (interior_flux), so their
-// derivatives are read off exactly from the values at zero and at unit traces.
+// The interior slots are affine in the six traces of the face point (interior_flux); their
+// derivatives are the closed forms of face_weights.
 // On entry gu holds the volume transpose's b; on exit gu, gv hold Jᵀλ.
 template <int NU, int NV>
 __global__ void __launch_bounds__(ADJ_THREADS) k_adj_face(const __grid_constant__ Basis<NU, NV> B,
@@ -238,24 +288,20 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_face(const __grid_constant_
           fi = j + (size_t)N * ((s == 2 ? k : k + 1) + (size_t)(N + 1) * i);
           c2p_a = F.vc2; afp_a = F.vaf; c2m_a = F.vc2m; afm_a = F.vafm; jc_a = F.vJC;
         }
-        const FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);
-        const double ho[3] = {hat(0, s, i, e), hat(1, s, i, e), hat(2, s, i, e)};
-        const double hn[3] = {hat(0, sn, i, nb), hat(1, sn, i, nb), hat(2, sn, i, nb)};
-        // own traces in the order (dum, dup, vm, vp, dvm, dvp): du, v, dv of the own side
-        const int own[3] = {plus ? 1 : 0, plus ? 3 : 2, plus ? 5 : 4};
-        double z[3][2];                                 // slots at zero traces: own role, neighbour role
-        interior_flux(F, cf, plus, 0, 0, 0, 0, 0, 0, z[0][0], z[1][0], z[2][0]);
-        interior_flux(F, cf, !plus, 0, 0, 0, 0, 0, 0, z[0][1], z[1][1], z[2][1]);
-#pragma unroll
-        for (int x = 0; x < 3; ++x) {
-          double in[6] = {0, 0, 0, 0, 0, 0};
-          in[own[x]] = 1.0;
-          double Ao, Do, Fo, An, Dn, Fn;
-          interior_flux(F, cf, plus, in[0], in[1], in[2], in[3], in[4], in[5], Ao, Do, Fo);
-          interior_flux(F, cf, !plus, in[0], in[1], in[2], in[3], in[4], in[5], An, Dn, Fn);
-          t[x] = (Ao - z[0][0]) * ho[0] + (Do - z[1][0]) * ho[1] + (Fo - z[2][0]) * ho[2] +
-                 (An - z[0][1]) * hn[0] + (Dn - z[1][1]) * hn[1] + (Fn - z[2][1]) * hn[2];
-        }
+        FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);
+        if (!F.one_sided) { cf.c2m = cf.c2p; cf.afm = cf.afp; }
+        const double ho0 = hat(0, s, i, e), ho1 = hat(1, s, i, e), ho2 = hat(2, s, i, e);
+        const double hn0 = hat(0, sn, i, nb), hn1 = hat(1, sn, i, nb), hn2 = hat(2, sn, i, nb);
+        const FaceWeights w = plus ? face_weights(F, cf, ho0, ho1, ho2, hn0, hn1, hn2)
+                                   : face_weights(F, cf, hn0, hn1, hn2, ho0, ho1, ho2);
+        const double th = F.theta, a = F.two_h;
+        const double pen = 0.5 * (cf.c2m + cf.c2p) * F.lu + 0.5 * (cf.afm + cf.afp) * F.lv;
+        const double tv = pen * w.wA + th * w.wP - (1.0 - th) * w.wM;   // ∂/∂vm; ∂/∂vp = -tv
+        // ∂/∂du of the own side: ∂J = ∓a c², ∂G = a θ c² (+) or a (1 - θ) c² (-); dv with α
+        const double kd = plus ? w.wS - th * w.wA : -((1.0 - th) * w.wA + w.wS);
+        t[0] = a * (plus ? cf.c2p : cf.c2m) * kd;
+        t[1] = plus ? -tv : tv;
+        t[2] = a * (plus ? cf.afp : cf.afm) * kd;
       }
 #pragma unroll
       for (int b = 0; b < NU; ++b) {
@@ -296,50 +342,66 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_face(const __grid_constant_
     for (int a = 0; a < NV; ++a) A.gv[e + Eu * (a + NV * b)] = gV[a][b];
 }
 
-// The slots of a physical side point as functions of the coefficients there (side_point's
-// formulas with c², α, c, β as arguments), for their derivatives in k_adj_param
-__device__ __forceinline__ void boundary_slots(const Fields &F, int s, double c2f, double af, double cf, double bf,
-                                               double v_fp, double gun, double gvn, double gu_ex, double gv_ex,
-                                               double v_ex, double sgn, double (&q)[3]) {
-  double F1, dv;
+// Derivatives of the weighted slots r = F1 h0 + q_D h1 + q_F h2 of a physical side point with
+// respect to the coefficients c², α, c, β there (side_point's formulas differentiated; the
+// traces and the data fixed): d[0..3]. With q_D = sgn α dv and q_F = -sgn c² dv,
+//   r = F1 h0 + dv · sgn (α h1 - c² h2).
+__device__ __forceinline__ void boundary_coef_partials(const Fields &F, int s, double c2f, double af, double cf,
+                                                       double bf, double v_fp, double gun, double gvn,
+                                                       double gu_ex, double gv_ex, double v_ex, double sgn,
+                                                       double h0, double h1, double h2, double (&d)[4]) {
+  double dF1[4], ddv[4], dv;
   if (F.kind[s] == 3) {
-    const double g2 = c2f * gu_ex + af * gv_ex;
-    const double rho_w = c2f * gun + af * gvn - g2;
-    dv = -(F.kap[s] / cf) * rho_w;
-    F1 = g2;
+    // wall: F1 = c² gu_ex + α gv_ex, dv = -(κ/c)(c² (gun - gu_ex) + α (gvn - gv_ex))
+    const double kc = F.kap[s] / cf, ru = gun - gu_ex, rv = gvn - gv_ex;
+    const double rw = c2f * ru + af * rv;
+    dv = -kc * rw;
+    dF1[0] = gu_ex; dF1[1] = gv_ex; dF1[2] = 0.0; dF1[3] = 0.0;
+    ddv[0] = -kc * ru; ddv[1] = -kc * rv; ddv[2] = kc * rw / cf; ddv[3] = 0.0;
   } else {
+    // absorbing family: ρ = η (c² (gun - gu_ex) + α (gvn - gv_ex)) + γ c (√(1 - kβv) v - √(1 - kβv_ex) v_ex),
+    // F1 = c² gun + α gvn - (η + σγ) ρ, dv = -(γ - ση) ρ / (c √(1 - kβv))
     const double g = F.gam[s], et = F.eta[s], sg = F.sig[s], kb = F.kb[s];
-    const double sqf = sqrt(1.0 - kb * bf * v_fp);
-    const double rho_num = et * (c2f * gun + af * gvn) + g * cf * sqf * v_fp;
-    const double rho_ex = et * (c2f * gu_ex + af * gv_ex) + g * cf * sqrt(1.0 - kb * bf * v_ex) * v_ex;
-    const double rho = rho_num - rho_ex;
-    F1 = c2f * gun + af * gvn - (et + sg * g) * rho;
-    dv = -(g - sg * et) / (cf * sqf) * rho;
+    const double sqf = sqrt(1.0 - kb * bf * v_fp), sqe = sqrt(1.0 - kb * bf * v_ex);
+    const double dsqf = -kb * v_fp / (2.0 * sqf), dsqe = -kb * v_ex / (2.0 * sqe);   // ∂/∂β
+    const double ru = gun - gu_ex, rv = gvn - gv_ex, rs = sqf * v_fp - sqe * v_ex;
+    const double rho = et * (c2f * ru + af * rv) + g * cf * rs;
+    const double drho[4] = {et * ru, et * rv, g * rs, g * cf * (v_fp * dsqf - v_ex * dsqe)};
+    const double es = et + sg * g, kd = -(g - sg * et), den = cf * sqf;
+    dF1[0] = gun - es * drho[0]; dF1[1] = gvn - es * drho[1]; dF1[2] = -es * drho[2]; dF1[3] = -es * drho[3];
+    dv = kd * rho / den;
+    ddv[0] = kd * drho[0] / den;
+    ddv[1] = kd * drho[1] / den;
+    ddv[2] = kd * (drho[2] / den - rho / (cf * den));
+    ddv[3] = kd * (drho[3] / den - rho * dsqf / (sqf * den));
   }
-  q[0] = F1;
-  q[1] = sgn * (af * dv);
-  q[2] = -sgn * (c2f * dv);
+  const double m = sgn * (af * h1 - c2f * h2);
+  d[0] = fma(dF1[0], h0, fma(ddv[0], m, -sgn * dv * h2));
+  d[1] = fma(dF1[1], h0, fma(ddv[1], m, sgn * dv * h1));
+  d[2] = fma(dF1[2], h0, ddv[2] * m);
+  d[3] = fma(dF1[3], h0, ddv[3] * m);
 }
 
 // k_adj_param: for the constant-coefficient kernels (c², α, β constant on each element), the
-// derivative of the stage's weighted output K̄·F(Y) with respect to the element's c², α and β,
-// added to gc2[e], gal[e], gbe[e]. With μ = M⁻¹K̄_v, ν = A_e⁻¹K̄_u and the forward outputs ut, vt
-// at Y (all from the adjoint evaluation just made at Y):
-//   volume   μ·∂R/∂p + ν·∂b/∂p   (R ∋ -(4/h²)(c²(K1U + UK1) + α(K1V + VK1)), b ∋ c²(K1V + VK1))
-//   u-solve  -ν·(∂A_e/∂c²) ut = -ν·(K1 ut + ut K1)
-//   mass     μ·(∂K/∂β) vt = Σ_points 2 W v_q vt_q μ_q
-//   faces    the slots' derivatives times their weights (the hats): at an interior point of a
-//            one-sided face, the element's own coefficient enters its own slots and the
-//            neighbour's (each slot is quadratic in one coefficient, so a central difference
-//            of step |c| is exact); at a continuous face the shared face value enters the own
-//            slots (the neighbour adds its own); on a physical side c², α, c = √c², β enter the
-//            own slots (central differences of relative step 1e-6).
+// derivative of the stage's weighted output K̄·F(Y) with respect to the element's c² and α
+// (and β through the faces), added to gc2[e], gal[e], gbe[e]; k_adj_mass adds the β-derivative
+// of the mass matrix. With μ = M⁻¹K̄_v, ν = A_e⁻¹K̄_u and the forward ut at Y (all from the
+// adjoint evaluation just made at Y), K1 symmetric:
+//   volume + u-solve   ∂/∂c² = <A1, V - ut> - (4/h²) <A2, U>,  ∂/∂α = -(4/h²) <A2, V>,
+//                      A1 = K1 ν + ν K1,  A2 = K1 μ + μ K1
+//                      (R ∋ -(4/h²)(c²(K1U + UK1) + α(K1V + VK1)), b ∋ c²(K1V + VK1),
+//                       ∂A_e/∂c² ut = K1 ut + ut K1)
+//   faces              the slots' derivatives times their weights: at an interior point of a
+//                      one-sided face the element's own one-sided coefficients enter its own
+//                      slots and the neighbour's; at a continuous face the shared face value
+//                      enters the own slots (the neighbour adds its own); on a physical side
+//                      c², α, c = √c², β enter the own slots.
 template <int NU, int NV>
 __global__ void __launch_bounds__(ADJ_THREADS) k_adj_param(const __grid_constant__ Basis<NU, NV> B,
                                                     const __grid_constant__ Fields F,
                                                     const __grid_constant__ StageIO S, const AdjIO A,
                                                     double *gc2, double *gal, double *gbe) {
-  constexpr int NQ = NU, QH = Basis<NU, NV>::QH;
+  constexpr int NQ = NU;
   const int E = F.E, N = F.N;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
@@ -348,56 +410,35 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_param(const __grid_constant
   const size_t Eu = (size_t)E;
   const TimeF tf = time_factors(S);
   double dc2 = 0.0, dal = 0.0, dbe = 0.0;
-  // ---- volume and u-solve: the element's blocks loaded once (V and μ padded to NU × NU)
+  // ---- volume and u-solve: ν and μ (padded to NU × NU) in registers, U, V, ut streamed
   {
-    double Ul[NU][NU], Vl[NU][NU], Ml[NU][NU], Nl[NU][NU], Tl[NU][NU];
+    double Nl[NU][NU], Ml[NU][NU];
 #pragma unroll
     for (int b = 0; b < NU; ++b)
 #pragma unroll
       for (int a = 0; a < NU; ++a) {
-        const size_t lu = e + Eu * (a + NU * b), lv = e + Eu * (a + NV * b);
-        const bool inv = a < NV && b < NV;
-        Ul[a][b] = S.xu[lu];
-        Nl[a][b] = A.nu[lu];
-        Tl[a][b] = S.ut[lu];
-        Vl[a][b] = inv ? S.xv[lv] : 0.0;
-        Ml[a][b] = inv ? A.mu[lv] : 0.0;
+        Nl[a][b] = A.nu[e + Eu * (a + NU * b)];
+        Ml[a][b] = (a < NV && b < NV) ? A.mu[e + Eu * (a + NV * b)] : 0.0;
       }
-#pragma unroll 1
-    for (int a = 0; a < NU; ++a)
 #pragma unroll
-      for (int b = 0; b < NU; ++b) {
-        double ku = 0, kv = 0, kt = 0;
+    for (int b = 0; b < NU; ++b)
 #pragma unroll
-        for (int c = 0; c < NU; ++c) {
-          const double l = B.K1[a][c], r = B.K1[c][b];
-          ku = fma(l, Ul[c][b], fma(Ul[a][c], r, ku));
-          kv = fma(l, Vl[c][b], fma(Vl[a][c], r, kv));
-          kt = fma(l, Tl[c][b], fma(Tl[a][c], r, kt));
+      for (int a = 0; a < NU; ++a) {
+        double a1 = 0.0, a2 = 0.0;
+#pragma unroll
+        for (int c = a & 1; c < NU; c += 2) {             // K1[a][c] = 0 for a + c odd
+          a1 = fma(B.K1[a][c], Nl[c][b], a1);
+          a2 = fma(B.K1[a][c], Ml[c][b], a2);
         }
-        const double m = Ml[a][b], n = Nl[a][b];
-        dc2 += -F.four_hh * m * ku - n * kt + n * kv;   // R (v-block: μ is zero outside), u-solve, b
-        dal += -F.four_hh * m * kv;
-      }
-  }
-  // ---- mass: Σ_points 2 W v_q vt_q μ_q (β constant on the element)
-  {
-    double Tv[QH][NV], Tt[QH][NV], Tm[QH][NV];
-    for (int r = 0; r < QH; ++r)
-      for (int b = 0; b < NV; ++b) {
-        double x = 0, y = 0, z = 0;
-        for (int a = 0; a < NV; ++a) {
-          x += B.Ph[r][a] * S.xv[e + Eu * (a + NV * b)];
-          y += B.Ph[r][a] * S.vt[e + Eu * (a + NV * b)];
-          z += B.Ph[r][a] * A.mu[e + Eu * (a + NV * b)];
+#pragma unroll
+        for (int c = b & 1; c < NU; c += 2) {
+          a1 = fma(Nl[a][c], B.K1[c][b], a1);
+          a2 = fma(Ml[a][c], B.K1[c][b], a2);
         }
-        Tv[r][b] = x; Tt[r][b] = y; Tm[r][b] = z;
-      }
-    for (int r = 0; r < QH; ++r)
-      for (int s2 = 0; s2 < QH; ++s2) {
-        double x = 0, y = 0, z = 0;
-        for (int b = 0; b < NV; ++b) { x += Tv[r][b] * B.Ph[s2][b]; y += Tt[r][b] * B.Ph[s2][b]; z += Tm[r][b] * B.Ph[s2][b]; }
-        dbe += 2.0 * (B.PhW[r][0] / B.Ph[r][0]) * (B.PhW[s2][0] / B.Ph[s2][0]) * x * y * z;
+        const size_t l = e + Eu * (a + NU * b);
+        const double V = (a < NV && b < NV) ? S.xv[e + Eu * (a + NV * b)] : 0.0;
+        dc2 = fma(a1, V - S.ut[l], fma(-F.four_hh * a2, S.xu[l], dc2));
+        dal = fma(-F.four_hh * a2, V, dal);
       }
   }
   // ---- faces
@@ -408,10 +449,12 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_param(const __grid_constant
     const double w = B.w[i];
     return fam == 0 ? F.two_h * w * h : fam == 1 ? F.four_hh * w * h : -w * h;
   };
+#pragma unroll 1
   for (int s = 0; s < 4; ++s) {
     const bool boundary = (s == 0 && j == 0) || (s == 1 && j == N - 1) || (s == 2 && k == 0) || (s == 3 && k == N - 1);
+#pragma unroll 1
     for (int i = 0; i < NQ; ++i) {
-      const double ho[3] = {hat(0, s, i, e), hat(1, s, i, e), hat(2, s, i, e)};
+      const double ho0 = hat(0, s, i, e), ho1 = hat(1, s, i, e), ho2 = hat(2, s, i, e);
       if (boundary) {
         const int m = s < 2 ? k : j;
         const double sgn = (s == 0 || s == 2) ? -1.0 : 1.0;
@@ -425,17 +468,9 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_param(const __grid_constant
         const double spn = F.bspn[s][m + (size_t)N * i], sp = F.bsp[s][m + (size_t)N * i];
         const double gu_ex = sgn * (tf.ct * spn - spn), gv_ex = sgn * (-F.omega * tf.st * spn);
         const double v_ex = -F.omega * tf.st * sp;
-        double x[4] = {c2f, af, cf, bf}, d[4];
-        for (int p = 0; p < 4; ++p) {
-          const double hstep = 1e-6 * (fabs(x[p]) > 1e-300 ? fabs(x[p]) : 1.0);
-          double qp[3], qm[3], y[4] = {x[0], x[1], x[2], x[3]};
-          y[p] = x[p] + hstep;
-          boundary_slots(F, s, y[0], y[1], y[2], y[3], v_fp, gun, gvn, gu_ex, gv_ex, v_ex, sgn, qp);
-          y[p] = x[p] - hstep;
-          boundary_slots(F, s, y[0], y[1], y[2], y[3], v_fp, gun, gvn, gu_ex, gv_ex, v_ex, sgn, qm);
-          d[p] = ((qp[0] - qm[0]) * ho[0] + (qp[1] - qm[1]) * ho[1] + (qp[2] - qm[2]) * ho[2]) / (2.0 * hstep);
-        }
-        dc2 += d[0] + d[2] / (2.0 * cf);        // c = √c²
+        double d[4];
+        boundary_coef_partials(F, s, c2f, af, cf, bf, v_fp, gun, gvn, gu_ex, gv_ex, v_ex, sgn, ho0, ho1, ho2, d);
+        dc2 += d[0] + d[2] / (2.0 * cf);                  // c = √c²
         dal += d[1];
         dbe += d[3];
       } else {
@@ -453,35 +488,33 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_param(const __grid_constant
           fi = j + (size_t)N * ((s == 2 ? k : k + 1) + (size_t)(N + 1) * i);
           c2p_a = F.vc2; afp_a = F.vaf; c2m_a = F.vc2m; afm_a = F.vafm; jc_a = F.vJC;
         }
-        const FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);
+        FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);
+        const bool os = F.one_sided;
+        if (!os) { cf.c2m = cf.c2p; cf.afm = cf.afp; }
         const double vm = T(1, sm, i, em), vp = T(1, spp, i, ep);
         const double dum = T(0, sm, i, em), dup = T(0, spp, i, ep);
         const double dvm = T(2, sm, i, em), dvp = T(2, spp, i, ep);
-        const double hn[3] = {hat(0, sn, i, nb), hat(1, sn, i, nb), hat(2, sn, i, nb)};
-        // weighted slots (own, and with the neighbour's role and weights on one-sided faces)
-        auto wslots = [&](const FaceCoef &c) {
-          double Ao, Do, Fo;
-          interior_flux(F, c, plus, dum, dup, vm, vp, dvm, dvp, Ao, Do, Fo);
-          double r = Ao * ho[0] + Do * ho[1] + Fo * ho[2];
-          if (F.one_sided) {
-            double An, Dn, Fn;
-            interior_flux(F, c, !plus, dum, dup, vm, vp, dvm, dvp, An, Dn, Fn);
-            r += An * hn[0] + Dn * hn[1] + Fn * hn[2];
-          }
-          return r;
-        };
-        // the element's own coefficient: its side's values on one-sided faces, the face value else
-        for (int p = 0; p < 2; ++p) {
-          FaceCoef cp = cf, cm = cf;
-          double *xp, *xm, x;
-          if (F.one_sided && !plus) { xp = p ? &cp.afm : &cp.c2m; xm = p ? &cm.afm : &cm.c2m; x = p ? cf.afm : cf.c2m; }
-          else { xp = p ? &cp.afp : &cp.c2p; xm = p ? &cm.afp : &cm.c2p; x = p ? cf.afp : cf.c2p; }
-          const double hstep = fabs(x) > 1e-300 ? fabs(x) : 1.0;
-          *xp = x + hstep;
-          *xm = x - hstep;
-          const double d = (wslots(cp) - wslots(cm)) / (2.0 * hstep);
-          if (p == 0) dc2 += d;
-          else dal += d;
+        // weights of both roles; a continuous face counts the own role only
+        const double hn0 = os ? hat(0, sn, i, nb) : 0.0, hn1 = os ? hat(1, sn, i, nb) : 0.0,
+                     hn2 = os ? hat(2, sn, i, nb) : 0.0;
+        const double hP0 = plus ? ho0 : hn0, hP1 = plus ? ho1 : hn1, hP2 = plus ? ho2 : hn2;
+        const double hM0 = plus ? hn0 : ho0, hM1 = plus ? hn1 : ho1, hM2 = plus ? hn2 : ho2;
+        const FaceWeights w = face_weights(F, cf, hP0, hP1, hP2, hM0, hM1, hM2);
+        // which sides' coefficients are the element's: its own side (one-sided), both (continuous)
+        const double dp = (!os || plus) ? 1.0 : 0.0, dm = (!os || !plus) ? 1.0 : 0.0;
+        const double th = F.theta, tau = F.tau, a = F.two_h;
+        const double J = a * (cf.c2m * dum - cf.c2p * dup + cf.afm * dvm - cf.afp * dvp) + cf.K;
+        const double sj = vm - vp;
+        const double dvsp = th * sj - tau * J, dvsm = -(1.0 - th) * sj - tau * J;
+        {
+          const double dJ = a * (dm * dum - dp * dup), dG = a * ((1.0 - th) * dm * dum + th * dp * dup);
+          const double dpen = 0.5 * (dm + dp) * F.lu;
+          dc2 += (dpen * sj - dG) * w.wA - dJ * w.wS + dp * dvsp * hP2 - dm * dvsm * hM2;
+        }
+        {
+          const double dJ = a * (dm * dvm - dp * dvp), dG = a * ((1.0 - th) * dm * dvm + th * dp * dvp);
+          const double dpen = 0.5 * (dm + dp) * F.lv;
+          dal += (dpen * sj - dG) * w.wA - dJ * w.wS - dp * dvsp * hP1 + dm * dvsm * hM1;
         }
       }
     }

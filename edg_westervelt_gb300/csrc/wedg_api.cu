@@ -381,9 +381,10 @@ int adjoint_buffers(wedg_ws *ws) {
 
 // Jᵀ(λ_u, λ_v) of the RHS at the state (u, v), time t, into (gu, gv); device pointers, on the
 // workspace stream (see wedg_adjoint.cuh for the steps). The forward RHS at the state runs first:
-// its traces, Chebyshev data and vt are inputs of the transpose.
+// its traces, Chebyshev data and vt are inputs of the transpose. With gpar (3E: c², α, β), the
+// derivatives of λ·RHS with respect to the per-element coefficients are added to it.
 int enqueue_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t, const double *lam_u,
-                        const double *lam_v, double *gu, double *gv) {
+                        const double *lam_v, double *gu, double *gv, double *gpar = nullptr) {
   int rc = adjoint_buffers(ws);
   if (rc) return rc;
   StageIO S{};
@@ -408,7 +409,8 @@ int enqueue_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t,
   Su.xu = lam_u;
   Su.ut = ws->adj_nu;
   ws->L.stage(ws->basis.data(), ws->F, Su, bs, ts, ws->stream);
-  const AdjIO A{ws->adj_mu, ws->adj_nu, ws->adj_nus, ws->adj_vt, ws->adj_hat, gu, gv};
+  const AdjIO A{ws->adj_mu, ws->adj_nu, ws->adj_nus, ws->adj_vt, ws->adj_hat, gu, gv, v,
+                gpar ? gpar + 2 * (size_t)ws->E : nullptr};
   ws->L.adj_hats(ws->basis.data(), ws->F, S, A, ws->stream);
   // the volume transposes: the volume terms of the state (-(h²/4) ν, μ)
   StageIO Sv = S;
@@ -421,6 +423,14 @@ int enqueue_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t,
   ws->L.adj_mass(ws->basis.data(), ws->F, S, A, ws->stream);
   ws->L.adj_face(ws->basis.data(), ws->F, S, A, ws->stream);
   ws->stats.kernel_launches += 6;
+  if (gpar) {
+    // K̄·∂F/∂p at the state: volume, u-solve and faces (the mass matrix's β-part is in k_adj_mass)
+    StageIO Sp = S;
+    Sp.ut = ws->adj_ut;
+    Sp.vt = ws->adj_vt;
+    ws->L.adj_param(ws->basis.data(), ws->F, Sp, A, gpar, gpar + ws->E, gpar + 2 * (size_t)ws->E, ws->stream);
+    ws->stats.kernel_launches += 1;
+  }
   CK(ws, cudaGetLastError());
   return WEDG_OK;
 }
@@ -1233,17 +1243,9 @@ int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam
       for (int s = 3; s >= 0; --s) {
         lin(ws->rk_kbar, ca[s], ws->rk_lam, cb[s], s == 3 ? nullptr : ws->rk_g, nullptr);
         const double *Y = ws->rk_seg[4 * (k - k0) + s];
-        if ((rc = enqueue_rhs_adjoint(ws, Y, Y + nU, ts[s], ws->rk_kbar, ws->rk_kbar + nU, ws->rk_g, ws->rk_g + nU)))
+        if ((rc = enqueue_rhs_adjoint(ws, Y, Y + nU, ts[s], ws->rk_kbar, ws->rk_kbar + nU, ws->rk_g, ws->rk_g + nU,
+                                      params ? ws->rk_par : nullptr)))
           return rc;
-        if (params) {
-          // K̄_s · ∂F/∂p at Y_s, from the adjoint evaluation just made (μ, ν, the slot weights, ut, vt)
-          StageIO Sp{};
-          Sp.xu = Y; Sp.xv = Y + nU;
-          stage_factors(ws, ts[s], Sp);
-          Sp.ut = ws->adj_ut; Sp.vt = ws->adj_vt;
-          const AdjIO A{ws->adj_mu, ws->adj_nu, ws->adj_nus, ws->adj_vt, ws->adj_hat, ws->rk_g, ws->rk_g + nU};
-          ws->L.adj_param(ws->basis.data(), ws->F, Sp, A, ws->rk_par, ws->rk_par + ws->E, ws->rk_par + 2 * ws->E, st);
-        }
         lin(ws->rk_acc, 1.0, s == 3 ? ws->rk_lam : ws->rk_acc, 1.0, ws->rk_g, nullptr);
       }
       std::swap(ws->rk_lam, ws->rk_acc);

@@ -84,6 +84,7 @@ struct Basis {
   double ElA[NU], E1D[NU], E1F[NU];  // (2/h) El, (4/h²) E1l, -E1l: the lift factors of a side
   double Ph[QH][NV];             // P_h_v[r, d]
   double PhW[QH][NV];            // w_h[r] P_h_v[r, d], with W2d_h = w_h w_h^T
+  double wh[QH];                 // w_h
   double K1[NU][NU];             // 1D stiffness S^T diag(w) S
   double Q[NU][NU];              // its eigenvectors, Q[row][col]; Q[.][0] = e_0
   double ilam2[NU][NU];          // 1 / (λ_i + λ_j), and 1 at (0, 0)

@@ -109,30 +109,49 @@ def test_rk4_adjoint_against_finite_differences(gpu, solver):
             assert abs(fd - ad) <= 1e-6 * abs(fd), (q, N, fd, ad)
 
 
-def test_misfit_gradient_against_finite_differences(gpu):
-    """The gradient of a receiver misfit with respect to c², α, β constant on 2 × 2 cells (the
-    parameter fields of the adjoint form) against central differences of the misfit along
-    seeded directions: forward runs with perturbed cell values."""
+MISFIT_CASES = {
+    # jumping cells: one-sided faces; every physical side absorbing_2beta
+    "one_sided": (2, dict(flux="upwind", mixed=False, boundary="absorbing_2beta")),
+    # every boundary kind, the alternating flux with its penalties, one-sided faces
+    "kinds": (2, dict(flux="alternating", mixed=False, kappa=0.6, sigma=0.3,
+                      boundary=dict(bot="wall", top="absorbing", lft="dirichlet", rgt="absorbing_2beta"))),
+    # one cell: constant coefficients, continuous faces; central flux
+    "continuous": (1, dict(flux="central", mixed=False, boundary=dict(bot="absorbing_2beta", top="wall",
+                                                                        lft="absorbing", rgt="absorbing_2beta"))),
+}
+
+
+@pytest.mark.parametrize("case", sorted(MISFIT_CASES))
+def test_misfit_gradient_against_finite_differences(gpu, case):
+    """The gradient of a receiver misfit with respect to c², α, β constant on m × m cells (the
+    parameter fields of the adjoint form) against central differences of the misfit along seeded
+    directions, one parameter field at a time: forward runs with perturbed cell values."""
+    m, kw = MISFIT_CASES[case]
     rng = np.random.default_rng(44)
     q, N, T = 2, 8, 0.06
-    c2 = rng.uniform(0.8, 1.5, (2, 2))
-    al = 10 ** rng.uniform(-4, -3, (2, 2))
-    be = rng.uniform(0.5, 3.0, (2, 2))
+    c2 = rng.uniform(0.8, 1.5, (m, m))
+    al = 10 ** rng.uniform(-4, -3, (m, m))
+    be = rng.uniform(0.5, 3.0, (m, m))
     g = (np.arange(4) + 0.5) / 4
     receivers = [(x, y) for y in g for x in g]
     u_obs = 1e-4 * rng.standard_normal(len(receivers))
     src = W.GaussianSource(x0=(0.4, 0.55), r0=0.15, omega=12 * math.pi, Ts=0.5)
-    kw = dict(flux="upwind", mixed=False, boundary="absorbing_2beta", source=src)
+    kw = dict(kw, source=src)
+    if m == 1:
+        pre, _ = W.precompute(q, N, mode="source", coefficients=W.piecewise_coefficients(c2, al, be), **kw)
+        assert not pre["one_sided"]
     J0, grad = W.misfit_gradient(q, N, T, c2, al, be, receivers, u_obs, every=7, **kw)
     assert J0 > 0
-    for _ in range(3):
-        d = {"c2": rng.standard_normal((2, 2)) * c2, "alpha": rng.standard_normal((2, 2)) * al,
-             "beta": rng.standard_normal((2, 2)) * be}
-        eps = 1e-6
+    base = {"c2": c2, "alpha": al, "beta": be}
+    for name in ("c2", "alpha", "beta"):
+        d = {k: (rng.standard_normal((m, m)) * base[k] if k == name else np.zeros((m, m))) for k in base}
+        # α enters the misfit weakly (α ~ 1e-4): a larger relative step keeps the difference of the
+        # misfits well above their rounding
+        eps = 1e-4 if name == "alpha" else 1e-6
         Jp = W.misfit_gradient(q, N, T, c2 + eps * d["c2"], al + eps * d["alpha"], be + eps * d["beta"],
                                receivers, u_obs, every=7, **kw)[0]
         Jm = W.misfit_gradient(q, N, T, c2 - eps * d["c2"], al - eps * d["alpha"], be - eps * d["beta"],
                                receivers, u_obs, every=7, **kw)[0]
         fd = (Jp - Jm) / (2 * eps)
-        ad = sum(float(np.sum(grad[k] * d[k])) for k in d)
-        assert abs(fd - ad) <= 1e-5 * abs(fd), (fd, ad)
+        ad = float(np.sum(grad[name] * d[name]))
+        assert abs(fd - ad) <= 1e-5 * abs(fd), (case, name, fd, ad)
