@@ -125,6 +125,7 @@ def lib():
     L.wedg_rk4_adjoint_forward.argtypes = [vp, _D, _D, ctypes.c_double, ctypes.c_double, ctypes.c_int64,
                                            ctypes.c_int64, _D, _D, _I64, _I64, ctypes.c_int]
     L.wedg_rk4_adjoint_reverse.argtypes = [vp, _D, _D, _D, _D, _D, _D, _D, ctypes.c_int]
+    L.wedg_set_adjoint_memory.argtypes = [vp, ctypes.c_int64]
     L.wedg_norms.argtypes = [ctypes.POINTER(NormArgs), _D]
     L.wedg_run_source.argtypes = [vp, _D, _D, _I64, _I64, ctypes.c_int, ctypes.POINTER(SourceRun), _I64,
                                   ctypes.POINTER(ctypes.c_int)]

@@ -110,6 +110,15 @@ struct wedg_ws {
   double rk_dt = 0;
   int64_t rk_nsteps = 0, rk_every = 1;
   std::vector<double> rk_t;
+  // the forward data of every stage of one segment, kept by the reverse sweep (see
+  // wedg_set_adjoint_memory): the stage RHS K = (ut | vt), traces, G, Chebyshev data
+  struct StageData {
+    double *k = nullptr, *tr = nullptr, *G = nullptr, *th = nullptr, *de = nullptr;
+    int *nst = nullptr, *bins = nullptr, *bin_count = nullptr;
+    int parity = 0;
+  };
+  std::vector<StageData> rk_keep;
+  int64_t adj_mem = -1;
   // optional per-launch timing (events recorded around each stage kernel)
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -265,8 +274,9 @@ void drain_events(wedg_ws *ws) {
   ws->ev_pending.clear();
 }
 
-// enqueue the two kernels of one stage
-int enqueue_stage(wedg_ws *ws, const StageIO &S) {
+// enqueue the three kernels of one stage (on the workspace's Fields, or on Fo)
+int enqueue_stage(wedg_ws *ws, const StageIO &S, const Fields *Fo = nullptr) {
+  const Fields &F = Fo ? *Fo : ws->F;
   const int tp = 128, bp = (ws->E + tp - 1) / tp;
   const int ts = stage_threads(ws->nu, ws->nv, ws->fast), bs = (ws->E + ts - 1) / ts;
   const int bm = 1;   // the mass kernels size their own grid
@@ -278,11 +288,11 @@ int enqueue_stage(wedg_ws *ws, const StageIO &S) {
     e0 = take_event(ws); e1 = take_event(ws); e2 = take_event(ws); e3 = take_event(ws);
     cudaEventRecord(e0, ws->stream);
   }
-  ws->L.prep(ws->basis.data(), ws->F, Sp, bp, tp, ws->stream);
+  ws->L.prep(ws->basis.data(), F, Sp, bp, tp, ws->stream);
   if (ws->timing) cudaEventRecord(e1, ws->stream);
-  ws->L.stage(ws->basis.data(), ws->F, Sp, bs, ts, ws->stream);
+  ws->L.stage(ws->basis.data(), F, Sp, bs, ts, ws->stream);
   if (ws->timing) cudaEventRecord(e2, ws->stream);
-  ws->L.mass(ws->basis.data(), ws->F, Sp, bm, CHEB_THREADS, ws->stream);
+  ws->L.mass(ws->basis.data(), F, Sp, bm, CHEB_THREADS, ws->stream);
   if (ws->timing) {
     cudaEventRecord(e3, ws->stream);
     ws->ev_pending.push_back({e0, e1, e2, e3});
@@ -379,10 +389,53 @@ int adjoint_buffers(wedg_ws *ws) {
   return WEDG_OK;
 }
 
-// Jᵀ(λ_u, λ_v) of the RHS at the state (u, v), time t, into (gu, gv); device pointers, on the
-// workspace stream (see wedg_adjoint.cuh for the steps). The forward RHS at the state runs first:
-// its traces, Chebyshev data and vt are inputs of the transpose. With gpar (3E: c², α, β), the
-// derivatives of λ·RHS with respect to the per-element coefficients are added to it.
+// The transpose of one RHS evaluation on the workspace stream (see wedg_adjoint.cuh for the
+// steps), after the forward evaluation at the state: Fs holds its traces and Chebyshev data, S
+// the state (xu, xv), its time factors and bin parity and the forward outputs (ut, vt). Writes
+// Jᵀ(λ_u, λ_v) to (gu, gv); with gpar (3E: c², α, β), the derivatives of λ·RHS with respect to
+// the per-element coefficients are added to it.
+int enqueue_adjoint_core(wedg_ws *ws, const Fields &Fs, const StageIO &S, const double *lam_u, const double *lam_v,
+                         double *gu, double *gv, double *gpar) {
+  const int ts = stage_threads(ws->nu, ws->nv, ws->fast), bs = (ws->E + ts - 1) / ts;
+  // μ = M(v)⁻¹ λ_v, on the Chebyshev data of the state
+  Fields Fm = Fs;
+  Fm.mrhs = const_cast<double *>(lam_v);
+  StageIO Sm = S;
+  Sm.mode = OUT_RHS;
+  Sm.vt = ws->adj_mu;
+  ws->L.mass(ws->basis.data(), Fm, Sm, 1, CHEB_THREADS, ws->stream);
+  // ν = A_e⁻¹ λ_u
+  StageIO Su = S;
+  Su.mode = OUT_ADJ_USOLVE;
+  Su.xu = lam_u;
+  Su.ut = ws->adj_nu;
+  ws->L.stage(ws->basis.data(), Fs, Su, bs, ts, ws->stream);
+  const AdjIO A{ws->adj_mu, ws->adj_nu, ws->adj_nus, S.vt, ws->adj_hat, gu, gv, S.xv,
+                gpar ? gpar + 2 * (size_t)ws->E : nullptr};
+  ws->L.adj_hats(ws->basis.data(), Fs, S, A, ws->stream);
+  // the volume transposes: the volume terms of the state (-(h²/4) ν, μ)
+  StageIO Sv = S;
+  Sv.mode = OUT_ADJ_VOLUME;
+  Sv.xu = ws->adj_nus;
+  Sv.xv = ws->adj_mu;
+  Sv.vt = gv;
+  Sv.ut = gu;
+  ws->L.stage(ws->basis.data(), Fs, Sv, bs, ts, ws->stream);
+  ws->L.adj_mass(ws->basis.data(), Fs, S, A, ws->stream);
+  ws->L.adj_face(ws->basis.data(), Fs, S, A, ws->stream);
+  ws->stats.kernel_launches += 6;
+  if (gpar) {
+    // K̄·∂F/∂p at the state: volume, u-solve and faces (the mass matrix's β-part is in k_adj_mass)
+    ws->L.adj_param(ws->basis.data(), Fs, S, A, gpar, gpar + ws->E, gpar + 2 * (size_t)ws->E, ws->stream);
+    ws->stats.kernel_launches += 1;
+  }
+  CK(ws, cudaGetLastError());
+  return WEDG_OK;
+}
+
+// Jᵀ(λ_u, λ_v) of the RHS at the state (u, v), time t, into (gu, gv); device pointers: the
+// forward RHS at the state first (its traces, Chebyshev data and vt are inputs of the
+// transpose), then the transpose.
 int enqueue_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t, const double *lam_u,
                         const double *lam_v, double *gu, double *gv, double *gpar = nullptr) {
   int rc = adjoint_buffers(ws);
@@ -396,43 +449,22 @@ int enqueue_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t,
   const int par = ws->parity;
   if ((rc = enqueue_stage(ws, S))) return rc;
   S.parity = par;
-  const int ts = stage_threads(ws->nu, ws->nv, ws->fast), bs = (ws->E + ts - 1) / ts;
-  // μ = M(v)⁻¹ λ_v, on the Chebyshev data of the state
-  Fields Fm = ws->F;
-  Fm.mrhs = const_cast<double *>(lam_v);
-  StageIO Sm = S;
-  Sm.vt = ws->adj_mu;
-  ws->L.mass(ws->basis.data(), Fm, Sm, 1, CHEB_THREADS, ws->stream);
-  // ν = A_e⁻¹ λ_u
-  StageIO Su = S;
-  Su.mode = OUT_ADJ_USOLVE;
-  Su.xu = lam_u;
-  Su.ut = ws->adj_nu;
-  ws->L.stage(ws->basis.data(), ws->F, Su, bs, ts, ws->stream);
-  const AdjIO A{ws->adj_mu, ws->adj_nu, ws->adj_nus, ws->adj_vt, ws->adj_hat, gu, gv, v,
-                gpar ? gpar + 2 * (size_t)ws->E : nullptr};
-  ws->L.adj_hats(ws->basis.data(), ws->F, S, A, ws->stream);
-  // the volume transposes: the volume terms of the state (-(h²/4) ν, μ)
-  StageIO Sv = S;
-  Sv.mode = OUT_ADJ_VOLUME;
-  Sv.xu = ws->adj_nus;
-  Sv.xv = ws->adj_mu;
-  Sv.vt = gv;
-  Sv.ut = gu;
-  ws->L.stage(ws->basis.data(), ws->F, Sv, bs, ts, ws->stream);
-  ws->L.adj_mass(ws->basis.data(), ws->F, S, A, ws->stream);
-  ws->L.adj_face(ws->basis.data(), ws->F, S, A, ws->stream);
-  ws->stats.kernel_launches += 6;
-  if (gpar) {
-    // K̄·∂F/∂p at the state: volume, u-solve and faces (the mass matrix's β-part is in k_adj_mass)
-    StageIO Sp = S;
-    Sp.ut = ws->adj_ut;
-    Sp.vt = ws->adj_vt;
-    ws->L.adj_param(ws->basis.data(), ws->F, Sp, A, gpar, gpar + ws->E, gpar + 2 * (size_t)ws->E, ws->stream);
-    ws->stats.kernel_launches += 1;
-  }
-  CK(ws, cudaGetLastError());
-  return WEDG_OK;
+  return enqueue_adjoint_core(ws, ws->F, S, lam_u, lam_v, gu, gv, gpar);
+}
+
+// The workspace's Fields with the per-stage arrays of kept stage data d
+Fields kept_fields(const wedg_ws *ws, const wedg_ws::StageData &d) {
+  Fields F = ws->F;
+  F.tr = d.tr; F.G = d.G; F.th = d.th; F.de = d.de;
+  F.nst = d.nst; F.bins = d.bins; F.bin_count = d.bin_count;
+  return F;
+}
+
+// bytes of the kept data of one stage
+size_t stage_data_bytes(const wedg_ws *ws) {
+  const size_t E = ws->E;
+  return sizeof(double) * E * ((size_t)ws->nu * ws->nu + ws->nv * ws->nv + 12 * ws->nq + ws->qh * ws->qh + 2) +
+         sizeof(int) * (E * (1 + NBIN) + 2 * NBIN);
 }
 
 int collect(wedg_ws *ws) {
@@ -1221,12 +1253,72 @@ int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam
   const int lb = 256, lg = (int)std::min<size_t>((n + lb - 1) / lb, 152 * 16);
   auto lin = [&](double *out, double a, const double *x, double b, const double *y, const double *z) {
     k_lincomb<<<lg, lb, 0, st>>>(n, out, a, x, b, y, z);
+    ws->stats.kernel_launches += 1;
   };
+  // keep the forward data of every stage of a segment when it fits the memory allowance
+  const int64_t seg = std::min<int64_t>(every, std::max<int64_t>(nsteps, 1));
+  const size_t keep_bytes = (size_t)(4 * seg) * stage_data_bytes(ws);
+  size_t have = 0;
+  for (size_t i = 0; i < ws->rk_keep.size(); ++i) have += stage_data_bytes(ws);
+  bool keep = false;
+  if (ws->adj_mem < 0) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) keep = keep_bytes <= (fr + have) / 2;
+  } else {
+    keep = keep_bytes <= (size_t)ws->adj_mem;
+  }
+  if (keep) {
+    const size_t E = ws->E;
+    const size_t nd = (size_t)ws->nu * ws->nu + ws->nv * ws->nv + 12 * ws->nq + ws->qh * ws->qh + 2;
+    while ((int64_t)ws->rk_keep.size() < 4 * seg) {
+      wedg_ws::StageData d;
+      double *b;
+      int *ib;
+      if ((rc = dalloc(ws, &b, nd * E)) || (rc = dalloc(ws, &ib, E * (1 + NBIN) + 2 * NBIN))) return rc;
+      d.k = b;
+      d.tr = d.k + n;
+      d.G = d.tr + 12 * (size_t)ws->nq * E;
+      d.th = d.G + (size_t)ws->qh * ws->qh * E;
+      d.de = d.th + E;
+      d.nst = ib;
+      d.bins = ib + E;
+      d.bin_count = ib + E * (1 + NBIN);
+      ws->rk_keep.push_back(d);
+    }
+  }
   // ---- reverse pass, segment by segment
   for (int64_t c = nchk - 1; c >= 0; --c) {
     const int64_t k0 = c * every, k1 = std::min(nsteps, k0 + every);
     CK(ws, cudaMemcpyAsync(ws->rk_y, ws->rk_chk[c], sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     for (int64_t k = k0; k < k1; ++k) {
+      if (keep) {
+        // the step as four RHS evaluations (their outputs and data kept) and the RK4 combinations:
+        // Y1 = y, Y_{s+1} = y + c_s K_s, y ← y + dt/6 (K1 + 2K2 + 2K3 + K4)
+        const double cs[3] = {0.5 * dt, 0.5 * dt, dt};
+        const double ts[4] = {t[k], t[k] + 0.5 * dt, t[k] + 0.5 * dt, t[k] + dt};
+        CK(ws, cudaMemcpyAsync(ws->rk_seg[4 * (k - k0)], ws->rk_y, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        for (int s = 0; s < 4; ++s) {
+          wedg_ws::StageData &d = ws->rk_keep[4 * (k - k0) + s];
+          const double *Y = ws->rk_seg[4 * (k - k0) + s];
+          StageIO S{};
+          S.xu = Y; S.xv = Y + nU;
+          stage_factors(ws, ts[s], S);
+          S.mode = OUT_RHS;
+          S.ut = d.k;
+          S.vt = d.k + nU;
+          CK(ws, cudaMemsetAsync(d.bin_count, 0, 2 * NBIN * sizeof(int), st));
+          d.parity = ws->parity;
+          const Fields Fk = kept_fields(ws, d);
+          if ((rc = enqueue_stage(ws, S, &Fk))) return rc;
+          if (s < 3) lin(ws->rk_seg[4 * (k - k0) + s + 1], cs[s], d.k, 1.0, ws->rk_y, nullptr);
+        }
+        const double *K[4] = {ws->rk_keep[4 * (k - k0)].k, ws->rk_keep[4 * (k - k0) + 1].k,
+                              ws->rk_keep[4 * (k - k0) + 2].k, ws->rk_keep[4 * (k - k0) + 3].k};
+        lin(ws->rk_acc, 2.0, K[1], 1.0, K[0], nullptr);
+        lin(ws->rk_acc, 2.0, K[2], 1.0, K[3], ws->rk_acc);
+        lin(ws->rk_y, dt / 6.0, ws->rk_acc, 1.0, ws->rk_y, nullptr);
+        continue;
+      }
       double *su[4], *sv[4];
       for (int s = 0; s < 4; ++s) {
         su[s] = ws->rk_seg[4 * (k - k0) + s];
@@ -1243,9 +1335,22 @@ int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam
       for (int s = 3; s >= 0; --s) {
         lin(ws->rk_kbar, ca[s], ws->rk_lam, cb[s], s == 3 ? nullptr : ws->rk_g, nullptr);
         const double *Y = ws->rk_seg[4 * (k - k0) + s];
-        if ((rc = enqueue_rhs_adjoint(ws, Y, Y + nU, ts[s], ws->rk_kbar, ws->rk_kbar + nU, ws->rk_g, ws->rk_g + nU,
-                                      params ? ws->rk_par : nullptr)))
-          return rc;
+        double *gpar = params ? ws->rk_par : nullptr;
+        if (keep) {
+          const wedg_ws::StageData &d = ws->rk_keep[4 * (k - k0) + s];
+          StageIO S{};
+          S.xu = Y; S.xv = Y + nU;
+          stage_factors(ws, ts[s], S);
+          S.parity = d.parity;
+          S.ut = d.k;
+          S.vt = d.k + nU;
+          rc = enqueue_adjoint_core(ws, kept_fields(ws, d), S, ws->rk_kbar, ws->rk_kbar + nU, ws->rk_g,
+                                    ws->rk_g + nU, gpar);
+        } else {
+          rc = enqueue_rhs_adjoint(ws, Y, Y + nU, ts[s], ws->rk_kbar, ws->rk_kbar + nU, ws->rk_g, ws->rk_g + nU,
+                                   gpar);
+        }
+        if (rc) return rc;
         lin(ws->rk_acc, 1.0, s == 3 ? ws->rk_lam : ws->rk_acc, 1.0, ws->rk_g, nullptr);
       }
       std::swap(ws->rk_lam, ws->rk_acc);
@@ -1262,6 +1367,12 @@ int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam
     CK(ws, cudaMemcpy(g_beta, ws->rk_par + 2 * ws->E, sizeof(double) * ws->E, out));
   }
   return rc;
+}
+
+int wedg_set_adjoint_memory(wedg_ws *ws, int64_t bytes) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  ws->adj_mem = bytes < 0 ? -1 : bytes;
+  return WEDG_OK;
 }
 
 int wedg_rk4_adjoint(wedg_ws *ws, const double *u0, const double *v0, double t0, double dt, int64_t nsteps,

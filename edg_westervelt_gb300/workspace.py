@@ -244,6 +244,11 @@ class Workspace:
         self._check(rc)
         return uT, vT
 
+    def set_adjoint_memory(self, nbytes):
+        """wedg_set_adjoint_memory: device bytes the reverse sweep may use to keep the forward
+        data of one checkpoint segment's stages (negative: half the free memory; 0: never)."""
+        self._check(L.lib().wedg_set_adjoint_memory(self._h, int(nbytes)))
+
     def rk4_adjoint_reverse(self, lam_u, lam_v, params=False):
         """wedg_rk4_adjoint_reverse: the reverse sweep of the last rk4_adjoint_forward for the
         final-time adjoint (λ_u, λ_v); returns (gu, gv) and, with params, the per-element

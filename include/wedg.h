@@ -220,6 +220,14 @@ int wedg_rk4_adjoint_forward(wedg_ws *ws, const double *u0, const double *v0, do
 int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam_v, double *gu, double *gv,
                              double *g_c2, double *g_alpha, double *g_beta, int where);
 
+/* Device memory the reverse sweep may use to keep, for every stage of one checkpoint segment,
+ * the stage's forward data (its right-hand side, traces and mass-solve data) while it
+ * recomputes the segment: with it the adjoint of a stage needs no second forward evaluation.
+ * bytes < 0 (the default): half of the free device memory at the sweep; 0: never keep (each
+ * stage's forward evaluation is repeated); > 0: keep when one segment's data fits in bytes.
+ * The gradients agree either way up to rounding. */
+int wedg_set_adjoint_memory(wedg_ws *ws, int64_t bytes);
+
 /* Batched form: many independent instances -- workspaces made by wedg_create, each with its
  * own N, degrees, flux, boundary kinds and coefficients -- advanced together. No counterpart in
  * the reference, whose batching is the caller's loop over instances. One RK4 step of every

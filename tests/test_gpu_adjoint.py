@@ -155,3 +155,40 @@ def test_misfit_gradient_against_finite_differences(gpu, case):
         fd = (Jp - Jm) / (2 * eps)
         ad = float(np.sum(grad[name] * d[name]))
         assert abs(fd - ad) <= 1e-5 * abs(fd), (case, name, fd, ad)
+
+
+@pytest.mark.parametrize("solver", ["chebyshev", "cg"])
+def test_reverse_sweep_kept_stage_data(gpu, solver):
+    """The reverse sweep that keeps each segment stage's forward data (wedg_set_adjoint_memory
+    large enough) against the one that evaluates every stage's forward RHS again (memory 0):
+    the same gradients up to rounding, with fewer kernel launches; a ragged last segment."""
+    rng = np.random.default_rng(45)
+    q, N, nsteps, every = 3, 6, 11, 4
+    c2 = rng.uniform(0.8, 1.5, (2, 2))
+    al = 10 ** rng.uniform(-4, -3, (2, 2))
+    be = rng.uniform(0.5, 3.0, (2, 2))
+    src = W.GaussianSource(x0=(0.4, 0.55), r0=0.15, omega=12 * math.pi, Ts=0.5)
+    pre, _ = W.precompute(q, N, mode="source", coefficients=W.piecewise_coefficients(c2, al, be), flux="central",
+                          mixed=True, source=src, mass_solver=solver, kappa=0.5,
+                          boundary=dict(bot="wall", top="absorbing", lft="dirichlet", rgt="absorbing_2beta"))
+    ws = W.Workspace(pre, N)
+    nu, nv = pre["qu1"], pre["qv1"]
+    u0 = np.zeros((N, N, nu, nu), order="F")
+    v0 = np.zeros((N, N, nv, nv), order="F")
+    dt = (1.0 / N) / (10 * q * q)
+    ws.rk4_adjoint_forward(u0, v0, 0.0, dt, nsteps, every=every)
+    lam_u = np.asfortranarray(rng.standard_normal((N, N, nu, nu)))
+    lam_v = np.asfortranarray(rng.standard_normal((N, N, nv, nv)))
+    out, launches = {}, {}
+    for mem in (0, 1 << 40):
+        ws.set_adjoint_memory(mem)
+        out[mem] = ws.rk4_adjoint_reverse(lam_u, lam_v, params=True)
+        launches[mem] = ws.stats()["kernel_launches"]
+    ws.set_adjoint_memory(-1)
+    auto = ws.rk4_adjoint_reverse(lam_u, lam_v, params=True)
+    for a, b, c in zip(out[0], out[1 << 40], auto):
+        scale = np.abs(a).max()
+        assert scale > 0
+        assert np.abs(a - b).max() <= 1e-10 * scale
+        assert np.array_equal(b, c)
+    assert launches[1 << 40] < launches[0]
