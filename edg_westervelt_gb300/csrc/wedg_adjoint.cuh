@@ -31,7 +31,7 @@ struct AdjIO {
   const double *nu;      // ν = A_e⁻¹ λ_u (NU²)
   double *nus;           // -(h²/4) ν, the u input of the volume transpose
   const double *vt;      // the forward vt at this state
-  double *hat;           // slot weights, [((fam·4 + side)·NQ + i) E + e], fam A, D, F (unscaled)
+  double *hat;           // slot weights, [((fam·4 + side)·NQ + i) E + e], fam A, D, F
   double *gu, *gv;       // the gradient; gu holds the volume's b on entry to k_adj_face
   const double *xv;      // the state's V (for the β-derivative of the mass matrix)
   double *gbe;           // per-element β-gradient that k_adj_mass adds to, or null
@@ -58,9 +58,10 @@ __device__ __forceinline__ FaceWeights face_weights(const Fields &F, const FaceC
   return w;
 }
 
-// k_adj_hats: the traces of μ (values and derivatives) and of ν (derivatives) on the four sides,
-// whose scaled values are the weights of the slots A, D and F (src/rhs.jl:412-473 transposed:
-// Â = (2/h) w_i tr_v(μ), D̂ = (4/h²) w_i tr_dv(μ), F̂ = -w_i tr_du(ν)); and nus.
+// k_adj_hats: the weights of the slots A, D and F at every side point, the scaled traces of μ
+// (values and derivatives) and of ν (derivatives) (src/rhs.jl:412-473 transposed:
+// Â = (2/h) w_i tr_v(μ), D̂ = (4/h²) w_i tr_dv(μ), F̂ = -w_i tr_du(ν), the scalings folded into
+// the end vectors ElA, E1D, E1F and the weighted values Pw); and nus.
 template <int NU, int NV>
 __global__ void __launch_bounds__(ADJ_THREADS) k_adj_hats(const __grid_constant__ Basis<NU, NV> B,
                                                    const __grid_constant__ Fields F, const AdjIO A) {
@@ -73,12 +74,12 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_hats(const __grid_constant_
   {
     double M[NV][NV];
     load_regs<NV>(M, A.mu, E, e);
-    trace4<NQ, NU, NV, false>(M, B.P, B.El, A.hat, 0, E, e);
-    trace4<NQ, NU, NV, true>(M, B.P, B.E1l, A.hat, 1, E, e);
+    trace4<NQ, NU, NV, false>(M, B.Pw, B.ElA, A.hat, 0, E, e);
+    trace4<NQ, NU, NV, true>(M, B.Pw, B.E1D, A.hat, 1, E, e);
   }
   double X[NU][NU];
   load_regs<NU>(X, A.nu, E, e);
-  trace4<NQ, NU, NU, true>(X, B.P, B.E1l, A.hat, 2, E, e);
+  trace4<NQ, NU, NU, true>(X, B.Pw, B.E1F, A.hat, 2, E, e);
 #pragma unroll
   for (int b = 0; b < NU; ++b)
 #pragma unroll
@@ -169,206 +170,92 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
   }
 }
 
-// Partial derivatives of the slots A, D, F of a physical side point with respect to the
-// element's traces (du, v, dv) there (the forward formulas of side_point, differentiated):
-// d[q][x], q = A, D, F and x = du, v, dv.
-template <int NU, int NV>
-__device__ __forceinline__ void boundary_partials(const Fields &F, const TimeF &S, int s, int j, int k, int e,
-                                                  int i, double (&d)[3][3]) {
-  constexpr int NQ = NU;
+// The data of a physical side point (side_point's inputs): the coefficients there, the
+// element's traces and the exact solution's data, with the outward sign sgn
+struct SideData {
+  double c2f, af, cf, bf, v_fp, gun, gvn, gu_ex, gv_ex, v_ex, sgn;
+};
+__device__ __forceinline__ SideData side_data(const Fields &F, const TimeF &tf, int s, int j, int k, int e, int i,
+                                              int NQ) {
   const int N = F.N;
-  const double *tr = F.tr;
+  const size_t Eu = (size_t)F.E;
   const int m = s < 2 ? k : j;
-  const double sgn = (s == 0 || s == 2) ? -1.0 : 1.0;
+  SideData p;
+  p.sgn = (s == 0 || s == 2) ? -1.0 : 1.0;
   size_t fi;
   const double *c2a, *afa, *cfa, *bfa;
   if (s < 2) { fi = (s == 0 ? 0 : N) + (size_t)(N + 1) * (k + (size_t)N * i); c2a = F.hc2; afa = F.haf; cfa = F.hcf; bfa = F.hbf; }
   else { fi = j + (size_t)N * ((s == 2 ? 0 : N) + (size_t)(N + 1) * i); c2a = F.vc2; afa = F.vaf; cfa = F.vcf; bfa = F.vbf; }
-  const double c2f = c2a[fi], af = afa[fi], cf = cfa[fi];
-  const double sth = sgn * F.two_h;                  // d gun / d du = d gvn / d dv
+  p.c2f = c2a[fi]; p.af = afa[fi]; p.cf = cfa[fi]; p.bf = bfa[fi];
+  const double *tr = F.tr;
+  p.v_fp = tr[((1 * 4 + s) * NQ + i) * Eu + e];
+  p.gun = p.sgn * (F.two_h * tr[((0 * 4 + s) * NQ + i) * Eu + e]);
+  p.gvn = p.sgn * (F.two_h * tr[((2 * 4 + s) * NQ + i) * Eu + e]);
+  const double spn = F.bspn[s][m + (size_t)N * i], sp = F.bsp[s][m + (size_t)N * i];
+  p.gu_ex = p.sgn * (tf.ct * spn - spn);
+  p.gv_ex = p.sgn * (-F.omega * tf.st * spn);
+  p.v_ex = -F.omega * tf.st * sp;
+  return p;
+}
+
+// Derivatives of the slots A, D, F of a physical side point with respect to the element's
+// traces (du, v, dv) there (side_point's formulas differentiated), contracted with the slot
+// weights h0, h1, h2: t[x] = Σ_q ∂q/∂x h_q.
+__device__ __forceinline__ void boundary_trace_partials(const Fields &F, int s, const SideData &p, double h0,
+                                                        double h1, double h2, double (&t)[3]) {
+  const double sth = p.sgn * F.two_h;                  // d gun / d du = d gvn / d dv
   double dF1[3] = {0, 0, 0}, ddv[3] = {0, 0, 0};
   if (F.kind[s] == 3) {
     // wall: F1 = g2 (data), dv = -(κ/c)(c² gun + α gvn - g2)
-    const double kc = -(F.kap[s] / cf);
-    ddv[0] = kc * c2f * sth;
-    ddv[2] = kc * af * sth;
+    const double kc = -(F.kap[s] / p.cf);
+    ddv[0] = kc * p.c2f * sth;
+    ddv[2] = kc * p.af * sth;
   } else {
-    const double v_fp = tr[((1 * 4 + s) * NQ + i) * (size_t)F.E + e];
-    const double gun = sgn * (F.two_h * tr[((0 * 4 + s) * NQ + i) * (size_t)F.E + e]);
-    const double gvn = sgn * (F.two_h * tr[((2 * 4 + s) * NQ + i) * (size_t)F.E + e]);
-    const double spn = F.bspn[s][m + (size_t)N * i], sp = F.bsp[s][m + (size_t)N * i];
-    const double gu_ex = sgn * (S.ct * spn - spn);
-    const double gv_ex = sgn * (-F.omega * S.st * spn);
-    const double v_ex = -F.omega * S.st * sp;
-    const double bf = bfa[fi];
     const double g = F.gam[s], et = F.eta[s], sg = F.sig[s], kb = F.kb[s];
-    const double sqf = sqrt(1.0 - kb * bf * v_fp);
-    const double dsqf = -kb * bf / (2.0 * sqf);
-    const double rho_num = et * (c2f * gun + af * gvn) + g * cf * sqf * v_fp;
-    const double rho_ex = et * (c2f * gu_ex + af * gv_ex) + g * cf * sqrt(1.0 - kb * bf * v_ex) * v_ex;
-    const double rho = rho_num - rho_ex;
-    const double drho[3] = {et * c2f * sth, g * cf * (sqf + v_fp * dsqf), et * af * sth};
-    const double ke = -(g - sg * et) / cf;
-    dF1[0] = c2f * sth - (et + sg * g) * drho[0];
+    const double sqf = sqrt(1.0 - kb * p.bf * p.v_fp);
+    const double dsqf = -kb * p.bf / (2.0 * sqf);
+    const double rho = et * (p.c2f * (p.gun - p.gu_ex) + p.af * (p.gvn - p.gv_ex)) +
+                       g * p.cf * (sqf * p.v_fp - sqrt(1.0 - kb * p.bf * p.v_ex) * p.v_ex);
+    const double drho[3] = {et * p.c2f * sth, g * p.cf * (sqf + p.v_fp * dsqf), et * p.af * sth};
+    const double ke = -(g - sg * et) / p.cf;
+    dF1[0] = p.c2f * sth - (et + sg * g) * drho[0];
     dF1[1] = -(et + sg * g) * drho[1];
-    dF1[2] = af * sth - (et + sg * g) * drho[2];
+    dF1[2] = p.af * sth - (et + sg * g) * drho[2];
     ddv[0] = ke * drho[0] / sqf;
     ddv[1] = ke * (drho[1] / sqf - rho * dsqf / (sqf * sqf));
     ddv[2] = ke * drho[2] / sqf;
   }
+  // D = sgn α dv, F = -sgn c² dv
+  const double m = p.sgn * (p.af * h1 - p.c2f * h2);
 #pragma unroll
-  for (int x = 0; x < 3; ++x) {
-    d[0][x] = dF1[x];
-    d[1][x] = sgn * (af * ddv[x]);
-    d[2][x] = -sgn * (c2f * ddv[x]);
-  }
-}
-
-// k_adj_face: the trace weights of the element, t̂_x(s, i) = Σ_slots ∂slot/∂x · ŝlot over the
-// element's own slots and (interior faces) the neighbour's slots of the shared point, for its
-// traces x = du, v, dv; then the trace transposes (k_prep's trace4 transposed) into gu, gv.
-// The interior slots are affine in the six traces of the face point (interior_flux); their
-// derivatives are the closed forms of face_weights.
-// On entry gu holds the volume transpose's b; on exit gu, gv hold Jᵀλ.
-template <int NU, int NV>
-__global__ void __launch_bounds__(ADJ_THREADS) k_adj_face(const __grid_constant__ Basis<NU, NV> B,
-                                                   const __grid_constant__ Fields F,
-                                                   const __grid_constant__ StageIO S, const AdjIO A) {
-  constexpr int NQ = NU;
-  const int E = F.E, N = F.N;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= E) return;
-  if (err_word(F) != ERR_NONE) return;
-  const int j = e % N, k = e / N;
-  const size_t Eu = (size_t)E;
-  const TimeF tf = time_factors(S);
-  auto hat = [&](int fam, int side, int i, int el) {
-    const double h = A.hat[((fam * 4 + side) * NQ + i) * Eu + el];
-    const double w = B.w[i];
-    return fam == 0 ? F.two_h * w * h : fam == 1 ? F.four_hh * w * h : -w * h;
-  };
-  double gU[NU][NU], gV[NV][NV];
-#pragma unroll
-  for (int b = 0; b < NU; ++b)
-#pragma unroll
-    for (int a = 0; a < NU; ++a) gU[a][b] = -F.four_hh * A.gu[e + Eu * (a + NU * b)];
-#pragma unroll
-  for (int b = 0; b < NV; ++b)
-#pragma unroll
-    for (int a = 0; a < NV; ++a) gV[a][b] = A.gv[e + Eu * (a + NV * b)];
-  gV[0][0] += A.nu[e];                                  // b[0][0] += V[0][0] transposed
-#pragma unroll 1
-  for (int s = 0; s < 4; ++s) {
-    const bool boundary = (s == 0 && j == 0) || (s == 1 && j == N - 1) || (s == 2 && k == 0) || (s == 3 && k == N - 1);
-    double qu[NU], qv[NV], qd[NV];                      // Σ_i P[i][b] t̂(s, i) per trace family
-#pragma unroll
-    for (int b = 0; b < NU; ++b) {
-      qu[b] = 0.0;
-      if (b < NV) { qv[b] = 0.0; qd[b] = 0.0; }
-    }
-#pragma unroll 1
-    for (int i = 0; i < NQ; ++i) {
-      double t[3] = {0.0, 0.0, 0.0};                    // t̂ for du, v, dv
-      if (boundary) {
-        double d[3][3];
-        boundary_partials<NU, NV>(F, tf, s, j, k, e, i, d);
-        const double h3[3] = {hat(0, s, i, e), hat(1, s, i, e), hat(2, s, i, e)};
-#pragma unroll
-        for (int x = 0; x < 3; ++x) t[x] = d[0][x] * h3[0] + d[1][x] * h3[1] + d[2][x] * h3[2];
-      } else {
-        const bool plus = (s == 0 || s == 2);
-        const int nb = s == 0 ? e - 1 : s == 1 ? e + 1 : s == 2 ? e - N : e + N;
-        const int sn = s ^ 1;                           // the neighbour's side of this face
-        size_t fi;
-        const double *c2p_a, *afp_a, *c2m_a, *afm_a, *jc_a;
-        if (s < 2) {
-          fi = (s == 0 ? j : j + 1) + (size_t)(N + 1) * (k + (size_t)N * i);
-          c2p_a = F.hc2; afp_a = F.haf; c2m_a = F.hc2m; afm_a = F.hafm; jc_a = F.hJC;
-        } else {
-          fi = j + (size_t)N * ((s == 2 ? k : k + 1) + (size_t)(N + 1) * i);
-          c2p_a = F.vc2; afp_a = F.vaf; c2m_a = F.vc2m; afm_a = F.vafm; jc_a = F.vJC;
-        }
-        FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);
-        if (!F.one_sided) { cf.c2m = cf.c2p; cf.afm = cf.afp; }
-        const double ho0 = hat(0, s, i, e), ho1 = hat(1, s, i, e), ho2 = hat(2, s, i, e);
-        const double hn0 = hat(0, sn, i, nb), hn1 = hat(1, sn, i, nb), hn2 = hat(2, sn, i, nb);
-        const FaceWeights w = plus ? face_weights(F, cf, ho0, ho1, ho2, hn0, hn1, hn2)
-                                   : face_weights(F, cf, hn0, hn1, hn2, ho0, ho1, ho2);
-        const double th = F.theta, a = F.two_h;
-        const double pen = 0.5 * (cf.c2m + cf.c2p) * F.lu + 0.5 * (cf.afm + cf.afp) * F.lv;
-        const double tv = pen * w.wA + th * w.wP - (1.0 - th) * w.wM;   // ∂/∂vm; ∂/∂vp = -tv
-        // ∂/∂du of the own side: ∂J = ∓a c², ∂G = a θ c² (+) or a (1 - θ) c² (-); dv with α
-        const double kd = plus ? w.wS - th * w.wA : -((1.0 - th) * w.wA + w.wS);
-        t[0] = a * (plus ? cf.c2p : cf.c2m) * kd;
-        t[1] = plus ? -tv : tv;
-        t[2] = a * (plus ? cf.afp : cf.afm) * kd;
-      }
-#pragma unroll
-      for (int b = 0; b < NU; ++b) {
-        const double p = B.P[i][b];
-        qu[b] = fma(p, t[0], qu[b]);
-        if (b < NV) {
-          qv[b] = fma(p, t[1], qv[b]);
-          qd[b] = fma(p, t[2], qd[b]);
-        }
-      }
-    }
-    // trace transposes: B/T sides contract the first index with the end values, L/R the second
-    const bool right = (s == 1 || s == 3);
-#pragma unroll
-    for (int a = 0; a < NU; ++a) {
-      const double sa = (a & 1) && right ? -1.0 : 1.0;  // Er = ±El, E1r = ∓E1l by mode parity
-      const double e1 = right ? -sa * B.E1l[a] : B.E1l[a];
-      const double e0 = right ? sa * B.El[a] : B.El[a];
-#pragma unroll
-      for (int b = 0; b < NU; ++b) {
-        if (s < 2) {
-          gU[a][b] = fma(e1, qu[b], gU[a][b]);
-          if (a < NV && b < NV) gV[a][b] = fma(e0, qv[b], fma(e1, qd[b], gV[a][b]));
-        } else {
-          gU[b][a] = fma(e1, qu[b], gU[b][a]);
-          if (a < NV && b < NV) gV[b][a] = fma(e0, qv[b], fma(e1, qd[b], gV[b][a]));
-        }
-      }
-    }
-  }
-#pragma unroll
-  for (int b = 0; b < NU; ++b)
-#pragma unroll
-    for (int a = 0; a < NU; ++a) A.gu[e + Eu * (a + NU * b)] = gU[a][b];
-#pragma unroll
-  for (int b = 0; b < NV; ++b)
-#pragma unroll
-    for (int a = 0; a < NV; ++a) A.gv[e + Eu * (a + NV * b)] = gV[a][b];
+  for (int x = 0; x < 3; ++x) t[x] = fma(dF1[x], h0, ddv[x] * m);
 }
 
 // Derivatives of the weighted slots r = F1 h0 + q_D h1 + q_F h2 of a physical side point with
-// respect to the coefficients c², α, c, β there (side_point's formulas differentiated; the
-// traces and the data fixed): d[0..3]. With q_D = sgn α dv and q_F = -sgn c² dv,
-//   r = F1 h0 + dv · sgn (α h1 - c² h2).
-__device__ __forceinline__ void boundary_coef_partials(const Fields &F, int s, double c2f, double af, double cf,
-                                                       double bf, double v_fp, double gun, double gvn,
-                                                       double gu_ex, double gv_ex, double v_ex, double sgn,
-                                                       double h0, double h1, double h2, double (&d)[4]) {
+// respect to the coefficients c², α, c, β there (the traces and the data fixed): d[0..3]. With
+// q_D = sgn α dv and q_F = -sgn c² dv, r = F1 h0 + dv · sgn (α h1 - c² h2).
+__device__ __forceinline__ void boundary_coef_partials(const Fields &F, int s, const SideData &p, double h0,
+                                                       double h1, double h2, double (&d)[4]) {
+  const double c2f = p.c2f, af = p.af, cf = p.cf, bf = p.bf, sgn = p.sgn;
   double dF1[4], ddv[4], dv;
   if (F.kind[s] == 3) {
     // wall: F1 = c² gu_ex + α gv_ex, dv = -(κ/c)(c² (gun - gu_ex) + α (gvn - gv_ex))
-    const double kc = F.kap[s] / cf, ru = gun - gu_ex, rv = gvn - gv_ex;
+    const double kc = F.kap[s] / cf, ru = p.gun - p.gu_ex, rv = p.gvn - p.gv_ex;
     const double rw = c2f * ru + af * rv;
     dv = -kc * rw;
-    dF1[0] = gu_ex; dF1[1] = gv_ex; dF1[2] = 0.0; dF1[3] = 0.0;
+    dF1[0] = p.gu_ex; dF1[1] = p.gv_ex; dF1[2] = 0.0; dF1[3] = 0.0;
     ddv[0] = -kc * ru; ddv[1] = -kc * rv; ddv[2] = kc * rw / cf; ddv[3] = 0.0;
   } else {
     // absorbing family: ρ = η (c² (gun - gu_ex) + α (gvn - gv_ex)) + γ c (√(1 - kβv) v - √(1 - kβv_ex) v_ex),
     // F1 = c² gun + α gvn - (η + σγ) ρ, dv = -(γ - ση) ρ / (c √(1 - kβv))
     const double g = F.gam[s], et = F.eta[s], sg = F.sig[s], kb = F.kb[s];
-    const double sqf = sqrt(1.0 - kb * bf * v_fp), sqe = sqrt(1.0 - kb * bf * v_ex);
-    const double dsqf = -kb * v_fp / (2.0 * sqf), dsqe = -kb * v_ex / (2.0 * sqe);   // ∂/∂β
-    const double ru = gun - gu_ex, rv = gvn - gv_ex, rs = sqf * v_fp - sqe * v_ex;
+    const double sqf = sqrt(1.0 - kb * bf * p.v_fp), sqe = sqrt(1.0 - kb * bf * p.v_ex);
+    const double dsqf = -kb * p.v_fp / (2.0 * sqf), dsqe = -kb * p.v_ex / (2.0 * sqe);   // ∂/∂β
+    const double ru = p.gun - p.gu_ex, rv = p.gvn - p.gv_ex, rs = sqf * p.v_fp - sqe * p.v_ex;
     const double rho = et * (c2f * ru + af * rv) + g * cf * rs;
-    const double drho[4] = {et * ru, et * rv, g * rs, g * cf * (v_fp * dsqf - v_ex * dsqe)};
+    const double drho[4] = {et * ru, et * rv, g * rs, g * cf * (p.v_fp * dsqf - p.v_ex * dsqe)};
     const double es = et + sg * g, kd = -(g - sg * et), den = cf * sqf;
-    dF1[0] = gun - es * drho[0]; dF1[1] = gvn - es * drho[1]; dF1[2] = -es * drho[2]; dF1[3] = -es * drho[3];
+    dF1[0] = p.gun - es * drho[0]; dF1[1] = p.gvn - es * drho[1]; dF1[2] = -es * drho[2]; dF1[3] = -es * drho[3];
     dv = kd * rho / den;
     ddv[0] = kd * drho[0] / den;
     ddv[1] = kd * drho[1] / den;
@@ -382,11 +269,15 @@ __device__ __forceinline__ void boundary_coef_partials(const Fields &F, int s, d
   d[3] = fma(dF1[3], h0, ddv[3] * m);
 }
 
-// k_adj_param: for the constant-coefficient kernels (c², α, β constant on each element), the
-// derivative of the stage's weighted output K̄·F(Y) with respect to the element's c² and α
-// (and β through the faces), added to gc2[e], gal[e], gbe[e]; k_adj_mass adds the β-derivative
-// of the mass matrix. With μ = M⁻¹K̄_v, ν = A_e⁻¹K̄_u and the forward ut at Y (all from the
-// adjoint evaluation just made at Y), K1 symmetric:
+// k_adj_face: the trace weights of the element, t̂_x(s, i) = Σ_slots ∂slot/∂x · ŝlot over the
+// element's own slots and (interior faces) the neighbour's slots of the shared point, for its
+// traces x = du, v, dv; then the trace transposes (k_prep's trace4 transposed) into gu, gv. On
+// entry gu holds the volume transpose's b; on exit gu, gv hold Jᵀλ.
+//
+// With PARAMS (the constant-coefficient kernels: c², α, β constant on each element), also the
+// derivative of the stage's weighted output K̄·F(Y) with respect to the element's c² and α (and
+// β through the faces), added to gc2[e], gal[e], gbe[e] (k_adj_mass adds the β-derivative of
+// the mass matrix). With μ = M⁻¹K̄_v, ν = A_e⁻¹K̄_u and the forward ut at Y, K1 symmetric:
 //   volume + u-solve   ∂/∂c² = <A1, V - ut> - (4/h²) <A2, U>,  ∂/∂α = -(4/h²) <A2, V>,
 //                      A1 = K1 ν + ν K1,  A2 = K1 μ + μ K1
 //                      (R ∋ -(4/h²)(c²(K1U + UK1) + α(K1V + VK1)), b ∋ c²(K1V + VK1),
@@ -396,11 +287,15 @@ __device__ __forceinline__ void boundary_coef_partials(const Fields &F, int s, d
 //                      slots and the neighbour's; at a continuous face the shared face value
 //                      enters the own slots (the neighbour adds its own); on a physical side
 //                      c², α, c = √c², β enter the own slots.
-template <int NU, int NV>
-__global__ void __launch_bounds__(ADJ_THREADS) k_adj_param(const __grid_constant__ Basis<NU, NV> B,
-                                                    const __grid_constant__ Fields F,
-                                                    const __grid_constant__ StageIO S, const AdjIO A,
-                                                    double *gc2, double *gal, double *gbe) {
+//
+// The points of a side come in mirrored pairs (i, NQ-1-i): the sums over the points are taken
+// from their sums (even modes) and differences (odd modes), and the transposes of the two
+// opposite sides (B and T, L and R) are applied together (Er = ±El, E1r = ∓E1l by mode parity).
+template <int NU, int NV, bool PARAMS>
+__global__ void __launch_bounds__(ADJ_THREADS) k_adj_face(const __grid_constant__ Basis<NU, NV> B,
+                                                   const __grid_constant__ Fields F,
+                                                   const __grid_constant__ StageIO S, const AdjIO A, double *gc2,
+                                                   double *gal, double *gbe) {
   constexpr int NQ = NU;
   const int E = F.E, N = F.N;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -410,8 +305,8 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_param(const __grid_constant
   const size_t Eu = (size_t)E;
   const TimeF tf = time_factors(S);
   double dc2 = 0.0, dal = 0.0, dbe = 0.0;
-  // ---- volume and u-solve: ν and μ (padded to NU × NU) in registers, U, V, ut streamed
-  {
+  if constexpr (PARAMS) {
+    // ---- volume and u-solve: ν and μ (padded to NU × NU) in registers, U, V, ut streamed
     double Nl[NU][NU], Ml[NU][NU];
 #pragma unroll
     for (int b = 0; b < NU; ++b)
@@ -441,87 +336,173 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_param(const __grid_constant
         dal = fma(-F.four_hh * a2, V, dal);
       }
   }
-  // ---- faces
+  double gU[NU][NU], gV[NV][NV];
+#pragma unroll
+  for (int b = 0; b < NU; ++b)
+#pragma unroll
+    for (int a = 0; a < NU; ++a) gU[a][b] = -F.four_hh * A.gu[e + Eu * (a + NU * b)];
+#pragma unroll
+  for (int b = 0; b < NV; ++b)
+#pragma unroll
+    for (int a = 0; a < NV; ++a) gV[a][b] = A.gv[e + Eu * (a + NV * b)];
+  gV[0][0] += A.nu[e];                                  // b[0][0] += V[0][0] transposed
   const double *tr = F.tr;
   auto T = [&](int fam, int side, int i, int el) { return tr[((fam * 4 + side) * NQ + i) * Eu + el]; };
-  auto hat = [&](int fam, int side, int i, int el) {
-    const double h = A.hat[((fam * 4 + side) * NQ + i) * Eu + el];
-    const double w = B.w[i];
-    return fam == 0 ? F.two_h * w * h : fam == 1 ? F.four_hh * w * h : -w * h;
-  };
-#pragma unroll 1
-  for (int s = 0; s < 4; ++s) {
-    const bool boundary = (s == 0 && j == 0) || (s == 1 && j == N - 1) || (s == 2 && k == 0) || (s == 3 && k == N - 1);
-#pragma unroll 1
-    for (int i = 0; i < NQ; ++i) {
-      const double ho0 = hat(0, s, i, e), ho1 = hat(1, s, i, e), ho2 = hat(2, s, i, e);
-      if (boundary) {
-        const int m = s < 2 ? k : j;
-        const double sgn = (s == 0 || s == 2) ? -1.0 : 1.0;
-        size_t fi;
-        const double *c2a, *afa, *cfa, *bfa;
-        if (s < 2) { fi = (s == 0 ? 0 : N) + (size_t)(N + 1) * (k + (size_t)N * i); c2a = F.hc2; afa = F.haf; cfa = F.hcf; bfa = F.hbf; }
-        else { fi = j + (size_t)N * ((s == 2 ? 0 : N) + (size_t)(N + 1) * i); c2a = F.vc2; afa = F.vaf; cfa = F.vcf; bfa = F.vbf; }
-        const double c2f = c2a[fi], af = afa[fi], cf = cfa[fi], bf = bfa[fi];
-        const double v_fp = T(1, s, i, e);
-        const double gun = sgn * (F.two_h * T(0, s, i, e)), gvn = sgn * (F.two_h * T(2, s, i, e));
-        const double spn = F.bspn[s][m + (size_t)N * i], sp = F.bsp[s][m + (size_t)N * i];
-        const double gu_ex = sgn * (tf.ct * spn - spn), gv_ex = sgn * (-F.omega * tf.st * spn);
-        const double v_ex = -F.omega * tf.st * sp;
+  auto hat = [&](int fam, int side, int i, int el) { return A.hat[((fam * 4 + side) * NQ + i) * Eu + el]; };
+  // t̂ (du, v, dv) at point i of side s, and the point's parameter terms
+  auto point = [&](int s, bool boundary, int i, double (&t)[3]) {
+    const double ho0 = hat(0, s, i, e), ho1 = hat(1, s, i, e), ho2 = hat(2, s, i, e);
+    if (boundary) {
+      const SideData p = side_data(F, tf, s, j, k, e, i, NQ);
+      boundary_trace_partials(F, s, p, ho0, ho1, ho2, t);
+      if constexpr (PARAMS) {
         double d[4];
-        boundary_coef_partials(F, s, c2f, af, cf, bf, v_fp, gun, gvn, gu_ex, gv_ex, v_ex, sgn, ho0, ho1, ho2, d);
-        dc2 += d[0] + d[2] / (2.0 * cf);                  // c = √c²
+        boundary_coef_partials(F, s, p, ho0, ho1, ho2, d);
+        dc2 += d[0] + d[2] / (2.0 * p.cf);              // c = √c²
         dal += d[1];
         dbe += d[3];
-      } else {
-        const bool plus = (s == 0 || s == 2);
-        const int nb = s == 0 ? e - 1 : s == 1 ? e + 1 : s == 2 ? e - N : e + N;
-        const int sn = s ^ 1;
-        const int sm = s < 2 ? 1 : 3, spp = s < 2 ? 0 : 2;
-        const int em = plus ? nb : e, ep = plus ? e : nb;
-        size_t fi;
-        const double *c2p_a, *afp_a, *c2m_a, *afm_a, *jc_a;
-        if (s < 2) {
-          fi = (s == 0 ? j : j + 1) + (size_t)(N + 1) * (k + (size_t)N * i);
-          c2p_a = F.hc2; afp_a = F.haf; c2m_a = F.hc2m; afm_a = F.hafm; jc_a = F.hJC;
+      }
+      return;
+    }
+    const bool plus = (s == 0 || s == 2);
+    const int nb = s == 0 ? e - 1 : s == 1 ? e + 1 : s == 2 ? e - N : e + N;
+    const int sn = s ^ 1;                               // the neighbour's side of this face
+    size_t fi;
+    const double *c2p_a, *afp_a, *c2m_a, *afm_a, *jc_a;
+    if (s < 2) {
+      fi = (s == 0 ? j : j + 1) + (size_t)(N + 1) * (k + (size_t)N * i);
+      c2p_a = F.hc2; afp_a = F.haf; c2m_a = F.hc2m; afm_a = F.hafm; jc_a = F.hJC;
+    } else {
+      fi = j + (size_t)N * ((s == 2 ? k : k + 1) + (size_t)(N + 1) * i);
+      c2p_a = F.vc2; afp_a = F.vaf; c2m_a = F.vc2m; afm_a = F.vafm; jc_a = F.vJC;
+    }
+    FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);
+    const bool os = F.one_sided;
+    if (!os) { cf.c2m = cf.c2p; cf.afm = cf.afp; }
+    const double hn0 = hat(0, sn, i, nb), hn1 = hat(1, sn, i, nb), hn2 = hat(2, sn, i, nb);
+    const FaceWeights w = plus ? face_weights(F, cf, ho0, ho1, ho2, hn0, hn1, hn2)
+                               : face_weights(F, cf, hn0, hn1, hn2, ho0, ho1, ho2);
+    const double th = F.theta, a = F.two_h;
+    const double pen = 0.5 * (cf.c2m + cf.c2p) * F.lu + 0.5 * (cf.afm + cf.afp) * F.lv;
+    const double tv = pen * w.wA + th * w.wP - (1.0 - th) * w.wM;   // ∂/∂vm; ∂/∂vp = -tv
+    // ∂/∂du of the own side: ∂J = ∓a c², ∂G = a θ c² (+) or a (1 - θ) c² (-); dv with α
+    const double kd = plus ? w.wS - th * w.wA : -((1.0 - th) * w.wA + w.wS);
+    t[0] = a * (plus ? cf.c2p : cf.c2m) * kd;
+    t[1] = plus ? -tv : tv;
+    t[2] = a * (plus ? cf.afp : cf.afm) * kd;
+    if constexpr (PARAMS) {
+      const int sm = s < 2 ? 1 : 3, spp = s < 2 ? 0 : 2;
+      const int em = plus ? nb : e, ep = plus ? e : nb;
+      const double vm = T(1, sm, i, em), vp = T(1, spp, i, ep);
+      const double dum = T(0, sm, i, em), dup = T(0, spp, i, ep);
+      const double dvm = T(2, sm, i, em), dvp = T(2, spp, i, ep);
+      // the weights of both roles on one-sided faces, of the own role on continuous ones
+      const FaceWeights wp = os ? w : plus ? face_weights(F, cf, ho0, ho1, ho2, 0.0, 0.0, 0.0)
+                                           : face_weights(F, cf, 0.0, 0.0, 0.0, ho0, ho1, ho2);
+      const double hP1 = plus ? ho1 : os ? hn1 : 0.0, hP2 = plus ? ho2 : os ? hn2 : 0.0;
+      const double hM1 = plus ? (os ? hn1 : 0.0) : ho1, hM2 = plus ? (os ? hn2 : 0.0) : ho2;
+      // which sides' coefficients are the element's: its own side (one-sided), both (continuous)
+      const double dp = (!os || plus) ? 1.0 : 0.0, dm = (!os || !plus) ? 1.0 : 0.0;
+      const double tau = F.tau;
+      const double J = a * (cf.c2m * dum - cf.c2p * dup + cf.afm * dvm - cf.afp * dvp) + cf.K;
+      const double sj = vm - vp;
+      const double dvsp = th * sj - tau * J, dvsm = -(1.0 - th) * sj - tau * J;
+      {
+        const double dJ = a * (dm * dum - dp * dup), dG = a * ((1.0 - th) * dm * dum + th * dp * dup);
+        const double dpen = 0.5 * (dm + dp) * F.lu;
+        dc2 += (dpen * sj - dG) * wp.wA - dJ * wp.wS + dp * dvsp * hP2 - dm * dvsm * hM2;
+      }
+      {
+        const double dJ = a * (dm * dvm - dp * dvp), dG = a * ((1.0 - th) * dm * dvm + th * dp * dvp);
+        const double dpen = 0.5 * (dm + dp) * F.lv;
+        dal += (dpen * sj - dG) * wp.wA - dJ * wp.wS - dp * dvsp * hP1 + dm * dvsm * hM1;
+      }
+    }
+  };
+  // sides in groups of NS: opposite sides together (B and T, then L and R) while the registers
+  // allow, else one at a time
+  constexpr int NS = NU <= 5 ? 2 : 1;
+#pragma unroll 1
+  for (int g0 = 0; g0 < 4; g0 += NS) {
+    double qu[NS][NU], qv[NS][NV], qd[NS][NV];          // Σ_i P[i][b] t̂(s, i) per side and family
+#pragma unroll
+    for (int h = 0; h < NS; ++h) {
+      const int s = g0 + h;
+      const bool boundary = (s == 0 && j == 0) || (s == 1 && j == N - 1) || (s == 2 && k == 0) || (s == 3 && k == N - 1);
+#pragma unroll
+      for (int b = 0; b < NU; ++b) {
+        qu[h][b] = 0.0;
+        if (b < NV) { qv[h][b] = 0.0; qd[h][b] = 0.0; }
+      }
+#pragma unroll 1
+      for (int i = 0; i < (NQ + 1) / 2; ++i) {
+        double t1[3], t2[3];
+        point(s, boundary, i, t1);
+        const bool mid = 2 * i + 1 == NQ;               // the middle point: the odd modes vanish
+        if (!mid) point(s, boundary, NQ - 1 - i, t2);
+#pragma unroll
+        for (int b = 0; b < NU; ++b) {
+          const double p = B.P[i][b];
+          const bool odd = b & 1;
+          if (mid && odd) continue;
+          const double su = mid ? t1[0] : odd ? t1[0] - t2[0] : t1[0] + t2[0];
+          qu[h][b] = fma(p, su, qu[h][b]);
+          if (b < NV) {
+            const double sv = mid ? t1[1] : odd ? t1[1] - t2[1] : t1[1] + t2[1];
+            const double sd = mid ? t1[2] : odd ? t1[2] - t2[2] : t1[2] + t2[2];
+            qv[h][b] = fma(p, sv, qv[h][b]);
+            qd[h][b] = fma(p, sd, qd[h][b]);
+          }
+        }
+      }
+    }
+    // trace transposes: B/T contract the first index with the end values, L/R the second; the
+    // far side's end vectors are Er[a] = (-1)^a El[a], E1r[a] = -(-1)^a E1l[a]
+    const bool tb = g0 < 2;
+    const bool right = NS == 1 && (g0 & 1);
+#pragma unroll
+    for (int a = 0; a < NU; ++a) {
+      const bool odd = a & 1;
+      const double e1 = B.E1l[a], e0 = B.El[a];
+#pragma unroll
+      for (int b = 0; b < NU; ++b) {
+        double cu, cv = 0.0, cd = 0.0;
+        if constexpr (NS == 2) {
+          cu = odd ? qu[0][b] + qu[1][b] : qu[0][b] - qu[1][b];
+          if (b < NV) {
+            cv = odd ? qv[0][b] - qv[1][b] : qv[0][b] + qv[1][b];
+            cd = odd ? qd[0][b] + qd[1][b] : qd[0][b] - qd[1][b];
+          }
         } else {
-          fi = j + (size_t)N * ((s == 2 ? k : k + 1) + (size_t)(N + 1) * i);
-          c2p_a = F.vc2; afp_a = F.vaf; c2m_a = F.vc2m; afm_a = F.vafm; jc_a = F.vJC;
+          const double s1 = right ? (odd ? 1.0 : -1.0) : 1.0, s0 = right ? (odd ? -1.0 : 1.0) : 1.0;
+          cu = s1 * qu[0][b];
+          if (b < NV) {
+            cv = s0 * qv[0][b];
+            cd = s1 * qd[0][b];
+          }
         }
-        FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);
-        const bool os = F.one_sided;
-        if (!os) { cf.c2m = cf.c2p; cf.afm = cf.afp; }
-        const double vm = T(1, sm, i, em), vp = T(1, spp, i, ep);
-        const double dum = T(0, sm, i, em), dup = T(0, spp, i, ep);
-        const double dvm = T(2, sm, i, em), dvp = T(2, spp, i, ep);
-        // weights of both roles; a continuous face counts the own role only
-        const double hn0 = os ? hat(0, sn, i, nb) : 0.0, hn1 = os ? hat(1, sn, i, nb) : 0.0,
-                     hn2 = os ? hat(2, sn, i, nb) : 0.0;
-        const double hP0 = plus ? ho0 : hn0, hP1 = plus ? ho1 : hn1, hP2 = plus ? ho2 : hn2;
-        const double hM0 = plus ? hn0 : ho0, hM1 = plus ? hn1 : ho1, hM2 = plus ? hn2 : ho2;
-        const FaceWeights w = face_weights(F, cf, hP0, hP1, hP2, hM0, hM1, hM2);
-        // which sides' coefficients are the element's: its own side (one-sided), both (continuous)
-        const double dp = (!os || plus) ? 1.0 : 0.0, dm = (!os || !plus) ? 1.0 : 0.0;
-        const double th = F.theta, tau = F.tau, a = F.two_h;
-        const double J = a * (cf.c2m * dum - cf.c2p * dup + cf.afm * dvm - cf.afp * dvp) + cf.K;
-        const double sj = vm - vp;
-        const double dvsp = th * sj - tau * J, dvsm = -(1.0 - th) * sj - tau * J;
-        {
-          const double dJ = a * (dm * dum - dp * dup), dG = a * ((1.0 - th) * dm * dum + th * dp * dup);
-          const double dpen = 0.5 * (dm + dp) * F.lu;
-          dc2 += (dpen * sj - dG) * w.wA - dJ * w.wS + dp * dvsp * hP2 - dm * dvsm * hM2;
-        }
-        {
-          const double dJ = a * (dm * dvm - dp * dvp), dG = a * ((1.0 - th) * dm * dvm + th * dp * dvp);
-          const double dpen = 0.5 * (dm + dp) * F.lv;
-          dal += (dpen * sj - dG) * w.wA - dJ * w.wS - dp * dvsp * hP1 + dm * dvsm * hM1;
+        if (tb) gU[a][b] = fma(e1, cu, gU[a][b]);
+        else gU[b][a] = fma(e1, cu, gU[b][a]);
+        if (a < NV && b < NV) {
+          if (tb) gV[a][b] = fma(e0, cv, fma(e1, cd, gV[a][b]));
+          else gV[b][a] = fma(e0, cv, fma(e1, cd, gV[b][a]));
         }
       }
     }
   }
-  gc2[e] += dc2;
-  gal[e] += dal;
-  gbe[e] += dbe;
+#pragma unroll
+  for (int b = 0; b < NU; ++b)
+#pragma unroll
+    for (int a = 0; a < NU; ++a) A.gu[e + Eu * (a + NU * b)] = gU[a][b];
+#pragma unroll
+  for (int b = 0; b < NV; ++b)
+#pragma unroll
+    for (int a = 0; a < NV; ++a) A.gv[e + Eu * (a + NV * b)] = gV[a][b];
+  if constexpr (PARAMS) {
+    gc2[e] += dc2;
+    gal[e] += dal;
+    gbe[e] += dbe;
+  }
 }
 
 }  // namespace wedg

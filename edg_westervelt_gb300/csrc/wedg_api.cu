@@ -422,13 +422,11 @@ int enqueue_adjoint_core(wedg_ws *ws, const Fields &Fs, const StageIO &S, const 
   Sv.ut = gu;
   ws->L.stage(ws->basis.data(), Fs, Sv, bs, ts, ws->stream);
   ws->L.adj_mass(ws->basis.data(), Fs, S, A, ws->stream);
-  ws->L.adj_face(ws->basis.data(), Fs, S, A, ws->stream);
+  // the faces; with gpar also K̄·∂F/∂p at the state: volume, u-solve and faces (the mass
+  // matrix's β-part is in k_adj_mass)
+  ws->L.adj_face(ws->basis.data(), Fs, S, A, gpar, gpar ? gpar + ws->E : nullptr,
+                 gpar ? gpar + 2 * (size_t)ws->E : nullptr, ws->stream);
   ws->stats.kernel_launches += 6;
-  if (gpar) {
-    // K̄·∂F/∂p at the state: volume, u-solve and faces (the mass matrix's β-part is in k_adj_mass)
-    ws->L.adj_param(ws->basis.data(), Fs, S, A, gpar, gpar + ws->E, gpar + 2 * (size_t)ws->E, ws->stream);
-    ws->stats.kernel_launches += 1;
-  }
   CK(ws, cudaGetLastError());
   return WEDG_OK;
 }

@@ -29,13 +29,14 @@ typedef void (*pack_fn)(const BasisHost &h, void *out);
 
 typedef void (*adj_fn)(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, cudaStream_t st);
 
-typedef void (*adj_param_fn)(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, double *gc2,
-                             double *gal, double *gbe, cudaStream_t st);
+// k_adj_face; with gc2 (and gal, gbe) non-null also the coefficient derivatives
+typedef void (*adj_face_fn)(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, double *gc2,
+                            double *gal, double *gbe, cudaStream_t st);
 
 struct Launchers {
   launch_fn prep = nullptr, stage = nullptr, mass = nullptr;
-  adj_fn adj_hats = nullptr, adj_mass = nullptr, adj_face = nullptr;
-  adj_param_fn adj_param = nullptr;
+  adj_fn adj_hats = nullptr, adj_mass = nullptr;
+  adj_face_fn adj_face = nullptr;
   pack_fn pack = nullptr;
   size_t basis_size = 0;
 };
@@ -104,22 +105,17 @@ void launch_adj_mass(const void *basis, const Fields &F, const StageIO &, const 
                                                                      A);
 }
 template <int NU, int NV>
-void launch_adj_face(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, cudaStream_t st) {
-  k_adj_face<NU, NV><<<(F.E + ADJ_THREADS - 1) / ADJ_THREADS, ADJ_THREADS, 0, st>>>(
-      *static_cast<const Basis<NU, NV> *>(basis), F, S, A);
-}
-
-template <int NU, int NV>
-void launch_adj_param(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, double *gc2, double *gal,
-                      double *gbe, cudaStream_t st) {
-  k_adj_param<NU, NV><<<(F.E + ADJ_THREADS - 1) / ADJ_THREADS, ADJ_THREADS, 0, st>>>(
-      *static_cast<const Basis<NU, NV> *>(basis), F, S, A, gc2, gal, gbe);
+void launch_adj_face(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, double *gc2, double *gal,
+                     double *gbe, cudaStream_t st) {
+  const Basis<NU, NV> &B = *static_cast<const Basis<NU, NV> *>(basis);
+  const int grid = (F.E + ADJ_THREADS - 1) / ADJ_THREADS;
+  if (gc2) k_adj_face<NU, NV, true><<<grid, ADJ_THREADS, 0, st>>>(B, F, S, A, gc2, gal, gbe);
+  else k_adj_face<NU, NV, false><<<grid, ADJ_THREADS, 0, st>>>(B, F, S, A, nullptr, nullptr, nullptr);
 }
 
 template <int NU, int NV>
 Launchers make_launchers(bool fast) {
   Launchers L;
-  L.adj_param = launch_adj_param<NU, NV>;
   L.adj_hats = launch_adj_hats<NU, NV>;
   L.adj_mass = launch_adj_mass<NU, NV>;
   L.adj_face = launch_adj_face<NU, NV>;
