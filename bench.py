@@ -282,6 +282,9 @@ def run_ours(args):
     if args.adjoint:
         print(json.dumps({"adjoint": run_adjoint(torch, args.adjoint_T)}), flush=True)
         return
+    if args.general_only:
+        print(json.dumps({"general": run_general(torch, dev, args.steps, args.warmup)}), flush=True)
+        return
 
     pre, _ = W.precompute(Q, NMESH, coefficients=W.constant_coefficients(**COEF), **KW)
     N, nu, nv, qh = NMESH, pre["qu1"], pre["qv1"], pre["q_high"]
@@ -371,10 +374,11 @@ def run_ours(args):
                "h2d_bytes_per_step": int(uh.nbytes + vh.nbytes), "d2h_bytes_per_step": int(uh.nbytes + vh.nbytes),
                "steps": ke, "api": "Workspace.rk4_steps (wedg_rk4_steps, WEDG_HOST)"}
 
-    batched = config3 = None
+    batched = config3 = general = None
     if world == 1 and not args.no_batched:
         batched = run_batched(torch, dev, max(4, 2 * args.steps), args.warmup)
         config3 = run_config3(torch, dev, args.steps, args.warmup)
+        general = run_general(torch, dev, args.steps, args.warmup)
 
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
@@ -441,6 +445,7 @@ def run_ours(args):
         "kernel_ms": kms,
         "batched": batched,
         "config3": config3,
+        "general": general,
         "zero_state": {"value": world * dof * 4 * zero["steps"] / (zero["ms"] / 1e3),
                        "ms_per_step": zero["ms"] / max(zero["steps"], 1), "cheb_steps_max": zero["cheb"],
                        "stage_ms": zero["prep_ms"] + zero["stage_ms"] + zero["mass_ms"]},
@@ -564,6 +569,60 @@ def device_steps_ms(torch, ws, u, v, t0, dt, steps, warmup):
     return e0.elapsed_time(e1)
 
 
+def run_general(torch, dev, steps, warmup):
+    """The headline workload with smoothly varying coefficients, so that the general kernels run
+    (per-element quadrature coefficients Cw, Aw and the packed inverse stiffness Ainv, the
+    reference's dominant byte stream): c = 1 + 0.1 cos(πx) cos(πy), α = 1e-6 (1 + 0.1 cos(πx)
+    cos(πy)), β = 8 (1 + 0.1 sin(πx) sin(πy)); N = 512, q = 6, the same sides, flux and steep
+    front state. DOF·stage/s, the stage kernels' times and the algorithmic HBM rate."""
+    import ctypes
+    import math
+    import edg_westervelt_gb300 as W
+    from edg_westervelt_gb300 import _lib as L
+    pi = math.pi
+    cc = lambda x, y: np.cos(pi * x) * np.cos(pi * y)
+    ss = lambda x, y: np.sin(pi * x) * np.sin(pi * y)
+    co = W.Coefficients(lambda x, y: 1 + 0.1 * cc(x, y),
+                        lambda x, y: -0.1 * pi * np.sin(pi * x) * np.cos(pi * y),
+                        lambda x, y: -0.1 * pi * np.cos(pi * x) * np.sin(pi * y),
+                        lambda x, y: 1e-6 * (1 + 0.1 * cc(x, y)),
+                        lambda x, y: -1e-7 * pi * np.sin(pi * x) * np.cos(pi * y),
+                        lambda x, y: -1e-7 * pi * np.cos(pi * x) * np.sin(pi * y),
+                        lambda x, y: 8.0 * (1 + 0.1 * ss(x, y)))
+    N = NMESH
+    t0 = time.perf_counter()
+    pre, _ = W.precompute(Q, N, coefficients=co, **KW)
+    ws = W.Workspace(pre, N)
+    setup_s = time.perf_counter() - t0
+    nu, nv, qh = pre["qu1"], pre["qv1"], pre["q_high"]
+    E = N * N
+    us, vs = synthetic_state(N, nu, nv, 0, "front")
+    u = torch.from_numpy(us.reshape(-1, order="F").copy()).to(dev)
+    v = torch.from_numpy(vs.reshape(-1, order="F").copy()).to(dev)
+    dt = (1.0 / N) / (10 * Q * Q)
+    lib = L.lib()
+    lib.wedg_time_kernels(ws._h, 1)
+    lib.wedg_kernel_times(ws._h, None, None, None, None, None, None, 1)
+    ms = device_steps_ms(torch, ws, u, v, T0, dt, steps, warmup)
+    pm, pn, sm, sn = (ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64())
+    mm, mn = ctypes.c_double(), ctypes.c_int64()
+    lib.wedg_kernel_times(ws._h, ctypes.byref(pm), ctypes.byref(pn), ctypes.byref(sm), ctypes.byref(sn),
+                          ctypes.byref(mm), ctypes.byref(mn), 1)
+    lib.wedg_time_kernels(ws._h, 0)
+    kms = {"k_prep": pm.value / max(pn.value, 1), "k_stage": sm.value / max(sn.value, 1),
+           "k_cheb": mm.value / max(mn.value, 1)}
+    stage_ms = sum(kms.values())
+    dof = E * (nu * nu + nv * nv)
+    bytes_stage = alg_bytes_per_element_stage(nu, nv, qh) * E
+    return {"workload": f"general kernels: N={N} q_u=q_v={Q}, source mode, c, alpha, beta varying by 10 % "
+                        "(cos/sin in x, y) around c=1, alpha=1e-6, beta=8; same sides, flux and front state",
+            "value": dof * 4 * steps / (ms / 1e3), "unit": "DOF·stage/s", "ms_per_step": ms / steps,
+            "steps": steps, "fast_path": bool(ws.stats()["fast_path"]), "setup_s": setup_s,
+            "kernel_ms": kms, "stage_alg_gbs": bytes_stage / (stage_ms / 1e3) / 1e9,
+            "note": "timing covers all warm-up and timed steps' kernels; stage_alg_gbs = the reference data "
+                    "model's bytes of one stage over the three stage kernels' mean time"}
+
+
 def run_config3(torch, dev, steps, warmup):
     """Plain method with jumping coefficients, initial-value mode: N = 256, q_u = 5, q_v = 4, c, α, β
     constant on 4 × 4 subsquares from default_rng(3) (c ~ U[0.5, 2], α log-uniform on [1e-6, 1e-3],
@@ -681,6 +740,8 @@ def main():
     ap.add_argument("--profile-only", action="store_true", help="only the main timed run (for ncu)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
     ap.add_argument("--batched-only", action="store_true", help="only the batched-form measurement")
+    ap.add_argument("--general-only", action="store_true",
+                    help="only the general-kernel measurement (varying coefficients; --mesh applies)")
     ap.add_argument("--adjoint", action="store_true", help="only the adjoint-form measurement (one gradient)")
     ap.add_argument("--adjoint-T", type=float, default=0.5, help="final time of the adjoint-form workload")
     args = ap.parse_args()

@@ -779,21 +779,41 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
           for (int b = 0; b < NV; ++b) { const double x = Vb(a, b); tv1[b] = fma(sa, x, tv1[b]); tv2[b] = fma(pa, x, tv2[b]); }
         }
       }
-      // the row at the points: g1[s] = Σ_b tu1[b] P[s][b], ... (independent over s)
+      // the row at the points: g1[s] = Σ_b tu1[b] P[s][b], g2[s] = Σ_b tu2[b] S[s][b], ... from the
+      // even and odd modes: P[m][b] = (-1)^b P[s][b] and S[m][b] = -(-1)^b S[s][b] at the mirror
+      // point m = NQ-1-s, so the point and its mirror are a sum and a difference
       double g1[NQ], g2[NQ], gv1[NQ], gv2[NQ];
 #pragma unroll
-      for (int s2 = 0; s2 < NQ; ++s2) { g1[s2] = 0; g2[s2] = 0; gv1[s2] = 0; gv2[s2] = 0; }
+      for (int s2 = 0; s2 < (NQ + 1) / 2; ++s2) {
+        double pe = 0, po = 0, se = 0, so = 0, qe = 0, qo = 0, te = 0, to = 0;
 #pragma unroll
-      for (int b = 0; b < NU; ++b) {
-#pragma unroll
-        for (int s2 = 0; s2 < NQ; ++s2) {
-          g1[s2] = fma(tu1[b], B.P[s2][b], g1[s2]);
-          g2[s2] = fma(tu2[b], B.S[s2][b], g2[s2]);
-          if (b < NV) {
-            gv1[s2] = fma(tv1[b], B.P[s2][b], gv1[s2]);
-            gv2[s2] = fma(tv2[b], B.S[s2][b], gv2[s2]);
+        for (int b = 0; b < NU; ++b) {
+          const double pb = B.P[s2][b], sb = B.S[s2][b];
+          if (b & 1) {
+            po = fma(tu1[b], pb, po); so = fma(tu2[b], sb, so);
+            if (b < NV) { qo = fma(tv1[b], pb, qo); to = fma(tv2[b], sb, to); }
+          } else {
+            pe = fma(tu1[b], pb, pe); se = fma(tu2[b], sb, se);
+            if (b < NV) { qe = fma(tv1[b], pb, qe); te = fma(tv2[b], sb, te); }
           }
         }
+        g1[s2] = pe + po; g2[s2] = se + so; gv1[s2] = qe + qo; gv2[s2] = te + to;
+        if (2 * s2 + 1 != NQ) {
+          const int m = NQ - 1 - s2;
+          g1[m] = pe - po; g2[m] = so - se; gv1[m] = qe - qo; gv2[m] = to - te;
+        }
+      }
+      // weighted by the coefficients, back to the modes: z1[b] = Σ_s h1[s] P[s][b], ... from the
+      // sums and differences of mirrored points
+      double h1[NQ], h2[NQ], b1[NQ], b2[NQ];
+#pragma unroll
+      for (int s2 = 0; s2 < NQ; ++s2) {
+        const size_t ci = (r + NQ * s2) * Eu + e;
+        const double cw = F.Cw[ci], aw = F.Aw[ci];
+        h1[s2] = fma(aw, gv1[s2], cw * g1[s2]);
+        h2[s2] = fma(aw, gv2[s2], cw * g2[s2]);
+        b1[s2] = cw * gv1[s2];
+        b2[s2] = cw * gv2[s2];
       }
       double z1[NV], z2[NV], y1[NU], y2[NU];
 #pragma unroll
@@ -801,15 +821,25 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
 #pragma unroll
       for (int b = 0; b < NU; ++b) { y1[b] = 0; y2[b] = 0; }
 #pragma unroll
-      for (int s2 = 0; s2 < NQ; ++s2) {
-        const size_t ci = (r + NQ * s2) * Eu + e;
-        const double cw = F.Cw[ci], aw = F.Aw[ci];
-        const double h1 = fma(aw, gv1[s2], cw * g1[s2]), h2 = fma(aw, gv2[s2], cw * g2[s2]);
-        const double b1 = cw * gv1[s2], b2 = cw * gv2[s2];
+      for (int s2 = 0; s2 < (NQ + 1) / 2; ++s2) {
+        const bool mid = 2 * s2 + 1 == NQ;
+        const int m = NQ - 1 - s2;
+        // P-weighted: even modes take the sum, odd the difference; S-weighted: the opposite
+        const double h1s = mid ? h1[s2] : h1[s2] + h1[m], h1d = mid ? 0.0 : h1[s2] - h1[m];
+        const double h2s = mid ? h2[s2] : h2[s2] + h2[m], h2d = mid ? 0.0 : h2[s2] - h2[m];
+        const double b1s = mid ? b1[s2] : b1[s2] + b1[m], b1d = mid ? 0.0 : b1[s2] - b1[m];
+        const double b2s = mid ? b2[s2] : b2[s2] + b2[m], b2d = mid ? 0.0 : b2[s2] - b2[m];
 #pragma unroll
-        for (int b = 0; b < NV; ++b) { z1[b] = fma(h1, B.P[s2][b], z1[b]); z2[b] = fma(h2, B.S[s2][b], z2[b]); }
-#pragma unroll
-        for (int b = 0; b < NU; ++b) { y1[b] = fma(b1, B.P[s2][b], y1[b]); y2[b] = fma(b2, B.S[s2][b], y2[b]); }
+        for (int b = 0; b < NU; ++b) {
+          const double pb = B.P[s2][b], sb = B.S[s2][b];
+          const bool odd = b & 1;
+          if (b < NV) {
+            z1[b] = fma(odd ? h1d : h1s, pb, z1[b]);
+            z2[b] = fma(odd ? h2s : h2d, sb, z2[b]);
+          }
+          y1[b] = fma(odd ? b1d : b1s, pb, y1[b]);
+          y2[b] = fma(odd ? b2s : b2d, sb, y2[b]);
+        }
       }
 #pragma unroll
       for (int b = 0; b < NV; ++b) { z1[b] *= -four_hh; z2[b] *= -four_hh; }
@@ -941,18 +971,39 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
     double *X = &Ub(0, 0), *bv = &bb(0, 0);       // UT and b as vectors a + NU c
 #pragma unroll 1
     for (int i = 0; i < n; ++i) X[i * BT] = 0.0;
+    // two columns jj, jj + 1 per pass: one read-modify-write of X[i] for both, twice the
+    // independent loads of Ainv in flight
 #pragma unroll 1
-    for (int jj = 0; jj < n; ++jj) {
-      const double bj = bv[jj * BT];
-      const double *Ai = F.Ainv + (size_t)(jj * (jj + 1) / 2) * Eu + e;
-      double s = 0;
+    for (int jj = 0; jj + 1 < n; jj += 2) {
+      const double bj = bv[jj * BT], bk = bv[(jj + 1) * BT];
+      const double *Aj = F.Ainv + (size_t)(jj * (jj + 1) / 2) * Eu + e;
+      const double *Ak = Aj + (size_t)(jj + 1) * Eu;
+      double sj = 0, sk = 0;
 #pragma unroll 4
       for (int i = 0; i < jj; ++i) {
-        const double a = Ai[(size_t)i * Eu];
-        X[i * BT] = fma(a, bj, X[i * BT]);
-        s = fma(a, bv[i * BT], s);
+        const double a = Aj[(size_t)i * Eu], c = Ak[(size_t)i * Eu];
+        const double bi = bv[i * BT];
+        X[i * BT] = fma(c, bk, fma(a, bj, X[i * BT]));
+        sj = fma(a, bi, sj);
+        sk = fma(c, bi, sk);
       }
-      X[jj * BT] = fma(Ai[(size_t)jj * Eu], bj, X[jj * BT] + s);
+      // the 2 × 2 corner: (jj, jj), (jj, jj + 1), (jj + 1, jj + 1)
+      const double ajj = Aj[(size_t)jj * Eu], ajk = Ak[(size_t)jj * Eu], akk = Ak[(size_t)(jj + 1) * Eu];
+      X[jj * BT] = fma(ajk, bk, fma(ajj, bj, X[jj * BT] + sj));
+      X[(jj + 1) * BT] = fma(akk, bk, fma(ajk, bj, X[(jj + 1) * BT] + sk));
+    }
+    if constexpr ((n & 1) != 0) {
+      const int jj = n - 1;
+      const double bj = bv[jj * BT];
+      const double *Aj = F.Ainv + (size_t)(jj * (jj + 1) / 2) * Eu + e;
+      double sj = 0;
+#pragma unroll 4
+      for (int i = 0; i < jj; ++i) {
+        const double a = Aj[(size_t)i * Eu];
+        X[i * BT] = fma(a, bj, X[i * BT]);
+        sj = fma(a, bv[i * BT], sj);
+      }
+      X[jj * BT] = fma(Aj[(size_t)jj * Eu], bj, X[jj * BT] + sj);
     }
   }
 
