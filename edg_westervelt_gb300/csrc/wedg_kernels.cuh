@@ -979,7 +979,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
       const double *Aj = F.Ainv + (size_t)(jj * (jj + 1) / 2) * Eu + e;
       const double *Ak = Aj + (size_t)(jj + 1) * Eu;
       double sj = 0, sk = 0;
-#pragma unroll 4
+#pragma unroll 8
       for (int i = 0; i < jj; ++i) {
         const double a = Aj[(size_t)i * Eu], c = Ak[(size_t)i * Eu];
         const double bi = bv[i * BT];

@@ -192,3 +192,51 @@ def test_reverse_sweep_kept_stage_data(gpu, solver):
         assert np.abs(a - b).max() <= 1e-10 * scale
         assert np.array_equal(b, c)
     assert launches[1 << 40] < launches[0]
+
+
+def test_misfit_gradient_against_oracle_differences(gpu):
+    """The GPU adjoint's misfit gradient against central differences of the misfit computed
+    by the oracle (the C restatement of the reference's RHS and RK4, run on the CPU): the
+    gradient is anchored on the reference's algorithm, not only on the GPU forward."""
+    from oracle.precompute import precompute as oracle_precompute
+    from oracle.rhs import OracleWorkspace
+    from edg_westervelt_gb300.solver import _locate, _vrow
+    rng = np.random.default_rng(46)
+    q, N, T = 2, 8, 0.06
+    c2 = rng.uniform(0.8, 1.5, (2, 2))
+    al = 10 ** rng.uniform(-4, -3, (2, 2))
+    be = rng.uniform(0.5, 3.0, (2, 2))
+    g = (np.arange(4) + 0.5) / 4
+    receivers = [(x, y) for y in g for x in g]
+    u_obs = 1e-4 * rng.standard_normal(len(receivers))
+    src = dict(x0=(0.4, 0.55), r0=0.15, omega=12 * math.pi, Ts=0.5)
+    kw = dict(flux="upwind", mixed=False, boundary="absorbing_2beta")
+    J0, grad = W.misfit_gradient(q, N, T, c2, al, be, receivers, u_obs, every=7, source=W.GaussianSource(**src),
+                                 **kw)
+
+    def J_oracle(c2_, al_, be_):
+        pre, _ = oracle_precompute(q, N, mode="source", coefficients=W.piecewise_coefficients(c2_, al_, be_),
+                                   source=oc.GaussianSource(**src), **kw)
+        nu, nv = pre["qu1"], pre["qv1"]
+        dt = (1.0 / N) / (10 * q * q)
+        nsteps = int(round(T / dt))
+        dt = T / nsteps
+        u = np.zeros((N, N, nu, nu), order="F")
+        v = np.zeros((N, N, nv, nv), order="F")
+        OracleWorkspace(pre).rk4_steps(u, v, 0.0, dt, nsteps)
+        J = 0.0
+        for (xr, yr), obs in zip(receivers, u_obs):
+            kr, xi = _locate(xr, N)
+            jr, eta = _locate(yr, N)
+            J += 0.5 * (float(_vrow(eta, nu) @ u[jr - 1, kr - 1] @ _vrow(xi, nu)) - obs) ** 2
+        return J
+
+    assert abs(J_oracle(c2, al, be) - J0) <= 1e-10 * J0
+    base = {"c2": c2, "alpha": al, "beta": be}
+    for name in ("c2", "alpha", "beta"):
+        d = {k: (rng.standard_normal((2, 2)) * base[k] if k == name else np.zeros((2, 2))) for k in base}
+        eps = 1e-4 if name == "alpha" else 1e-6
+        fd = (J_oracle(c2 + eps * d["c2"], al + eps * d["alpha"], be + eps * d["beta"]) -
+              J_oracle(c2 - eps * d["c2"], al - eps * d["alpha"], be - eps * d["beta"])) / (2 * eps)
+        ad = float(np.sum(grad[name] * d[name]))
+        assert abs(fd - ad) <= 1e-5 * abs(fd), (name, fd, ad)
