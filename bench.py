@@ -524,6 +524,21 @@ def run_batched(torch, dev, steps, warmup):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     done, fin, _ = batch.rk4_steps(us, vs, t, dts, steps)
+    tb_default = time.perf_counter() - t0
+    advance(steps)
+    assert all(d == steps for d in done) and all(fin)
+    # the autotuner: launch shapes per bucket of degrees, on copies of the present states
+    t0 = time.perf_counter()
+    batch.autotune(us, vs, t, dts, steps=2)
+    t_tune = time.perf_counter() - t0
+    shapes = {}
+    for w in wss:
+        shapes[f"q_u={w.nu - 1},q_v={w.nv - 1}"] = list(w.launch_shape)
+    batch.rk4_steps(us, vs, t, dts, 1)                            # captures the tuned graph
+    advance(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    done, fin, _ = batch.rk4_steps(us, vs, t, dts, steps)
     tb = time.perf_counter() - t0
     advance(steps)
     assert all(d == steps for d in done) and all(fin)
@@ -542,6 +557,10 @@ def run_batched(torch, dev, steps, warmup):
             "value": vb, "unit": "DOF·stage/s", "ms_per_step": tb / steps * 1e3,
             "plain_loop_value": vp, "plain_loop_ms_per_step": tp / steps * 1e3, "speedup_vs_plain_loop": vb / vp,
             "setup_s": t_setup,
+            "autotune": {"default_ms_per_step": tb_default / steps * 1e3, "tuned_ms_per_step": tb / steps * 1e3,
+                         "tune_s": t_tune, "shapes": shapes,
+                         "note": "threads per block of k_prep and of the mass solves, per bucket of degrees "
+                                 "(Batch.autotune); value and ms_per_step are the tuned run's"},
             "timing": "host clock around each call (each call returns synchronised); states resident on the GPU",
             "batched": "Batch.rk4_steps: one CUDA graph of one RK4 step of every instance, replayed per step",
             "plain_loop": "Workspace.rk4_steps for each instance in turn"}

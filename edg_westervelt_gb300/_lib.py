@@ -126,6 +126,10 @@ def lib():
                                            ctypes.c_int64, _D, _D, _I64, _I64, ctypes.c_int]
     L.wedg_rk4_adjoint_reverse.argtypes = [vp, _D, _D, _D, _D, _D, _D, _D, ctypes.c_int]
     L.wedg_set_adjoint_memory.argtypes = [vp, ctypes.c_int64]
+    L.wedg_set_launch_shape.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.wedg_get_launch_shape.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.wedg_autotune.argtypes = [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int64, _D]
+    L.wedg_batch_autotune.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), _D, _D, ctypes.c_int64, _D]
     L.wedg_norms.argtypes = [ctypes.POINTER(NormArgs), _D]
     L.wedg_run_source.argtypes = [vp, _D, _D, _I64, _I64, ctypes.c_int, ctypes.POINTER(SourceRun), _I64,
                                   ctypes.POINTER(ctypes.c_int)]

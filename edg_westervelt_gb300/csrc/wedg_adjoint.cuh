@@ -97,14 +97,14 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
   constexpr int QH = T::QH, U = T::U, NE = T::NE, J = T::J;
   __shared__ double sh[T::TPB * T::SLOT];
   __shared__ double Phs[QH * NV], PhWs[QH * NV];
-  for (int i = threadIdx.x; i < QH * NV; i += CHEB_THREADS) {
+  for (int i = threadIdx.x; i < QH * NV; i += blockDim.x) {
     Phs[i] = B.Ph[i / NV][i % NV];
     PhWs[i] = B.PhW[i / NV][i % NV];
   }
   __syncthreads();
   TeamPos tp;
   if (!team_pos<NU, NV>(tp)) return;
-  const int e = blockIdx.x * T::TPB + tp.slot;
+  const int e = blockIdx.x * ((int)(blockDim.x >> 5) * T::TPW) + tp.slot;
   if (e >= F.E) return;
   if (err_word(F) != ERR_NONE) return;
   const int u = tp.u;

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -63,6 +64,11 @@ __global__ void k_lincomb(size_t n, double *out, double a, const double *x, doub
   }
 }
 
+// The candidates of the autotuners, tried one coordinate at a time (k_prep's block, then the
+// mass solves'); a candidate replaces the best so far only when it is faster by more than 2 %
+const int kTuneThreads[3] = {32, 64, 128};
+constexpr double kTuneGain = 0.98;
+
 Launchers get_launchers(int nu, int nv, bool fast) {
   switch (nu) {
     case 2: return launchers_q1(nv, fast);
@@ -96,6 +102,11 @@ struct wedg_ws {
   double *su = nullptr, *sv = nullptr, *accu = nullptr, *accv = nullptr;
   long long *steps_done = nullptr;
   int parity = 0;   // bin-count buffer of the next stage
+  // launch shapes (set by wedg_set_launch_shape or the autotuners): threads per block of k_prep
+  // (one element per thread) and of the mass solves (teams of threads per element); shape_gen
+  // counts the changes, so that a captured batch graph is captured again after one
+  int prep_threads = 128, mass_threads = CHEB_THREADS;
+  int64_t shape_gen = 0;
   // adjoint scratch (allocated on first use): μ, ν, -(h²/4)ν, forward ut and vt, slot weights
   double *adj_mu = nullptr, *adj_nu = nullptr, *adj_nus = nullptr, *adj_ut = nullptr, *adj_vt = nullptr;
   double *adj_hat = nullptr;
@@ -277,7 +288,7 @@ void drain_events(wedg_ws *ws) {
 // enqueue the three kernels of one stage (on the workspace's Fields, or on Fo)
 int enqueue_stage(wedg_ws *ws, const StageIO &S, const Fields *Fo = nullptr) {
   const Fields &F = Fo ? *Fo : ws->F;
-  const int tp = 128, bp = (ws->E + tp - 1) / tp;
+  const int tp = ws->prep_threads, bp = (ws->E + tp - 1) / tp;
   const int ts = stage_threads(ws->nu, ws->nv, ws->fast), bs = (ws->E + ts - 1) / ts;
   const int bm = 1;   // the mass kernels size their own grid
   StageIO Sp = S;
@@ -292,7 +303,7 @@ int enqueue_stage(wedg_ws *ws, const StageIO &S, const Fields *Fo = nullptr) {
   if (ws->timing) cudaEventRecord(e1, ws->stream);
   ws->L.stage(ws->basis.data(), F, Sp, bs, ts, ws->stream);
   if (ws->timing) cudaEventRecord(e2, ws->stream);
-  ws->L.mass(ws->basis.data(), F, Sp, bm, CHEB_THREADS, ws->stream);
+  ws->L.mass(ws->basis.data(), F, Sp, bm, ws->mass_threads, ws->stream);
   if (ws->timing) {
     cudaEventRecord(e3, ws->stream);
     ws->ev_pending.push_back({e0, e1, e2, e3});
@@ -403,7 +414,7 @@ int enqueue_adjoint_core(wedg_ws *ws, const Fields &Fs, const StageIO &S, const 
   StageIO Sm = S;
   Sm.mode = OUT_RHS;
   Sm.vt = ws->adj_mu;
-  ws->L.mass(ws->basis.data(), Fm, Sm, 1, CHEB_THREADS, ws->stream);
+  ws->L.mass(ws->basis.data(), Fm, Sm, 1, ws->mass_threads, ws->stream);
   // ν = A_e⁻¹ λ_u
   StageIO Su = S;
   Su.mode = OUT_ADJ_USOLVE;
@@ -565,6 +576,7 @@ struct wedg_batch {
   // what the captured graph was made for
   std::vector<double *> gu, gv;
   std::vector<double> gdt;
+  std::vector<int64_t> gshape;   // the instances' shape_gen
   int gstop = -1;
   // per instance: device factor table of 2 chunks (the kernels index it by step mod 2 chunks)
   std::vector<double *> d_tf;
@@ -949,7 +961,8 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
   }
   // ---- the graph of one step of every instance, captured again when its key changed
   bool same = b->exec && b->gstop == (stop_nonfinite ? 1 : 0);
-  for (int i = 0; i < n && same; ++i) same = b->gu[i] == u_dev[i] && b->gv[i] == v_dev[i] && b->gdt[i] == dt[i];
+  for (int i = 0; i < n && same; ++i)
+    same = b->gu[i] == u_dev[i] && b->gv[i] == v_dev[i] && b->gdt[i] == dt[i] && b->gshape[i] == b->ws[i]->shape_gen;
   if (!same) {
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
@@ -982,6 +995,8 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
     b->gu.assign(u_dev, u_dev + n);
     b->gv.assign(v_dev, v_dev + n);
     b->gdt.assign(dt, dt + n);
+    b->gshape.resize(n);
+    for (int i = 0; i < n; ++i) b->gshape[i] = b->ws[i]->shape_gen;
     b->gstop = stop_nonfinite ? 1 : 0;
   }
   // ---- the steps, one chunk of factor tables at a time (double-buffered, host and device)
@@ -1015,6 +1030,66 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
     if (rc != WEDG_OK && first == WEDG_OK) first = rc;
   }
   return first;
+}
+
+int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_dev, const double *t0,
+                        const double *dt, int64_t steps, double *best_ms) {
+  if (!b || !u_dev || !v_dev || !t0 || !dt || steps < 1) return WEDG_ERR_ARGUMENT;
+  const int n = (int)b->ws.size();
+  std::vector<double *> su(n), sv(n);
+  std::vector<double> t1(n);
+  for (int i = 0; i < n; ++i) {
+    if (!u_dev[i] || !v_dev[i]) return WEDG_ERR_ARGUMENT;
+    su[i] = b->ws[i]->d_u;
+    sv[i] = b->ws[i]->d_v;
+    t1[i] = t0[i] + dt[i];
+  }
+  // buckets of instances with the same degrees (the same kernels)
+  std::vector<std::pair<int, int>> keys;
+  std::vector<std::vector<int>> bucket;
+  for (int i = 0; i < n; ++i) {
+    const std::pair<int, int> key(b->ws[i]->nu, b->ws[i]->nv);
+    size_t k = 0;
+    while (k < keys.size() && keys[k] != key) ++k;
+    if (k == keys.size()) { keys.push_back(key); bucket.emplace_back(); }
+    bucket[k].push_back(i);
+  }
+  // steps steps of the batch from copies of the states, after one untimed step (which captures
+  // the graph), with the present shapes
+  auto trial = [&](double &ms) -> int {
+    for (int i = 0; i < n; ++i) {
+      wedg_ws *w = b->ws[i];
+      const size_t bU = sizeof(double) * w->E * w->nu * w->nu, bV = sizeof(double) * w->E * w->nv * w->nv;
+      cudaError_t e = cudaMemcpyAsync(su[i], u_dev[i], bU, cudaMemcpyDeviceToDevice, w->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(sv[i], v_dev[i], bV, cudaMemcpyDeviceToDevice, w->stream);
+      if (e != cudaSuccess) return cuda_fail(w, e, "wedg_batch_autotune");
+    }
+    int rc = wedg_batch_rk4_steps(b, su.data(), sv.data(), t0, dt, 1, 0, nullptr, nullptr, nullptr);
+    if (rc != WEDG_OK && rc != WEDG_WARN_CG_NOT_CONVERGED) return rc;
+    const auto c0 = std::chrono::steady_clock::now();
+    rc = wedg_batch_rk4_steps(b, su.data(), sv.data(), t1.data(), dt, steps, 0, nullptr, nullptr, nullptr);
+    ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c0).count();
+    return (rc == WEDG_WARN_CG_NOT_CONVERGED) ? WEDG_OK : rc;
+  };
+  double best = 0;
+  int rc = trial(best);
+  for (size_t k = 0; k < keys.size() && rc == WEDG_OK; ++k) {
+    const std::vector<int> &ids = bucket[k];
+    int bp = b->ws[ids[0]]->prep_threads, bm = b->ws[ids[0]]->mass_threads;
+    for (int c = 0; c < 2 && rc == WEDG_OK; ++c)
+      for (int q = 0; q < 3 && rc == WEDG_OK; ++q) {
+        const int p = c == 0 ? kTuneThreads[q] : bp, m = c == 0 ? bm : kTuneThreads[q];
+        if (p == bp && m == bm) continue;
+        for (int i : ids) wedg_set_launch_shape(b->ws[i], p, m);
+        double ms = 0;
+        rc = trial(ms);
+        if (rc == WEDG_OK && ms < kTuneGain * best) { best = ms; bp = p; bm = m; }
+      }
+    for (int i : ids) wedg_set_launch_shape(b->ws[i], bp, bm);
+  }
+  if (rc != WEDG_OK) return rc;
+  if (best_ms) *best_ms = best / steps;
+  return WEDG_OK;
 }
 
 int wedg_run_source(wedg_ws *ws, double *u, double *v, const int64_t u_shape[4], const int64_t v_shape[4],
@@ -1365,6 +1440,71 @@ int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam
     CK(ws, cudaMemcpy(g_beta, ws->rk_par + 2 * ws->E, sizeof(double) * ws->E, out));
   }
   return rc;
+}
+
+int wedg_set_launch_shape(wedg_ws *ws, int prep_threads, int mass_threads) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  auto ok = [](int t) { return t >= 32 && t <= CHEB_THREADS && t % 32 == 0; };
+  if (!ok(prep_threads) || !ok(mass_threads))
+    return argument_error(ws, "launch shapes are 32, 64, 96 or 128 threads per block");
+  if (prep_threads != ws->prep_threads || mass_threads != ws->mass_threads) {
+    ws->prep_threads = prep_threads;
+    ws->mass_threads = mass_threads;
+    ++ws->shape_gen;
+  }
+  return WEDG_OK;
+}
+
+int wedg_get_launch_shape(const wedg_ws *ws, int *prep_threads, int *mass_threads) {
+  if (!ws) return WEDG_ERR_ARGUMENT;
+  if (prep_threads) *prep_threads = ws->prep_threads;
+  if (mass_threads) *mass_threads = ws->mass_threads;
+  return WEDG_OK;
+}
+
+int wedg_autotune(wedg_ws *ws, const double *u_dev, const double *v_dev, double t0, double dt, int64_t steps,
+                  double *best_ms) {
+  if (!ws || !u_dev || !v_dev || steps < 1) return WEDG_ERR_ARGUMENT;
+  const size_t bU = sizeof(double) * ws->E * ws->nu * ws->nu, bV = sizeof(double) * ws->E * ws->nv * ws->nv;
+  cudaEvent_t e0 = take_event(ws), e1 = take_event(ws);
+  // steps RK4 steps from copies of the state (in the workspace's own state buffers), after one
+  // untimed step, with the shapes (p, m)
+  auto trial = [&](int p, int m, double &ms) -> int {
+    int rc = wedg_set_launch_shape(ws, p, m);
+    if (rc) return rc;
+    CK(ws, cudaMemcpyAsync(ws->d_u, u_dev, bU, cudaMemcpyDeviceToDevice, ws->stream));
+    CK(ws, cudaMemcpyAsync(ws->d_v, v_dev, bV, cudaMemcpyDeviceToDevice, ws->stream));
+    if ((rc = reset_flags(ws)) || (rc = enqueue_rk4(ws, ws->d_u, ws->d_v, t0, dt, 0))) return rc;
+    CK(ws, cudaEventRecord(e0, ws->stream));
+    double t = t0 + dt;
+    for (int64_t it = 0; it < steps; ++it, t += dt)
+      if ((rc = enqueue_rk4(ws, ws->d_u, ws->d_v, t, dt, 0))) return rc;
+    CK(ws, cudaEventRecord(e1, ws->stream));
+    CK(ws, cudaStreamSynchronize(ws->stream));
+    rc = collect(ws);
+    if (rc != WEDG_OK && rc != WEDG_WARN_CG_NOT_CONVERGED) return rc;
+    float f = 0;
+    CK(ws, cudaEventElapsedTime(&f, e0, e1));
+    ms = f;
+    return WEDG_OK;
+  };
+  int bp = ws->prep_threads, bm = ws->mass_threads;
+  double best = 0;
+  int rc = trial(bp, bm, best);
+  for (int c = 0; c < 2 && rc == WEDG_OK; ++c)
+    for (int k = 0; k < 3 && rc == WEDG_OK; ++k) {
+      const int p = c == 0 ? kTuneThreads[k] : bp, m = c == 0 ? bm : kTuneThreads[k];
+      if (p == bp && m == bm) continue;
+      double ms = 0;
+      rc = trial(p, m, ms);
+      if (rc == WEDG_OK && ms < kTuneGain * best) { best = ms; bp = p; bm = m; }
+    }
+  ws->ev_pool.push_back(e0);
+  ws->ev_pool.push_back(e1);
+  if (rc != WEDG_OK) return rc;
+  wedg_set_launch_shape(ws, bp, bm);
+  if (best_ms) *best_ms = best / steps;
+  return WEDG_OK;
 }
 
 int wedg_set_adjoint_memory(wedg_ws *ws, int64_t bytes) {

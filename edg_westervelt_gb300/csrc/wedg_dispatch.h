@@ -79,17 +79,18 @@ void launch_stage(const void *basis, const Fields &F, const StageIO &S, int bloc
   k_stage<NU, NV, FAST><<<blocks, threads, smem, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S);
 }
 
-// The mass solve: k_cheb or k_cg, a team of threads per element (static shared memory; the
-// grid follows from F.E, `blocks` only says whether to launch)
+// The mass solve: k_cheb or k_cg, a team of threads per element (static shared memory sized
+// for CHEB_THREADS). `threads` (32, 64, 96 or 128) sets the warps of a block and with them its
+// elements; the grid follows from F.E, `blocks` only says whether to launch.
 template <int NU, int NV>
 void launch_mass(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads, cudaStream_t st) {
   if (blocks <= 0) return;
-  (void)threads;
   const Basis<NU, NV> &B = *static_cast<const Basis<NU, NV> *>(basis);
-  constexpr int tpb = ChebTeam<NU, NV>::TPB;
+  threads = (threads >= 32 && threads <= CHEB_THREADS && threads % 32 == 0) ? threads : CHEB_THREADS;
+  const int tpb = (threads / 32) * ChebTeam<NU, NV>::TPW;
   const int grid = (F.E + tpb - 1) / tpb;
-  if (F.cg) k_cg<NU, NV><<<grid, CHEB_THREADS, 0, st>>>(B, F, S);
-  else k_cheb<NU, NV><<<grid, CHEB_THREADS, 0, st>>>(B, F, S);
+  if (F.cg) k_cg<NU, NV><<<grid, threads, 0, st>>>(B, F, S);
+  else k_cheb<NU, NV><<<grid, threads, 0, st>>>(B, F, S);
 }
 
 // The adjoint kernels (wedg_adjoint.cuh): element grids of 128 threads, the mass term on the team grid

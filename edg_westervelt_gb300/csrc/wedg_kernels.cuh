@@ -1176,7 +1176,7 @@ __device__ __forceinline__ void team_K(const Basis<NU, NV> &B, const Fields &F, 
   __shared__ double sh[T::TPB * T::SLOT];                                                       \
   __shared__ double Phs[T::QH * NV], PhWs[T::QH * NV];                                          \
   __shared__ int pref[NBIN];                                                                    \
-  for (int i = threadIdx.x; i < T::QH * NV; i += CHEB_THREADS) {                               \
+  for (int i = threadIdx.x; i < T::QH * NV; i += blockDim.x) {                                 \
     Phs[i] = B.Ph[i / NV][i % NV];                                                              \
     PhWs[i] = B.PhW[i / NV][i % NV];                                                            \
   }                                                                                             \
@@ -1187,7 +1187,7 @@ __device__ __forceinline__ void team_K(const Basis<NU, NV> &B, const Fields &F, 
   __syncthreads();                                                                              \
   TeamPos tp;                                                                                   \
   if (!team_pos<NU, NV>(tp)) return;                                                            \
-  const int g = blockIdx.x * T::TPB + tp.slot;                                                  \
+  const int g = blockIdx.x * ((int)(blockDim.x >> 5) * T::TPW) + tp.slot;                      \
   if (g >= F.E) return;                                                                         \
   if (err_word(F) != ERR_NONE) return;                                                          \
   const int u = tp.u;                                                                           \

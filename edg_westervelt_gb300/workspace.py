@@ -244,6 +244,28 @@ class Workspace:
         self._check(rc)
         return uT, vT
 
+    @property
+    def launch_shape(self):
+        """(k_prep threads per block, mass-solve threads per block) (wedg_get_launch_shape)."""
+        p, m = ctypes.c_int(), ctypes.c_int()
+        self._check(L.lib().wedg_get_launch_shape(self._h, ctypes.byref(p), ctypes.byref(m)))
+        return p.value, m.value
+
+    def set_launch_shape(self, prep_threads, mass_threads):
+        """wedg_set_launch_shape: 32, 64, 96 or 128 threads per block each; results do not
+        depend on them."""
+        self._check(L.lib().wedg_set_launch_shape(self._h, int(prep_threads), int(mass_threads)))
+
+    def autotune(self, u, v, t0, dt, steps=4):
+        """wedg_autotune on the CUDA state tensors (u, v), which are left unchanged: keeps the
+        fastest launch shape; returns the best milliseconds per RK4 step."""
+        if not (_is_device(u) and _is_device(v)):
+            raise TypeError("autotune takes CUDA tensors")
+        best = ctypes.c_double(0.0)
+        self._check(L.lib().wedg_autotune(self._h, ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(v.data_ptr()),
+                                          float(t0), float(dt), int(steps), ctypes.byref(best)))
+        return best.value
+
     def set_adjoint_memory(self, nbytes):
         """wedg_set_adjoint_memory: device bytes the reverse sweep may use to keep the forward
         data of one checkpoint segment's stages (negative: half the free memory; 0: never)."""
@@ -378,6 +400,25 @@ class Batch:
         for i, w in enumerate(self.ws):
             w._check(st[i])
         return [int(x) for x in done], [bool(x) for x in fin], [int(x) for x in st]
+
+    def autotune(self, us, vs, t0s, dts, steps=3):
+        """wedg_batch_autotune: the launch shapes of every bucket of instances with the same
+        degrees, against the time of the whole batch's step from copies of the states (left
+        unchanged). Returns the best milliseconds per batch step."""
+        n = len(self.ws)
+        if not (len(us) == len(vs) == len(t0s) == len(dts) == n):
+            raise ValueError("one state, t0 and dt per instance")
+        pu = (ctypes.c_void_p * n)(*[u.data_ptr() for u in us])
+        pv = (ctypes.c_void_p * n)(*[v.data_ptr() for v in vs])
+        t0 = np.array(t0s, dtype=np.float64)
+        dt = np.array(dts, dtype=np.float64)
+        best = ctypes.c_double(0.0)
+        rc = L.lib().wedg_batch_autotune(self._h, pu, pv, _ptr(t0), _ptr(dt), int(steps), ctypes.byref(best))
+        if rc != L.WEDG_OK:
+            for w in self.ws:
+                w._check(rc)
+            raise RuntimeError(f"wedg_batch_autotune failed: {L.lib().wedg_status_string(rc).decode()}")
+        return best.value
 
 
 def edg_rhs_(ws, u, v, t, N, h, pre):

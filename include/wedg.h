@@ -220,6 +220,20 @@ int wedg_rk4_adjoint_forward(wedg_ws *ws, const double *u0, const double *v0, do
 int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam_v, double *gu, double *gv,
                              double *g_c2, double *g_alpha, double *g_beta, int where);
 
+/* Launch shapes: threads per block of k_prep (one element per thread) and of the mass solves
+ * (a team of threads per element, so the block's warps set its elements): 32, 64, 96 or 128
+ * each, 128 by default. Results do not depend on them (every element's arithmetic is its own);
+ * only the time does. */
+int wedg_set_launch_shape(wedg_ws *ws, int prep_threads, int mass_threads);
+int wedg_get_launch_shape(const wedg_ws *ws, int *prep_threads, int *mass_threads);
+
+/* Autotuner of the launch shapes: times `steps` RK4 steps (after one untimed step) from copies
+ * of the device state (u_dev, v_dev; left unchanged) for 32, 64 and 128 threads per block of
+ * k_prep, then of the mass solves, and keeps the fastest (a candidate must gain 2 %). Returns
+ * the best time per step in *best_ms (may be NULL). */
+int wedg_autotune(wedg_ws *ws, const double *u_dev, const double *v_dev, double t0, double dt, int64_t steps,
+                  double *best_ms);
+
 /* Device memory the reverse sweep may use to keep, for every stage of one checkpoint segment,
  * the stage's forward data (its right-hand side, traces and mass-solve data) while it
  * recomputes the segment: with it the adjoint of a stage needs no second forward evaluation.
@@ -250,6 +264,14 @@ void wedg_batch_destroy(wedg_batch *b);
 int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_dev, const double *t0,
                          const double *dt, int64_t nsteps, int stop_nonfinite, int64_t *steps_done, int *finite,
                          int *status);
+
+/* Autotuner of the batch: per bucket of instances with the same degrees (the same kernels),
+ * the launch shapes of wedg_autotune tried one coordinate at a time against the time of the
+ * whole batch's step (graph replays from copies of the states, which are left unchanged; each
+ * trial after one untimed step that captures the graph). The other buckets keep their shapes
+ * while one is tuned. Returns the best time per step of the batch in *best_ms (may be NULL). */
+int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_dev, const double *t0,
+                        const double *dt, int64_t steps, double *best_ms);
 
 /* Error norms on the device (src/solver.jl:774-836). With uB = vB = NULL: `_mms_errors`, the
  * L² errors of the state A against the manufactured solution u = cos(ωT)Φ (the solver stores
