@@ -57,17 +57,15 @@ __host__ __device__ constexpr int qhigh(int nu, int nv) {
   return ((3 * (nv - 1) + 1) / 2 + 1) > nu ? ((3 * (nv - 1) + 1) / 2 + 1) : nu;
 }
 
-// Shared memory of k_stage per thread: the general kernels keep U, b, V and R_v (2 NU² + 2 NV²
-// doubles), the constant-coefficient kernels only b and R_v (NU² + NV²).
+// Shared memory of k_stage per thread: b and R_v (NU² + NV² doubles); the general kernels give
+// R_v NU² doubles, because the packed-inverse u-solve writes its result there once R_v is spent.
+// Both read U and V from HBM.
 __host__ __device__ constexpr int stage_doubles(int nu, int nv, bool fast) {
-  return fast ? nu * nu + nv * nv : 2 * nu * nu + 2 * nv * nv;
+  return fast ? nu * nu + nv * nv : 2 * nu * nu;
 }
-// Threads per block of k_stage: the general kernels fit one block in the 227 KB of one block,
-// the constant-coefficient kernels two blocks per SM (228 KB per SM, 1 KB of it per block
-// reserved).
+// Threads per block of k_stage: two blocks per SM (228 KB per SM, 1 KB of it per block reserved)
 __host__ __device__ constexpr int stage_threads(int nu, int nv, bool fast) {
-  return fast ? (2 * (128 * stage_doubles(nu, nv, true) * 8 + 1024) <= 233472 ? 128 : 96)
-              : (128 * stage_doubles(nu, nv, false) * 8 <= 232448 ? 128 : 96);
+  return 2 * (128 * stage_doubles(nu, nv, fast) * 8 + 1024) <= 233472 ? 128 : 96;
 }
 __host__ __device__ constexpr size_t stage_smem(int nu, int nv, bool fast) {
   return (size_t)stage_threads(nu, nv, fast) * stage_doubles(nu, nv, fast) * sizeof(double);
@@ -548,7 +546,7 @@ __device__ __forceinline__ void side_point(const Basis<NU, NV> &B, const Fields 
 // k_stage: fluxes, lifts, volume, source, u-equation; the mass right-hand side to HBM
 // ----------------------------------------------------------------------------
 template <int NU, int NV, bool FAST>
-__global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
+__global__ void __launch_bounds__(stage_threads(NU, NV, FAST), 2)
     k_stage(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
             const __grid_constant__ StageIO S) {
   constexpr int NQ = NU, BT = stage_threads(NU, NV, FAST);
@@ -562,11 +560,9 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
   const double two_h = F.two_h, four_hh = F.four_hh;
   const TimeF tf = time_factors(S);
   // thread-private blocks: b (NU², the u-equation right-hand side, then UT) and R_v (NV², the
-  // v-equation right-hand side); the general kernels also keep U (NU²) and V (NV²)
+  // v-equation right-hand side; in the general kernels its space, NU², then takes UT)
   Blk<NU, BT> bb{smem + tid};
   Blk<NV, BT> Rv{smem + NU * NU * BT + tid};
-  Blk<NU, BT> Ub{smem + (NU * NU + NV * NV) * BT + tid};
-  Blk<NV, BT> Vb{smem + (2 * NU * NU + NV * NV) * BT + tid};
 
   // ---- faces and lifts (src/rhs.jl:421-473): Rv (v-equation), b = -Fu (u-equation).
   //      The numerical flux slots A, D, F of a side are projected on the modes, Y[b] =
@@ -675,20 +671,10 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
     }
   }
 
-  // ---- state of the stage (the general kernels keep it in shared memory; the
-  //      constant-coefficient kernels read it from HBM, by columns and by rows)
+  // ---- the state of the stage is read from HBM (by rows of modes in the general kernels, by
+  //      columns and by rows in the constant-coefficient kernels)
   const size_t Eu = (size_t)E;
   if (S.mode != OUT_ADJ_USOLVE) {
-  if constexpr (!FAST) {
-#pragma unroll 1
-    for (int b = 0; b < NV; ++b)
-#pragma unroll
-      for (int a = 0; a < NV; ++a) Vb(a, b) = S.xv[e + Eu * (a + NV * b)];
-#pragma unroll 1
-    for (int b = 0; b < NU; ++b)
-#pragma unroll
-      for (int a = 0; a < NU; ++a) Ub(a, b) = S.xu[e + Eu * (a + NU * b)];
-  }
 
   // ---- volume terms (src/rhs.jl:309-333): Rv += -4/h² [(c²∇φ_v,∇u_h) + (α∇φ_v,∇v_h)],
   //      b += (c²∇φ_u, ∇v_h)
@@ -773,10 +759,18 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
       for (int a = 0; a < NU; ++a) {
         const double sa = B.S[r][a], pa = B.P[r][a];
 #pragma unroll
-        for (int b = 0; b < NU; ++b) { const double x = Ub(a, b); tu1[b] = fma(sa, x, tu1[b]); tu2[b] = fma(pa, x, tu2[b]); }
+        for (int b = 0; b < NU; ++b) {
+          const double x = S.xu[e + Eu * (a + NU * b)];
+          tu1[b] = fma(sa, x, tu1[b]);
+          tu2[b] = fma(pa, x, tu2[b]);
+        }
         if (a < NV) {
 #pragma unroll
-          for (int b = 0; b < NV; ++b) { const double x = Vb(a, b); tv1[b] = fma(sa, x, tv1[b]); tv2[b] = fma(pa, x, tv2[b]); }
+          for (int b = 0; b < NV; ++b) {
+            const double x = S.xv[e + Eu * (a + NV * b)];
+            tv1[b] = fma(sa, x, tv1[b]);
+            tv2[b] = fma(pa, x, tv2[b]);
+          }
         }
       }
       // the row at the points: g1[s] = Σ_b tu1[b] P[s][b], g2[s] = Σ_b tu2[b] S[s][b], ... from the
@@ -893,11 +887,11 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
 
   // ---- u-equation (src/rhs.jl:352-382): A_e UT = VB - Fu + e_1 V[0][0]
   if (!adjoint) {
-    if constexpr (FAST) bb(0, 0) += S.xv[e];
-    else bb(0, 0) += Vb(0, 0);
+    bb(0, 0) += S.xv[e];
   }
-  // UT: in place of b (constant-coefficient kernels), in place of U (general kernels, U is dead)
-  Blk<NU, BT> UT = FAST ? bb : Ub;
+  // UT: in place of b (constant-coefficient kernels), in the space of R_v (general kernels: R_v is
+  // spent once the mass right-hand side is written)
+  Blk<NU, BT> UT = FAST ? bb : Blk<NU, BT>{smem + NU * NU * BT + tid};
   if constexpr (FAST) {
     // A_e = c² (K1 ⊗ I + I ⊗ K1) + e_0 e_0^T is diagonal in the eigenbasis Q ⊗ Q of K1 (whose
     // first eigenvector is e_0 with λ_0 = 0): UT = Q [ (Q^T b Q) ∘ L ] Q^T, L = 1/(c²(λ_i+λ_j)), 1 at (0,0).
@@ -968,7 +962,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), FAST ? 2 : 1)
   } else {
     // packed upper triangle of the symmetric inverse, by columns: entry (i, j), i ≤ j, in row j(j+1)/2 + i
     constexpr int n = NU * NU;
-    double *X = &Ub(0, 0), *bv = &bb(0, 0);       // UT and b as vectors a + NU c
+    double *X = &UT(0, 0), *bv = &bb(0, 0);       // UT and b as vectors a + NU c
 #pragma unroll 1
     for (int i = 0; i < n; ++i) X[i * BT] = 0.0;
     // two columns jj, jj + 1 per pass: one read-modify-write of X[i] for both, twice the
