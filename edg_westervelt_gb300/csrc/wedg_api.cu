@@ -1085,7 +1085,7 @@ int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_de
         rc = trial(ms);
         if (rc == WEDG_OK && ms < kTuneGain * best) { best = ms; bp = p; bm = m; }
       }
-    for (int i : ids) wedg_set_launch_shape(b->ws[i], bp, bm);
+    for (int i : ids) wedg_set_launch_shape(b->ws[i], bp, bm);   // also after a failed trial
   }
   if (rc != WEDG_OK) return rc;
   if (best_ms) *best_ms = best / steps;
@@ -1501,8 +1501,8 @@ int wedg_autotune(wedg_ws *ws, const double *u_dev, const double *v_dev, double 
     }
   ws->ev_pool.push_back(e0);
   ws->ev_pool.push_back(e1);
+  wedg_set_launch_shape(ws, bp, bm);            // the best shape so far, also after a failed trial
   if (rc != WEDG_OK) return rc;
-  wedg_set_launch_shape(ws, bp, bm);
   if (best_ms) *best_ms = best / steps;
   return WEDG_OK;
 }
