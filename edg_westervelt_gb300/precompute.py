@@ -117,6 +117,27 @@ def _packed_inverses(Cw_blocks, Phi_xi, Phi_eta, chunk=2048):
     return out
 
 
+def _distinct_rows(a, limit=None):
+    """The distinct rows of a (E, n) array and each row's index among them, as
+    np.unique(a, axis=0, return_inverse=True) gives them up to their order, without sorting
+    the rows: all rows equal (constant coefficients) is checked directly, otherwise the rows
+    are grouped by a projection key (a 1D sort) and the groups are checked to hold equal rows,
+    with the row sort as the fallback when a key is shared by different rows. With `limit`,
+    (None, None) when there are more distinct rows than that."""
+    if a.shape[0] == 0 or np.array_equal(a, np.broadcast_to(a[0], a.shape)):
+        return a[:1], np.zeros(a.shape[0], dtype=np.int64)
+    key = a @ np.random.default_rng(0).uniform(1.0, 2.0, a.shape[1])
+    ukey, first, inv = np.unique(key, return_index=True, return_inverse=True)
+    if limit is not None and ukey.shape[0] > limit:
+        return None, None                    # at least as many distinct rows as distinct keys
+    uniq = a[first]
+    if not np.array_equal(uniq[inv], a):
+        uniq, inv = np.unique(a, axis=0, return_inverse=True)
+        if limit is not None and uniq.shape[0] > limit:
+            return None, None
+    return uniq, inv.reshape(-1)
+
+
 def precompute(q, N, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, boundary="absorbing_2beta",
                sigma_dirichlet=None, kappa=0.0, phase=(0.0, 0.0), coefficients=None, mode="mms", kx=1, ky=1,
                source=None, mass_solver="chebyshev", initial_profile=None, inverses="device"):
@@ -195,8 +216,8 @@ def precompute(q, N, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, 
     cw_cols = np.transpose(cw_e, (0, 2, 1)).reshape(E, qu1 * qu1)      # vec in column-major (r fastest)
     if inverses not in ("device", "host"):
         raise ValueError(f"inverses must be \"device\" or \"host\", not {inverses!r}")
-    uniq, inv = np.unique(cw_cols, axis=0, return_inverse=True)
-    if inverses == "device" and uniq.shape[0] > 64:
+    uniq, inv = _distinct_rows(cw_cols, limit=64 if inverses == "device" else None)
+    if inverses == "device" and uniq is None:
         Ainv_u = None                         # computed by the GPU workspace from Cw
     else:
         packed = _packed_inverses(uniq, Phi_xi_u, Phi_eta_u)
@@ -231,7 +252,10 @@ def precompute(q, N, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, 
     # ---- manufactured-solution data at the high-order points (solver.jl:570-602)
     XH = np.broadcast_to(xloc_h[None, :, None, :], (N, N, q_high, q_high))
     YH = np.broadcast_to(yloc_h[:, None, :, None], (N, N, q_high, q_high))
-    if initial_profile is None:
+    src_on = mode == "source"
+    if src_on:
+        pass                                  # source mode: no manufactured-solution data
+    elif initial_profile is None:
         sp = np.cos(2 * pi * kx * XH + px) * np.sin(2 * pi * ky * YH + py)
         sp_x = -2 * pi * kx * np.sin(2 * pi * kx * XH + px) * np.sin(2 * pi * ky * YH + py)
         sp_y = 2 * pi * ky * np.cos(2 * pi * kx * XH + px) * np.cos(2 * pi * ky * YH + py)
@@ -241,7 +265,6 @@ def precompute(q, N, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, 
         ip = initial_profile
         sp, sp_x, sp_y = (evaluate(ip[n], XH, YH) for n in ("u0", "u0_x", "u0_y"))
         sp_xx, sp_yy = evaluate(ip["u0_xx"], XH, YH), evaluate(ip["u0_yy"], XH, YH)
-    src_on = mode == "source"
     mms_BF = _F(evaluate(C.beta, XH, YH))
     if src_on:
         mms_SP = mms_Cdiv = mms_Ddiv = np.zeros((N, N, q_high, q_high), order="F")
