@@ -200,3 +200,32 @@ def test_precompute_leaves_many_distinct_inverses_to_the_device():
     assert pre_c["Ainv_u"] is not None                        # one shared matrix: inverted on the host
     with pytest.raises(ValueError):
         W.precompute(2, 3, inverses="gpu")
+
+
+def test_distinct_rows_matches_a_row_sort():
+    """The grouping of equal element stiffnesses (precompute) against np.unique(axis=0): all
+    rows equal, a few repeated rows, rows whose projection keys coincide although the rows
+    differ (the row sort decides then), and the limit above which the device computes the
+    inverses."""
+    from edg_westervelt_gb300.precompute import _distinct_rows
+    rng = np.random.default_rng(8)
+    a = np.broadcast_to(rng.standard_normal(9), (50, 9)).copy()
+    u, inv = _distinct_rows(a)
+    assert u.shape == (1, 9) and np.array_equal(u[inv], a)
+    for _ in range(20):
+        rows = rng.standard_normal((int(rng.integers(2, 7)), 9))
+        a = rows[rng.integers(0, rows.shape[0], 60)]
+        u, inv = _distinct_rows(a)
+        assert u.shape == np.unique(a, axis=0).shape and np.array_equal(u[inv], a)
+    # two different rows with the same key: the key is a · r for a fixed r, so move along a
+    # direction orthogonal to r
+    r = np.random.default_rng(0).uniform(1.0, 2.0, 9)
+    d = np.zeros(9)
+    d[0], d[1] = r[1], -r[0]
+    x = rng.standard_normal(9)
+    a = np.stack([x, x + d, x, x + d])
+    u, inv = _distinct_rows(a)
+    assert u.shape[0] == 2 and np.array_equal(u[inv], a)
+    assert _distinct_rows(rng.standard_normal((100, 4)), limit=64) == (None, None)
+    u, inv = _distinct_rows(rng.standard_normal((10, 4)), limit=64)
+    assert u.shape[0] == 10
