@@ -220,10 +220,11 @@ int wedg_rk4_adjoint_forward(wedg_ws *ws, const double *u0, const double *v0, do
 int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam_v, double *gu, double *gv,
                              double *g_c2, double *g_alpha, double *g_beta, int where);
 
-/* Launch shapes: threads per block of k_prep (one element per thread) and of the mass solves
- * (a team of threads per element, so the block's warps set its elements): 32, 64, 96 or 128
- * each, 128 by default. Results do not depend on them (every element's arithmetic is its own);
- * only the time does. */
+/* Launch shapes (no counterpart in the reference, whose parallel regions are the nblocks
+ * element blocks of src/rhs.jl:130-180): threads per block of k_prep (one element per thread)
+ * and of the mass solves (a team of threads per element, so the block's warps set its
+ * elements): 32, 64, 96 or 128 each, 128 by default. Results do not depend on them (every
+ * element's arithmetic is its own); only the time does. */
 int wedg_set_launch_shape(wedg_ws *ws, int prep_threads, int mass_threads);
 int wedg_get_launch_shape(const wedg_ws *ws, int *prep_threads, int *mass_threads);
 
@@ -234,7 +235,8 @@ int wedg_get_launch_shape(const wedg_ws *ws, int *prep_threads, int *mass_thread
 int wedg_autotune(wedg_ws *ws, const double *u_dev, const double *v_dev, double t0, double dt, int64_t steps,
                   double *best_ms);
 
-/* Device memory the reverse sweep may use to keep, for every stage of one checkpoint segment,
+/* (No counterpart in the reference, which has no adjoint.) Device memory the reverse sweep may
+ * use to keep, for every stage of one checkpoint segment,
  * the stage's forward data (its right-hand side, traces and mass-solve data) while it
  * recomputes the segment: with it the adjoint of a stage needs no second forward evaluation.
  * bytes < 0 (the default): half of the free device memory at the sweep; 0: never keep (each
