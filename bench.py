@@ -759,6 +759,8 @@ def main():
     ap.add_argument("--profile-only", action="store_true", help="only the main timed run (for ncu)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
     ap.add_argument("--batched-only", action="store_true", help="only the batched-form measurement")
+    ap.add_argument("--mass-solver", default="chebyshev", choices=["chebyshev", "cg"],
+                    help="mass solver of the main workload (profiling runs of the CG kernel)")
     ap.add_argument("--general-only", action="store_true",
                     help="only the general-kernel measurement (varying coefficients; --mesh applies)")
     ap.add_argument("--adjoint", action="store_true", help="only the adjoint-form measurement (one gradient)")
@@ -767,6 +769,7 @@ def main():
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     NMESH = args.mesh
+    KW["mass_solver"] = args.mass_solver
     if args.impl == "reference":
         run_reference(args)
     else:
