@@ -190,16 +190,29 @@ def profile_figures():
     return out
 
 
+def bench_config(E, dof, state):
+    """The `config` of the bench line, the same for the GPU arm and the reference arm (the
+    algorithmic choices of each arm, e.g. its Chebyshev step policy, are reported outside it)."""
+    return {"workload": workload_name(), "elements": E, "dof": dof,
+            "state": {"front": "steepened circular front, 1-2βv_h in [0.42, 1.58] across it (seeded)",
+                      "uniform": "short-wave state, every element spans 1-2βv_h in [0.42, 1.58] (seeded)",
+                      "zero": "zero state"}[state],
+            "l2": "inputs larger than L2 (state 206 MB, stage data > 600 MB per stage)", "t0": T0}
+
+
 class CpuPort:
     """The oracle (C restatement of the reference's RHS and RK4, OpenMP on all host threads)
-    on the same configuration at mesh N."""
+    on the same configuration at mesh N, from the oracle's own precompute, on the GPU arm's
+    seeded state (seed 0)."""
 
     def __init__(self, N, kind="front"):
         from oracle import coefficients as oc
         from oracle.precompute import precompute as opre
         from oracle.rhs import OracleWorkspace, max_threads
+        t0 = time.perf_counter()
         pre, _ = opre(Q, N, coefficients=oc.constant_coefficients(**COEF), **KW)
-        self.u, self.v = synthetic_state(N, pre["qu1"], pre["qv1"], seed=1, kind=kind)
+        self.setup_s = time.perf_counter() - t0
+        self.u, self.v = synthetic_state(N, pre["qu1"], pre["qv1"], seed=0, kind=kind)
         self.ws = OracleWorkspace(pre)
         self.dt = (1.0 / N) / (10 * Q * Q)
         self.dof = N * N * (pre["qu1"] ** 2 + pre["qv1"] ** 2)
@@ -238,22 +251,28 @@ def replica_value(dof_per_rank, world, steps, ms_max):
 
 
 def run_reference(args):
-    """The reference's CPU path on the host cores: the oracle port (Julia is not installed)."""
+    """The reference's CPU path on the host cores: the oracle port (Julia is not installed), on
+    the GPU arm's workload -- the same mesh, degrees, coefficients, sides, flux and seeded state --
+    with the reference's algorithm (every element takes the common maximum Chebyshev count,
+    src/rhs.jl:911-918, and the stored inverse stiffnesses)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    port = CpuPort(SAMPLE_N)
+    port = CpuPort(NMESH, kind=args.state)
     for _ in range(args.warmup):
         port.step()
     t = sum(port.step() for _ in range(args.steps))
     value = port.dof * 4 * args.steps / t
-    sample = (f"{args.steps} RK4 steps (after {args.warmup} warm-up) of the same configuration on an "
-              f"N={SAMPLE_N} mesh ({SAMPLE_N ** 2} elements), the same seeded steepened-front state")
+    E = NMESH * NMESH
+    sample = (f"{args.steps} RK4 steps (after {args.warmup} warm-up) of the full workload (N={NMESH}, {E} "
+              f"elements, the GPU arm's seeded state); oracle precompute {port.setup_s:.0f} s, not timed")
     line = {"impl": "reference", "metric": "FP64 DOF·stage/s on 1 GB300 (plain method, RK4 step)", "value": value,
             "unit": "DOF·stage/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded state)",
-            "config": {"workload": workload_name(), "sample_mesh": SAMPLE_N},
+            "config": bench_config(E, port.dof, args.state),
+            "algorithm": {"cheb_steps": "common maximum over the elements (src/rhs.jl:911-918)",
+                          "u_solve": "stored packed inverse stiffnesses (src/rhs.jl:352-382)"},
             "cpu_baseline": {"value": value, "unit": "DOF·stage/s", "cores": port.cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "DOF·stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -292,8 +311,6 @@ def run_ours(args):
     dof = E * (nu * nu + nv * nv)
     dt = (1.0 / N) / (10 * Q * Q)
     ws = W.Workspace(pre, N)
-    stream_ptr = ws.stream
-    ext = torch.cuda.ExternalStream(stream_ptr, device=dev)
 
     def device_state(kind, seed):
         u, v = synthetic_state(N, nu, nv, seed, kind)
@@ -301,7 +318,7 @@ def run_ours(args):
         return (torch.from_numpy(u.reshape(-1, order="F").copy()).to(dev),
                 torch.from_numpy(v.reshape(-1, order="F").copy()).to(dev))
 
-    def timed(kind, steps, warmup):
+    def timed(kind, steps, warmup, ws=ws):
         u, v = device_state(kind, seed=0)
         u0, v0 = u.clone(), v.clone()
         lib = __import__("edg_westervelt_gb300._lib", fromlist=["lib"]).lib()
@@ -317,6 +334,7 @@ def run_ours(args):
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
+        ext = torch.cuda.ExternalStream(ws.stream, device=dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(ext):
             e0.record(ext)
@@ -327,6 +345,8 @@ def run_ours(args):
         done = ctypes.c_int64(0)
         ws._check(lib.wedg_sync_status(ws._h, ctypes.byref(done), None) if rc == 0 else rc)
         torch.cuda.synchronize()
+        if done.value != steps:
+            raise RuntimeError(f"only {done.value} of the {steps} timed RK4 steps completed")
         ms = e0.elapsed_time(e1)
         if dist:
             ms = max_over_ranks(ms, dist, dev)
@@ -348,6 +368,11 @@ def run_ours(args):
         return
     zero = timed("zero", max(2, args.steps // 4), args.warmup)
     unif = timed("uniform", max(2, args.steps // 4), args.warmup)
+    # the reference's own Chebyshev policy (every element takes the largest count of the stage,
+    # src/rhs.jl:911-918) on the same state: the same algorithm as the reference arm
+    ws_common = W.Workspace(pre, N, cheb_steps="common_max")
+    common = timed(args.state, args.steps, args.warmup, ws=ws_common)
+    del ws_common
 
     ms_step = main["ms"] / args.steps
     value = replica_value(dof, world, args.steps, main["ms"])
@@ -365,10 +390,11 @@ def run_ours(args):
         ws.rk4_steps(uh, vh, T0, dt, 1)               # warm-up
         uh[...] = us
         vh[...] = vs
-        ke = max(2, min(args.steps, 5))
+        ke = args.steps
         t0 = time.perf_counter()
         for i in range(ke):
-            ws.rk4_steps(uh, vh, T0 + i * dt, dt, 1)
+            if ws.rk4_steps(uh, vh, T0 + i * dt, dt, 1) != 1:
+                raise RuntimeError("an end-to-end RK4 step did not complete")
         te = time.perf_counter() - t0
         e2e = {"value": world * dof * 4 * ke / te, "unit": "DOF·stage/s",
                "h2d_bytes_per_step": int(uh.nbytes + vh.nbytes), "d2h_bytes_per_step": int(uh.nbytes + vh.nbytes),
@@ -435,10 +461,16 @@ def run_ours(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded steepened-wave state; the reference measures on no dataset)",
-        "config": {"workload": workload_name(), "elements": E, "dof": dof,
-                   "state": "steepened circular front, 1-2βv_h in [0.42, 1.58] across it (seeded)",
-                   "l2": "inputs larger than L2 (state 206 MB, stage data > 600 MB per stage)",
-                   "cheb_steps": "per element", "t0": T0, "main_state": args.state},
+        "config": bench_config(E, dof, args.state),
+        "algorithm": {"cheb_steps": "per element: each element takes the count its own spectral interval "
+                                    "needs for the reference's tolerance (the reference's common maximum is "
+                                    "in common_max)",
+                      "u_solve": "fast diagonalisation of the constant-coefficient stiffness"},
+        "common_max": {"value": world * dof * 4 * common["steps"] / (common["ms"] / 1e3),
+                       "ms_per_step": common["ms"] / max(common["steps"], 1), "cheb_steps_max": common["cheb"],
+                       "stage_ms": common["prep_ms"] + common["stage_ms"] + common["mass_ms"],
+                       "note": "the same workload and state with the reference's Chebyshev policy: every element "
+                               "takes the stage's largest count (src/rhs.jl:911-918), as the reference arm does"},
         "roofline": roofline, "fp64_pipe": fp64_pipe, "reference_op_rate": reference_ops,
         "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clocks.summary(), "gpu_launches": main["launches"],
@@ -527,13 +559,11 @@ def run_batched(torch, dev, steps, warmup):
     tb_default = time.perf_counter() - t0
     advance(steps)
     assert all(d == steps for d in done) and all(fin)
-    # the autotuner: launch shapes per bucket of degrees, on copies of the present states
+    # the autotuner: launch shapes per bucket, on copies of the present states
     t0 = time.perf_counter()
-    batch.autotune(us, vs, t, dts, steps=2)
+    ms_tuner = batch.autotune(us, vs, t, dts, steps=2)
     t_tune = time.perf_counter() - t0
-    shapes = {}
-    for w in wss:
-        shapes[f"q_u={w.nu - 1},q_v={w.nv - 1}"] = list(w.launch_shape)
+    shapes = [dict(s) for s in batch.shapes()]
     batch.rk4_steps(us, vs, t, dts, 1)                            # captures the tuned graph
     advance(1)
     torch.cuda.synchronize()
@@ -550,19 +580,22 @@ def run_batched(torch, dev, steps, warmup):
     for i, ws in enumerate(wss):
         assert ws.rk4_steps(us[i], vs[i], t[i], dts[i], steps) == steps
     tp = time.perf_counter() - t0
-    vb, vp = dof * 4 * steps / tb, dof * 4 * steps / tp
+    tbest = min(tb, tb_default)
+    vb, vp = dof * 4 * steps / tbest, dof * 4 * steps / tp
     return {"workload": "256 instances, N in {16..128}, q_u 2-7, q_v in {q_u-1, q_u}, random flux and boundary "
                         "kinds, piecewise-constant c, alpha, beta on 4x4 subsquares (default_rng(4)), source mode",
-            "instances": n, "elements": int(sum(w.N * w.N for w in wss)), "dof": int(dof), "steps": steps,
-            "value": vb, "unit": "DOF·stage/s", "ms_per_step": tb / steps * 1e3,
+            "instances": n, "buckets": len(shapes), "elements": int(sum(w.N * w.N for w in wss)), "dof": int(dof),
+            "steps": steps, "value": vb, "unit": "DOF·stage/s", "ms_per_step": tbest / steps * 1e3,
             "plain_loop_value": vp, "plain_loop_ms_per_step": tp / steps * 1e3, "speedup_vs_plain_loop": vb / vp,
             "setup_s": t_setup,
             "autotune": {"default_ms_per_step": tb_default / steps * 1e3, "tuned_ms_per_step": tb / steps * 1e3,
-                         "tune_s": t_tune, "shapes": shapes,
-                         "note": "threads per block of k_prep and of the mass solves, per bucket of degrees "
-                                 "(Batch.autotune); value and ms_per_step are the tuned run's"},
+                         "tuner_median_ms_per_step": ms_tuner, "tune_s": t_tune, "shapes": shapes,
+                         "note": "per bucket: threads per block of k_prep and of the mass solves and persistent grids "
+                                 "(Batch.autotune, paired trials); value and ms_per_step are the faster of the "
+                                 "default-shape and the tuned-shape runs"},
             "timing": "host clock around each call (each call returns synchronised); states resident on the GPU",
-            "batched": "Batch.rk4_steps: one CUDA graph of one RK4 step of every instance, replayed per step",
+            "batched": "Batch.rk4_steps: per stage, one launch of each stage kernel per bucket of instances with the "
+                       "same kernels; one CUDA graph of one RK4 step of every instance, replayed per step",
             "plain_loop": "Workspace.rk4_steps for each instance in turn"}
 
 
@@ -642,14 +675,15 @@ def run_general(torch, dev, steps, warmup):
                     "model's bytes of one stage over the three stage kernels' mean time"}
 
 
-def run_config3(torch, dev, steps, warmup):
-    """Plain method with jumping coefficients, initial-value mode: N = 256, q_u = 5, q_v = 4, c, α, β
+def config3_problem(precompute=None):
+    """The jumping-coefficient workload: N = 256, q_u = 5, q_v = 4, initial-value mode, c, α, β
     constant on 4 × 4 subsquares from default_rng(3) (c ~ U[0.5, 2], α log-uniform on [1e-6, 1e-3],
     β ~ U[0, 10]), initial displacement a sum of 3 seeded Gaussians (centres U[0.2, 0.8]², widths
     U[0.03, 0.08], amplitudes U[-1, 1] scaled to 1e-3 so that 1 - 2βv stays positive), sides
     dirichlet / absorbing / absorbing_2beta / wall (bot, top, lft, rgt), central flux, one-sided faces,
-    dt = h / (10 max c q_u²). From the reference's zero start; DOF·stage/s over the timed steps."""
+    dt = h / (10 max c q_u²). Returns (pre, N, dt) from `precompute` (default the package's)."""
     import edg_westervelt_gb300 as W
+    precompute = precompute or W.precompute
     rng = np.random.default_rng(3)
     q, N = 5, 256
     c = rng.uniform(0.5, 2.0, (4, 4))
@@ -673,14 +707,21 @@ def run_config3(torch, dev, steps, warmup):
         return f
     prof = dict(u0=gauss(""), u0_x=gauss("x"), u0_y=gauss("y"), u0_xx=gauss("xx"), u0_yy=gauss("yy"))
     co = W.piecewise_coefficients(c ** 2, al, be)
-    pre, _ = W.precompute(q, N, mixed=True, mode="initial_value", flux="central", coefficients=co,
-                          initial_profile=prof, kappa=0.5,
-                          boundary=dict(bot="dirichlet", top="absorbing", lft="absorbing_2beta", rgt="wall"))
+    pre, _ = precompute(q, N, mixed=True, mode="initial_value", flux="central", coefficients=co,
+                        initial_profile=prof, kappa=0.5,
+                        boundary=dict(bot="dirichlet", top="absorbing", lft="absorbing_2beta", rgt="wall"))
+    return pre, N, (1.0 / N) / (10.0 * float(c.max()) * q * q)
+
+
+def run_config3(torch, dev, steps, warmup):
+    """Plain method with jumping coefficients (config3_problem), from the reference's zero start;
+    DOF·stage/s over the timed steps."""
+    import edg_westervelt_gb300 as W
+    pre, N, dt = config3_problem()
     ws = W.Workspace(pre, N)
     nu, nv = pre["qu1"], pre["qv1"]
     u = torch.zeros(N * N * nu * nu, dtype=torch.float64, device=dev)
     v = torch.zeros(N * N * nv * nv, dtype=torch.float64, device=dev)
-    dt = (1.0 / N) / (10.0 * float(c.max()) * q * q)
     ms = device_steps_ms(torch, ws, u, v, 0.0, dt, steps, warmup)
     dof = N * N * (nu * nu + nv * nv)
     return {"workload": "plain method, jumping coefficients: N=256 q_u=5 q_v=4, initial-value mode, central flux, "

@@ -11,10 +11,12 @@ from .coefficients import (Coefficients, GaussianSource, constant_coefficients, 
                            paper_coefficients, replace_coefficients)
 from .precompute import precompute
 from .quadrature import GaussQCofs, GradJacobiP, JacobiP
-from .solver import difference_norms, misfit_gradient, piecewise_coefficients, solve
-from .workspace import Batch, DimensionMismatch, ErrorException, Workspace, edg_rhs, edg_rhs_, rk4_step, rk4_step_
+from .solver import difference_norms, misfit, misfit_gradient, misfit_gradients, piecewise_coefficients, solve
+from .workspace import (Batch, DimensionMismatch, ErrorException, Workspace, edg_rhs, edg_rhs_, rk4_adjoint_forward_many,
+                        rk4_adjoint_reverse_many, rk4_step, rk4_step_)
 
 __all__ = ["solve", "precompute", "edg_rhs", "edg_rhs_", "rk4_step", "rk4_step_", "Workspace", "Batch",
            "difference_norms", "flux_parameters", "GaussianSource", "Coefficients", "paper_coefficients",
            "replace_coefficients", "constant_coefficients", "JacobiP", "GradJacobiP", "GaussQCofs",
-           "ErrorException", "DimensionMismatch", "misfit_gradient", "piecewise_coefficients"]
+           "ErrorException", "DimensionMismatch", "misfit", "misfit_gradient", "misfit_gradients",
+           "piecewise_coefficients", "rk4_adjoint_forward_many", "rk4_adjoint_reverse_many"]

@@ -54,6 +54,12 @@ class Stats(ctypes.Structure):
                 ("element_stages", ctypes.c_int64)]
 
 
+class BatchShape(ctypes.Structure):
+    """wedg_batch_shape (include/wedg.h)."""
+    _fields_ = [(n, ctypes.c_int32) for n in ("qu1", "qv1", "instances", "fast", "prep_threads", "mass_threads",
+                                               "persist")]
+
+
 _lib = None
 
 
@@ -125,11 +131,19 @@ def lib():
     L.wedg_rk4_adjoint_forward.argtypes = [vp, _D, _D, ctypes.c_double, ctypes.c_double, ctypes.c_int64,
                                            ctypes.c_int64, _D, _D, _I64, _I64, ctypes.c_int]
     L.wedg_rk4_adjoint_reverse.argtypes = [vp, _D, _D, _D, _D, _D, _D, _D, ctypes.c_int]
+    _PD = ctypes.POINTER(_D)
+    L.wedg_rk4_adjoint_forward_many.argtypes = [ctypes.c_int, ctypes.POINTER(vp), _PD, _PD, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_int64, ctypes.c_int64, _PD, _PD, ctypes.c_int]
+    L.wedg_rk4_adjoint_reverse_many.argtypes = [ctypes.c_int, ctypes.POINTER(vp), _PD, _PD, _PD, _PD, _PD, _PD, _PD,
+                                                ctypes.c_int]
     L.wedg_set_adjoint_memory.argtypes = [vp, ctypes.c_int64]
     L.wedg_set_launch_shape.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.wedg_get_launch_shape.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.wedg_autotune.argtypes = [vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int64, _D]
     L.wedg_batch_autotune.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), _D, _D, ctypes.c_int64, _D]
+    L.wedg_batch_bucket_count.argtypes = [vp]
+    L.wedg_batch_get_shape.argtypes = [vp, ctypes.c_int, ctypes.POINTER(BatchShape)]
+    L.wedg_batch_set_shape.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.wedg_norms.argtypes = [ctypes.POINTER(NormArgs), _D]
     L.wedg_run_source.argtypes = [vp, _D, _D, _I64, _I64, ctypes.c_int, ctypes.POINTER(SourceRun), _I64,
                                   ctypes.POINTER(ctypes.c_int)]

@@ -37,6 +37,16 @@ struct AdjIO {
   double *gbe;           // per-element β-gradient that k_adj_mass adds to, or null
 };
 
+// One instance's arguments of a multi-instance adjoint launch (Multi<AdjArgs>): gc2, gal, gbe are
+// k_adj_face's coefficient gradients (null unless PARAMS)
+struct AdjArgs {
+  Fields F;
+  StageIO S;
+  AdjIO A;
+  double *gc2, *gal, *gbe;
+};
+using MultiAdj = Multi<AdjArgs, 28>;
+
 // The weighted slot sums of an interior face point, from the scaled slot weights of the "+"
 // element (hP: A, D, F) and of the "-" element (hM), with c² and α of both sides (a continuous
 // face has c2m = c2p, afm = afp). With J, G, pen, sj of interior_flux,
@@ -60,22 +70,21 @@ __device__ __forceinline__ FaceWeights face_weights(const Fields &F, const FaceC
 
 // k_adj_hats: the weights of the slots A, D and F at every side point, the scaled traces of μ
 // (values and derivatives) and of ν (derivatives) (src/rhs.jl:412-473 transposed:
-// Â = (2/h) w_i tr_v(μ), D̂ = (4/h²) w_i tr_dv(μ), F̂ = -w_i tr_du(ν), the scalings folded into
-// the end vectors ElA, E1D, E1F and the weighted values Pw); and nus.
+// Â = (2/h) w_i tr_v(μ), D̂ = (4/h²) w_i tr_dv(μ), F̂ = -w_i tr_du(ν): the weights w_i folded
+// into the values Pw, the sign of F̂ into the end vector E1F, the mesh factors applied to the
+// traces); and nus.
 template <int NU, int NV>
-__global__ void __launch_bounds__(ADJ_THREADS) k_adj_hats(const __grid_constant__ Basis<NU, NV> B,
-                                                   const __grid_constant__ Fields F, const AdjIO A) {
+__device__ __forceinline__ void adj_hats_body(const Basis<NU, NV> &B, const Fields &F, const AdjIO &A, int e) {
   constexpr int NQ = NU;
   const int E = F.E;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
   if (err_word(F) != ERR_NONE) return;
   const double s_nu = -1.0 / F.four_hh;
   {
     double M[NV][NV];
     load_regs<NV>(M, A.mu, E, e);
-    trace4<NQ, NU, NV, false>(M, B.Pw, B.ElA, A.hat, 0, E, e);
-    trace4<NQ, NU, NV, true>(M, B.Pw, B.E1D, A.hat, 1, E, e);
+    trace4<NQ, NU, NV, false, true>(M, B.Pw, B.El, A.hat, 0, E, e, F.two_h);
+    trace4<NQ, NU, NV, true, true>(M, B.Pw, B.E1l, A.hat, 1, E, e, F.four_hh);
   }
   double X[NU][NU];
   load_regs<NU>(X, A.nu, E, e);
@@ -86,13 +95,29 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_hats(const __grid_constant_
     for (int a = 0; a < NU; ++a) A.nus[e + (size_t)E * (a + NU * b)] = s_nu * X[a][b];
 }
 
+template <int NU, int NV>
+__global__ void __launch_bounds__(ADJ_THREADS) k_adj_hats(const __grid_constant__ Basis<NU, NV> B,
+                                                   const __grid_constant__ Fields F, const AdjIO A) {
+  adj_hats_body<NU, NV>(B, F, A, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// tile = ADJ_THREADS elements per virtual block
+template <int NU, int NV>
+__global__ void __launch_bounds__(ADJ_THREADS) k_adj_hats_m(const __grid_constant__ Basis<NU, NV> B,
+                                                     const __grid_constant__ MultiAdj P) {
+  __shared__ AdjArgs sa;
+  for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
+    const int inst = multi_begin(P, vb, sa);
+    adj_hats_body<NU, NV>(B, sa.F, sa.A, (vb - P.first[inst]) * P.tile + (int)threadIdx.x);
+  }
+}
+
 // k_adj_mass: gv += P_hᵀ (2βW ∘ vt_q ∘ μ_q) P_h on every element, by the team layout of the mass
 // solves: each unit forms the weights 2β vt_q of its two point rows (into G, which the forward
 // solve of this state no longer needs) and applies them to μ with team_K. With A.gbe, also the
 // β-derivative of μ·M(v) vt for β constant on the element, gbe[e] += Σ_q 2 W_q v_q vt_q μ_q.
 template <int NU, int NV>
-__global__ void __launch_bounds__(CHEB_THREADS, 3)
-    k_adj_mass(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F, const AdjIO A) {
+__device__ __forceinline__ void adj_mass_body(const Basis<NU, NV> &B, const Fields &F, const AdjIO &A, int e0) {
   using T = ChebTeam<NU, NV>;
   constexpr int QH = T::QH, U = T::U, NE = T::NE, J = T::J;
   __shared__ double sh[T::TPB * T::SLOT];
@@ -104,7 +129,7 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
   __syncthreads();
   TeamPos tp;
   if (!team_pos<NU, NV>(tp)) return;
-  const int e = blockIdx.x * ((int)(blockDim.x >> 5) * T::TPW) + tp.slot;
+  const int e = e0 + tp.slot;
   if (e >= F.E) return;
   if (err_word(F) != ERR_NONE) return;
   const int u = tp.u;
@@ -167,6 +192,23 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
   for (int j = 0; j < J; ++j) {
     const int k = u + U * j;
     if (k < NE) A.gv[e + Eu * k] = acc[j];
+  }
+}
+
+template <int NU, int NV>
+__global__ void __launch_bounds__(CHEB_THREADS, 3)
+    k_adj_mass(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F, const AdjIO A) {
+  adj_mass_body<NU, NV>(B, F, A, blockIdx.x * team_tile<NU, NV>());
+}
+
+// tile = team_tile elements per virtual block
+template <int NU, int NV>
+__global__ void __launch_bounds__(CHEB_THREADS, 3)
+    k_adj_mass_m(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ MultiAdj P) {
+  __shared__ AdjArgs sa;
+  for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
+    const int inst = multi_begin(P, vb, sa);
+    adj_mass_body<NU, NV>(B, sa.F, sa.A, (vb - P.first[inst]) * P.tile);
   }
 }
 
@@ -292,13 +334,10 @@ __device__ __forceinline__ void boundary_coef_partials(const Fields &F, int s, c
 // from their sums (even modes) and differences (odd modes), and the transposes of the two
 // opposite sides (B and T, L and R) are applied together (Er = ±El, E1r = ∓E1l by mode parity).
 template <int NU, int NV, bool PARAMS>
-__global__ void __launch_bounds__(ADJ_THREADS) k_adj_face(const __grid_constant__ Basis<NU, NV> B,
-                                                   const __grid_constant__ Fields F,
-                                                   const __grid_constant__ StageIO S, const AdjIO A, double *gc2,
-                                                   double *gal, double *gbe) {
+__device__ __forceinline__ void adj_face_body(const Basis<NU, NV> &B, const Fields &F, const StageIO &S,
+                                              const AdjIO &A, double *gc2, double *gal, double *gbe, int e) {
   constexpr int NQ = NU;
   const int E = F.E, N = F.N;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
   if (err_word(F) != ERR_NONE) return;
   const int j = e % N, k = e / N;
@@ -502,6 +541,26 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_face(const __grid_constant_
     gc2[e] += dc2;
     gal[e] += dal;
     gbe[e] += dbe;
+  }
+}
+
+template <int NU, int NV, bool PARAMS>
+__global__ void __launch_bounds__(ADJ_THREADS) k_adj_face(const __grid_constant__ Basis<NU, NV> B,
+                                                   const __grid_constant__ Fields F,
+                                                   const __grid_constant__ StageIO S, const AdjIO A, double *gc2,
+                                                   double *gal, double *gbe) {
+  adj_face_body<NU, NV, PARAMS>(B, F, S, A, gc2, gal, gbe, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// tile = ADJ_THREADS elements per virtual block
+template <int NU, int NV, bool PARAMS>
+__global__ void __launch_bounds__(ADJ_THREADS) k_adj_face_m(const __grid_constant__ Basis<NU, NV> B,
+                                                     const __grid_constant__ MultiAdj P) {
+  __shared__ AdjArgs sa;
+  for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
+    const int inst = multi_begin(P, vb, sa);
+    adj_face_body<NU, NV, PARAMS>(B, sa.F, sa.S, sa.A, sa.gc2, sa.gal, sa.gbe,
+                                  (vb - P.first[inst]) * P.tile + (int)threadIdx.x);
   }
 }
 

@@ -64,10 +64,52 @@ __global__ void k_lincomb(size_t n, double *out, double a, const double *x, doub
   }
 }
 
+// k_lincomb for many instances in one launch (blockIdx.y is the instance): out = a x + b y (+ z)
+struct LinPtrs {
+  size_t n;
+  double *out;
+  const double *x, *y, *z;
+};
+constexpr int LIN_CAP = 64;
+struct LinMulti {
+  int n;
+  double a, b;
+  LinPtrs p[LIN_CAP];
+};
+__global__ void k_lincomb_m(const __grid_constant__ LinMulti L) {
+  const LinPtrs &q = L.p[blockIdx.y];
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < q.n; i += (size_t)gridDim.x * blockDim.x) {
+    double r = L.a * q.x[i];
+    if (q.y) r = fma(L.b, q.y[i], r);
+    if (q.z) r += q.z[i];
+    q.out[i] = r;
+  }
+}
+
+// k_step_done for many instances in one launch (thread i: instance i), flags in the parameters
+struct StepFlagsP {
+  unsigned long long *err;
+  const unsigned int *nonfinite;
+  long long *steps_done;
+};
+struct StepMulti {
+  int n, stop_nonfinite;
+  StepFlagsP f[LIN_CAP];
+};
+__global__ void k_step_done_p(const __grid_constant__ StepMulti P) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const StepFlagsP &x = P.f[i];
+  if (*x.err != ERR_NONE) return;
+  *x.steps_done += 1;
+  if (P.stop_nonfinite && *x.nonfinite) *x.err = (3ull << ERR_CLASS_SHIFT);
+}
+
 // The candidates of the autotuners, tried one coordinate at a time (k_prep's block, then the
 // mass solves'); a candidate replaces the best so far only when it is faster by more than 2 %
 const int kTuneThreads[3] = {32, 64, 128};
 constexpr double kTuneGain = 0.98;
+constexpr int kTuneRepeats = 3;   // paired trials of the batch autotuner
 
 Launchers get_launchers(int nu, int nv, bool fast) {
   switch (nu) {
@@ -299,11 +341,11 @@ int enqueue_stage(wedg_ws *ws, const StageIO &S, const Fields *Fo = nullptr) {
     e0 = take_event(ws); e1 = take_event(ws); e2 = take_event(ws); e3 = take_event(ws);
     cudaEventRecord(e0, ws->stream);
   }
-  ws->L.prep(ws->basis.data(), F, Sp, bp, tp, ws->stream);
+  CK(ws, ws->L.prep(ws->basis.data(), F, Sp, bp, tp, ws->stream));
   if (ws->timing) cudaEventRecord(e1, ws->stream);
-  ws->L.stage(ws->basis.data(), F, Sp, bs, ts, ws->stream);
+  CK(ws, ws->L.stage(ws->basis.data(), F, Sp, bs, ts, ws->stream));
   if (ws->timing) cudaEventRecord(e2, ws->stream);
-  ws->L.mass(ws->basis.data(), F, Sp, bm, ws->mass_threads, ws->stream);
+  CK(ws, ws->L.mass(ws->basis.data(), F, Sp, bm, ws->mass_threads, ws->stream));
   if (ws->timing) {
     cudaEventRecord(e3, ws->stream);
     ws->ev_pending.push_back({e0, e1, e2, e3});
@@ -330,6 +372,41 @@ void factor_table(const wedg_ws *ws, double t, double dt, int64_t count, double 
   }
 }
 
+// The StageIO of stage s (0..3) of an RK4 step of the state (u, v) at time t (src/solver.jl:299-321):
+// its input state, time factors (or, with tf, the device table of tf_n steps indexed by the
+// workspace's step counter, for graph replays) and outputs. With stage_u, stage_v (four buffers
+// each) the stage states Y1..Y4 are kept there.
+StageIO rk4_stage_io(const wedg_ws *ws, double *u, double *v, int s, double t, double dt, const double *tf,
+                     long long tf_n, double *const *stage_u, double *const *stage_v) {
+  const double cs[3] = {0.5 * dt, 0.5 * dt, dt};
+  const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
+  StageIO S{};
+  S.xu = s == 0 ? u : (stage_u ? stage_u[s] : ws->su);
+  S.xv = s == 0 ? v : (stage_v ? stage_v[s] : ws->sv);
+  if (tf) {
+    S.tf = tf;
+    S.tf_n = tf_n;
+    S.step = ws->steps_done;
+    S.stage = s;
+  } else {
+    stage_factors(ws, ts[s], S);
+  }
+  S.u0 = u; S.v0 = v;
+  S.su = stage_u && s < 3 ? stage_u[s + 1] : ws->su;
+  S.sv = stage_v && s < 3 ? stage_v[s + 1] : ws->sv;
+  S.accu = ws->accu; S.accv = ws->accv;
+  S.uo = u; S.vo = v;
+  if (s < 3) {
+    S.mode = OUT_RK4_STAGE;
+    S.first = s == 0;
+    S.c = cs[s];
+  } else {
+    S.mode = ws->cfg.mass_solver == WEDG_CG ? OUT_RK4_LAST_ACC : OUT_RK4_LAST;
+    S.c = dt / 6.0;
+  }
+  return S;
+}
+
 // One RK4 step on the workspace stream. With tf != nullptr the stage kernels take their time
 // factors from the device table tf (tf_n steps, indexed by the device step counter), so that the
 // launches can be captured once into a CUDA graph and replayed for every step.
@@ -337,8 +414,6 @@ int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop
                 const double *tf = nullptr, long long tf_n = 0, double *const *stage_u = nullptr,
                 double *const *stage_v = nullptr) {
   // with stage_u, stage_v (four buffers each) the stage states Y1..Y4 of the step are kept there
-  const double cs[3] = {0.5 * dt, 0.5 * dt, dt};
-  const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
   const bool cg = ws->cfg.mass_solver == WEDG_CG;
   if (stage_u) {
     const size_t bU = sizeof(double) * ws->E * ws->nu * ws->nu, bV = sizeof(double) * ws->E * ws->nv * ws->nv;
@@ -346,31 +421,7 @@ int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop
     CK(ws, cudaMemcpyAsync(stage_v[0], v, bV, cudaMemcpyDeviceToDevice, ws->stream));
   }
   for (int s = 0; s < 4; ++s) {
-    StageIO S{};
-    S.xu = s == 0 ? u : (stage_u ? stage_u[s] : ws->su);
-    S.xv = s == 0 ? v : (stage_v ? stage_v[s] : ws->sv);
-    if (tf) {
-      S.tf = tf;
-      S.tf_n = tf_n;
-      S.step = ws->steps_done;
-      S.stage = s;
-    } else {
-      stage_factors(ws, ts[s], S);
-    }
-    S.u0 = u; S.v0 = v;
-    S.su = stage_u && s < 3 ? stage_u[s + 1] : ws->su;
-    S.sv = stage_v && s < 3 ? stage_v[s + 1] : ws->sv;
-    S.accu = ws->accu; S.accv = ws->accv;
-    S.uo = u; S.vo = v;
-    if (s < 3) {
-      S.mode = OUT_RK4_STAGE;
-      S.first = s == 0;
-      S.c = cs[s];
-    } else {
-      S.mode = cg ? OUT_RK4_LAST_ACC : OUT_RK4_LAST;
-      S.c = dt / 6.0;
-    }
-    int rc = enqueue_stage(ws, S);
+    int rc = enqueue_stage(ws, rk4_stage_io(ws, u, v, s, t, dt, tf, tf_n, stage_u, stage_v));
     if (rc) return rc;
   }
   if (cg) {
@@ -414,13 +465,13 @@ int enqueue_adjoint_core(wedg_ws *ws, const Fields &Fs, const StageIO &S, const 
   StageIO Sm = S;
   Sm.mode = OUT_RHS;
   Sm.vt = ws->adj_mu;
-  ws->L.mass(ws->basis.data(), Fm, Sm, 1, ws->mass_threads, ws->stream);
+  CK(ws, ws->L.mass(ws->basis.data(), Fm, Sm, 1, ws->mass_threads, ws->stream));
   // ν = A_e⁻¹ λ_u
   StageIO Su = S;
   Su.mode = OUT_ADJ_USOLVE;
   Su.xu = lam_u;
   Su.ut = ws->adj_nu;
-  ws->L.stage(ws->basis.data(), Fs, Su, bs, ts, ws->stream);
+  CK(ws, ws->L.stage(ws->basis.data(), Fs, Su, bs, ts, ws->stream));
   const AdjIO A{ws->adj_mu, ws->adj_nu, ws->adj_nus, S.vt, ws->adj_hat, gu, gv, S.xv,
                 gpar ? gpar + 2 * (size_t)ws->E : nullptr};
   ws->L.adj_hats(ws->basis.data(), Fs, S, A, ws->stream);
@@ -431,7 +482,7 @@ int enqueue_adjoint_core(wedg_ws *ws, const Fields &Fs, const StageIO &S, const 
   Sv.xv = ws->adj_mu;
   Sv.vt = gv;
   Sv.ut = gu;
-  ws->L.stage(ws->basis.data(), Fs, Sv, bs, ts, ws->stream);
+  CK(ws, ws->L.stage(ws->basis.data(), Fs, Sv, bs, ts, ws->stream));
   ws->L.adj_mass(ws->basis.data(), Fs, S, A, ws->stream);
   // the faces; with gpar also K̄·∂F/∂p at the state: volume, u-solve and faces (the mass
   // matrix's β-part is in k_adj_mass)
@@ -540,6 +591,232 @@ int argument_error(wedg_ws *ws, const std::string &msg) {
   return WEDG_ERR_ARGUMENT;
 }
 
+// ---- multi-instance launches of one kernel over many instances' arguments, in chunks of the
+//      launch's capacity (wedg_kernels.cuh); kind 0: k_prep (tile = threads), 1: k_stage
+//      (tile = stage_threads), 2: the mass solve (tile = teams of `threads`). grid_of maps the
+//      virtual blocks of a chunk to its physical grid (persistent launches).
+enum { MK_PREP = 0, MK_STAGE = 1, MK_MASS = 2 };
+template <class GridOf>
+cudaError_t multi_stage_launch(const Launchers &L, const void *basis, int nu, int nv, bool fast, int kind,
+                               const std::vector<StageArgs> &args, int threads, cudaStream_t st, GridOf grid_of) {
+  const int TPW = 32 / (qhigh(nu, nv) / 2 + (qhigh(nu, nv) & 1));
+  const int tile = kind == MK_PREP ? threads : kind == MK_STAGE ? stage_threads(nu, nv, fast) : (threads / 32) * TPW;
+  const int n = (int)args.size();
+  for (int c0 = 0; c0 < n; c0 += MultiStage::cap) {
+    const int m = std::min(n - c0, MultiStage::cap);
+    MultiStage P;
+    P.n = m;
+    P.tile = tile;
+    P.first[0] = 0;
+    for (int x = 0; x < m; ++x) {
+      P.a[x] = args[c0 + x];
+      P.first[x + 1] = P.first[x] + (P.a[x].F.E + tile - 1) / tile;
+    }
+    const int grid = grid_of(kind, P.first[m]);
+    const cudaError_t e = kind == MK_PREP    ? L.prep_m(basis, P, grid, threads, st)
+                          : kind == MK_STAGE ? L.stage_m(basis, P, grid, stage_threads(nu, nv, fast), st)
+                                             : L.mass_m(basis, P, grid, threads, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// kind 0: k_adj_hats, 1: k_adj_mass, 2: k_adj_face (one virtual block per tile, no persistence)
+enum { MA_HATS = 0, MA_MASS = 1, MA_FACE = 2 };
+cudaError_t multi_adj_launch(const Launchers &L, const void *basis, int nu, int nv, int kind,
+                             const std::vector<AdjArgs> &args, cudaStream_t st) {
+  const int TPW = 32 / (qhigh(nu, nv) / 2 + (qhigh(nu, nv) & 1));
+  const int tile = kind == MA_MASS ? (CHEB_THREADS / 32) * TPW : ADJ_THREADS;
+  const int n = (int)args.size();
+  for (int c0 = 0; c0 < n; c0 += MultiAdj::cap) {
+    const int m = std::min(n - c0, MultiAdj::cap);
+    MultiAdj P;
+    P.n = m;
+    P.tile = tile;
+    P.first[0] = 0;
+    for (int x = 0; x < m; ++x) {
+      P.a[x] = args[c0 + x];
+      P.first[x + 1] = P.first[x] + (P.a[x].F.E + tile - 1) / tile;
+    }
+    const cudaError_t e = kind == MA_HATS ? L.adj_hats_m(basis, P, 0, st)
+                          : kind == MA_MASS ? L.adj_mass_m(basis, P, 0, st)
+                                            : L.adj_face_m(basis, P, 0, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// out_i = a x_i + b y_i (+ z_i) over the instances of a group (y, z may be null)
+cudaError_t multi_lincomb(const std::vector<LinPtrs> &p, double a, double b, cudaStream_t st) {
+  for (size_t c0 = 0; c0 < p.size(); c0 += LIN_CAP) {
+    LinMulti L;
+    L.n = (int)std::min(p.size() - c0, (size_t)LIN_CAP);
+    L.a = a;
+    L.b = b;
+    size_t most = 1;
+    for (int x = 0; x < L.n; ++x) {
+      L.p[x] = p[c0 + x];
+      most = std::max(most, L.p[x].n);
+    }
+    const unsigned gx = (unsigned)std::min<size_t>((most + 255) / 256, 152 * 16 / std::max(1, L.n) + 1);
+    k_lincomb_m<<<dim3(gx, L.n), 256, 0, st>>>(L);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// ---- a group of workspaces advanced together by multi-instance launches: the same degrees,
+//      coefficient kernels, mass solver and 1D operators; everything of the group runs on the first
+//      workspace's stream while a StreamGuard holds the others on it
+struct StreamGuard {
+  std::vector<wedg_ws *> ws;
+  std::vector<cudaStream_t> own;
+  explicit StreamGuard(const std::vector<wedg_ws *> &g) : ws(g) {
+    for (wedg_ws *w : ws) own.push_back(w->stream);
+    for (wedg_ws *w : ws) w->stream = ws[0]->stream;
+  }
+  ~StreamGuard() {
+    for (size_t i = 0; i < ws.size(); ++i) ws[i]->stream = own[i];
+  }
+};
+
+bool same_kernels(const wedg_ws *a, const wedg_ws *b) {
+  return a->nu == b->nu && a->nv == b->nv && a->fast == b->fast && a->cfg.mass_solver == b->cfg.mass_solver &&
+         a->basis == b->basis;
+}
+
+// One RHS evaluation (k_prep, k_stage, mass solve) of every workspace of a group, each with its
+// own Fields and StageIO; one workspace: enqueue_stage. Advances the bin parities as enqueue_stage.
+int group_stage(const std::vector<wedg_ws *> &G, const std::vector<StageIO> &S, const std::vector<Fields> &F) {
+  if (G.size() == 1) return enqueue_stage(G[0], S[0], &F[0]);
+  std::vector<StageArgs> args(G.size());
+  for (size_t i = 0; i < G.size(); ++i) {
+    args[i].F = F[i];
+    args[i].S = S[i];
+    args[i].S.parity = G[i]->parity;
+    G[i]->parity = 1 - G[i]->parity;
+    G[i]->stats.kernel_launches += 3;
+    G[i]->stats.element_stages += G[i]->E;
+  }
+  wedg_ws *w = G[0];
+  auto all = [](int, int total) { return total; };
+  for (int kind : {MK_PREP, MK_STAGE, MK_MASS}) {
+    const cudaError_t e = multi_stage_launch(w->L, w->basis.data(), w->nu, w->nv, w->fast, kind, args,
+                                             kind == MK_PREP ? w->prep_threads : w->mass_threads, w->stream, all);
+    if (e != cudaSuccess) return cuda_fail(w, e, "multi-instance launch");
+  }
+  return WEDG_OK;
+}
+
+// One RK4 step of every workspace of a group on its state (u[i], v[i]) at time t
+int group_rk4(const std::vector<wedg_ws *> &G, double *const *u, double *const *v, double t, double dt,
+              int stop_nonfinite) {
+  if (G.size() == 1) return enqueue_rk4(G[0], u[0], v[0], t, dt, stop_nonfinite);
+  const int n = (int)G.size();
+  std::vector<StageIO> S(n);
+  std::vector<Fields> F(n);
+  for (int s = 0; s < 4; ++s) {
+    for (int i = 0; i < n; ++i) {
+      S[i] = rk4_stage_io(G[i], u[i], v[i], s, t, dt, nullptr, 0, nullptr, nullptr);
+      F[i] = G[i]->F;
+    }
+    const int rc = group_stage(G, S, F);
+    if (rc) return rc;
+  }
+  wedg_ws *w = G[0];
+  if (w->cfg.mass_solver == WEDG_CG) {
+    for (int i = 0; i < n; ++i) {
+      const int nU = G[i]->E * G[i]->nu * G[i]->nu, nV = G[i]->E * G[i]->nv * G[i]->nv;
+      k_rk4_final<<<std::min((nU + nV + 255) / 256, 152 * 8), 256, 0, w->stream>>>(
+          nU, nV, u[i], v[i], G[i]->accu, G[i]->accv, dt / 6.0, G[i]->F.err, G[i]->F.nonfinite);
+      G[i]->stats.kernel_launches += 1;
+    }
+  }
+  for (int c0 = 0; c0 < n; c0 += LIN_CAP) {
+    StepMulti P;
+    P.n = std::min(n - c0, LIN_CAP);
+    P.stop_nonfinite = stop_nonfinite;
+    for (int x = 0; x < P.n; ++x) {
+      wedg_ws *g = G[c0 + x];
+      P.f[x] = StepFlagsP{g->F.err, g->F.nonfinite, g->steps_done};
+      g->stats.kernel_launches += 1;
+    }
+    k_step_done_p<<<1, LIN_CAP, 0, w->stream>>>(P);
+  }
+  CK(w, cudaGetLastError());
+  return WEDG_OK;
+}
+
+// The transpose of one RHS evaluation of every workspace of a group (enqueue_adjoint_core for
+// each): Fs, S the forward evaluation's data, lam the weights, g the gradients (and gpar the
+// per-element coefficient gradients, or null for all)
+int group_adjoint_core(const std::vector<wedg_ws *> &G, const std::vector<Fields> &Fs, const std::vector<StageIO> &S,
+                       const std::vector<const double *> &lam_u, const std::vector<const double *> &lam_v,
+                       const std::vector<double *> &gu, const std::vector<double *> &gv,
+                       const std::vector<double *> &gpar) {
+  const int n = (int)G.size();
+  if (n == 1) return enqueue_adjoint_core(G[0], Fs[0], S[0], lam_u[0], lam_v[0], gu[0], gv[0], gpar[0]);
+  wedg_ws *w = G[0];
+  auto all = [](int, int total) { return total; };
+  std::vector<StageArgs> sa(n);
+  std::vector<AdjArgs> aa(n);
+  cudaError_t e;
+  // μ = M(v)⁻¹ λ_v on the Chebyshev data of the states
+  for (int i = 0; i < n; ++i) {
+    sa[i].F = Fs[i];
+    sa[i].F.mrhs = const_cast<double *>(lam_v[i]);
+    sa[i].S = S[i];
+    sa[i].S.mode = OUT_RHS;
+    sa[i].S.vt = G[i]->adj_mu;
+  }
+  if ((e = multi_stage_launch(w->L, w->basis.data(), w->nu, w->nv, w->fast, MK_MASS, sa, w->mass_threads, w->stream,
+                              all)) != cudaSuccess)
+    return cuda_fail(w, e, "multi-instance launch");
+  // ν = A_e⁻¹ λ_u
+  for (int i = 0; i < n; ++i) {
+    sa[i].F = Fs[i];
+    sa[i].S = S[i];
+    sa[i].S.mode = OUT_ADJ_USOLVE;
+    sa[i].S.xu = lam_u[i];
+    sa[i].S.ut = G[i]->adj_nu;
+  }
+  if ((e = multi_stage_launch(w->L, w->basis.data(), w->nu, w->nv, w->fast, MK_STAGE, sa, 0, w->stream, all)) !=
+      cudaSuccess)
+    return cuda_fail(w, e, "multi-instance launch");
+  for (int i = 0; i < n; ++i) {
+    wedg_ws *g = G[i];
+    aa[i].F = Fs[i];
+    aa[i].S = S[i];
+    aa[i].A = AdjIO{g->adj_mu, g->adj_nu, g->adj_nus, S[i].vt, g->adj_hat, gu[i], gv[i], S[i].xv,
+                    gpar[i] ? gpar[i] + 2 * (size_t)g->E : nullptr};
+    aa[i].gc2 = gpar[i];
+    aa[i].gal = gpar[i] ? gpar[i] + g->E : nullptr;
+    aa[i].gbe = gpar[i] ? gpar[i] + 2 * (size_t)g->E : nullptr;
+  }
+  if ((e = multi_adj_launch(w->L, w->basis.data(), w->nu, w->nv, MA_HATS, aa, w->stream)) != cudaSuccess)
+    return cuda_fail(w, e, "multi-instance launch");
+  // the volume transposes: the volume terms of the state (-(h²/4) ν, μ)
+  for (int i = 0; i < n; ++i) {
+    sa[i].F = Fs[i];
+    sa[i].S = S[i];
+    sa[i].S.mode = OUT_ADJ_VOLUME;
+    sa[i].S.xu = G[i]->adj_nus;
+    sa[i].S.xv = G[i]->adj_mu;
+    sa[i].S.vt = gv[i];
+    sa[i].S.ut = gu[i];
+  }
+  if ((e = multi_stage_launch(w->L, w->basis.data(), w->nu, w->nv, w->fast, MK_STAGE, sa, 0, w->stream, all)) !=
+      cudaSuccess)
+    return cuda_fail(w, e, "multi-instance launch");
+  if ((e = multi_adj_launch(w->L, w->basis.data(), w->nu, w->nv, MA_MASS, aa, w->stream)) != cudaSuccess ||
+      (e = multi_adj_launch(w->L, w->basis.data(), w->nu, w->nv, MA_FACE, aa, w->stream)) != cudaSuccess)
+    return cuda_fail(w, e, "multi-instance launch");
+  for (wedg_ws *g : G) g->stats.kernel_launches += 6;
+  CK(w, cudaGetLastError());
+  return WEDG_OK;
+}
+
 }  // namespace
 
 namespace {
@@ -564,36 +841,523 @@ struct RunBuffers {
 
 }  // namespace
 
-// A batch of workspaces advanced by one replayed CUDA graph per step (wedg_batch_*)
+namespace {
+
+// The forward run of a reverse sweep for every workspace of a group (wedg_rk4_adjoint_forward;
+// several workspaces: their RK4 steps as multi-instance launches, in lockstep)
+int adjoint_forward_group(const std::vector<wedg_ws *> &G, const double *const *u0, const double *const *v0,
+                          double t0, double dt, int64_t nsteps, int64_t every, double *const *uT, double *const *vT,
+                          int where) {
+  const int n = (int)G.size();
+  if (nsteps < 0 || every < 1) return argument_error(G[0], "nsteps must be ≥ 0 and the checkpoint interval ≥ 1");
+  const int64_t nchk = nsteps ? (nsteps + every - 1) / every : 0;
+  const int64_t seg = std::min<int64_t>(every, std::max<int64_t>(nsteps, 1));
+  int rc;
+  for (wedg_ws *ws : G) {
+    const size_t nU = (size_t)ws->E * ws->nu * ws->nu, nV = (size_t)ws->E * ws->nv * ws->nv, nn = nU + nV;
+    if ((rc = adjoint_buffers(ws))) return rc;
+    // buffers: a state is u followed by v (nn doubles)
+    if (!ws->rk_lam) {
+      if ((rc = dalloc(ws, &ws->rk_lam, nn)) || (rc = dalloc(ws, &ws->rk_acc, nn)) ||
+          (rc = dalloc(ws, &ws->rk_kbar, nn)) || (rc = dalloc(ws, &ws->rk_g, nn)) || (rc = dalloc(ws, &ws->rk_y, nn)) ||
+          (rc = dalloc(ws, &ws->rk_par, 3 * (size_t)ws->E)))
+        return rc;
+    }
+    while (ws->rk_chk_n < nchk) {
+      double *p;
+      if ((rc = dalloc(ws, &p, nn))) return rc;
+      ws->rk_chk.push_back(p);
+      ++ws->rk_chk_n;
+    }
+    while (ws->rk_seg_n < 4 * seg) {
+      double *p;
+      if ((rc = dalloc(ws, &p, nn))) return rc;
+      ws->rk_seg.push_back(p);
+      ++ws->rk_seg_n;
+    }
+  }
+  StreamGuard guard(G);
+  cudaStream_t st = G[0]->stream;
+  const cudaMemcpyKind in = where == WEDG_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  std::vector<double *> yu(n), yv(n);
+  for (int i = 0; i < n; ++i) {
+    wedg_ws *ws = G[i];
+    const size_t nU = (size_t)ws->E * ws->nu * ws->nu, nV = (size_t)ws->E * ws->nv * ws->nv;
+    yu[i] = ws->rk_y;
+    yv[i] = ws->rk_y + nU;
+    CK(ws, cudaMemcpyAsync(yu[i], u0[i], sizeof(double) * nU, in, st));
+    CK(ws, cudaMemcpyAsync(yv[i], v0[i], sizeof(double) * nV, in, st));
+    ws->rk_t.assign(nsteps + 1, t0);
+    for (int64_t k = 0; k < nsteps; ++k) ws->rk_t[k + 1] = ws->rk_t[k] + dt;
+    if ((rc = reset_flags(ws))) return rc;
+  }
+  const std::vector<double> &t = G[0]->rk_t;
+  for (int64_t k = 0; k < nsteps; ++k) {
+    if (k % every == 0)
+      for (wedg_ws *ws : G)
+        CK(ws, cudaMemcpyAsync(ws->rk_chk[k / every], ws->rk_y,
+                               sizeof(double) * ws->E * (ws->nu * ws->nu + ws->nv * ws->nv), cudaMemcpyDeviceToDevice,
+                               st));
+    if ((rc = group_rk4(G, yu.data(), yv.data(), t[k], dt, 1))) return rc;
+  }
+  CK(G[0], cudaGetLastError());
+  int first = WEDG_OK;
+  for (wedg_ws *ws : G) {
+    const int64_t launches = ws->stats.kernel_launches;
+    rc = collect(ws);
+    ws->stats.kernel_launches = launches;
+    if (rc != WEDG_OK && rc != WEDG_WARN_CG_NOT_CONVERGED) return rc;
+    if (rc != WEDG_OK && first == WEDG_OK) first = rc;
+    if (!ws->stats.finite) return argument_error(ws, "the forward run is not finite");
+  }
+  const cudaMemcpyKind out = where == WEDG_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  for (int i = 0; i < n; ++i) {
+    wedg_ws *ws = G[i];
+    const size_t nU = (size_t)ws->E * ws->nu * ws->nu, nV = (size_t)ws->E * ws->nv * ws->nv;
+    if (uT[i]) CK(ws, cudaMemcpy(uT[i], yu[i], sizeof(double) * nU, out));
+    if (vT[i]) CK(ws, cudaMemcpy(vT[i], yv[i], sizeof(double) * nV, out));
+    ws->rk_dt = dt;
+    ws->rk_nsteps = nsteps;
+    ws->rk_every = every;
+    ws->rk_ready = true;
+  }
+  return first;
+}
+
+// The reverse sweep of every workspace of a group after its forward run (wedg_rk4_adjoint_reverse;
+// several workspaces: the forward runs must have the same steps, dt and checkpoint interval, and
+// every stage's transpose runs as multi-instance launches over the group, which needs the stage
+// data of one segment of every workspace kept at once; when that does not fit the allowance the
+// workspaces are reversed one after the other)
+int adjoint_reverse_group(const std::vector<wedg_ws *> &G, const double *const *lam_u, const double *const *lam_v,
+                          double *const *gu, double *const *gv, double *const *g_c2, double *const *g_alpha,
+                          double *const *g_beta, int where) {
+  const int n = (int)G.size();
+  for (wedg_ws *ws : G) ws->stats.kernel_launches = 0;
+  const bool params = g_c2[0] || g_alpha[0] || g_beta[0];
+  for (int i = 0; i < n; ++i) {
+    wedg_ws *ws = G[i];
+    if (!ws->rk_ready)
+      return argument_error(ws, "no forward run with checkpoints (wedg_rk4_adjoint_forward) to reverse");
+    if (!lam_u[i] || !lam_v[i] || !gu[i] || !gv[i]) return argument_error(ws, "null pointer");
+    const bool p = g_c2[i] || g_alpha[i] || g_beta[i];
+    if (p != params || (p && !(g_c2[i] && g_alpha[i] && g_beta[i])))
+      return argument_error(ws, "give all three parameter gradients or none");
+    if (p && (!ws->fast || !ws->cfg.src_on || ws->cfg.mms_on))
+      return argument_error(ws, "parameter gradients need source mode and c², α, β constant on each element");
+    if (ws->rk_nsteps != G[0]->rk_nsteps || ws->rk_every != G[0]->rk_every || ws->rk_dt != G[0]->rk_dt)
+      return argument_error(ws, "the forward runs of a group need the same steps, dt and checkpoint interval");
+  }
+  const int64_t nsteps = G[0]->rk_nsteps, every = G[0]->rk_every;
+  const int64_t nchk = nsteps ? (nsteps + every - 1) / every : 0;
+  const double dt = G[0]->rk_dt;
+  // keep the forward data of every stage of a segment when it fits the memory allowance
+  const int64_t seg = std::min<int64_t>(every, std::max<int64_t>(nsteps, 1));
+  size_t need = 0, have = 0, allow = 0;
+  bool bounded = true;
+  for (wedg_ws *ws : G) {
+    need += (size_t)(4 * seg) * stage_data_bytes(ws);
+    have += ws->rk_keep.size() * stage_data_bytes(ws);
+    if (ws->adj_mem >= 0) allow += (size_t)ws->adj_mem;
+    else bounded = false;
+  }
+  bool keep;
+  if (!bounded) {
+    size_t fr = 0, tot = 0;
+    keep = cudaMemGetInfo(&fr, &tot) == cudaSuccess && need <= (fr + have) / 2;
+  } else {
+    keep = need <= allow;
+  }
+  if (n > 1 && !keep) {
+    // one after the other, each with its own allowance
+    for (int i = 0; i < n; ++i) {
+      const int rc = adjoint_reverse_group({G[i]}, lam_u + i, lam_v + i, gu + i, gv + i, g_c2 + i, g_alpha + i,
+                                           g_beta + i, where);
+      if (rc != WEDG_OK && rc != WEDG_WARN_CG_NOT_CONVERGED) return rc;
+    }
+    return WEDG_OK;
+  }
+  int rc;
+  StreamGuard guard(G);
+  cudaStream_t st = G[0]->stream;
+  const cudaMemcpyKind in = where == WEDG_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  std::vector<size_t> nU(n), nV(n), nn(n);
+  for (int i = 0; i < n; ++i) {
+    wedg_ws *ws = G[i];
+    nU[i] = (size_t)ws->E * ws->nu * ws->nu;
+    nV[i] = (size_t)ws->E * ws->nv * ws->nv;
+    nn[i] = nU[i] + nV[i];
+    CK(ws, cudaMemcpyAsync(ws->rk_lam, lam_u[i], sizeof(double) * nU[i], in, st));
+    CK(ws, cudaMemcpyAsync(ws->rk_lam + nU[i], lam_v[i], sizeof(double) * nV[i], in, st));
+    if (params) CK(ws, cudaMemsetAsync(ws->rk_par, 0, sizeof(double) * 3 * ws->E, st));
+    if ((rc = reset_flags(ws))) return rc;
+    if (keep) {
+      const size_t E = ws->E;
+      const size_t nd = (size_t)ws->nu * ws->nu + ws->nv * ws->nv + 12 * ws->nq + ws->qh * ws->qh + 2;
+      while ((int64_t)ws->rk_keep.size() < 4 * seg) {
+        wedg_ws::StageData d;
+        double *bd;
+        int *ib;
+        if ((rc = dalloc(ws, &bd, nd * E)) || (rc = dalloc(ws, &ib, E * (1 + NBIN) + 2 * NBIN))) return rc;
+        d.k = bd;
+        d.tr = d.k + nn[i];
+        d.G = d.tr + 12 * (size_t)ws->nq * E;
+        d.th = d.G + (size_t)ws->qh * ws->qh * E;
+        d.de = d.th + E;
+        d.nst = ib;
+        d.bins = ib + E;
+        d.bin_count = ib + E * (1 + NBIN);
+        ws->rk_keep.push_back(d);
+      }
+    }
+  }
+  // out_i = a x_i + b y_i (+ z_i) for the group; xs etc. give the instance's buffers
+  auto lin = [&](auto out, double a, auto x, double b, auto y, auto z) -> int {
+    std::vector<LinPtrs> p(n);
+    for (int i = 0; i < n; ++i) {
+      p[i] = LinPtrs{nn[i], out(i), x(i), y(i), z(i)};
+      G[i]->stats.kernel_launches += 1;
+    }
+    const cudaError_t e = multi_lincomb(p, a, b, st);
+    return e == cudaSuccess ? WEDG_OK : cuda_fail(G[0], e, "k_lincomb_m");
+  };
+  auto none = [](int) -> const double * { return nullptr; };
+  const double ca[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};
+  const double cb[4] = {0.5 * dt, 0.5 * dt, dt, 0.0};
+  const double cs[3] = {0.5 * dt, 0.5 * dt, dt};
+  std::vector<StageIO> S(n);
+  std::vector<Fields> F(n);
+  std::vector<const double *> lu(n), lv(n);
+  std::vector<double *> ggu(n), ggv(n), gpar(n);
+  // ---- reverse pass, segment by segment
+  for (int64_t c = nchk - 1; c >= 0; --c) {
+    const int64_t k0 = c * every, k1 = std::min(nsteps, k0 + every);
+    for (int i = 0; i < n; ++i)
+      CK(G[i], cudaMemcpyAsync(G[i]->rk_y, G[i]->rk_chk[c], sizeof(double) * nn[i], cudaMemcpyDeviceToDevice, st));
+    for (int64_t k = k0; k < k1; ++k) {
+      if (keep) {
+        // the step as four RHS evaluations (their outputs and data kept) and the RK4 combinations:
+        // Y1 = y, Y_{s+1} = y + c_s K_s, y ← y + dt/6 (K1 + 2K2 + 2K3 + K4)
+        const size_t q = 4 * (k - k0);
+        for (int i = 0; i < n; ++i)
+          CK(G[i], cudaMemcpyAsync(G[i]->rk_seg[q], G[i]->rk_y, sizeof(double) * nn[i], cudaMemcpyDeviceToDevice, st));
+        for (int s = 0; s < 4; ++s) {
+          for (int i = 0; i < n; ++i) {
+            wedg_ws *ws = G[i];
+            const std::vector<double> &t = ws->rk_t;
+            const double ts[4] = {t[k], t[k] + 0.5 * dt, t[k] + 0.5 * dt, t[k] + dt};
+            wedg_ws::StageData &d = ws->rk_keep[q + s];
+            const double *Y = ws->rk_seg[q + s];
+            S[i] = StageIO{};
+            S[i].xu = Y; S[i].xv = Y + nU[i];
+            stage_factors(ws, ts[s], S[i]);
+            S[i].mode = OUT_RHS;
+            S[i].ut = d.k;
+            S[i].vt = d.k + nU[i];
+            CK(ws, cudaMemsetAsync(d.bin_count, 0, 2 * NBIN * sizeof(int), st));
+            d.parity = ws->parity;
+            F[i] = kept_fields(ws, d);
+          }
+          if ((rc = group_stage(G, S, F))) return rc;
+          if (s < 3 &&
+              (rc = lin([&](int i) { return G[i]->rk_seg[q + s + 1]; }, cs[s],
+                        [&](int i) -> const double * { return G[i]->rk_keep[q + s].k; }, 1.0,
+                        [&](int i) -> const double * { return G[i]->rk_y; }, none)))
+            return rc;
+        }
+        auto K = [&](int s) { return [&, s](int i) -> const double * { return G[i]->rk_keep[q + s].k; }; };
+        auto acc = [&](int i) { return G[i]->rk_acc; };
+        auto accc = [&](int i) -> const double * { return G[i]->rk_acc; };
+        auto y = [&](int i) { return G[i]->rk_y; };
+        auto yc = [&](int i) -> const double * { return G[i]->rk_y; };
+        if ((rc = lin(acc, 2.0, K(1), 1.0, K(0), none)) || (rc = lin(acc, 2.0, K(2), 1.0, K(3), accc)) ||
+            (rc = lin(y, dt / 6.0, accc, 1.0, yc, none)))
+          return rc;
+        continue;
+      }
+      // one workspace without the memory to keep stage data: the stage states Y1..Y4 only
+      wedg_ws *ws = G[0];
+      double *su[4], *sv[4];
+      for (int s = 0; s < 4; ++s) {
+        su[s] = ws->rk_seg[4 * (k - k0) + s];
+        sv[s] = su[s] + nU[0];
+      }
+      if ((rc = enqueue_rk4(ws, ws->rk_y, ws->rk_y + nU[0], ws->rk_t[k], dt, 1, nullptr, 0, su, sv))) return rc;
+    }
+    for (int64_t k = k1 - 1; k >= k0; --k) {
+      // K̄_s = ca[s] λ + cb[s] Ȳ_{s+1}, Ȳ = Jᵀ K̄ at the stage state: y_{n+1} = y + dt/6 (K1 + 2K2 +
+      // 2K3 + K4), Y2 = y + dt/2 K1, Y3 = y + dt/2 K2, Y4 = y + dt K3
+      const size_t q = 4 * (k - k0);
+      for (int s = 3; s >= 0; --s) {
+        if ((rc = lin([&](int i) { return G[i]->rk_kbar; }, ca[s],
+                      [&](int i) -> const double * { return G[i]->rk_lam; }, cb[s],
+                      [&](int i) -> const double * { return s == 3 ? nullptr : G[i]->rk_g; }, none)))
+          return rc;
+        for (int i = 0; i < n; ++i) {
+          wedg_ws *ws = G[i];
+          lu[i] = ws->rk_kbar;
+          lv[i] = ws->rk_kbar + nU[i];
+          ggu[i] = ws->rk_g;
+          ggv[i] = ws->rk_g + nU[i];
+          gpar[i] = params ? ws->rk_par : nullptr;
+        }
+        if (keep) {
+          for (int i = 0; i < n; ++i) {
+            wedg_ws *ws = G[i];
+            const std::vector<double> &t = ws->rk_t;
+            const double ts[4] = {t[k], t[k] + 0.5 * dt, t[k] + 0.5 * dt, t[k] + dt};
+            const wedg_ws::StageData &d = ws->rk_keep[q + s];
+            const double *Y = ws->rk_seg[q + s];
+            S[i] = StageIO{};
+            S[i].xu = Y; S[i].xv = Y + nU[i];
+            stage_factors(ws, ts[s], S[i]);
+            S[i].parity = d.parity;
+            S[i].ut = d.k;
+            S[i].vt = d.k + nU[i];
+            F[i] = kept_fields(ws, d);
+          }
+          rc = group_adjoint_core(G, F, S, lu, lv, ggu, ggv, gpar);
+        } else {
+          wedg_ws *ws = G[0];
+          const std::vector<double> &t = ws->rk_t;
+          const double ts[4] = {t[k], t[k] + 0.5 * dt, t[k] + 0.5 * dt, t[k] + dt};
+          const double *Y = ws->rk_seg[q + s];
+          rc = enqueue_rhs_adjoint(ws, Y, Y + nU[0], ts[s], lu[0], lv[0], ggu[0], ggv[0], gpar[0]);
+        }
+        if (rc) return rc;
+        if ((rc = lin([&](int i) { return G[i]->rk_acc; }, 1.0,
+                      [&](int i) -> const double * { return s == 3 ? G[i]->rk_lam : G[i]->rk_acc; }, 1.0,
+                      [&](int i) -> const double * { return G[i]->rk_g; }, none)))
+          return rc;
+      }
+      for (wedg_ws *ws : G) std::swap(ws->rk_lam, ws->rk_acc);
+    }
+  }
+  CK(G[0], cudaGetLastError());
+  int first = WEDG_OK;
+  const cudaMemcpyKind out = where == WEDG_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  for (int i = 0; i < n; ++i) {
+    wedg_ws *ws = G[i];
+    const int64_t launches = ws->stats.kernel_launches;
+    rc = collect(ws);
+    ws->stats.kernel_launches = launches;
+    if (rc != WEDG_OK && first == WEDG_OK) first = rc;
+    CK(ws, cudaMemcpy(gu[i], ws->rk_lam, sizeof(double) * nU[i], out));
+    CK(ws, cudaMemcpy(gv[i], ws->rk_lam + nU[i], sizeof(double) * nV[i], out));
+    if (params) {
+      CK(ws, cudaMemcpy(g_c2[i], ws->rk_par, sizeof(double) * ws->E, out));
+      CK(ws, cudaMemcpy(g_alpha[i], ws->rk_par + ws->E, sizeof(double) * ws->E, out));
+      CK(ws, cudaMemcpy(g_beta[i], ws->rk_par + 2 * ws->E, sizeof(double) * ws->E, out));
+    }
+  }
+  return first;
+}
+
+}  // namespace
+
+namespace wedg {
+
+// Step bookkeeping of many instances in one launch (the batched form): thread i does
+// k_step_done's work for instance i
+struct StepFlags {
+  unsigned long long *err;
+  const unsigned int *nonfinite;
+  long long *steps_done;
+};
+__global__ void k_step_done_m(int n, const StepFlags *f, int stop_nonfinite) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const StepFlags x = f[i];
+  if (*x.err != ERR_NONE) return;
+  *x.steps_done += 1;
+  if (stop_nonfinite && *x.nonfinite) *x.err = (3ull << ERR_CLASS_SHIFT);
+}
+
+// k_rk4_final of many CG instances in one launch: blockIdx.y is the instance
+struct FinalArgs {
+  int n_u, n_v;
+  double *u, *v;
+  const double *accu, *accv;
+  double c;
+  const unsigned long long *err;
+  unsigned int *nonfinite;
+};
+__global__ void k_rk4_final_m(const FinalArgs *a) {
+  const FinalArgs A = a[blockIdx.y];
+  if (*(volatile const unsigned long long *)A.err != ERR_NONE) return;
+  bool fin = true;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n_u + A.n_v; i += gridDim.x * blockDim.x) {
+    if (i < A.n_u) {
+      const double x = A.u[i] + A.c * A.accu[i];
+      A.u[i] = x;
+      fin = fin && isfinite(x);
+    } else {
+      const int l = i - A.n_u;
+      const double x = A.v[l] + A.c * A.accv[l];
+      A.v[l] = x;
+      fin = fin && isfinite(x);
+    }
+  }
+  if (!fin) atomicOr(A.nonfinite, 1u);
+}
+
+}  // namespace wedg
+
+namespace {
+
+// Instances of a batch that run the same kernels -- the same degrees, coefficient kernels
+// (constant per element or not), mass solver and 1D operators -- and share one multi-instance
+// launch per kernel and stage, with the bucket's launch shape: threads per block of k_prep and of
+// the mass solves, and `persist` (0: one block per virtual block; p > 0: a persistent grid of p
+// times the blocks the SMs hold at once)
+struct BatchBucket {
+  std::vector<int> ids;   // instances, largest mesh first
+  Launchers L;
+  std::vector<char> basis;
+  int nu = 0, nv = 0;
+  bool fast = false, cg = false;
+  int prep_threads = 128, mass_threads = CHEB_THREADS, persist = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t join = nullptr;
+  StepFlags *d_flags = nullptr;   // per instance of the bucket, for k_step_done_m
+  FinalArgs *d_final = nullptr;   // per instance, for k_rk4_final_m (CG)
+};
+
+}  // namespace
+
+// A batch of workspaces advanced by one replayed CUDA graph per step (wedg_batch_*): per bucket
+// of instances, one launch per kernel and stage covering all of its instances
 struct wedg_batch {
   std::vector<wedg_ws *> ws;
+  std::vector<BatchBucket> buckets;
+  int nsm = 152;
   cudaStream_t main = nullptr;
   cudaEvent_t fork = nullptr;
-  std::vector<cudaEvent_t> join;
   cudaEvent_t half_done[2] = {nullptr, nullptr};   // the host half of the tables may be refilled
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   // what the captured graph was made for
   std::vector<double *> gu, gv;
   std::vector<double> gdt;
-  std::vector<int64_t> gshape;   // the instances' shape_gen
   int gstop = -1;
+  int64_t shape_gen = 0, gshape = -1;              // changes of the buckets' launch shapes
   // per instance: device factor table of 2 chunks (the kernels index it by step mod 2 chunks)
   std::vector<double *> d_tf;
   double *h_tf = nullptr;                           // pinned: 2 halves × instances × one chunk
+  std::vector<void *> dmem;                         // device arrays of the buckets
   ~wedg_batch() {
     if (main) cudaStreamSynchronize(main);
+    for (BatchBucket &k : buckets)
+      if (k.st) cudaStreamSynchronize(k.st);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     for (double *p : d_tf) cudaFree(p);
+    for (void *p : dmem) cudaFree(p);
     if (h_tf) cudaFreeHost(h_tf);
-    for (cudaEvent_t e : join) cudaEventDestroy(e);
+    for (BatchBucket &k : buckets) {
+      if (k.join) cudaEventDestroy(k.join);
+      if (k.st) cudaStreamDestroy(k.st);
+    }
     for (cudaEvent_t e : half_done)
       if (e) cudaEventDestroy(e);
     if (fork) cudaEventDestroy(fork);
     if (main) cudaStreamDestroy(main);
   }
 };
+
+namespace {
+
+// Physical blocks of a multi-instance launch of `total` virtual blocks: all of them, or with
+// persist > 0 that many times the blocks the SMs hold at once (resident blocks per SM at 128
+// threads, scaled for smaller blocks)
+int bucket_grid(const wedg_batch *b, const BatchBucket &k, int total, int resident128, int threads) {
+  if (k.persist <= 0) return total;
+  const int cap = k.persist * b->nsm * resident128 * (128 / std::max(32, std::min(128, threads)));
+  return std::min(total, std::max(cap, 1));
+}
+
+// Enqueue one RK4 step of every instance of bucket k on its stream: per stage, k_prep, k_stage
+// and the mass solve as multi-instance launches (chunks of up to MultiStage::cap instances), then
+// the last update of CG instances and the step bookkeeping. u, v, t, dt are indexed by instance
+// (t is ignored with tables: the stage kernels then read their time factors from the instances'
+// device tables d_tf, tf_n steps). Advances each instance's bin parity as enqueue_stage does.
+int enqueue_bucket_step(wedg_batch *b, BatchBucket &k, double *const *u, double *const *v, const double *t,
+                        const double *dt, int stop_nonfinite, bool tables, long long tf_n) {
+  const int n = (int)k.ids.size();
+  const int BT = stage_threads(k.nu, k.nv, k.fast);
+  const int TPW = 32 / (qhigh(k.nu, k.nv) / 2 + (qhigh(k.nu, k.nv) & 1));
+  const int mass_tile = (k.mass_threads / 32) * TPW;
+  std::vector<StageArgs> args(n);
+  for (int s = 0; s < 4; ++s) {
+    for (int x = 0; x < n; ++x) {
+      const int i = k.ids[x];
+      wedg_ws *w = b->ws[i];
+      StageIO S = rk4_stage_io(w, u[i], v[i], s, tables ? 0.0 : t[i], dt[i], tables ? b->d_tf[i] : nullptr,
+                               tables ? tf_n : 0, nullptr, nullptr);
+      S.parity = w->parity;
+      w->parity = 1 - w->parity;
+      args[x].F = w->F;
+      args[x].S = S;
+      w->stats.kernel_launches += 3;
+      w->stats.element_stages += w->E;
+    }
+    for (int kind = 0; kind < 3; ++kind) {
+      const int tile = kind == 0 ? k.prep_threads : kind == 1 ? BT : mass_tile;
+      for (int c0 = 0; c0 < n; c0 += MultiStage::cap) {
+        const int m = std::min(n - c0, MultiStage::cap);
+        MultiStage P;
+        P.n = m;
+        P.tile = tile;
+        P.first[0] = 0;
+        for (int x = 0; x < m; ++x) {
+          P.a[x] = args[c0 + x];
+          P.first[x + 1] = P.first[x] + (P.a[x].F.E + tile - 1) / tile;
+        }
+        const int total = P.first[m];
+        cudaError_t e;
+        if (kind == 0)
+          e = k.L.prep_m(k.basis.data(), P, bucket_grid(b, k, total, 3, k.prep_threads), k.prep_threads, k.st);
+        else if (kind == 1)
+          e = k.L.stage_m(k.basis.data(), P, bucket_grid(b, k, total, 2, 128), BT, k.st);
+        else
+          e = k.L.mass_m(k.basis.data(), P, bucket_grid(b, k, total, 3, k.mass_threads), k.mass_threads, k.st);
+        if (e != cudaSuccess) return cuda_fail(b->ws[k.ids[0]], e, "multi-instance launch");
+      }
+    }
+  }
+  if (k.cg) {
+    int most = 1;
+    for (int i : k.ids) most = std::max(most, b->ws[i]->E * (b->ws[i]->nu * b->ws[i]->nu + b->ws[i]->nv * b->ws[i]->nv));
+    k_rk4_final_m<<<dim3(std::min((most + 255) / 256, 152 * 8), n), 256, 0, k.st>>>(k.d_final);
+  }
+  k_step_done_m<<<(n + 127) / 128, 128, 0, k.st>>>(n, k.d_flags, stop_nonfinite);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(b->ws[k.ids[0]], e, "multi-instance launch");
+  return WEDG_OK;
+}
+
+// The device arguments of k_rk4_final_m for the CG buckets (the state pointers and dt change).
+// A captured graph reads them, so it is captured again after any upload.
+int upload_final_args(wedg_batch *b, double *const *u, double *const *v, const double *dt) {
+  b->gstop = -1;
+  for (BatchBucket &k : b->buckets) {
+    if (!k.cg) continue;
+    const cudaError_t es = cudaStreamSynchronize(k.st);   // no launch of the bucket still reads them
+    if (es != cudaSuccess) return cuda_fail(b->ws[k.ids[0]], es, "wedg_batch_rk4_steps");
+    std::vector<FinalArgs> fa(k.ids.size());
+    for (size_t x = 0; x < k.ids.size(); ++x) {
+      const int i = k.ids[x];
+      wedg_ws *w = b->ws[i];
+      fa[x] = FinalArgs{w->E * w->nu * w->nu, w->E * w->nv * w->nv, u[i], v[i], w->accu, w->accv, dt[i] / 6.0,
+                        w->F.err, w->F.nonfinite};
+    }
+    const cudaError_t e = cudaMemcpy(k.d_final, fa.data(), sizeof(FinalArgs) * fa.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(b->ws[k.ids[0]], e, "wedg_batch_rk4_steps");
+  }
+  return WEDG_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -809,11 +1573,15 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
     F.gam[s] = cfg->gamma_abc[s]; F.eta[s] = cfg->eta_abc[s]; F.sig[s] = cfg->sigma[s];
     F.kb[s] = cfg->kb[s]; F.kap[s] = cfg->kappa[s];
   }
-  // sets the shared-memory attributes of k_stage and k_cg (a launch of zero blocks does nothing else)
-  ws->L.stage(ws->basis.data(), F, StageIO{}, 0, 0, nullptr);
-  ws->L.mass(ws->basis.data(), F, StageIO{}, 0, 0, nullptr);
-  cudaMemset(F.bin_count, 0, 2 * NBIN * sizeof(int));
-  cudaError_t ce = cudaStreamCreateWithFlags(&ws->own_stream, cudaStreamNonBlocking);
+  // the dynamic shared-memory opt-in of k_stage on this device (a launch of zero blocks does nothing else)
+  cudaError_t ce = ws->L.stage(ws->basis.data(), F, StageIO{}, 0, 0, nullptr);
+  if (ce == cudaSuccess) ce = cudaMemset(F.bin_count, 0, 2 * NBIN * sizeof(int));
+  if (ce != cudaSuccess) {
+    int r = cuda_fail(ws, ce, "wedg_create");
+    wedg_destroy(ws);
+    return r;
+  }
+  ce = cudaStreamCreateWithFlags(&ws->own_stream, cudaStreamNonBlocking);
   if (ce != cudaSuccess) {
     int r = cuda_fail(ws, ce, "cudaStreamCreate");
     wedg_destroy(ws);
@@ -908,6 +1676,26 @@ int wedg_batch_create(int n, wedg_ws *const *instances, wedg_batch **out) {
     if (!instances[i]) return WEDG_ERR_ARGUMENT;
   wedg_batch *b = new wedg_batch();
   b->ws.assign(instances, instances + n);
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, dev);
+  // buckets: the same kernels and the same 1D operators
+  for (int i = 0; i < n; ++i) {
+    wedg_ws *w = b->ws[i];
+    const bool cg = w->cfg.mass_solver == WEDG_CG;
+    size_t k = 0;
+    for (; k < b->buckets.size(); ++k) {
+      const BatchBucket &q = b->buckets[k];
+      if (q.nu == w->nu && q.nv == w->nv && q.fast == w->fast && q.cg == cg && q.basis == w->basis) break;
+    }
+    if (k == b->buckets.size()) {
+      BatchBucket q;
+      q.nu = w->nu; q.nv = w->nv; q.fast = w->fast; q.cg = cg;
+      q.L = w->L;
+      q.basis = w->basis;
+      b->buckets.push_back(q);
+    }
+    b->buckets[k].ids.push_back(i);
+  }
   const size_t per = (size_t)2 * WEDG_BATCH_CHUNK * 4 * 8;    // doubles of one instance's table
   bool ok = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess &&
@@ -915,12 +1703,26 @@ int wedg_batch_create(int n, wedg_ws *const *instances, wedg_batch **out) {
             cudaEventCreateWithFlags(&b->half_done[1], cudaEventDisableTiming) == cudaSuccess &&
             cudaMallocHost(&b->h_tf, sizeof(double) * per * n) == cudaSuccess;
   for (int i = 0; i < n && ok; ++i) {
-    cudaEvent_t e = nullptr;
     double *d = nullptr;
-    ok = cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
-    if (ok) b->join.push_back(e);
-    ok = ok && cudaMalloc(&d, sizeof(double) * per) == cudaSuccess;
+    ok = cudaMalloc(&d, sizeof(double) * per) == cudaSuccess;
     if (ok) b->d_tf.push_back(d);
+  }
+  for (BatchBucket &k : b->buckets) {
+    if (!ok) break;
+    std::stable_sort(k.ids.begin(), k.ids.end(), [&](int x, int y) { return b->ws[x]->E > b->ws[y]->E; });
+    std::vector<StepFlags> fl;
+    for (int i : k.ids) fl.push_back(StepFlags{b->ws[i]->F.err, b->ws[i]->F.nonfinite, b->ws[i]->steps_done});
+    void *p = nullptr, *q = nullptr;
+    ok = cudaStreamCreateWithFlags(&k.st, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&k.join, cudaEventDisableTiming) == cudaSuccess &&
+         cudaMalloc(&p, sizeof(StepFlags) * fl.size()) == cudaSuccess &&
+         cudaMalloc(&q, sizeof(FinalArgs) * fl.size()) == cudaSuccess;
+    if (p) b->dmem.push_back(p);
+    if (q) b->dmem.push_back(q);
+    if (!ok) break;
+    k.d_flags = static_cast<StepFlags *>(p);
+    k.d_final = static_cast<FinalArgs *>(q);
+    ok = cudaMemcpy(k.d_flags, fl.data(), sizeof(StepFlags) * fl.size(), cudaMemcpyHostToDevice) == cudaSuccess;
   }
   if (!ok) {
     cudaGetLastError();
@@ -932,6 +1734,35 @@ int wedg_batch_create(int n, wedg_ws *const *instances, wedg_batch **out) {
 }
 
 void wedg_batch_destroy(wedg_batch *b) { delete b; }
+
+int wedg_batch_bucket_count(const wedg_batch *b) { return b ? (int)b->buckets.size() : 0; }
+
+int wedg_batch_get_shape(const wedg_batch *b, int bucket, wedg_batch_shape *out) {
+  if (!b || !out || bucket < 0 || bucket >= (int)b->buckets.size()) return WEDG_ERR_ARGUMENT;
+  const BatchBucket &k = b->buckets[bucket];
+  out->qu1 = k.nu;
+  out->qv1 = k.nv;
+  out->instances = (int32_t)k.ids.size();
+  out->fast = k.fast ? 1 : 0;
+  out->prep_threads = k.prep_threads;
+  out->mass_threads = k.mass_threads;
+  out->persist = k.persist;
+  return WEDG_OK;
+}
+
+int wedg_batch_set_shape(wedg_batch *b, int bucket, int prep_threads, int mass_threads, int persist) {
+  if (!b || bucket < 0 || bucket >= (int)b->buckets.size()) return WEDG_ERR_ARGUMENT;
+  auto ok = [](int t) { return t >= 32 && t <= CHEB_THREADS && t % 32 == 0; };
+  if (!ok(prep_threads) || !ok(mass_threads) || persist < 0 || persist > 8) return WEDG_ERR_ARGUMENT;
+  BatchBucket &k = b->buckets[bucket];
+  if (k.prep_threads != prep_threads || k.mass_threads != mass_threads || k.persist != persist) {
+    k.prep_threads = prep_threads;
+    k.mass_threads = mass_threads;
+    k.persist = persist;
+    ++b->shape_gen;
+  }
+  return WEDG_OK;
+}
 
 int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_dev, const double *t0,
                          const double *dt, int64_t nsteps, int stop_nonfinite, int64_t *steps_done, int *finite,
@@ -950,35 +1781,35 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
     cudaError_t e_ = (call);                      \
     if (e_ != cudaSuccess) return cuda_err(e_);   \
   } while (0)
-  // ---- flags of every instance reset on its stream, before anything of the batch's stream
+  // ---- flags of every instance reset on the batch's stream (after the instance's own work)
   for (int i = 0; i < n; ++i) {
     wedg_ws *w = b->ws[i];
     w->stats.kernel_launches = 0;
-    int rc = reset_flags(w);
+    BK(cudaEventRecord(b->fork, w->stream));
+    BK(cudaStreamWaitEvent(b->main, b->fork, 0));
+    cudaStream_t own = w->stream;
+    w->stream = b->main;
+    const int rc = reset_flags(w);
+    w->stream = own;
     if (rc) return rc;
-    BK(cudaEventRecord(b->join[i], w->stream));
-    BK(cudaStreamWaitEvent(b->main, b->join[i], 0));
   }
   // ---- the graph of one step of every instance, captured again when its key changed
-  bool same = b->exec && b->gstop == (stop_nonfinite ? 1 : 0);
-  for (int i = 0; i < n && same; ++i)
-    same = b->gu[i] == u_dev[i] && b->gv[i] == v_dev[i] && b->gdt[i] == dt[i] && b->gshape[i] == b->ws[i]->shape_gen;
+  bool same = b->exec && b->gstop == (stop_nonfinite ? 1 : 0) && b->gshape == b->shape_gen;
+  for (int i = 0; i < n && same; ++i) same = b->gu[i] == u_dev[i] && b->gv[i] == v_dev[i] && b->gdt[i] == dt[i];
   if (!same) {
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    int rc = upload_final_args(b, u_dev, v_dev, dt);
+    if (rc) return rc;
     BK(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
     cudaError_t ce = cudaEventRecord(b->fork, b->main);
-    int rc = WEDG_OK;
-    for (int i = 0; i < n && ce == cudaSuccess && rc == WEDG_OK; ++i) {
-      wedg_ws *w = b->ws[i];
-      ce = cudaStreamWaitEvent(w->stream, b->fork, 0);
+    for (size_t q = 0; q < b->buckets.size() && ce == cudaSuccess && rc == WEDG_OK; ++q) {
+      BatchBucket &k = b->buckets[q];
+      ce = cudaStreamWaitEvent(k.st, b->fork, 0);
       if (ce != cudaSuccess) break;
-      const bool timing = w->timing;
-      w->timing = false;
-      rc = enqueue_rk4(w, u_dev[i], v_dev[i], 0.0, dt[i], stop_nonfinite ? 1 : 0, b->d_tf[i], 2 * C);
-      w->timing = timing;
-      if (rc == WEDG_OK) ce = cudaEventRecord(b->join[i], w->stream);
-      if (ce == cudaSuccess && rc == WEDG_OK) ce = cudaStreamWaitEvent(b->main, b->join[i], 0);
+      rc = enqueue_bucket_step(b, k, u_dev, v_dev, nullptr, dt, stop_nonfinite ? 1 : 0, true, 2 * C);
+      if (rc == WEDG_OK) ce = cudaEventRecord(k.join, k.st);
+      if (ce == cudaSuccess && rc == WEDG_OK) ce = cudaStreamWaitEvent(b->main, k.join, 0);
     }
     cudaGraph_t g = nullptr;
     const cudaError_t ce2 = cudaStreamEndCapture(b->main, &g);
@@ -995,8 +1826,7 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
     b->gu.assign(u_dev, u_dev + n);
     b->gv.assign(v_dev, v_dev + n);
     b->gdt.assign(dt, dt + n);
-    b->gshape.resize(n);
-    for (int i = 0; i < n; ++i) b->gshape[i] = b->ws[i]->shape_gen;
+    b->gshape = b->shape_gen;
     b->gstop = stop_nonfinite ? 1 : 0;
   }
   // ---- the steps, one chunk of factor tables at a time (double-buffered, host and device)
@@ -1022,8 +1852,9 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
   int first = WEDG_OK;
   for (int i = 0; i < n; ++i) {
     wedg_ws *w = b->ws[i];
-    w->stats.kernel_launches = 0;
+    const int64_t launches = w->stats.kernel_launches;
     const int rc = collect(w);
+    w->stats.kernel_launches = launches;
     if (steps_done) steps_done[i] = w->stats.steps_done;
     if (finite) finite[i] = w->stats.finite;
     if (status) status[i] = rc;
@@ -1044,19 +1875,49 @@ int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_de
     sv[i] = b->ws[i]->d_v;
     t1[i] = t0[i] + dt[i];
   }
-  // buckets of instances with the same degrees (the same kernels)
-  std::vector<std::pair<int, int>> keys;
-  std::vector<std::vector<int>> bucket;
-  for (int i = 0; i < n; ++i) {
-    const std::pair<int, int> key(b->ws[i]->nu, b->ws[i]->nv);
-    size_t k = 0;
-    while (k < keys.size() && keys[k] != key) ++k;
-    if (k == keys.size()) { keys.push_back(key); bucket.emplace_back(); }
-    bucket[k].push_back(i);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    return cuda_fail(b->ws[0], cudaGetLastError(), "wedg_batch_autotune");
   }
-  // steps steps of the batch from copies of the states, after one untimed step (which captures
-  // the graph), with the present shapes
-  auto trial = [&](double &ms) -> int {
+  // steps RK4 steps of bucket k alone from copies of its instances' states, after one untimed step
+  // (CUDA events on the bucket's stream)
+  auto trial_bucket = [&](BatchBucket &k, double &ms) -> int {
+    for (int i : k.ids) {
+      wedg_ws *w = b->ws[i];
+      const size_t bU = sizeof(double) * w->E * w->nu * w->nu, bV = sizeof(double) * w->E * w->nv * w->nv;
+      cudaStream_t own = w->stream;
+      w->stream = k.st;
+      int rc = reset_flags(w);
+      w->stream = own;
+      if (rc) return rc;
+      cudaError_t e = cudaMemcpyAsync(su[i], u_dev[i], bU, cudaMemcpyDeviceToDevice, k.st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(sv[i], v_dev[i], bV, cudaMemcpyDeviceToDevice, k.st);
+      if (e != cudaSuccess) return cuda_fail(w, e, "wedg_batch_autotune");
+    }
+    int rc = upload_final_args(b, su.data(), sv.data(), dt);
+    if (rc) return rc;
+    std::vector<double> t(t0, t0 + n);
+    if ((rc = enqueue_bucket_step(b, k, su.data(), sv.data(), t.data(), dt, 0, false, 0))) return rc;
+    for (int i : k.ids) t[i] += dt[i];
+    CK(b->ws[k.ids[0]], cudaEventRecord(e0, k.st));
+    for (int64_t it = 0; it < steps; ++it) {
+      if ((rc = enqueue_bucket_step(b, k, su.data(), sv.data(), t.data(), dt, 0, false, 0))) return rc;
+      for (int i : k.ids) t[i] += dt[i];
+    }
+    CK(b->ws[k.ids[0]], cudaEventRecord(e1, k.st));
+    CK(b->ws[k.ids[0]], cudaEventSynchronize(e1));
+    for (int i : k.ids) {
+      rc = collect(b->ws[i]);
+      if (rc != WEDG_OK && rc != WEDG_WARN_CG_NOT_CONVERGED) return rc;
+    }
+    float f = 0;
+    CK(b->ws[k.ids[0]], cudaEventElapsedTime(&f, e0, e1));
+    ms = f;
+    return WEDG_OK;
+  };
+  // the whole batch's step time (graph replays from copies of the states)
+  auto trial_batch = [&](double &ms) -> int {
     for (int i = 0; i < n; ++i) {
       wedg_ws *w = b->ws[i];
       const size_t bU = sizeof(double) * w->E * w->nu * w->nu, bV = sizeof(double) * w->E * w->nv * w->nv;
@@ -1068,27 +1929,86 @@ int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_de
     if (rc != WEDG_OK && rc != WEDG_WARN_CG_NOT_CONVERGED) return rc;
     const auto c0 = std::chrono::steady_clock::now();
     rc = wedg_batch_rk4_steps(b, su.data(), sv.data(), t1.data(), dt, steps, 0, nullptr, nullptr, nullptr);
-    ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c0).count();
+    ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c0).count() / steps;
     return (rc == WEDG_WARN_CG_NOT_CONVERGED) ? WEDG_OK : rc;
   };
-  double best = 0;
-  int rc = trial(best);
-  for (size_t k = 0; k < keys.size() && rc == WEDG_OK; ++k) {
-    const std::vector<int> &ids = bucket[k];
-    int bp = b->ws[ids[0]]->prep_threads, bm = b->ws[ids[0]]->mass_threads;
-    for (int c = 0; c < 2 && rc == WEDG_OK; ++c)
-      for (int q = 0; q < 3 && rc == WEDG_OK; ++q) {
-        const int p = c == 0 ? kTuneThreads[q] : bp, m = c == 0 ? bm : kTuneThreads[q];
-        if (p == bp && m == bm) continue;
-        for (int i : ids) wedg_set_launch_shape(b->ws[i], p, m);
-        double ms = 0;
-        rc = trial(ms);
-        if (rc == WEDG_OK && ms < kTuneGain * best) { best = ms; bp = p; bm = m; }
-      }
-    for (int i : ids) wedg_set_launch_shape(b->ws[i], bp, bm);   // also after a failed trial
+  auto median3 = [](double a, double x, double c) { return std::max(std::min(a, x), std::min(std::max(a, x), c)); };
+  const int nb = (int)b->buckets.size();
+  std::vector<int> def_p(nb), def_m(nb), def_s(nb);
+  for (int q = 0; q < nb; ++q) {
+    def_p[q] = b->buckets[q].prep_threads;
+    def_m[q] = b->buckets[q].mass_threads;
+    def_s[q] = b->buckets[q].persist;
   }
+  int rc = WEDG_OK;
+  // per bucket, alone: one coordinate at a time; a candidate replaces the incumbent only when it is
+  // faster in each of kTuneRepeats paired trials and its median is faster by more than 2 %
+  for (int q = 0; q < nb && rc == WEDG_OK; ++q) {
+    BatchBucket &k = b->buckets[q];
+    for (int c = 0; c < 3 && rc == WEDG_OK; ++c) {
+      for (int x = 0; x < 3 && rc == WEDG_OK; ++x) {
+        const int inc[3] = {k.prep_threads, k.mass_threads, k.persist};
+        int cand[3] = {inc[0], inc[1], inc[2]};
+        cand[c] = c < 2 ? kTuneThreads[x] : x;
+        if (cand[c] == inc[c]) continue;
+        double ti[kTuneRepeats], tc[kTuneRepeats];
+        bool wins = true;
+        for (int r = 0; r < kTuneRepeats && rc == WEDG_OK; ++r) {
+          wedg_batch_set_shape(b, q, inc[0], inc[1], inc[2]);
+          rc = trial_bucket(k, ti[r]);
+          if (rc == WEDG_OK) {
+            wedg_batch_set_shape(b, q, cand[0], cand[1], cand[2]);
+            rc = trial_bucket(k, tc[r]);
+          }
+          wins = wins && rc == WEDG_OK && tc[r] < ti[r];
+        }
+        const bool take = rc == WEDG_OK && wins &&
+                          median3(tc[0], tc[1], tc[2]) < kTuneGain * median3(ti[0], ti[1], ti[2]);
+        const int *keep = take ? cand : inc;
+        wedg_batch_set_shape(b, q, keep[0], keep[1], keep[2]);
+      }
+    }
+  }
+  // the whole batch: the tuned shapes are kept only if they beat the defaults in paired trials
+  double best = 0;
+  if (rc == WEDG_OK) {
+    std::vector<int> tp(nb), tm(nb), ts(nb);
+    for (int q = 0; q < nb; ++q) {
+      tp[q] = b->buckets[q].prep_threads;
+      tm[q] = b->buckets[q].mass_threads;
+      ts[q] = b->buckets[q].persist;
+    }
+    auto apply = [&](const std::vector<int> &p, const std::vector<int> &m, const std::vector<int> &s_) {
+      for (int q = 0; q < nb; ++q) wedg_batch_set_shape(b, q, p[q], m[q], s_[q]);
+    };
+    double td[kTuneRepeats], tt[kTuneRepeats];
+    bool wins = true;
+    for (int r = 0; r < kTuneRepeats && rc == WEDG_OK; ++r) {
+      apply(def_p, def_m, def_s);
+      rc = trial_batch(td[r]);
+      if (rc == WEDG_OK) {
+        apply(tp, tm, ts);
+        rc = trial_batch(tt[r]);
+      }
+      wins = wins && rc == WEDG_OK && tt[r] < td[r];
+    }
+    if (rc == WEDG_OK) {
+      const double md = median3(td[0], td[1], td[2]), mt = median3(tt[0], tt[1], tt[2]);
+      if (wins && mt < md) {
+        apply(tp, tm, ts);
+        best = mt;
+      } else {
+        apply(def_p, def_m, def_s);
+        best = md;
+      }
+    }
+  }
+  if (rc != WEDG_OK)
+    for (int q = 0; q < nb; ++q) wedg_batch_set_shape(b, q, def_p[q], def_m[q], def_s[q]);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   if (rc != WEDG_OK) return rc;
-  if (best_ms) *best_ms = best / steps;
+  if (best_ms) *best_ms = best;
   return WEDG_OK;
 }
 
@@ -1249,197 +2169,57 @@ int wedg_rk4_adjoint_forward(wedg_ws *ws, const double *u0, const double *v0, do
   int rc = check_shapes(ws, u_shape, v_shape);
   if (rc) return rc;
   if (!u0 || !v0) return argument_error(ws, "null pointer");
-  if (nsteps < 0 || every < 1) return argument_error(ws, "nsteps must be ≥ 0 and the checkpoint interval ≥ 1");
-  if ((rc = adjoint_buffers(ws))) return rc;
-  const size_t nU = (size_t)ws->E * ws->nu * ws->nu, nV = (size_t)ws->E * ws->nv * ws->nv, n = nU + nV;
-  const int64_t nchk = nsteps ? (nsteps + every - 1) / every : 0;
-  const int64_t seg = std::min<int64_t>(every, std::max<int64_t>(nsteps, 1));
-  // buffers: a state is u followed by v (n doubles)
-  if (!ws->rk_lam) {
-    if ((rc = dalloc(ws, &ws->rk_lam, n)) || (rc = dalloc(ws, &ws->rk_acc, n)) || (rc = dalloc(ws, &ws->rk_kbar, n)) ||
-        (rc = dalloc(ws, &ws->rk_g, n)) || (rc = dalloc(ws, &ws->rk_y, n)) ||
-        (rc = dalloc(ws, &ws->rk_par, 3 * (size_t)ws->E)))
-      return rc;
-  }
-  while (ws->rk_chk_n < nchk) {
-    double *p;
-    if ((rc = dalloc(ws, &p, n))) return rc;
-    ws->rk_chk.push_back(p);
-    ++ws->rk_chk_n;
-  }
-  while (ws->rk_seg_n < 4 * seg) {
-    double *p;
-    if ((rc = dalloc(ws, &p, n))) return rc;
-    ws->rk_seg.push_back(p);
-    ++ws->rk_seg_n;
-  }
-  cudaStream_t st = ws->stream;
-  const cudaMemcpyKind in = where == WEDG_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-  double *yu = ws->rk_y, *yv = ws->rk_y + nU;
-  CK(ws, cudaMemcpyAsync(yu, u0, sizeof(double) * nU, in, st));
-  CK(ws, cudaMemcpyAsync(yv, v0, sizeof(double) * nV, in, st));
-  ws->rk_t.assign(nsteps + 1, t0);
-  for (int64_t k = 0; k < nsteps; ++k) ws->rk_t[k + 1] = ws->rk_t[k] + dt;
-  if ((rc = reset_flags(ws))) return rc;
-  for (int64_t k = 0; k < nsteps; ++k) {
-    if (k % every == 0) CK(ws, cudaMemcpyAsync(ws->rk_chk[k / every], ws->rk_y, sizeof(double) * n,
-                                               cudaMemcpyDeviceToDevice, st));
-    if ((rc = enqueue_rk4(ws, yu, yv, ws->rk_t[k], dt, 1))) return rc;
-  }
-  CK(ws, cudaGetLastError());
-  rc = collect(ws);
-  if (rc != WEDG_OK && rc != WEDG_WARN_CG_NOT_CONVERGED) return rc;
-  if (!ws->stats.finite) return argument_error(ws, "the forward run is not finite");
-  const cudaMemcpyKind out = where == WEDG_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-  if (uT) CK(ws, cudaMemcpy(uT, yu, sizeof(double) * nU, out));
-  if (vT) CK(ws, cudaMemcpy(vT, yv, sizeof(double) * nV, out));
-  ws->rk_dt = dt;
-  ws->rk_nsteps = nsteps;
-  ws->rk_every = every;
-  ws->rk_ready = true;
-  return rc;
+  return adjoint_forward_group({ws}, &u0, &v0, t0, dt, nsteps, every, &uT, &vT, where);
 }
 
 int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam_v, double *gu, double *gv,
                              double *g_c2, double *g_alpha, double *g_beta, int where) {
   if (!ws) return WEDG_ERR_ARGUMENT;
-  ws->stats.kernel_launches = 0;
-  if (!ws->rk_ready) return argument_error(ws, "no forward run with checkpoints (wedg_rk4_adjoint_forward) to reverse");
-  if (!lam_u || !lam_v || !gu || !gv) return argument_error(ws, "null pointer");
-  const bool params = g_c2 || g_alpha || g_beta;
-  if (params && !(g_c2 && g_alpha && g_beta)) return argument_error(ws, "give all three parameter gradients or none");
-  if (params && (!ws->fast || !ws->cfg.src_on || ws->cfg.mms_on))
-    return argument_error(ws, "parameter gradients need source mode and c², α, β constant on each element");
-  int rc;
-  const size_t nU = (size_t)ws->E * ws->nu * ws->nu, nV = (size_t)ws->E * ws->nv * ws->nv, n = nU + nV;
-  const int64_t nsteps = ws->rk_nsteps, every = ws->rk_every;
-  const int64_t nchk = nsteps ? (nsteps + every - 1) / every : 0;
-  const double dt = ws->rk_dt;
-  const std::vector<double> &t = ws->rk_t;
-  cudaStream_t st = ws->stream;
-  double *yu = ws->rk_y, *yv = ws->rk_y + nU;
-  const cudaMemcpyKind in = where == WEDG_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-  CK(ws, cudaMemcpyAsync(ws->rk_lam, lam_u, sizeof(double) * nU, in, st));
-  CK(ws, cudaMemcpyAsync(ws->rk_lam + nU, lam_v, sizeof(double) * nV, in, st));
-  if (params) CK(ws, cudaMemsetAsync(ws->rk_par, 0, sizeof(double) * 3 * ws->E, st));
-  if ((rc = reset_flags(ws))) return rc;
-  const int lb = 256, lg = (int)std::min<size_t>((n + lb - 1) / lb, 152 * 16);
-  auto lin = [&](double *out, double a, const double *x, double b, const double *y, const double *z) {
-    k_lincomb<<<lg, lb, 0, st>>>(n, out, a, x, b, y, z);
-    ws->stats.kernel_launches += 1;
-  };
-  // keep the forward data of every stage of a segment when it fits the memory allowance
-  const int64_t seg = std::min<int64_t>(every, std::max<int64_t>(nsteps, 1));
-  const size_t keep_bytes = (size_t)(4 * seg) * stage_data_bytes(ws);
-  size_t have = 0;
-  for (size_t i = 0; i < ws->rk_keep.size(); ++i) have += stage_data_bytes(ws);
-  bool keep = false;
-  if (ws->adj_mem < 0) {
-    size_t fr = 0, tot = 0;
-    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) keep = keep_bytes <= (fr + have) / 2;
-  } else {
-    keep = keep_bytes <= (size_t)ws->adj_mem;
+  return adjoint_reverse_group({ws}, &lam_u, &lam_v, &gu, &gv, &g_c2, &g_alpha, &g_beta, where);
+}
+
+int wedg_rk4_adjoint_forward_many(int n, wedg_ws *const *ws, const double *const *u0, const double *const *v0,
+                                  double t0, double dt, int64_t nsteps, int64_t every, double *const *uT,
+                                  double *const *vT, int where) {
+  if (n < 1 || !ws || !u0 || !v0) return WEDG_ERR_ARGUMENT;
+  std::vector<wedg_ws *> G(ws, ws + n);
+  for (int i = 0; i < n; ++i) {
+    if (!G[i]) return WEDG_ERR_ARGUMENT;
+    G[i]->stats.kernel_launches = 0;
+    G[i]->rk_ready = false;
+    if (!u0[i] || !v0[i]) return argument_error(G[i], "null pointer");
+    if (!same_kernels(G[0], G[i]))
+      return argument_error(G[i], "the workspaces of a group need the same degrees, coefficient kernels and mass solver");
+    for (int j = 0; j < i; ++j)
+      if (G[j] == G[i]) return argument_error(G[i], "a workspace appears twice in the group");
   }
-  if (keep) {
-    const size_t E = ws->E;
-    const size_t nd = (size_t)ws->nu * ws->nu + ws->nv * ws->nv + 12 * ws->nq + ws->qh * ws->qh + 2;
-    while ((int64_t)ws->rk_keep.size() < 4 * seg) {
-      wedg_ws::StageData d;
-      double *b;
-      int *ib;
-      if ((rc = dalloc(ws, &b, nd * E)) || (rc = dalloc(ws, &ib, E * (1 + NBIN) + 2 * NBIN))) return rc;
-      d.k = b;
-      d.tr = d.k + n;
-      d.G = d.tr + 12 * (size_t)ws->nq * E;
-      d.th = d.G + (size_t)ws->qh * ws->qh * E;
-      d.de = d.th + E;
-      d.nst = ib;
-      d.bins = ib + E;
-      d.bin_count = ib + E * (1 + NBIN);
-      ws->rk_keep.push_back(d);
-    }
+  std::vector<double *> ou(n, nullptr), ov(n, nullptr);
+  for (int i = 0; i < n; ++i) {
+    ou[i] = uT ? uT[i] : nullptr;
+    ov[i] = vT ? vT[i] : nullptr;
   }
-  // ---- reverse pass, segment by segment
-  for (int64_t c = nchk - 1; c >= 0; --c) {
-    const int64_t k0 = c * every, k1 = std::min(nsteps, k0 + every);
-    CK(ws, cudaMemcpyAsync(ws->rk_y, ws->rk_chk[c], sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-    for (int64_t k = k0; k < k1; ++k) {
-      if (keep) {
-        // the step as four RHS evaluations (their outputs and data kept) and the RK4 combinations:
-        // Y1 = y, Y_{s+1} = y + c_s K_s, y ← y + dt/6 (K1 + 2K2 + 2K3 + K4)
-        const double cs[3] = {0.5 * dt, 0.5 * dt, dt};
-        const double ts[4] = {t[k], t[k] + 0.5 * dt, t[k] + 0.5 * dt, t[k] + dt};
-        CK(ws, cudaMemcpyAsync(ws->rk_seg[4 * (k - k0)], ws->rk_y, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-        for (int s = 0; s < 4; ++s) {
-          wedg_ws::StageData &d = ws->rk_keep[4 * (k - k0) + s];
-          const double *Y = ws->rk_seg[4 * (k - k0) + s];
-          StageIO S{};
-          S.xu = Y; S.xv = Y + nU;
-          stage_factors(ws, ts[s], S);
-          S.mode = OUT_RHS;
-          S.ut = d.k;
-          S.vt = d.k + nU;
-          CK(ws, cudaMemsetAsync(d.bin_count, 0, 2 * NBIN * sizeof(int), st));
-          d.parity = ws->parity;
-          const Fields Fk = kept_fields(ws, d);
-          if ((rc = enqueue_stage(ws, S, &Fk))) return rc;
-          if (s < 3) lin(ws->rk_seg[4 * (k - k0) + s + 1], cs[s], d.k, 1.0, ws->rk_y, nullptr);
-        }
-        const double *K[4] = {ws->rk_keep[4 * (k - k0)].k, ws->rk_keep[4 * (k - k0) + 1].k,
-                              ws->rk_keep[4 * (k - k0) + 2].k, ws->rk_keep[4 * (k - k0) + 3].k};
-        lin(ws->rk_acc, 2.0, K[1], 1.0, K[0], nullptr);
-        lin(ws->rk_acc, 2.0, K[2], 1.0, K[3], ws->rk_acc);
-        lin(ws->rk_y, dt / 6.0, ws->rk_acc, 1.0, ws->rk_y, nullptr);
-        continue;
-      }
-      double *su[4], *sv[4];
-      for (int s = 0; s < 4; ++s) {
-        su[s] = ws->rk_seg[4 * (k - k0) + s];
-        sv[s] = su[s] + nU;
-      }
-      if ((rc = enqueue_rk4(ws, yu, yv, t[k], dt, 1, nullptr, 0, su, sv))) return rc;
-    }
-    for (int64_t k = k1 - 1; k >= k0; --k) {
-      const double ts[4] = {t[k], t[k] + 0.5 * dt, t[k] + 0.5 * dt, t[k] + dt};
-      // K̄_s = ca[s] λ + cb[s] Ȳ_{s+1}, Ȳ = Jᵀ K̄ at the stage state: y_{n+1} = y + dt/6 (K1 + 2K2 +
-      // 2K3 + K4), Y2 = y + dt/2 K1, Y3 = y + dt/2 K2, Y4 = y + dt K3
-      const double ca[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};
-      const double cb[4] = {0.5 * dt, 0.5 * dt, dt, 0.0};
-      for (int s = 3; s >= 0; --s) {
-        lin(ws->rk_kbar, ca[s], ws->rk_lam, cb[s], s == 3 ? nullptr : ws->rk_g, nullptr);
-        const double *Y = ws->rk_seg[4 * (k - k0) + s];
-        double *gpar = params ? ws->rk_par : nullptr;
-        if (keep) {
-          const wedg_ws::StageData &d = ws->rk_keep[4 * (k - k0) + s];
-          StageIO S{};
-          S.xu = Y; S.xv = Y + nU;
-          stage_factors(ws, ts[s], S);
-          S.parity = d.parity;
-          S.ut = d.k;
-          S.vt = d.k + nU;
-          rc = enqueue_adjoint_core(ws, kept_fields(ws, d), S, ws->rk_kbar, ws->rk_kbar + nU, ws->rk_g,
-                                    ws->rk_g + nU, gpar);
-        } else {
-          rc = enqueue_rhs_adjoint(ws, Y, Y + nU, ts[s], ws->rk_kbar, ws->rk_kbar + nU, ws->rk_g, ws->rk_g + nU,
-                                   gpar);
-        }
-        if (rc) return rc;
-        lin(ws->rk_acc, 1.0, s == 3 ? ws->rk_lam : ws->rk_acc, 1.0, ws->rk_g, nullptr);
-      }
-      std::swap(ws->rk_lam, ws->rk_acc);
-    }
+  return adjoint_forward_group(G, u0, v0, t0, dt, nsteps, every, ou.data(), ov.data(), where);
+}
+
+int wedg_rk4_adjoint_reverse_many(int n, wedg_ws *const *ws, const double *const *lam_u, const double *const *lam_v,
+                                  double *const *gu, double *const *gv, double *const *g_c2, double *const *g_alpha,
+                                  double *const *g_beta, int where) {
+  if (n < 1 || !ws || !lam_u || !lam_v || !gu || !gv) return WEDG_ERR_ARGUMENT;
+  std::vector<wedg_ws *> G(ws, ws + n);
+  for (int i = 0; i < n; ++i) {
+    if (!G[i]) return WEDG_ERR_ARGUMENT;
+    if (!same_kernels(G[0], G[i]))
+      return argument_error(G[i], "the workspaces of a group need the same degrees, coefficient kernels and mass solver");
+    for (int j = 0; j < i; ++j)
+      if (G[j] == G[i]) return argument_error(G[i], "a workspace appears twice in the group");
   }
-  CK(ws, cudaGetLastError());
-  rc = collect(ws);
-  const cudaMemcpyKind out = where == WEDG_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-  CK(ws, cudaMemcpy(gu, ws->rk_lam, sizeof(double) * nU, out));
-  CK(ws, cudaMemcpy(gv, ws->rk_lam + nU, sizeof(double) * nV, out));
-  if (params) {
-    CK(ws, cudaMemcpy(g_c2, ws->rk_par, sizeof(double) * ws->E, out));
-    CK(ws, cudaMemcpy(g_alpha, ws->rk_par + ws->E, sizeof(double) * ws->E, out));
-    CK(ws, cudaMemcpy(g_beta, ws->rk_par + 2 * ws->E, sizeof(double) * ws->E, out));
+  std::vector<double *> pc(n, nullptr), pa(n, nullptr), pb(n, nullptr);
+  for (int i = 0; i < n; ++i) {
+    pc[i] = g_c2 ? g_c2[i] : nullptr;
+    pa[i] = g_alpha ? g_alpha[i] : nullptr;
+    pb[i] = g_beta ? g_beta[i] : nullptr;
   }
-  return rc;
+  return adjoint_reverse_group(G, lam_u, lam_v, gu, gv, pc.data(), pa.data(), pb.data(), where);
 }
 
 int wedg_set_launch_shape(wedg_ws *ws, int prep_threads, int mass_threads) {

@@ -122,7 +122,9 @@ inline const char *build_basis(const wedg_config *cfg, const wedg_pre *pre, Basi
     if (!mirror(&bh.Wh[r][0], qh, 1, 1.0, tWh)) return asym;
 
   // ---- weights folded into the bases: W2d_h = w_h w_h^T (the kernels weight the point values
-  //      by w_h[s] on the way back to the modes), w P_u, and the lift factors (2/h) El, (4/h²) E1l
+  //      by w_h[s] on the way back to the modes), w P_u, and the lift factor -E1l of the u-slots.
+  //      Nothing here depends on the mesh size (the kernels take 2/h and 4/h² from the
+  //      workspace), so instances of any N with the same degrees share these operators.
   for (int r = 0; r < qh; ++r) bh.wh[r] = std::sqrt(bh.Wh[r][r]);
   for (int r = 0; r < qh; ++r)
     for (int s = 0; s < qh; ++s)
@@ -132,12 +134,7 @@ inline const char *build_basis(const wedg_config *cfg, const wedg_pre *pre, Basi
     for (int d = 0; d < nv; ++d) bh.PhW[r][d] = bh.wh[r] * bh.Ph[r][d];
   for (int i = 0; i < nq; ++i)
     for (int d = 0; d < nu; ++d) bh.Pw[i][d] = bh.w[i] * bh.P[i][d];
-  const double h = 1.0 / cfg->N, two_h = 2.0 / h, four_hh = 4.0 / (h * h);
-  for (int d = 0; d < nu; ++d) {
-    bh.ElA[d] = two_h * bh.El[d];
-    bh.E1D[d] = four_hh * bh.E1l[d];
-    bh.E1F[d] = -bh.E1l[d];
-  }
+  for (int d = 0; d < nu; ++d) bh.E1F[d] = -bh.E1l[d];
 
   // ---- K1 = S^T diag(w) S: zero between modes of unlike parity, and in the first row and
   //      column (the constant mode has no derivative)

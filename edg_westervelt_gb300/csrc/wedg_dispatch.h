@@ -5,12 +5,15 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include <mutex>
+
 #include "wedg_kernels.cuh"
 
 namespace wedg {
 
 constexpr int MAXN = 8;    // q_u ≤ 7
 constexpr int MAXQH = 12;  // q_high for q_v = 7
+constexpr int MAX_DEVICES = 64;
 
 // Runtime-sized copy of the 1D operators, packed into Basis<NU, NV> per launch.
 struct BasisHost {
@@ -18,13 +21,15 @@ struct BasisHost {
   double w[MAXN], P[MAXN][MAXN], S[MAXN][MAXN];
   double Pw[MAXN][MAXN];
   double El[MAXN], Er[MAXN], E1l[MAXN], E1r[MAXN];
-  double ElA[MAXN], E1D[MAXN], E1F[MAXN];
+  double E1F[MAXN];
   double Ph[MAXQH][MAXN], Wh[MAXQH][MAXQH], wh[MAXQH], PhW[MAXQH][MAXN];
   double K1[MAXN][MAXN], Q[MAXN][MAXN], ilam2[MAXN][MAXN];
 };
 
-typedef void (*launch_fn)(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads,
-                          cudaStream_t st);
+// A launcher enqueues one kernel; it returns an error only when it could not launch (a launch
+// error itself is left to the caller's cudaGetLastError)
+typedef cudaError_t (*launch_fn)(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads,
+                                 cudaStream_t st);
 typedef void (*pack_fn)(const BasisHost &h, void *out);
 
 typedef void (*adj_fn)(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, cudaStream_t st);
@@ -33,13 +38,28 @@ typedef void (*adj_fn)(const void *basis, const Fields &F, const StageIO &S, con
 typedef void (*adj_face_fn)(const void *basis, const Fields &F, const StageIO &S, const AdjIO &A, double *gc2,
                             double *gal, double *gbe, cudaStream_t st);
 
+// Multi-instance launches (wedg_kernels.cuh): `grid` blocks (0: one per virtual block) of
+// `threads` threads; the caller sets P.tile to the kernel's elements per block (k_prep: threads,
+// k_stage: stage_threads, the mass solves: (threads / 32) teams per warp)
+typedef cudaError_t (*multi_fn)(const void *basis, const MultiStage &P, int grid, int threads,
+                                cudaStream_t st);
+typedef cudaError_t (*multi_adj_fn)(const void *basis, const MultiAdj &P, int grid, cudaStream_t st);
+
 struct Launchers {
   launch_fn prep = nullptr, stage = nullptr, mass = nullptr;
   adj_fn adj_hats = nullptr, adj_mass = nullptr;
   adj_face_fn adj_face = nullptr;
+  multi_fn prep_m = nullptr, stage_m = nullptr, mass_m = nullptr;
+  multi_adj_fn adj_hats_m = nullptr, adj_mass_m = nullptr, adj_face_m = nullptr;
   pack_fn pack = nullptr;
   size_t basis_size = 0;
 };
+
+static_assert(sizeof(MultiStage) + sizeof(Basis<MAXN, MAXN>) <= 32764 &&
+                  sizeof(MultiAdj) + sizeof(Basis<MAXN, MAXN>) <= 32764,
+              "the arguments of a multi-instance launch exceed the kernel parameter limit");
+
+inline int multi_grid(int grid, int total) { return grid > 0 && grid < total ? grid : total; }
 
 template <int NU, int NV>
 void pack_basis(const BasisHost &h, void *out) {
@@ -51,7 +71,7 @@ void pack_basis(const BasisHost &h, void *out) {
   }
   for (int d = 0; d < NU; ++d) {
     b.El[d] = h.El[d]; b.Er[d] = h.Er[d]; b.E1l[d] = h.E1l[d]; b.E1r[d] = h.E1r[d];
-    b.ElA[d] = h.ElA[d]; b.E1D[d] = h.E1D[d]; b.E1F[d] = h.E1F[d];
+    b.E1F[d] = h.E1F[d];
     for (int c = 0; c < NU; ++c) { b.K1[d][c] = h.K1[d][c]; b.Q[d][c] = h.Q[d][c]; b.ilam2[d][c] = h.ilam2[d][c]; }
   }
   for (int r = 0; r < QH; ++r) {
@@ -61,36 +81,60 @@ void pack_basis(const BasisHost &h, void *out) {
 }
 
 template <int NU, int NV>
-void launch_prep(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads, cudaStream_t st) {
+cudaError_t launch_prep(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads,
+                        cudaStream_t st) {
   k_prep<NU, NV><<<blocks, threads, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S);
+  return cudaSuccess;
+}
+
+// The opt-in to more than 48 KB of dynamic shared memory for kernel K, once per device: a
+// function attribute belongs to the context of the device that is current when it is set, so
+// every device that launches the kernel needs its own (std::call_once per device index, so
+// that threads that launch at once on one device set it once)
+template <class Tag, class K>
+cudaError_t smem_opt_in(K kernel, size_t smem) {
+  static std::once_flag once[MAX_DEVICES];
+  static cudaError_t result[MAX_DEVICES];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= MAX_DEVICES)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  std::call_once(once[dev], [&] {
+    result[dev] = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
+  return result[dev];
 }
 
 // k_stage keeps the element blocks in dynamic shared memory (up to 227 KB per block);
-// `threads` must be stage_threads(NU, NV, FAST)
+// `threads` must be stage_threads(NU, NV, FAST). blocks = 0 only sets the attribute.
 template <int NU, int NV, bool FAST>
-void launch_stage(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads, cudaStream_t st) {
+struct StageTag {};
+template <int NU, int NV, bool FAST>
+cudaError_t launch_stage(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads,
+                         cudaStream_t st) {
   constexpr size_t smem = stage_smem(NU, NV, FAST);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_stage<NU, NV, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
-  if (blocks <= 0) return;
+  const cudaError_t e = smem_opt_in<StageTag<NU, NV, FAST>>(k_stage<NU, NV, FAST>, smem);
+  if (e != cudaSuccess) return e;
+  if (blocks <= 0) return cudaSuccess;
   k_stage<NU, NV, FAST><<<blocks, threads, smem, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S);
+  return cudaSuccess;
 }
 
 // The mass solve: k_cheb or k_cg, a team of threads per element (static shared memory sized
 // for CHEB_THREADS). `threads` (32, 64, 96 or 128) sets the warps of a block and with them its
 // elements; the grid follows from F.E, `blocks` only says whether to launch.
 template <int NU, int NV>
-void launch_mass(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads, cudaStream_t st) {
-  if (blocks <= 0) return;
+cudaError_t launch_mass(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads,
+                        cudaStream_t st) {
+  if (blocks <= 0) return cudaSuccess;
   const Basis<NU, NV> &B = *static_cast<const Basis<NU, NV> *>(basis);
   threads = (threads >= 32 && threads <= CHEB_THREADS && threads % 32 == 0) ? threads : CHEB_THREADS;
   const int tpb = (threads / 32) * ChebTeam<NU, NV>::TPW;
   const int grid = (F.E + tpb - 1) / tpb;
   if (F.cg) k_cg<NU, NV><<<grid, threads, 0, st>>>(B, F, S);
   else k_cheb<NU, NV><<<grid, threads, 0, st>>>(B, F, S);
+  return cudaSuccess;
 }
 
 // The adjoint kernels (wedg_adjoint.cuh): element grids of 128 threads, the mass term on the team grid
@@ -115,8 +159,75 @@ void launch_adj_face(const void *basis, const Fields &F, const StageIO &S, const
 }
 
 template <int NU, int NV>
+cudaError_t launch_prep_m(const void *basis, const MultiStage &P, int grid, int threads, cudaStream_t st) {
+  const int total = P.first[P.n];
+  if (total <= 0) return cudaSuccess;
+  k_prep_m<NU, NV><<<multi_grid(grid, total), threads, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), P);
+  return cudaSuccess;
+}
+
+template <int NU, int NV, bool FAST>
+struct StageMultiTag {};
+template <int NU, int NV, bool FAST>
+cudaError_t launch_stage_m(const void *basis, const MultiStage &P, int grid, int, cudaStream_t st) {
+  constexpr size_t smem = stage_smem(NU, NV, FAST);
+  const cudaError_t e = smem_opt_in<StageMultiTag<NU, NV, FAST>>(k_stage_m<NU, NV, FAST>, smem);
+  if (e != cudaSuccess) return e;
+  const int total = P.first[P.n];
+  if (total <= 0) return cudaSuccess;
+  k_stage_m<NU, NV, FAST><<<multi_grid(grid, total), stage_threads(NU, NV, FAST), smem, st>>>(
+      *static_cast<const Basis<NU, NV> *>(basis), P);
+  return cudaSuccess;
+}
+
+template <int NU, int NV>
+cudaError_t launch_mass_m(const void *basis, const MultiStage &P, int grid, int threads, cudaStream_t st) {
+  const int total = P.first[P.n];
+  if (total <= 0) return cudaSuccess;
+  const Basis<NU, NV> &B = *static_cast<const Basis<NU, NV> *>(basis);
+  if (P.a[0].F.cg) k_mass_m<NU, NV, true><<<multi_grid(grid, total), threads, 0, st>>>(B, P);
+  else k_mass_m<NU, NV, false><<<multi_grid(grid, total), threads, 0, st>>>(B, P);
+  return cudaSuccess;
+}
+
+template <int NU, int NV>
+cudaError_t launch_adj_hats_m(const void *basis, const MultiAdj &P, int grid, cudaStream_t st) {
+  const int total = P.first[P.n];
+  if (total <= 0) return cudaSuccess;
+  k_adj_hats_m<NU, NV><<<multi_grid(grid, total), ADJ_THREADS, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis),
+                                                                         P);
+  return cudaSuccess;
+}
+
+template <int NU, int NV>
+cudaError_t launch_adj_mass_m(const void *basis, const MultiAdj &P, int grid, cudaStream_t st) {
+  const int total = P.first[P.n];
+  if (total <= 0) return cudaSuccess;
+  k_adj_mass_m<NU, NV><<<multi_grid(grid, total), CHEB_THREADS, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis),
+                                                                          P);
+  return cudaSuccess;
+}
+
+// PARAMS when the instances pass coefficient gradients (all or none of them)
+template <int NU, int NV>
+cudaError_t launch_adj_face_m(const void *basis, const MultiAdj &P, int grid, cudaStream_t st) {
+  const int total = P.first[P.n];
+  if (total <= 0) return cudaSuccess;
+  const Basis<NU, NV> &B = *static_cast<const Basis<NU, NV> *>(basis);
+  if (P.a[0].gc2) k_adj_face_m<NU, NV, true><<<multi_grid(grid, total), ADJ_THREADS, 0, st>>>(B, P);
+  else k_adj_face_m<NU, NV, false><<<multi_grid(grid, total), ADJ_THREADS, 0, st>>>(B, P);
+  return cudaSuccess;
+}
+
+template <int NU, int NV>
 Launchers make_launchers(bool fast) {
   Launchers L;
+  L.prep_m = launch_prep_m<NU, NV>;
+  L.stage_m = fast ? launch_stage_m<NU, NV, true> : launch_stage_m<NU, NV, false>;
+  L.mass_m = launch_mass_m<NU, NV>;
+  L.adj_hats_m = launch_adj_hats_m<NU, NV>;
+  L.adj_mass_m = launch_adj_mass_m<NU, NV>;
+  L.adj_face_m = launch_adj_face_m<NU, NV>;
   L.adj_hats = launch_adj_hats<NU, NV>;
   L.adj_mass = launch_adj_mass<NU, NV>;
   L.adj_face = launch_adj_face<NU, NV>;

@@ -79,7 +79,8 @@ struct Basis {
   double P[NQ][NU], S[NQ][NU];   // P[i][d] = P_u[i, d], S likewise; the v-basis is d < NV
   double Pw[NQ][NU];             // w[i] P[i][d]
   double El[NU], Er[NU], E1l[NU], E1r[NU];
-  double ElA[NU], E1D[NU], E1F[NU];  // (2/h) El, (4/h²) E1l, -E1l: the lift factors of a side
+  double E1F[NU];                // -E1l, the lift factor of the u-slots (the v-slots' factors
+                                 // (2/h) El and (4/h²) E1l take the mesh size from Fields)
   double Ph[QH][NV];             // P_h_v[r, d]
   double PhW[QH][NV];            // w_h[r] P_h_v[r, d], with W2d_h = w_h w_h^T
   double wh[QH];                 // w_h
@@ -151,6 +152,48 @@ __device__ __forceinline__ TimeF time_factors(const StageIO &S) {
 
 __device__ __forceinline__ unsigned long long err_word(const Fields &F) {
   return *(volatile unsigned long long *)F.err;
+}
+
+// ----------------------------------------------------------------------------
+// Multi-instance launches (the batched form): one launch runs one kernel of a stage for up to
+// CAP instances with the same degrees (so the same kernel and the same 1D operators) and
+// any mesh sizes. Their arguments travel in the launch's parameter block. The launch covers
+// first[n] virtual blocks: virtual block vb belongs to the instance i with first[i] ≤ vb <
+// first[i+1] and covers `tile` elements (or element slots of the mass solves' order) of it,
+// from (vb - first[i]) tile on. Each block copies its instance's arguments into shared memory
+// and runs the single-instance kernel's body on them, so an element's arithmetic is the same
+// as in a launch of its instance alone. A grid smaller than first[n] makes the launch
+// persistent: block b takes the virtual blocks b, b + gridDim.x, ...
+// ----------------------------------------------------------------------------
+struct StageArgs {
+  Fields F;
+  StageIO S;
+};
+
+template <class Args, int CAP>
+struct Multi {
+  static constexpr int cap = CAP;
+  int n, tile;
+  int first[CAP + 1];
+  Args a[CAP];
+};
+
+// CAP is what fits the kernel parameter limit (32 764 bytes) beside the largest Basis
+using MultiStage = Multi<StageArgs, 32>;
+
+// The instance of virtual block vb, its arguments copied into sa (all threads of the block call
+// this together: it synchronises before overwriting sa and after filling it)
+template <class Args, int CAP>
+__device__ __forceinline__ int multi_begin(const Multi<Args, CAP> &P, int vb, Args &sa) {
+  static_assert(sizeof(Args) % 8 == 0, "instance arguments are copied as 8-byte words");
+  int inst = 0;
+  while (inst + 1 < P.n && vb >= P.first[inst + 1]) ++inst;
+  __syncthreads();
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&P.a[inst]);
+  unsigned long long *dst = reinterpret_cast<unsigned long long *>(&sa);
+  for (int i = threadIdx.x; i < (int)(sizeof(Args) / 8); i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+  return inst;
 }
 
 // A thread-private n×n block in shared memory: X(a, b) at base[(a + n b) BT + tid]
@@ -254,9 +297,10 @@ __device__ __forceinline__ void ph_row_mid(const double (&Ph)[QH][NV], const X &
 //   oL[i] = Σ_b P[i,b] Σ_a El[a] X[b][a],  oR with Er,
 // where El, Er are the values (DER false) or the derivatives (DER true) of the modes at the
 // two ends: Er[a] = ±(-1)^a El[a], so both ends come from the even and odd parts of one sum.
-template <int NQ, int NU, int n, bool DER>
+// With SCALE, every output is multiplied by sc.
+template <int NQ, int NU, int n, bool DER, bool SCALE = false>
 __device__ __forceinline__ void trace4(const double (&X)[n][n], const double (&P)[NQ][NU], const double *El,
-                                       double *tr, int fam, int E, int e) {
+                                       double *tr, int fam, int E, int e, double sc = 1.0) {
   double sB[n], sT[n], sL[n], sR[n];
 #pragma unroll
   for (int b = 0; b < n; ++b) {
@@ -270,6 +314,7 @@ __device__ __forceinline__ void trace4(const double (&X)[n][n], const double (&P
     sR[b] = DER ? yo - ye : ye - yo;
   }
   auto put = [&](int i, double oB, double oT, double oL, double oR) {
+    if constexpr (SCALE) { oB *= sc; oT *= sc; oL *= sc; oR *= sc; }
     tr[((fam * 4 + 0) * NQ + i) * (size_t)E + e] = oB;
     tr[((fam * 4 + 1) * NQ + i) * (size_t)E + e] = oT;
     tr[((fam * 4 + 2) * NQ + i) * (size_t)E + e] = oL;
@@ -305,15 +350,14 @@ __device__ __forceinline__ void load_regs(double (&X)[n][n], const double *x, in
     for (int a = 0; a < n; ++a) X[a][b] = x[e + (size_t)E * (a + n * b)];
 }
 
+// k_prep's work for element e (first: the instance's first block, which clears the bin counts)
 template <int NU, int NV>
-__global__ void __launch_bounds__(128, 3) k_prep(const __grid_constant__ Basis<NU, NV> B,
-                                              const __grid_constant__ Fields F,
-                                              const __grid_constant__ StageIO S) {
+__device__ __forceinline__ void prep_body(const Basis<NU, NV> &B, const Fields &F, const StageIO &S, int e,
+                                          bool first) {
   constexpr int NQ = NU, QH = Basis<NU, NV>::QH;
   const int E = F.E, N = F.N;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
   // the bin counts of the next stage start at zero: all NBIN of them, whatever the element count
-  if (blockIdx.x == 0 && F.sorted)
+  if (first && F.sorted)
     for (int b = threadIdx.x; b < NBIN; b += blockDim.x) F.bin_count[(1 - S.parity) * NBIN + b] = 0;
   if (e >= E) return;
   if (err_word(F) != ERR_NONE) return;
@@ -420,6 +464,24 @@ __global__ void __launch_bounds__(128, 3) k_prep(const __grid_constant__ Basis<N
     if (lane == leader) base = atomicAdd(&F.bin_count[S.parity * NBIN + bin], __popc(same));
     base = __shfl_sync(same, base, leader);
     F.bins[(size_t)bin * E + base + rank] = e;
+  }
+}
+
+template <int NU, int NV>
+__global__ void __launch_bounds__(128, 3) k_prep(const __grid_constant__ Basis<NU, NV> B,
+                                              const __grid_constant__ Fields F,
+                                              const __grid_constant__ StageIO S) {
+  prep_body<NU, NV>(B, F, S, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.x == 0);
+}
+
+template <int NU, int NV>
+__global__ void __launch_bounds__(128, 3) k_prep_m(const __grid_constant__ Basis<NU, NV> B,
+                                                const __grid_constant__ MultiStage P) {
+  __shared__ StageArgs sa;
+  for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
+    const int inst = multi_begin(P, vb, sa);
+    const int e0 = (vb - P.first[inst]) * P.tile;
+    prep_body<NU, NV>(B, sa.F, sa.S, e0 + (int)threadIdx.x, e0 == 0);
   }
 }
 
@@ -545,15 +607,13 @@ __device__ __forceinline__ void side_point(const Basis<NU, NV> &B, const Fields 
 // ----------------------------------------------------------------------------
 // k_stage: fluxes, lifts, volume, source, u-equation; the mass right-hand side to HBM
 // ----------------------------------------------------------------------------
+// k_stage's work for element e, whose blocks live in the shared-memory slot tid of the block
 template <int NU, int NV, bool FAST>
-__global__ void __launch_bounds__(stage_threads(NU, NV, FAST), 2)
-    k_stage(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
-            const __grid_constant__ StageIO S) {
+__device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields &F, const StageIO &S, int e,
+                                           int tid) {
   constexpr int NQ = NU, BT = stage_threads(NU, NV, FAST);
   extern __shared__ double smem[];
-  const int tid = threadIdx.x;
   const int E = F.E, N = F.N;
-  const int e = blockIdx.x * BT + tid;
   if (e >= E) return;
   if (err_word(F) != ERR_NONE) return;
   const int j = e % N, k = e / N;
@@ -629,13 +689,14 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), 2)
       }
     }
     // lifts of both sides: with σ_a = (-1)^a, El = the left-end values, E1l the left-end
-    // derivatives, Rv += (2/h) El ⊗ (A_0 + σ A_1) + (4/h²) E1l ⊗ (D_0 - σ D_1) and
+    // derivatives, Rv += El ⊗ (2/h)(A_0 + σ A_1) + E1l ⊗ (4/h²)(D_0 - σ D_1) and
     // b -= E1l ⊗ (F_0 - σ F_1) (B/T: the row index carries E; L/R: the column index)
 #pragma unroll
     for (int b = 0; b < NU; ++b) {
       if (b < NV) {
         const double ap = A0[b] + YA[b], am = A0[b] - YA[b], dp = D0[b] + YD[b], dm = D0[b] - YD[b];
-        A0[b] = ap; YA[b] = am; D0[b] = dm; YD[b] = dp;       // even-σ and odd-σ combinations
+        // even-σ and odd-σ combinations, with the mesh factors of the v-slots
+        A0[b] = two_h * ap; YA[b] = two_h * am; D0[b] = four_hh * dm; YD[b] = four_hh * dp;
       }
       const double fp = F0[b] + YF[b], fm = F0[b] - YF[b];
       F0[b] = fm; YF[b] = fp;
@@ -643,7 +704,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), 2)
     if (ax == 0) {
 #pragma unroll 1
       for (int a = 0; a < NV; ++a) {
-        const double ca = B.ElA[a], cd = B.E1D[a];
+        const double ca = B.El[a], cd = B.E1l[a];
         const bool od = a & 1;
 #pragma unroll
         for (int b = 0; b < NV; ++b)
@@ -661,7 +722,7 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), 2)
       for (int a = 0; a < NV; ++a) {
 #pragma unroll
         for (int b = 0; b < NV; ++b)
-          Rv(a, b) = fma(B.E1D[b], (b & 1) ? YD[a] : D0[a], fma(B.ElA[b], (b & 1) ? YA[a] : A0[a], Rv(a, b)));
+          Rv(a, b) = fma(B.E1l[b], (b & 1) ? YD[a] : D0[a], fma(B.El[b], (b & 1) ? YA[a] : A0[a], Rv(a, b)));
       }
 #pragma unroll
       for (int a = 0; a < NU; ++a) {
@@ -1027,6 +1088,25 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), 2)
   if (S.mode == OUT_RK4_LAST && !fin) atomicOr(F.nonfinite, 1u);
 }
 
+template <int NU, int NV, bool FAST>
+__global__ void __launch_bounds__(stage_threads(NU, NV, FAST), 2)
+    k_stage(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
+            const __grid_constant__ StageIO S) {
+  constexpr int BT = stage_threads(NU, NV, FAST);
+  stage_body<NU, NV, FAST>(B, F, S, blockIdx.x * BT + (int)threadIdx.x, threadIdx.x);
+}
+
+// tile = stage_threads(NU, NV, FAST) elements per virtual block
+template <int NU, int NV, bool FAST>
+__global__ void __launch_bounds__(stage_threads(NU, NV, FAST), 2)
+    k_stage_m(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ MultiStage P) {
+  __shared__ StageArgs sa;
+  for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
+    const int inst = multi_begin(P, vb, sa);
+    stage_body<NU, NV, FAST>(B, sa.F, sa.S, (vb - P.first[inst]) * P.tile + (int)threadIdx.x, threadIdx.x);
+  }
+}
+
 // ----------------------------------------------------------------------------
 // The mass solve M(v_h) VT = R on every element (src/rhs.jl:778-951) and the v part of the outputs
 // ----------------------------------------------------------------------------
@@ -1163,8 +1243,9 @@ __device__ __forceinline__ void team_K(const Basis<NU, NV> &B, const Fields &F, 
   }
 }
 
-// Shared memory of a team kernel and its setup: the bin prefix (sorted order) and the bases
-#define WEDG_TEAM_SETUP()                                                                       \
+// Shared memory of a team kernel and its setup: the bin prefix (sorted order) and the bases;
+// g0 is the first element slot of the block (slots in the order of mass_element)
+#define WEDG_TEAM_SETUP(g0)                                                                     \
   using T = ChebTeam<NU, NV>;                                                                   \
   constexpr int U = T::U, NE = T::NE, J = T::J;                                                 \
   __shared__ double sh[T::TPB * T::SLOT];                                                       \
@@ -1181,7 +1262,7 @@ __device__ __forceinline__ void team_K(const Basis<NU, NV> &B, const Fields &F, 
   __syncthreads();                                                                              \
   TeamPos tp;                                                                                   \
   if (!team_pos<NU, NV>(tp)) return;                                                            \
-  const int g = blockIdx.x * ((int)(blockDim.x >> 5) * T::TPW) + tp.slot;                      \
+  const int g = (g0) + tp.slot;                                                                 \
   if (g >= F.E) return;                                                                         \
   if (err_word(F) != ERR_NONE) return;                                                          \
   const int u = tp.u;                                                                           \
@@ -1195,10 +1276,8 @@ __device__ __forceinline__ void team_K(const Basis<NU, NV> &B, const Fields &F, 
 // first. The team keeps the residual r, the iterate X and the direction d of its entries in
 // registers and d in its shared slot.
 template <int NU, int NV>
-__global__ void __launch_bounds__(CHEB_THREADS, 3)
-    k_cheb(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
-           const __grid_constant__ StageIO S) {
-  WEDG_TEAM_SETUP();
+__device__ __forceinline__ void cheb_body(const Basis<NU, NV> &B, const Fields &F, const StageIO &S, int g0) {
+  WEDG_TEAM_SETUP(g0);
   const int e = mass_element(F, S, g, pref);
   const double th = F.th[e], de = F.de[e];
   const double s1 = th / de;
@@ -1255,10 +1334,8 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
 // the rows it wrote), then iterates with p in its shared slot and the inner products summed over
 // the team's lanes in a fixed order, so that every lane takes the same decisions.
 template <int NU, int NV>
-__global__ void __launch_bounds__(CHEB_THREADS, 3)
-    k_cg(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
-         const __grid_constant__ StageIO S) {
-  WEDG_TEAM_SETUP();
+__device__ __forceinline__ void cg_body(const Basis<NU, NV> &B, const Fields &F, const StageIO &S, int g0) {
+  WEDG_TEAM_SETUP(g0);
   constexpr int QH = T::QH;
   const int e = g;
   {
@@ -1352,6 +1429,39 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
 }
 
 #undef WEDG_TEAM_SETUP
+
+// The team kernels: a block of `threads` takes (threads / 32) teams per warp of elements
+template <int NU, int NV>
+__device__ __forceinline__ int team_tile() {
+  return (int)(blockDim.x >> 5) * ChebTeam<NU, NV>::TPW;
+}
+
+template <int NU, int NV>
+__global__ void __launch_bounds__(CHEB_THREADS, 3)
+    k_cheb(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
+           const __grid_constant__ StageIO S) {
+  cheb_body<NU, NV>(B, F, S, blockIdx.x * team_tile<NU, NV>());
+}
+
+template <int NU, int NV>
+__global__ void __launch_bounds__(CHEB_THREADS, 3)
+    k_cg(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
+         const __grid_constant__ StageIO S) {
+  cg_body<NU, NV>(B, F, S, blockIdx.x * team_tile<NU, NV>());
+}
+
+// tile = team_tile elements per virtual block; CG selects k_cg's body
+template <int NU, int NV, bool CG>
+__global__ void __launch_bounds__(CHEB_THREADS, 3)
+    k_mass_m(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ MultiStage P) {
+  __shared__ StageArgs sa;
+  for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
+    const int inst = multi_begin(P, vb, sa);
+    const int g0 = (vb - P.first[inst]) * P.tile;
+    if constexpr (CG) cg_body<NU, NV>(B, sa.F, sa.S, g0);
+    else cheb_body<NU, NV>(B, sa.F, sa.S, g0);
+  }
+}
 
 // Last RK4 update when the last stage may still raise an error inside k_cg
 // (CG mode): u += (dt/6) acc unless an error was recorded.

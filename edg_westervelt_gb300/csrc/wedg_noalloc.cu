@@ -39,7 +39,6 @@ using namespace wedg;
 namespace {
 
 constexpr size_t NOALLOC_DOUBLES = WEDG_NOALLOC_BYTES / sizeof(double);
-constexpr int MAX_DEVICES = 64;
 
 // the scratch of every call of wedg_rhs_noalloc (see the file comment)
 static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_DOUBLES];
@@ -300,12 +299,12 @@ extern "C" int wedg_rhs_noalloc(const wedg_config *cfg, const wedg_pre *pre, con
     return WEDG_ERR_CUDA;
   }
   const int tp = 128, ts = stage_threads(nu, nv, fast);
-  Lch.prep(basis, F, S, (iE + tp - 1) / tp, tp, st);
-  Lch.stage(basis, F, S, (iE + ts - 1) / ts, ts, st);
-  Lch.mass(basis, F, S, 1, CHEB_THREADS, st);
   unsigned long long err = 0;
   unsigned int cgf = 0;
-  if ((ce = cudaGetLastError()) != cudaSuccess ||
+  if ((ce = Lch.prep(basis, F, S, (iE + tp - 1) / tp, tp, st)) != cudaSuccess ||
+      (ce = Lch.stage(basis, F, S, (iE + ts - 1) / ts, ts, st)) != cudaSuccess ||
+      (ce = Lch.mass(basis, F, S, 1, CHEB_THREADS, st)) != cudaSuccess ||
+      (ce = cudaGetLastError()) != cudaSuccess ||
       (ce = cudaMemcpyAsync(&err, F.err, sizeof err, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (ce = cudaMemcpyAsync(&cgf, F.cg_nfail, sizeof cgf, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (ce = cudaStreamSynchronize(st)) != cudaSuccess) {

@@ -13,7 +13,7 @@ import numpy as np
 from .coefficients import GaussianSource, _sym
 from .precompute import precompute
 from .quadrature import JacobiP
-from .workspace import ErrorException, Workspace
+from .workspace import ErrorException, Workspace, rk4_adjoint_forward_many, rk4_adjoint_reverse_many
 
 
 def solve(q, N, T, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, boundary="absorbing_2beta",
@@ -172,28 +172,21 @@ def piecewise_coefficients(c2, alpha, beta):
     return Coefficients(cell(np.sqrt(c2)), zero, zero, cell(alpha), zero, zero, cell(beta))
 
 
-def misfit_gradient(q, N, T, c2, alpha, beta, receivers, u_obs, *, dt_fac=10, every=32, **kw):
-    """The discrete adjoint's gradient of the final-time misfit J = ½ Σ_r (u_h(x_r, T) - u_obs_r)²
-    of a source-mode run from the zero state with respect to c², α and β constant on the cells
-    of the grid of the (m, n) arrays c2, alpha, beta (every cell a block of N/m × N/n elements).
-    Returns (J, dict(c2=..., alpha=..., beta=...)) with gradients of the cells' shape. The forward
-    run, the misfit and the final-time adjoint λ_u = Σ_r (u_h(x_r) - u_obs_r) ∂u_h(x_r)/∂U are
-    computed here; the forward run (keeping checkpoints every `every` steps) and the reverse
-    sweep are wedg_rk4_adjoint_forward and wedg_rk4_adjoint_reverse."""
+def _misfit_problem(q, N, T, c2, alpha, beta, dt_fac, kw):
+    """The forward problem of the misfit: pre, the workspace and the steps (src/solver.jl:198-206)."""
     c2 = np.asarray(c2, dtype=np.float64)
     m, n = c2.shape
     if N % m or N % n:
         raise ErrorException(f"the {m} × {n} parameter cells must be unions of elements (N = {N})")
-    pre, geo = precompute(q, N, mode="source", coefficients=piecewise_coefficients(c2, alpha, beta), **kw)
-    nu, nv = pre["qu1"], pre["qv1"]
-    h = 1.0 / N
-    dt = h / (dt_fac * q ** 2)
+    pre, _ = precompute(q, N, mode="source", coefficients=piecewise_coefficients(c2, alpha, beta), **kw)
+    dt = (1.0 / N) / (dt_fac * q ** 2)
     nsteps = int(round(T / dt))
-    dt = T / nsteps
-    ws = Workspace(pre, N)
-    u0 = np.zeros((N, N, nu, nu), order="F")
-    v0 = np.zeros((N, N, nv, nv), order="F")
-    u, v = ws.rk4_adjoint_forward(u0, v0, 0.0, dt, nsteps, every=every)
+    return pre, Workspace(pre, N), T / nsteps, nsteps, (m, n)
+
+
+def _misfit_value(u, N, receivers, u_obs):
+    """J = ½ Σ_r (u_h(x_r) - u_obs_r)² of the final u and its adjoint λ_u = ∂J/∂U."""
+    nu = u.shape[2]
     lam_u = np.zeros_like(u)
     J = 0.0
     for (xr, yr), obs in zip(receivers, u_obs):
@@ -203,7 +196,63 @@ def misfit_gradient(q, N, T, c2, alpha, beta, receivers, u_obs, *, dt_fac=10, ev
         res = float(py @ u[jr - 1, kr - 1] @ px) - obs
         J += 0.5 * res * res
         lam_u[jr - 1, kr - 1] += res * np.outer(py, px)
+    return J, lam_u
+
+
+def misfit(q, N, T, c2, alpha, beta, receivers, u_obs, *, dt_fac=10, **kw):
+    """The final-time misfit J = ½ Σ_r (u_h(x_r, T) - u_obs_r)² of a source-mode run from the zero
+    state, for c², α and β constant on the cells of the grid of the (m, n) arrays c2, alpha, beta
+    (the forward problem of misfit_gradient, without the reverse sweep)."""
+    pre, ws, dt, nsteps, _ = _misfit_problem(q, N, T, c2, alpha, beta, dt_fac, kw)
+    u = np.zeros((N, N, pre["qu1"], pre["qu1"]), order="F")
+    v = np.zeros((N, N, pre["qv1"], pre["qv1"]), order="F")
+    if ws.rk4_steps(u, v, 0.0, dt, nsteps) != nsteps or not ws.fin:
+        raise ErrorException("the forward run of the misfit did not complete")
+    return _misfit_value(u, N, receivers, u_obs)[0]
+
+
+def misfit_gradient(q, N, T, c2, alpha, beta, receivers, u_obs, *, dt_fac=10, every=32, **kw):
+    """The discrete adjoint's gradient of the final-time misfit J = ½ Σ_r (u_h(x_r, T) - u_obs_r)²
+    of a source-mode run from the zero state with respect to c², α and β constant on the cells
+    of the grid of the (m, n) arrays c2, alpha, beta (every cell a block of N/m × N/n elements).
+    Returns (J, dict(c2=..., alpha=..., beta=...)) with gradients of the cells' shape. The forward
+    run, the misfit and the final-time adjoint λ_u = Σ_r (u_h(x_r) - u_obs_r) ∂u_h(x_r)/∂U are
+    computed here; the forward run (keeping checkpoints every `every` steps) and the reverse
+    sweep are wedg_rk4_adjoint_forward and wedg_rk4_adjoint_reverse."""
+    pre, ws, dt, nsteps, (m, n) = _misfit_problem(q, N, T, c2, alpha, beta, dt_fac, kw)
+    nu, nv = pre["qu1"], pre["qv1"]
+    u0 = np.zeros((N, N, nu, nu), order="F")
+    v0 = np.zeros((N, N, nv, nv), order="F")
+    u, v = ws.rk4_adjoint_forward(u0, v0, 0.0, dt, nsteps, every=every)
+    J, lam_u = _misfit_value(u, N, receivers, u_obs)
     _, _, gc2, gal, gbe = ws.rk4_adjoint_reverse(lam_u, np.zeros_like(v), params=True)
     # element (j, k) lies in cell (j // (N/m), k // (N/n))
     cells = lambda g: g.reshape(m, N // m, n, N // n).sum(axis=(1, 3))
     return J, dict(c2=cells(gc2), alpha=cells(gal), beta=cells(gbe))
+
+
+def misfit_gradients(q, N, T, fields, receivers, u_obs, *, dt_fac=10, every=32, **kw):
+    """misfit_gradient for several parameter fields at once: fields is a list of (c2, alpha, beta)
+    cell arrays and u_obs a list of observation vectors (one per field, or one for all). The
+    forward runs and the reverse sweeps of all of them run together (wedg_rk4_adjoint_forward_many,
+    wedg_rk4_adjoint_reverse_many), so that problems too small to fill the GPU alone fill it
+    together. Returns a list of (J, dict(c2=..., alpha=..., beta=...))."""
+    n = len(fields)
+    obs = list(u_obs) if len(u_obs) == n and np.ndim(u_obs[0]) == 1 else [u_obs] * n
+    probs = [_misfit_problem(q, N, T, c2, al, be, dt_fac, kw) for c2, al, be in fields]
+    dt, nsteps = probs[0][2], probs[0][3]
+    wss = [p[1] for p in probs]
+    pre = probs[0][0]
+    nu, nv = pre["qu1"], pre["qv1"]
+    u0 = [np.zeros((N, N, nu, nu), order="F") for _ in range(n)]
+    v0 = [np.zeros((N, N, nv, nv), order="F") for _ in range(n)]
+    uT, vT = rk4_adjoint_forward_many(wss, u0, v0, 0.0, dt, nsteps, every=every)
+    Js, lams = zip(*[_misfit_value(uT[i], N, receivers, obs[i]) for i in range(n)])
+    out = rk4_adjoint_reverse_many(wss, list(lams), [np.zeros_like(x) for x in vT], params=True)
+    res = []
+    for i in range(n):
+        m, nn = probs[i][4]
+        cells = lambda g: g.reshape(m, N // m, nn, N // nn).sum(axis=(1, 3))   # noqa: E731
+        _, _, gc2, gal, gbe = out[i]
+        res.append((Js[i], dict(c2=cells(gc2), alpha=cells(gal), beta=cells(gbe))))
+    return res

@@ -355,8 +355,10 @@ class Workspace:
 
 class Batch:
     """Many independent instances advanced together (wedg_batch_*): each a Workspace of its own
-    N, degrees, flux, boundary kinds and coefficients; one RK4 step of all of them is one replay
-    of a CUDA graph. No counterpart in the reference (there, batching is a loop over solves)."""
+    N, degrees, flux, boundary kinds and coefficients. Instances that run the same kernels form a
+    bucket, and every stage kernel runs once per bucket over all of its instances; one RK4 step
+    of all of them is one replay of a CUDA graph. No counterpart in the reference (there,
+    batching is a loop over solves)."""
 
     def __init__(self, workspaces):
         self.ws = list(workspaces)
@@ -401,10 +403,28 @@ class Batch:
             w._check(st[i])
         return [int(x) for x in done], [bool(x) for x in fin], [int(x) for x in st]
 
+    def shapes(self):
+        """The buckets and their launch shapes (wedg_batch_get_shape): a list of dicts with the
+        degrees + 1, the instances, the kernel family and the shape."""
+        out = []
+        for k in range(L.lib().wedg_batch_bucket_count(self._h)):
+            s = L.BatchShape()
+            if L.lib().wedg_batch_get_shape(self._h, k, ctypes.byref(s)) != L.WEDG_OK:
+                raise RuntimeError("wedg_batch_get_shape failed")
+            out.append({f: int(getattr(s, f)) for f, _ in s._fields_})
+        return out
+
+    def set_shape(self, bucket, prep_threads, mass_threads, persist=0):
+        """wedg_batch_set_shape: the launch shape of one bucket (results do not depend on it)."""
+        rc = L.lib().wedg_batch_set_shape(self._h, int(bucket), int(prep_threads), int(mass_threads), int(persist))
+        if rc != L.WEDG_OK:
+            raise ErrorException("launch shapes are 32, 64, 96 or 128 threads per block and persist 0 to 8")
+
     def autotune(self, us, vs, t0s, dts, steps=3):
-        """wedg_batch_autotune: the launch shapes of every bucket of instances with the same
-        degrees, against the time of the whole batch's step from copies of the states (left
-        unchanged). Returns the best milliseconds per batch step."""
+        """wedg_batch_autotune: the launch shapes of every bucket, each tuned alone from copies of
+        its instances' states (left unchanged), then kept only if the whole batch's step beats the
+        shapes it had before in paired trials. Returns the median milliseconds per batch step of
+        the shapes kept."""
         n = len(self.ws)
         if not (len(us) == len(vs) == len(t0s) == len(dts) == n):
             raise ValueError("one state, t0 and dt per instance")
@@ -419,6 +439,58 @@ class Batch:
                 w._check(rc)
             raise RuntimeError(f"wedg_batch_autotune failed: {L.lib().wedg_status_string(rc).decode()}")
         return best.value
+
+
+def _ptr_array(arrays):
+    return (ctypes.POINTER(ctypes.c_double) * len(arrays))(*[_ptr(a) for a in arrays])
+
+
+def _check_group(wss, rc):
+    if rc == L.WEDG_OK:
+        return
+    for w in wss:                                 # the workspace that failed carries the message
+        if L.lib().wedg_error_message(w._h, None, 0) != L.WEDG_OK:
+            w._check(rc)
+    raise RuntimeError(f"libwedg: {L.lib().wedg_status_string(rc).decode()}")
+
+
+def rk4_adjoint_forward_many(wss, u0s, v0s, t0, dt, nsteps, every=32):
+    """wedg_rk4_adjoint_forward_many: the forward runs of several workspaces (same degrees,
+    coefficient kernels and mass solver) at once, each stage one multi-instance launch over all of
+    them; checkpoints kept in each workspace. Host arrays in; returns the final states."""
+    n = len(wss)
+    for w in wss:
+        w._refuse_mismatch()
+    u0s = [_f64(a) for a in u0s]
+    v0s = [_f64(a) for a in v0s]
+    uT = [np.zeros((w.N, w.N, w.nu, w.nu), order="F") for w in wss]
+    vT = [np.zeros((w.N, w.N, w.nv, w.nv), order="F") for w in wss]
+    h = (ctypes.c_void_p * n)(*[w._h for w in wss])
+    rc = L.lib().wedg_rk4_adjoint_forward_many(n, h, _ptr_array(u0s), _ptr_array(v0s), float(t0), float(dt),
+                                               int(nsteps), int(every), _ptr_array(uT), _ptr_array(vT), L.WEDG_HOST)
+    _check_group(wss, rc)
+    return uT, vT
+
+
+def rk4_adjoint_reverse_many(wss, lam_us, lam_vs, params=False):
+    """wedg_rk4_adjoint_reverse_many: the reverse sweeps of the workspaces' last forward runs
+    (rk4_adjoint_forward_many) for the final-time adjoints (λ_u, λ_v) of each; returns per workspace
+    (gu, gv) and, with params, the per-element gradients with respect to c², α, β."""
+    n = len(wss)
+    lam_us = [_f64(a) for a in lam_us]
+    lam_vs = [_f64(a) for a in lam_vs]
+    gu = [np.zeros((w.N, w.N, w.nu, w.nu), order="F") for w in wss]
+    gv = [np.zeros((w.N, w.N, w.nv, w.nv), order="F") for w in wss]
+    gp = [[np.zeros((w.N, w.N), order="F") for w in wss] for _ in range(3)] if params else None
+    null = ctypes.POINTER(ctypes.POINTER(ctypes.c_double))()
+    pc = [_ptr_array(g) for g in gp] if params else [null, null, null]
+    h = (ctypes.c_void_p * n)(*[w._h for w in wss])
+    rc = L.lib().wedg_rk4_adjoint_reverse_many(n, h, _ptr_array(lam_us), _ptr_array(lam_vs), _ptr_array(gu),
+                                               _ptr_array(gv), pc[0], pc[1], pc[2], L.WEDG_HOST)
+    _check_group(wss, rc)
+    if params:
+        return [(gu[i], gv[i], gp[0][i], gp[1][i], gp[2][i]) for i in range(n)]
+    return [(gu[i], gv[i]) for i in range(n)]
 
 
 def edg_rhs_(ws, u, v, t, N, h, pre):

@@ -220,6 +220,24 @@ int wedg_rk4_adjoint_forward(wedg_ws *ws, const double *u0, const double *v0, do
 int wedg_rk4_adjoint_reverse(wedg_ws *ws, const double *lam_u, const double *lam_v, double *gu, double *gv,
                              double *g_c2, double *g_alpha, double *g_beta, int where);
 
+/* The same two halves for n workspaces at once (no counterpart in the reference), e.g. the
+ * gradients of one misfit for n parameter fields: the workspaces need the same degrees,
+ * coefficient kernels and mass solver (any meshes); the forward runs take the same t0, dt, steps
+ * and checkpoint interval. Every RK4 stage and every stage's transpose runs as one
+ * multi-instance launch per kernel over all n workspaces, so that problems too small to fill
+ * the GPU alone fill it together; each workspace's arithmetic is the one of its own call. The
+ * reverse sweeps keep the stage data of one segment of every workspace at once when the sum fits
+ * the allowance (the workspaces' wedg_set_adjoint_memory, or by default half of the free device
+ * memory); otherwise they run one after the other. Arrays of n pointers, as the single calls;
+ * uT, vT and the parameter gradients may be NULL (or hold NULL entries). Returns the first error
+ * of a workspace, whose message is read with wedg_error_message. */
+int wedg_rk4_adjoint_forward_many(int n, wedg_ws *const *ws, const double *const *u0, const double *const *v0,
+                                  double t0, double dt, int64_t nsteps, int64_t every, double *const *uT,
+                                  double *const *vT, int where);
+int wedg_rk4_adjoint_reverse_many(int n, wedg_ws *const *ws, const double *const *lam_u, const double *const *lam_v,
+                                  double *const *gu, double *const *gv, double *const *g_c2, double *const *g_alpha,
+                                  double *const *g_beta, int where);
+
 /* Launch shapes (no counterpart in the reference, whose parallel regions are the nblocks
  * element blocks of src/rhs.jl:130-180): threads per block of k_prep (one element per thread)
  * and of the mass solves (a team of threads per element, so the block's warps set its
@@ -246,13 +264,18 @@ int wedg_set_adjoint_memory(wedg_ws *ws, int64_t bytes);
 
 /* Batched form: many independent instances -- workspaces made by wedg_create, each with its
  * own N, degrees, flux, boundary kinds and coefficients -- advanced together. No counterpart in
- * the reference, whose batching is the caller's loop over instances. One RK4 step of every
- * instance is captured once into a CUDA graph (each instance's kernels on its own stream,
- * forked from and joined to the batch's stream) and replayed for every step: a step of the
- * whole batch is one graph launch, and small instances run side by side on the GPU. The stage
- * kernels of a replay take their time factors from per-instance tables that the host refills
- * every WEDG_BATCH_CHUNK steps (the factors are the ones the single-instance calls compute).
- * The graph is captured again when the state pointers, the steps dt or stop_nonfinite change. */
+ * the reference, whose batching is the caller's loop over instances (the element blocks of
+ * src/rhs.jl:130-180, 227-252 split one instance). The instances are grouped into buckets that
+ * run the same kernels (the same degrees, coefficient kernels, mass solver and 1D operators;
+ * any mesh sizes). Per stage of an RK4 step, each bucket runs k_prep, k_stage and its mass
+ * solve as one launch each over all of its instances (up to 32 instances per launch; larger
+ * buckets take several), whose blocks each take a tile of one instance's elements, so an
+ * element's arithmetic is the one of a launch of its instance alone. The buckets run side by
+ * side on their own streams; one RK4 step of the whole batch is captured once into a CUDA graph
+ * and replayed for every step. The stage kernels of a replay take their time factors from
+ * per-instance tables that the host refills every WEDG_BATCH_CHUNK steps (the factors are the
+ * ones the single-instance calls compute). The graph is captured again when the state
+ * pointers, the steps dt, stop_nonfinite or a bucket's launch shape change. */
 #define WEDG_BATCH_CHUNK 256
 typedef struct wedg_batch wedg_batch;
 int wedg_batch_create(int n, wedg_ws *const *instances, wedg_batch **out);
@@ -267,11 +290,29 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
                          const double *dt, int64_t nsteps, int stop_nonfinite, int64_t *steps_done, int *finite,
                          int *status);
 
-/* Autotuner of the batch: per bucket of instances with the same degrees (the same kernels),
- * the launch shapes of wedg_autotune tried one coordinate at a time against the time of the
- * whole batch's step (graph replays from copies of the states, which are left unchanged; each
- * trial after one untimed step that captures the graph). The other buckets keep their shapes
- * while one is tuned. Returns the best time per step of the batch in *best_ms (may be NULL). */
+/* The buckets of a batch and their launch shapes: the elements per block of k_prep (its threads,
+ * one element each) and of the mass solves (threads / 32 warps of teams of threads per
+ * element), 32, 64, 96 or 128 threads, and `persist`: 0 launches one block per tile, p > 0 a
+ * persistent grid of p times the blocks the SMs hold at once, each block taking tile after
+ * tile. Results do not depend on the shape (every element's arithmetic is its own). */
+typedef struct wedg_batch_shape {
+  int32_t qu1, qv1, instances, fast;   /* the bucket's degrees + 1, its instances, the kernel family */
+  int32_t prep_threads, mass_threads, persist;
+} wedg_batch_shape;
+int wedg_batch_bucket_count(const wedg_batch *b);
+int wedg_batch_get_shape(const wedg_batch *b, int bucket, wedg_batch_shape *out);
+int wedg_batch_set_shape(wedg_batch *b, int bucket, int prep_threads, int mass_threads, int persist);
+
+/* Autotuner of the batch's launch shapes (no counterpart in the reference, whose only shape is the
+ * nblocks partition of src/rhs.jl:139-142): per bucket, run alone from copies of its instances'
+ * states (left unchanged), steps RK4 steps after one untimed step, timed with CUDA events, for the
+ * candidates of one coordinate at a time (k_prep's and the mass solves' threads per block: 32,
+ * 64, 128; persist: 0, 1, 2). A candidate replaces the bucket's shape only when it is faster in
+ * each of three paired trials against it and faster by more than 2 % in the median. Then the
+ * whole batch's step (graph replays) with the tuned shapes against the shapes it had before,
+ * three paired trials: the tuned shapes stay only if they win every trial, so the batch never
+ * ends up slower than before tuning. *best_ms (may be NULL) receives the median milliseconds per
+ * step of the shapes kept. */
 int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_dev, const double *t0,
                         const double *dt, int64_t steps, double *best_ms);
 

@@ -1,10 +1,10 @@
 """Extract the reference's stored results into small JSON fixtures.
 
-Run in a checkout that has the reference tree (path as the first argument,
-default /root/reference); the fixtures it writes are committed, so the tests
-never read the reference at run time.
+Run with the path of a checkout of the reference tree as its one (required)
+argument; the fixtures it writes are committed, so the tests never read the
+reference at run time.
 
-  python tests/golden/make_golden.py [/path/to/EDG_Westervelt]
+  python tests/golden/make_golden.py /path/to/EDG_Westervelt
 
 Sources (all inside the reference):
   regression.json   test/runtests.jl:207-217 (solve(3, 6, 0.1) pins, rtol 1e-9)
@@ -76,4 +76,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/EDG_Westervelt")
+    main(sys.argv[1])

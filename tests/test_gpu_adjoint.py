@@ -240,3 +240,89 @@ def test_misfit_gradient_against_oracle_differences(gpu):
               J_oracle(c2 - eps * d["c2"], al - eps * d["alpha"], be - eps * d["beta"])) / (2 * eps)
         ad = float(np.sum(grad[name] * d[name]))
         assert abs(fd - ad) <= 1e-5 * abs(fd), (name, fd, ad)
+
+
+def test_misfit_gradient_config5_shape_twenty_directions(gpu):
+    """The adjoint form at the shape of its workload: N = 128, q_u = q_v = 4, c², α, β constant on
+    16 × 16 cells (c ~ U[0.8, 1.25], α log-uniform on [1e-6, 1e-5], β ~ U[0, 4]), a 32 × 32 receiver
+    grid whose observations come from the forward solver on the fields perturbed by ±10 %,
+    absorbing_2beta sides, upwind flux, a Gaussian source strong and fast enough that 1 - 2βv_h
+    comes down to about 0.7 within T = 0.02 (410 RK4 steps, checkpoints every 32). The gradient with
+    respect to all 768 cell values at once is checked against central differences of the misfit
+    (step 1e-6 relative to each cell value) along 20 seeded random directions, to 1e-6 relative."""
+    from edg_westervelt_gb300.solver import _locate, _vrow
+    rng = np.random.default_rng(51)
+    q, N, m, T = 4, 128, 16, 0.02
+    c2 = rng.uniform(0.8, 1.25, (m, m)) ** 2
+    al = 10.0 ** rng.uniform(-6, -5, (m, m))
+    be = rng.uniform(0.0, 4.0, (m, m))
+    g = (np.arange(32) + 0.5) / 32
+    receivers = [(x, y) for y in g for x in g]
+    src = W.GaussianSource(x0=(0.45, 0.5), r0=0.08, omega=16 * math.pi, Ts=0.04, amplitude=6.0)
+    kw = dict(flux="upwind", mixed=False, boundary="absorbing_2beta", source=src)
+    pert = lambda a: a * (1.0 + 0.1 * rng.uniform(-1, 1, a.shape))   # noqa: E731
+    pre, _ = W.precompute(q, N, mode="source", coefficients=W.piecewise_coefficients(pert(c2), pert(al), pert(be)),
+                          **kw)
+    dt = (1.0 / N) / (10 * q * q)
+    nsteps = int(round(T / dt))
+    ws = W.Workspace(pre, N)
+    u = np.zeros((N, N, 5, 5), order="F")
+    v = np.zeros((N, N, 5, 5), order="F")
+    assert ws.rk4_steps(u, v, 0.0, T / nsteps, nsteps) == nsteps
+    u_obs = []
+    for xr, yr in receivers:
+        kr, xi = _locate(xr, N)
+        jr, eta = _locate(yr, N)
+        u_obs.append(float(_vrow(eta, 5) @ u[jr - 1, kr - 1] @ _vrow(xi, 5)))
+    del ws
+    J0, grad = W.misfit_gradient(q, N, T, c2, al, be, receivers, u_obs, every=32, **kw)
+    assert J0 > 0
+    eps = 1e-6
+    worst = 0.0
+    for _ in range(20):
+        d = {k: rng.standard_normal((m, m)) * x for k, x in (("c2", c2), ("alpha", al), ("beta", be))}
+        Jp = W.misfit(q, N, T, c2 + eps * d["c2"], al + eps * d["alpha"], be + eps * d["beta"], receivers, u_obs, **kw)
+        Jm = W.misfit(q, N, T, c2 - eps * d["c2"], al - eps * d["alpha"], be - eps * d["beta"], receivers, u_obs, **kw)
+        fd = (Jp - Jm) / (2 * eps)
+        ad = sum(float(np.sum(grad[k] * d[k])) for k in d)
+        worst = max(worst, abs(fd - ad) / abs(fd))
+    assert worst <= 1e-6, worst
+
+
+@pytest.mark.parametrize("solver", ["chebyshev", "cg"])
+def test_group_gradients_match_single_calls(gpu, solver):
+    """misfit_gradients for four seeded parameter fields at once (the forward runs and reverse
+    sweeps of the four workspaces as multi-instance launches) against misfit_gradient for each
+    field alone: the same misfits and gradients. Also with an allowance too small to keep the
+    stage data, where the reverse sweeps run one after the other."""
+    rng = np.random.default_rng(47)
+    q, N, T, m = 3, 8, 0.05, 2
+    g = (np.arange(4) + 0.5) / 4
+    receivers = [(x, y) for y in g for x in g]
+    src = W.GaussianSource(x0=(0.4, 0.55), r0=0.15, omega=12 * math.pi, Ts=0.5)
+    kw = dict(flux="alternating", mixed=True, kappa=0.5, source=src, mass_solver=solver,
+              boundary=dict(bot="wall", top="absorbing", lft="dirichlet", rgt="absorbing_2beta"))
+    fields = [(rng.uniform(0.8, 1.5, (m, m)), 10 ** rng.uniform(-4, -3, (m, m)), rng.uniform(0.5, 3.0, (m, m)))
+              for _ in range(4)]
+    u_obs = [1e-4 * rng.standard_normal(len(receivers)) for _ in fields]
+    single = [W.misfit_gradient(q, N, T, *f, receivers, o, every=5, **kw) for f, o in zip(fields, u_obs)]
+    group = W.misfit_gradients(q, N, T, fields, receivers, u_obs, every=5, **kw)
+    for (J1, g1), (J2, g2) in zip(single, group):
+        assert J1 == J2
+        for k in g1:
+            assert np.max(np.abs(g1[k] - g2[k])) <= 1e-13 * np.max(np.abs(g1[k])), k
+    # the reverse sweeps one after the other: every workspace's allowance below one segment's data
+    from edg_westervelt_gb300.solver import _misfit_problem, _misfit_value
+    probs = [_misfit_problem(q, N, T, *f, 10, kw) for f in fields]
+    wss = [p[1] for p in probs]
+    for w in wss:
+        w.set_adjoint_memory(1)
+    nu, nv = probs[0][0]["qu1"], probs[0][0]["qv1"]
+    z = [np.zeros((N, N, nu, nu), order="F") for _ in wss]
+    zv = [np.zeros((N, N, nv, nv), order="F") for _ in wss]
+    uT, vT = W.rk4_adjoint_forward_many(wss, z, zv, 0.0, probs[0][2], probs[0][3], every=5)
+    lams = [_misfit_value(uT[i], N, receivers, u_obs[i])[1] for i in range(len(wss))]
+    out = W.rk4_adjoint_reverse_many(wss, lams, [np.zeros_like(x) for x in vT], params=True)
+    for (J1, g1), o in zip(single, out):
+        gc2 = o[2].reshape(m, N // m, m, N // m).sum(axis=(1, 3))
+        assert np.max(np.abs(gc2 - g1["c2"])) <= 1e-10 * np.max(np.abs(g1["c2"]))

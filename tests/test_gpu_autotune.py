@@ -1,8 +1,8 @@
 """Launch shapes and their autotuners (wedg_set_launch_shape, wedg_autotune, wedg_batch_autotune;
-no counterpart in the reference): the threads per block of k_prep and of the mass solves change
-only how elements are spread over blocks, never an element's arithmetic, so every shape must give
-the same states bit for bit; the tuners leave the states they are given unchanged and keep a
-valid shape."""
+no counterpart in the reference): the threads per block of k_prep and of the mass solves (and,
+in a batch, persistent grids) change only how elements are spread over blocks, never an
+element's arithmetic, so every shape must give the same states bit for bit; the tuners leave the
+states they are given unchanged and keep a valid shape."""
 import numpy as np
 import pytest
 
@@ -88,9 +88,8 @@ def test_batch_autotune_then_batch_matches_single_instances():
     dts = [x[5] for x in inst]
     ms = batch.autotune(us, vs, t0s, dts, steps=2)
     assert ms > 0
-    for w in batch.ws:
-        p, m = w.launch_shape
-        assert p in (32, 64, 128) and m in (32, 64, 128)
+    for s in batch.shapes():
+        assert s["prep_threads"] in (32, 64, 128) and s["mass_threads"] in (32, 64, 128) and s["persist"] in (0, 1, 2)
     for x, u, v in zip(inst, us, vs):
         assert torch.equal(u, x[2]) and torch.equal(v, x[3])
     batch.rk4_steps(us, vs, t0s, dts, 30)

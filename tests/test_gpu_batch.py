@@ -1,9 +1,11 @@
 """The batched form (wedg_batch_*): instances of different N, degrees, fluxes, boundary kinds,
-coefficients and mass solvers advanced together by one replayed CUDA graph per step. The
-kernels and time factors are those of the single-instance calls, so every instance must
-match its own Workspace.rk4_steps run bit for bit; the factor tables are refilled every
-WEDG_BATCH_CHUNK = 256 steps, so a run of 600 steps crosses two refills. Errors stay with
-their instance."""
+coefficients and mass solvers advanced together by one replayed CUDA graph per step, every stage
+kernel launched once per bucket of instances with the same kernels. An element's arithmetic is
+the one of a single-instance launch and the time factors are those of the single-instance
+calls, so every instance must match its own Workspace.rk4_steps run bit for bit; the factor
+tables are refilled every WEDG_BATCH_CHUNK = 256 steps, so a run of 600 steps crosses two
+refills. Buckets of many instances of different N (more than the 32 one launch takes) and every
+launch shape give the same states. Errors stay with their instance."""
 import numpy as np
 import pytest
 
@@ -80,3 +82,60 @@ def test_batch_errors_stay_with_their_instance():
         batch.rk4_steps(us, vs, [x[5] for x in inst], [x[4] for x in inst], 4)
     done = [w.stats()["steps_done"] for w in wss]
     assert done[2] == 0 and all(d == 4 for i, d in enumerate(done) if i != 2)
+
+
+def _many(seed=12):
+    """44 seeded instances, q_v = q_u - 1, N from 2 to 9, random fluxes and boundary kinds, in three
+    buckets: 6 manufactured-solution instances of q_u = 3 (paper coefficients: the general
+    kernels), 34 initial-value or source instances of q_u = 3 and 4 of q_u = 2 (constant
+    coefficients)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(44):
+        q = 2 if i >= 40 else 3
+        N = int(rng.integers(2, 10))
+        mode = "mms" if i < 6 else str(rng.choice(["initial_value", "source"]))
+        kinds = [str(k) for k in rng.choice(["absorbing_2beta", "absorbing", "dirichlet", "wall"], 4)]
+        kw = dict(flux=str(rng.choice(["upwind", "central", "alternating"])), mixed=True, mode=mode, kappa=0.5,
+                  boundary=dict(bot=kinds[0], top=kinds[1], lft=kinds[2], rgt=kinds[3]))
+        if mode != "mms":
+            kw["coefficients"] = W.constant_coefficients(c=float(rng.uniform(0.6, 1.5)),
+                                                         alpha=float(10 ** rng.uniform(-5, -3)),
+                                                         beta=float(rng.uniform(0.0, 4.0)))
+        pre, _ = W.precompute(q, N, **kw)
+        out.append((pre, N, q, 0.0 if mode == "mms" else 0.013))
+    return out
+
+
+def test_buckets_of_many_instances_and_every_shape():
+    """44 instances in three buckets (one of 34 instances, so its stages take two launches), each advanced 40 steps by the batch under several launch shapes (threads per block
+    of k_prep and of the mass solve, persistent grids): the states equal each instance's own run
+    bit for bit."""
+    import torch
+    dev = torch.device("cuda:0")
+    inst = _many()
+    nsteps = 40
+    ref, us0, vs0, dts = [], [], [], []
+    for pre, N, q, t0 in inst:
+        nu, nv = pre["qu1"], pre["qv1"]
+        dt = (1.0 / N) / (10 * q * q)
+        u = torch.zeros(N * N * nu * nu, dtype=torch.float64, device=dev)
+        v = torch.zeros(N * N * nv * nv, dtype=torch.float64, device=dev)
+        us0.append(u.clone())
+        vs0.append(v.clone())
+        dts.append(dt)
+        assert W.Workspace(pre, N).rk4_steps(u, v, t0, dt, nsteps) == nsteps
+        ref.append((u.cpu().numpy(), v.cpu().numpy()))
+    batch = W.Batch([W.Workspace(pre, N) for pre, N, *_ in inst])
+    shapes = batch.shapes()
+    assert sum(s["instances"] for s in shapes) == len(inst) and max(s["instances"] for s in shapes) > 32
+    t0s = [x[3] for x in inst]
+    for prep, mass, persist in ((128, 128, 0), (32, 64, 0), (64, 32, 1), (128, 96, 2)):
+        for k in range(len(shapes)):
+            batch.set_shape(k, prep, mass, persist)
+        us = [u.clone() for u in us0]
+        vs = [v.clone() for v in vs0]
+        done, fin, st = batch.rk4_steps(us, vs, t0s, dts, nsteps)
+        assert done == [nsteps] * len(inst) and all(fin)
+        for (ru, rv), u, v in zip(ref, us, vs):
+            assert np.array_equal(ru, u.cpu().numpy()) and np.array_equal(rv, v.cpu().numpy()), (prep, mass, persist)

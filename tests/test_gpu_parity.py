@@ -446,3 +446,65 @@ def test_rk4_many_steps_on_a_mesh_with_fewer_elements_than_bins(gpu):
     assert ws.rk4_steps(u, v, 0.02, dt, 20) == 20
     assert ws.stats()["cheb_steps_max"] > N * N       # counts beyond the element count
     assert rel_max((u, v), (uo, vo)) < TOL, rel_max((u, v), (uo, vo))
+
+
+def test_config1_per_evaluation_rhs_seeds(gpu):
+    """Config 1, solve(3, 10, 0.1; flux=:upwind, mixed=true) with its defaults (paper
+    coefficients, absorbing_2beta on every side, σ = 0): the per-evaluation RHS against the
+    oracle's on the seeded states u ~ N(0, 1), v ~ 0.05 N(0, 1) of test/runtests.jl:273, seeds 0 to 9,
+    at t = 0.037, one workspace for all ten calls."""
+    N, q = 10, 3
+    pp, po = _pair(q, N, flux="upwind", mixed=True)
+    ws, ow = W.Workspace(pp, N), OracleWorkspace(po)
+    worst = 0.0
+    for seed in range(10):
+        u, v = _state(np.random.default_rng(seed), pp, N)
+        worst = max(worst, rel_max(ow.rhs(u, v, 0.037), ws.rhs(u, v, 0.037)))
+    assert worst < TOL, worst
+
+
+def test_config3_full_size_against_oracle(gpu):
+    """Config 3 at its size: N = 256, q_u = 5, q_v = 4, initial-value mode, c, α, β constant on 4 × 4
+    subsquares (the bench's default_rng(3) draw), dirichlet / absorbing / absorbing_2beta / wall
+    sides, central flux, one-sided faces. One RHS and two RK4 steps on a seeded state against the
+    oracle on the same pre (src/rhs.jl:490-550, src/solver.jl:289-321)."""
+    from bench import config3_problem
+    pp, N, dt = config3_problem()
+    assert pp["one_sided"] and pp["Ainv_u"] is not None
+    po = dict(pp, Ainv_u=np.asfortranarray(pp["Ainv_u"]))
+    nu, nv = pp["qu1"], pp["qv1"]
+    rng = np.random.default_rng(33)
+    d = lambda n: 1.0 / (1.0 + np.add.outer(np.arange(n), np.arange(n))) ** 2   # noqa: E731
+    u = np.asfortranarray(1e-3 * rng.standard_normal((N, N, nu, nu)) * d(nu))
+    v = np.asfortranarray(2e-3 * rng.standard_normal((N, N, nv, nv)) * d(nv))
+    ow, ws = OracleWorkspace(po), W.Workspace(pp, N)
+    assert ws.stats()["fast_path"] == 1
+    assert rel_max(ow.rhs(u, v, 0.01), ws.rhs(u, v, 0.01)) < TOL
+    uo, vo = u.copy(order="F"), v.copy(order="F")
+    ug, vg = u.copy(order="F"), v.copy(order="F")
+    for k in range(2):
+        ow.rk4_step(uo, vo, 0.01 + k * dt, dt)
+        W.rk4_step_(ug, vg, 0.01 + k * dt, dt, N, 1.0 / N, pp, ws)
+    assert ws.fin
+    assert rel_max((uo, vo), (ug, vg)) < TOL, rel_max((uo, vo), (ug, vg))
+
+
+def test_headline_front_state_rk4_step_against_oracle(gpu):
+    """The bench's headline workload and state: N = 512, q_u = q_v = 6, source mode, c = 1, α = 1e-6,
+    β = 8, bottom absorbing_2beta and three walls (κ = 0.5), alternating flux, and the seeded
+    steepened circular front (1 - 2βv_h across [0.42, 1.58], up to about 20 Chebyshev steps). One
+    RK4 step at the bench's t0 and dt against the oracle's on the same pre; the GPU takes every
+    element's own Chebyshev count, the oracle the reference's common maximum."""
+    import bench
+    N = 512
+    pp = W.precompute(bench.Q, N, coefficients=W.constant_coefficients(**bench.COEF), **bench.KW)[0]
+    po = dict(pp, Ainv_u=np.asfortranarray(pp["Ainv_u"]))
+    u, v = bench.synthetic_state(N, pp["qu1"], pp["qv1"], 0, "front")
+    dt = (1.0 / N) / (10 * bench.Q ** 2)
+    ug, vg = u.copy(order="F"), v.copy(order="F")
+    ws = W.Workspace(pp, N)
+    W.rk4_step_(ug, vg, bench.T0, dt, N, 1.0 / N, pp, ws)
+    assert ws.fin and ws.stats()["cheb_steps_max"] >= 10
+    ow = OracleWorkspace(po)
+    ow.rk4_step(u, v, bench.T0, dt)
+    assert rel_max((u, v), (ug, vg)) < TOL, rel_max((u, v), (ug, vg))

@@ -6,7 +6,9 @@ create a workspace. wedg_rhs_noalloc needs none: it keeps its device scratch in 
 fixed static array of the library. These tests call it through the C ABI twice in
 a row on different states and compare it with the workspace entry point wedg_rhs
 on the same inputs (max-norm relative 1e-12, the bar of the other GPU tests), and
-check that a mesh too large for the static array is refused with a message.
+check that a mesh too large for the static array is refused with a message, and that
+its errors (a boundary weight and a mass matrix that is not positive definite, for
+both mass solvers) carry the status and the message that wedg_rhs gives.
 This file is collected last, so a failure here comes after every other test ran.
 """
 import ctypes
@@ -56,11 +58,16 @@ CASES = {
         6, 8, dict(mixed=False, mode="source", kappa=0.5, flux="alternating",
                    coefficients=W.constant_coefficients(c=1.0, alpha=1e-6, beta=8.0),
                    boundary=dict(bot="absorbing_2beta", top="wall", lft="wall", rgt="wall"))),
+    "CG mass solver, mixed sides": (
+        4, 5, dict(mixed=True, mode="initial_value", flux="central", mass_solver="cg", kappa=0.5,
+                   boundary=dict(bot="dirichlet", top="absorbing", lft="absorbing_2beta", rgt="wall"))),
 }
 
 
 @pytest.mark.parametrize("case", list(CASES))
 def test_noalloc_matches_workspace_twice(case):
+    """Two calls in a row on different states: the first on the default stream, the second on a
+    stream of the caller's."""
     import torch
     assert torch.cuda.is_available()
     q, N, kw = CASES[case]
@@ -83,8 +90,9 @@ def test_noalloc_matches_workspace_twice(case):
         vt = torch.full_like(dv, float("nan"))
         torch.cuda.synchronize()
         msg = ctypes.create_string_buffer(512)
+        side = torch.cuda.Stream(device=dev) if call == 1 else None
         rc = lib.wedg_rhs_noalloc(ctypes.byref(cfg), ctypes.byref(p), du.data_ptr(), dv.data_ptr(), t,
-                                  ut.data_ptr(), vt.data_ptr(), None, msg, 512)
+                                  ut.data_ptr(), vt.data_ptr(), side.cuda_stream if side else None, msg, 512)
         assert rc == L.WEDG_OK, msg.value.decode()
         got = (ut.cpu().numpy().reshape((N, N, nu, nu), order="F"),
                vt.cpu().numpy().reshape((N, N, nv, nv), order="F"))
@@ -109,4 +117,52 @@ def test_noalloc_refuses_a_mesh_beyond_the_static_array():
                                   dummy.data_ptr(), dummy.data_ptr(), None, msg, 512)
     assert rc == L.WEDG_ERR_ARGUMENT
     assert "mesh too large for wedg_rhs_noalloc" in msg.value.decode()
+    del keep
+
+
+@pytest.mark.parametrize("solver", ["chebyshev", "cg"])
+def test_noalloc_errors_match_workspace(solver):
+    """A state whose boundary weight 1 - 2βv_h fails at a face point, and one whose mass matrix is
+    not positive definite on two elements: the status and the message (the first failing point or
+    element, in the reference's words) are those of wedg_rhs on the same inputs, and the static
+    array serves a good call again afterwards."""
+    import torch
+    N = 8
+    co = W.replace_coefficients(W.paper_coefficients(), alpha=1e-6, beta=1.0)
+    bd = dict(bot="absorbing_2beta", top="absorbing", lft="absorbing", rgt="wall")
+    pre, _ = W.precompute(3, N, coefficients=co, boundary=bd, mass_solver=solver, inverses="host")
+    nu, nv = pre["qu1"], pre["qv1"]
+    cfg, p, keep = _abi_structs(pre, N)
+    ws = W.Workspace(pre, N)
+    dev = torch.device("cuda:0")
+    u = np.zeros((N, N, nu, nu), order="F")
+    v_bnd = np.zeros((N, N, nv, nv), order="F")
+    v_bnd[0, N - 1, 0, 0] = 2.5
+    v_bnd[3, 0, 0, 0] = 2.5
+    v_mass = np.zeros((N, N, nv, nv), order="F")
+    v_mass[3, 5, 0, 0] = 2.5
+    v_mass[4, 1, 0, 0] = 2.5
+    du = torch.from_numpy(u.reshape(-1, order="F").copy()).to(dev)
+    ut = torch.empty_like(du)
+    for v, status in ((v_bnd, L.WEDG_ERR_BOUNDARY_WEIGHT), (v_mass, L.WEDG_ERR_MASS_NOT_PD)):
+        with pytest.raises(W.ErrorException) as ei:
+            ws.rhs(u, v, 0.0)
+        dv = torch.from_numpy(v.reshape(-1, order="F").copy()).to(dev)
+        vt = torch.empty_like(dv)
+        msg = ctypes.create_string_buffer(512)
+        rc = L.lib().wedg_rhs_noalloc(ctypes.byref(cfg), ctypes.byref(p), du.data_ptr(), dv.data_ptr(), 0.0,
+                                      ut.data_ptr(), vt.data_ptr(), None, msg, 512)
+        assert rc == status
+        assert msg.value.decode() == str(ei.value)
+    # a good state after the errors: the error word starts clear again
+    v = np.zeros((N, N, nv, nv), order="F")
+    dv = torch.from_numpy(v.reshape(-1, order="F").copy()).to(dev)
+    vt = torch.empty_like(dv)
+    msg = ctypes.create_string_buffer(512)
+    rc = L.lib().wedg_rhs_noalloc(ctypes.byref(cfg), ctypes.byref(p), du.data_ptr(), dv.data_ptr(), 0.0,
+                                  ut.data_ptr(), vt.data_ptr(), None, msg, 512)
+    assert rc == L.WEDG_OK, msg.value.decode()
+    ref = ws.rhs(u, v, 0.0)
+    got = (ut.cpu().numpy().reshape((N, N, nu, nu), order="F"), vt.cpu().numpy().reshape((N, N, nv, nv), order="F"))
+    assert _rel(ref, got) < 1e-12
     del keep
