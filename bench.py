@@ -400,11 +400,13 @@ def run_ours(args):
                "h2d_bytes_per_step": int(uh.nbytes + vh.nbytes), "d2h_bytes_per_step": int(uh.nbytes + vh.nbytes),
                "steps": ke, "api": "Workspace.rk4_steps (wedg_rk4_steps, WEDG_HOST)"}
 
-    batched = config3 = general = None
+    batched = config3 = general = adjoint = None
     if world == 1 and not args.no_batched:
         batched = run_batched(torch, dev, max(4, 2 * args.steps), args.warmup)
         config3 = run_config3(torch, dev, args.steps, args.warmup)
         general = run_general(torch, dev, args.steps, args.warmup)
+    if world == 1 and not args.no_adjoint:
+        adjoint = run_adjoint(torch, args.adjoint_T)
 
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
@@ -476,6 +478,7 @@ def run_ours(args):
         "clocks": clocks.summary(), "gpu_launches": main["launches"],
         "kernel_ms": kms,
         "batched": batched,
+        "adjoint": adjoint,
         "config3": config3,
         "general": general,
         "zero_state": {"value": world * dof * 4 * zero["steps"] / (zero["ms"] / 1e3),
@@ -730,26 +733,32 @@ def run_config3(torch, dev, steps, warmup):
             "dof": dof, "one_sided": bool(pre["one_sided"]), "fast_path": bool(ws.stats()["fast_path"])}
 
 
-def run_adjoint(torch, T, every=32):
-    """The adjoint form: one gradient of J = ½ Σ_r (u_h(x_r, T) - u_obs_r)² over a 32 × 32 receiver
-    grid (cell centres) with respect to c², α, β constant on 16 × 16 cells (c ~ U[0.8, 1.25],
-    α log-uniform on [1e-6, 1e-5] -- larger α makes the explicit RK4 step unstable at this dt --
-    β ~ U[0, 4]), forward N = 128,
-    q_u = q_v = 4, absorbing_2beta sides, Gaussian source, checkpoints every 32 steps; u_obs from
-    the forward solver on the field perturbed by ±10 % (default_rng(5)). Timed: one forward solve
-    (the misfit) and one gradient (misfit_gradient: forward, reverse sweep, parameter sums)."""
-    import edg_westervelt_gb300 as W
-    from edg_westervelt_gb300.solver import _locate, _vrow
-    rng = np.random.default_rng(5)
-    q, N, m = 4, 128, 16
+def adjoint_problem(seed=5, m=16):
+    """The adjoint form's workload: c², α, β constant on m × m cells (c ~ U[0.8, 1.25], α log-uniform on
+    [1e-6, 1e-5] -- larger α makes the explicit RK4 step unstable at this dt -- β ~ U[0, 4]) from
+    default_rng(seed), a 32 × 32 receiver grid at the cell centres, forward N = 128, q_u = q_v = 4,
+    absorbing_2beta sides, upwind flux, Gaussian source. Returns (rng, fields, receivers, kw)."""
+    rng = np.random.default_rng(seed)
     c2 = rng.uniform(0.8, 1.25, (m, m)) ** 2
     al = 10.0 ** rng.uniform(-6, -5, (m, m))
     be = rng.uniform(0.0, 4.0, (m, m))
     g = (np.arange(32) + 0.5) / 32
     receivers = [(x, y) for y in g for x in g]
-    kw = dict(flux="upwind", mixed=False, boundary="absorbing_2beta")
-    # observations: the forward solver on the perturbed field
-    pert = lambda a: a * (1.0 + 0.1 * rng.uniform(-1, 1, a.shape))
+    return rng, (c2, al, be), receivers, dict(flux="upwind", mixed=False, boundary="absorbing_2beta")
+
+
+def run_adjoint(torch, T, every=32, batch=16, batch_T=0.125):
+    """The adjoint form (config 5): the gradient of J = ½ Σ_r (u_h(x_r, T) - u_obs_r)² with respect to
+    the 3 × 16 × 16 cell values (adjoint_problem), u_obs from the forward solver on the field
+    perturbed by ±10 %, checkpoints every 32 steps. Timed: one forward solve (Workspace.rk4_steps),
+    one gradient (misfit_gradient: forward with checkpoints, misfit, reverse sweep with the parameter
+    sensitivities, cell sums) and a batch of `batch` gradients for different seeded fields at once
+    (misfit_gradients: every stage of all of them as multi-instance launches) over batch_T."""
+    import edg_westervelt_gb300 as W
+    from edg_westervelt_gb300.solver import _locate, _vrow
+    q, N = 4, 128
+    rng, (c2, al, be), receivers, kw = adjoint_problem()
+    pert = lambda a: a * (1.0 + 0.1 * rng.uniform(-1, 1, a.shape))   # noqa: E731
     pre, _ = W.precompute(q, N, mode="source", coefficients=W.piecewise_coefficients(pert(c2), pert(al), pert(be)),
                           **kw)
     dt = (1.0 / N) / (10 * q * q)
@@ -765,7 +774,7 @@ def run_adjoint(torch, T, every=32):
         jr, eta = _locate(yr, N)
         u_obs.append(float(_vrow(eta, 5) @ u[jr - 1, kr - 1] @ _vrow(xi, 5)))
     del ws
-    # one forward solve of the unperturbed field (device time of the step loop, host clock)
+    # one forward solve of the unperturbed field (the step loop, host state in and out)
     pre, _ = W.precompute(q, N, mode="source", coefficients=W.piecewise_coefficients(c2, al, be), **kw)
     ws = W.Workspace(pre, N)
     u[...] = 0.0
@@ -778,12 +787,34 @@ def run_adjoint(torch, T, every=32):
     t0 = time.perf_counter()
     J, grad = W.misfit_gradient(q, N, T, c2, al, be, receivers, u_obs, every=every, **kw)
     t_grad = time.perf_counter() - t0
-    return {"workload": f"misfit gradient, N={N} q_u=q_v={q}, 16x16 cells of c2, alpha, beta, 32x32 receivers, "
-                        f"absorbing_2beta, Gaussian source, T={T} ({nsteps} RK4 steps), checkpoints every {every}",
-            "value": t_grad, "unit": "s/grad", "forward_s": t_fwd, "grad_over_forward": t_grad / t_fwd,
-            "misfit": J, "grad_norms": {k: float(np.linalg.norm(vv)) for k, vv in grad.items()},
-            "timing": "host clock around misfit_gradient (forward solve, misfit, reverse sweep with the parameter "
-                      "sensitivities, cell sums) and around one forward solve (Workspace.rk4_steps, host state)"}
+    out = {"workload": f"misfit gradient, N={N} q_u=q_v={q}, 16x16 cells of c2, alpha, beta, 32x32 receivers, "
+                       f"absorbing_2beta, Gaussian source, T={T} ({nsteps} RK4 steps), checkpoints every {every}",
+           "value": t_grad, "unit": "s/grad", "forward_s": t_fwd, "grad_over_forward": t_grad / t_fwd,
+           "misfit": J, "grad_norms": {k: float(np.linalg.norm(vv)) for k, vv in grad.items()},
+           "timing": "host clock around misfit_gradient (precompute, workspace, forward with checkpoints, misfit, "
+                     "reverse sweep with the parameter sensitivities, cell sums) and around one forward solve "
+                     "(Workspace.rk4_steps, host state; precompute not included)"}
+    if batch:
+        # batch different seeded fields, the same observations
+        fields = []
+        for _ in range(batch):
+            fields.append((rng.uniform(0.8, 1.25, c2.shape) ** 2, 10.0 ** rng.uniform(-6, -5, al.shape),
+                           rng.uniform(0.0, 4.0, be.shape)))
+        bsteps = int(round(batch_T / ((1.0 / N) / (10 * q * q))))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = W.misfit_gradients(q, N, batch_T, fields, receivers, u_obs, every=every, **kw)
+        t_batch = time.perf_counter() - t0
+        per_grad = t_batch / batch
+        out["batch"] = {"gradients": batch, "T": batch_T, "steps": bsteps, "s": t_batch, "s_per_grad": per_grad,
+                        "s_per_grad_at_T": per_grad * nsteps / bsteps,
+                        "speedup_vs_single_per_step": (t_grad / nsteps) / (per_grad / bsteps),
+                        "grad_over_forward_per_step": (per_grad / bsteps) / (t_fwd / nsteps),
+                        "misfits": [float(r[0]) for r in res[:3]],
+                        "note": "misfit_gradients: the forward runs and reverse sweeps of all gradients together, "
+                                "each stage one multi-instance launch per kernel; s_per_grad_at_T scales the "
+                                "per-gradient time by the steps of T"}
+    return out
 
 
 def main():
@@ -806,6 +837,7 @@ def main():
                     help="only the general-kernel measurement (varying coefficients; --mesh applies)")
     ap.add_argument("--adjoint", action="store_true", help="only the adjoint-form measurement (one gradient)")
     ap.add_argument("--adjoint-T", type=float, default=0.5, help="final time of the adjoint-form workload")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-form measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

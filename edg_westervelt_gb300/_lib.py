@@ -54,6 +54,20 @@ class Stats(ctypes.Structure):
                 ("element_stages", ctypes.c_int64)]
 
 
+class FaceValues(ctypes.Structure):
+    """wedg_face_values (include/wedg.h)."""
+    _fields_ = [("at", _D), ("lo", _D), ("hi", _D), ("jump_scale", ctypes.c_double), ("value", ctypes.c_double)]
+
+
+class Points(ctypes.Structure):
+    """wedg_points (include/wedg.h)."""
+    _fields_ = ([("c_q", _D), ("alpha_q", _D), ("beta_h", _D), ("c_value", ctypes.c_double),
+                 ("alpha_value", ctypes.c_double), ("beta_value", ctypes.c_double)]
+                + [(n, FaceValues) for n in ("hc", "ha", "hb", "vc", "va", "vb", "hg0", "vg0")]
+                + [(n, _D) for n in ("sp_h", "cdiv_h", "ddiv_h", "xloc_h", "yloc_h")]
+                + [(n, ctypes.c_double) for n in ("src_amp", "src_x0", "src_y0", "src_r0")])
+
+
 class BatchShape(ctypes.Structure):
     """wedg_batch_shape (include/wedg.h)."""
     _fields_ = [(n, ctypes.c_int32) for n in ("qu1", "qv1", "instances", "fast", "prep_threads", "mass_threads",
@@ -98,6 +112,10 @@ def lib():
     L = ctypes.CDLL(LIB_PATH)
     vp = ctypes.c_void_p
     L.wedg_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Pre), ctypes.POINTER(vp)]
+    L.wedg_create_points.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Pre), ctypes.POINTER(Points),
+                                     ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(vp)]
+    L.wedg_one_sided.argtypes = [vp]
+    L.wedg_export.argtypes = [vp, ctypes.c_char_p, _D, ctypes.c_size_t]
     L.wedg_destroy.argtypes = [vp]
     L.wedg_destroy.restype = None
     L.wedg_rhs.argtypes = [vp, _D, _D, ctypes.c_double, _D, _D, _I64, _I64, ctypes.c_int]

@@ -158,6 +158,7 @@ struct wedg_ws {
   int64_t rk_chk_n = 0, rk_seg_n = 0;
   double *rk_lam = nullptr, *rk_acc = nullptr, *rk_kbar = nullptr, *rk_g = nullptr, *rk_y = nullptr;
   double *rk_par = nullptr;   // per-element gradients with respect to c², α, β
+  double *rk_ry = nullptr, *rk_racc = nullptr;   // the recompute's state and RK4 sum when it runs beside the reverse
   // the forward run the next reverse sweep differentiates
   bool rk_ready = false;
   double rk_dt = 0;
@@ -167,7 +168,7 @@ struct wedg_ws {
   // wedg_set_adjoint_memory): the stage RHS K = (ut | vt), traces, G, Chebyshev data
   struct StageData {
     double *k = nullptr, *tr = nullptr, *G = nullptr, *th = nullptr, *de = nullptr;
-    int *nst = nullptr, *bins = nullptr, *bin_count = nullptr;
+    int *nst = nullptr, *bins = nullptr, *bin_count = nullptr, *nmax = nullptr;
     int parity = 0;
   };
   std::vector<StageData> rk_keep;
@@ -292,7 +293,7 @@ int reset_flags(wedg_ws *ws) {
   CK(ws, cudaMemsetAsync(ws->F.err, 0xFF, sizeof(unsigned long long), ws->stream));
   CK(ws, cudaMemsetAsync(ws->F.cg_nfail, 0, sizeof(unsigned int), ws->stream));
   CK(ws, cudaMemsetAsync(ws->F.nonfinite, 0, sizeof(unsigned int), ws->stream));
-  CK(ws, cudaMemsetAsync(ws->F.nmax, 0, sizeof(int), ws->stream));
+  CK(ws, cudaMemsetAsync(ws->F.nmax, 0, 3 * sizeof(int), ws->stream));
   CK(ws, cudaMemsetAsync(ws->F.nsum, 0, sizeof(unsigned long long), ws->stream));
   CK(ws, cudaMemsetAsync(ws->F.bin_count, 0, 2 * NBIN * sizeof(int), ws->stream));
   ws->parity = 0;
@@ -516,7 +517,7 @@ int enqueue_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t,
 Fields kept_fields(const wedg_ws *ws, const wedg_ws::StageData &d) {
   Fields F = ws->F;
   F.tr = d.tr; F.G = d.G; F.th = d.th; F.de = d.de;
-  F.nst = d.nst; F.bins = d.bins; F.bin_count = d.bin_count;
+  F.nst = d.nst; F.bins = d.bins; F.bin_count = d.bin_count; F.nmax = d.nmax;
   return F;
 }
 
@@ -524,7 +525,7 @@ Fields kept_fields(const wedg_ws *ws, const wedg_ws::StageData &d) {
 size_t stage_data_bytes(const wedg_ws *ws) {
   const size_t E = ws->E;
   return sizeof(double) * E * ((size_t)ws->nu * ws->nu + ws->nv * ws->nv + 12 * ws->nq + ws->qh * ws->qh + 2) +
-         sizeof(int) * (E * (1 + NBIN) + 2 * NBIN);
+         sizeof(int) * (E * (1 + NBIN) + 2 * NBIN + 4);
 }
 
 int collect(wedg_ws *ws) {
@@ -540,7 +541,7 @@ int collect(wedg_ws *ws) {
   CK(ws, cudaMemcpy(&err, ws->F.err, sizeof err, cudaMemcpyDeviceToHost));
   CK(ws, cudaMemcpy(&cgf, ws->F.cg_nfail, sizeof cgf, cudaMemcpyDeviceToHost));
   CK(ws, cudaMemcpy(&nonf, ws->F.nonfinite, sizeof nonf, cudaMemcpyDeviceToHost));
-  CK(ws, cudaMemcpy(&nmax, ws->F.nmax, sizeof nmax, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(&nmax, ws->F.nmax + 2, sizeof nmax, cudaMemcpyDeviceToHost));
   CK(ws, cudaMemcpy(&done, ws->steps_done, sizeof done, cudaMemcpyDeviceToHost));
   ws->stats.cg_not_converged = (int32_t)cgf;
   ws->stats.finite = nonf ? 0 : 1;
@@ -961,12 +962,21 @@ int adjoint_reverse_group(const std::vector<wedg_ws *> &G, const double *const *
     if (ws->adj_mem >= 0) allow += (size_t)ws->adj_mem;
     else bounded = false;
   }
-  bool keep;
+  // with room for two segments' data, the forward data of the next segment (back in time) is
+  // recomputed on a second stream while the present segment is reversed: the two overlap on a GPU
+  // that one problem of this size does not fill
+  size_t extra = 0;                            // the second set's stage states and the recompute's buffers
+  for (wedg_ws *ws : G)
+    extra += sizeof(double) * (size_t)ws->E * (ws->nu * ws->nu + ws->nv * ws->nv) * (4 * seg + 2);
+  bool keep, pipe;
   if (!bounded) {
     size_t fr = 0, tot = 0;
-    keep = cudaMemGetInfo(&fr, &tot) == cudaSuccess && need <= (fr + have) / 2;
+    const bool info = cudaMemGetInfo(&fr, &tot) == cudaSuccess;
+    keep = info && need <= (fr + have) / 2;
+    pipe = info && nchk > 1 && 2 * need + extra <= (fr + have) / 2;
   } else {
     keep = need <= allow;
+    pipe = nchk > 1 && 2 * need + extra <= allow;
   }
   if (n > 1 && !keep) {
     // one after the other, each with its own allowance
@@ -979,7 +989,9 @@ int adjoint_reverse_group(const std::vector<wedg_ws *> &G, const double *const *
   }
   int rc;
   StreamGuard guard(G);
-  cudaStream_t st = G[0]->stream;
+  cudaStream_t st = G[0]->stream;               // the reverse sweep
+  cudaStream_t sr = st;                         // the recompute (its own stream when pipelined)
+  const int nset = pipe ? 2 : 1;
   const cudaMemcpyKind in = where == WEDG_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   std::vector<size_t> nU(n), nV(n), nn(n);
   for (int i = 0; i < n; ++i) {
@@ -994,11 +1006,11 @@ int adjoint_reverse_group(const std::vector<wedg_ws *> &G, const double *const *
     if (keep) {
       const size_t E = ws->E;
       const size_t nd = (size_t)ws->nu * ws->nu + ws->nv * ws->nv + 12 * ws->nq + ws->qh * ws->qh + 2;
-      while ((int64_t)ws->rk_keep.size() < 4 * seg) {
+      while ((int64_t)ws->rk_keep.size() < nset * 4 * seg) {
         wedg_ws::StageData d;
         double *bd;
         int *ib;
-        if ((rc = dalloc(ws, &bd, nd * E)) || (rc = dalloc(ws, &ib, E * (1 + NBIN) + 2 * NBIN))) return rc;
+        if ((rc = dalloc(ws, &bd, nd * E)) || (rc = dalloc(ws, &ib, E * (1 + NBIN) + 2 * NBIN + 4))) return rc;
         d.k = bd;
         d.tr = d.k + nn[i];
         d.G = d.tr + 12 * (size_t)ws->nq * E;
@@ -1007,18 +1019,51 @@ int adjoint_reverse_group(const std::vector<wedg_ws *> &G, const double *const *
         d.nst = ib;
         d.bins = ib + E;
         d.bin_count = ib + E * (1 + NBIN);
+        d.nmax = d.bin_count + 2 * NBIN;
         ws->rk_keep.push_back(d);
       }
+      while (ws->rk_seg_n < nset * 4 * seg) {
+        double *p;
+        if ((rc = dalloc(ws, &p, nn[i]))) return rc;
+        ws->rk_seg.push_back(p);
+        ++ws->rk_seg_n;
+      }
+      if (pipe && !ws->rk_ry && ((rc = dalloc(ws, &ws->rk_ry, nn[i])) || (rc = dalloc(ws, &ws->rk_racc, nn[i]))))
+        return rc;
     }
   }
-  // out_i = a x_i + b y_i (+ z_i) for the group; xs etc. give the instance's buffers
-  auto lin = [&](auto out, double a, auto x, double b, auto y, auto z) -> int {
+  // streams and events of the pipeline (destroyed on every return path)
+  struct PipeRes {
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    ~PipeRes() {
+      if (s) {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+      }
+      for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
+    }
+  } pr;
+  cudaEvent_t *ev_rec = pr.ev, *ev_adj = pr.ev + 2, &ev_start = pr.ev[4];
+  if (pipe) {
+    CK(G[0], cudaStreamCreateWithFlags(&pr.s, cudaStreamNonBlocking));
+    for (cudaEvent_t &e : pr.ev) CK(G[0], cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    sr = pr.s;
+    CK(G[0], cudaEventRecord(ev_start, st));    // the recompute starts after this call's set-up
+    CK(G[0], cudaStreamWaitEvent(sr, ev_start, 0));
+  }
+  auto on = [&](cudaStream_t x) {
+    for (wedg_ws *ws : G) ws->stream = x;
+  };
+  // out_i = a x_i + b y_i (+ z_i) for the group on stream x; out etc. give the instance's buffers
+  auto lin_on = [&](cudaStream_t x, auto out, double a, auto xs, double b, auto y, auto z) -> int {
     std::vector<LinPtrs> p(n);
     for (int i = 0; i < n; ++i) {
-      p[i] = LinPtrs{nn[i], out(i), x(i), y(i), z(i)};
+      p[i] = LinPtrs{nn[i], out(i), xs(i), y(i), z(i)};
       G[i]->stats.kernel_launches += 1;
     }
-    const cudaError_t e = multi_lincomb(p, a, b, st);
+    const cudaError_t e = multi_lincomb(p, a, b, x);
     return e == cudaSuccess ? WEDG_OK : cuda_fail(G[0], e, "k_lincomb_m");
   };
   auto none = [](int) -> const double * { return nullptr; };
@@ -1029,70 +1074,83 @@ int adjoint_reverse_group(const std::vector<wedg_ws *> &G, const double *const *
   std::vector<Fields> F(n);
   std::vector<const double *> lu(n), lv(n);
   std::vector<double *> ggu(n), ggv(n), gpar(n);
-  // ---- reverse pass, segment by segment
-  for (int64_t c = nchk - 1; c >= 0; --c) {
+  // ---- the forward data of segment c into set `set` (stream sr): every stage's RHS evaluated
+  //      with its outputs and data kept, and the RK4 combinations: Y1 = y, Y_{s+1} = y + c_s K_s,
+  //      y ← y + dt/6 (K1 + 2K2 + 2K3 + K4)
+  auto recompute = [&](int64_t c, int set) -> int {
     const int64_t k0 = c * every, k1 = std::min(nsteps, k0 + every);
+    const size_t base = (size_t)set * 4 * seg;
+    on(sr);
+    auto y = [&](int i) { return pipe ? G[i]->rk_ry : G[i]->rk_y; };
+    auto yc = [&](int i) -> const double * { return pipe ? G[i]->rk_ry : G[i]->rk_y; };
+    auto acc = [&](int i) { return pipe ? G[i]->rk_racc : G[i]->rk_acc; };
+    auto accc = [&](int i) -> const double * { return pipe ? G[i]->rk_racc : G[i]->rk_acc; };
     for (int i = 0; i < n; ++i)
-      CK(G[i], cudaMemcpyAsync(G[i]->rk_y, G[i]->rk_chk[c], sizeof(double) * nn[i], cudaMemcpyDeviceToDevice, st));
+      CK(G[i], cudaMemcpyAsync(y(i), G[i]->rk_chk[c], sizeof(double) * nn[i], cudaMemcpyDeviceToDevice, sr));
     for (int64_t k = k0; k < k1; ++k) {
-      if (keep) {
-        // the step as four RHS evaluations (their outputs and data kept) and the RK4 combinations:
-        // Y1 = y, Y_{s+1} = y + c_s K_s, y ← y + dt/6 (K1 + 2K2 + 2K3 + K4)
-        const size_t q = 4 * (k - k0);
-        for (int i = 0; i < n; ++i)
-          CK(G[i], cudaMemcpyAsync(G[i]->rk_seg[q], G[i]->rk_y, sizeof(double) * nn[i], cudaMemcpyDeviceToDevice, st));
-        for (int s = 0; s < 4; ++s) {
-          for (int i = 0; i < n; ++i) {
-            wedg_ws *ws = G[i];
-            const std::vector<double> &t = ws->rk_t;
-            const double ts[4] = {t[k], t[k] + 0.5 * dt, t[k] + 0.5 * dt, t[k] + dt};
-            wedg_ws::StageData &d = ws->rk_keep[q + s];
-            const double *Y = ws->rk_seg[q + s];
-            S[i] = StageIO{};
-            S[i].xu = Y; S[i].xv = Y + nU[i];
-            stage_factors(ws, ts[s], S[i]);
-            S[i].mode = OUT_RHS;
-            S[i].ut = d.k;
-            S[i].vt = d.k + nU[i];
-            CK(ws, cudaMemsetAsync(d.bin_count, 0, 2 * NBIN * sizeof(int), st));
-            d.parity = ws->parity;
-            F[i] = kept_fields(ws, d);
-          }
-          if ((rc = group_stage(G, S, F))) return rc;
-          if (s < 3 &&
-              (rc = lin([&](int i) { return G[i]->rk_seg[q + s + 1]; }, cs[s],
-                        [&](int i) -> const double * { return G[i]->rk_keep[q + s].k; }, 1.0,
-                        [&](int i) -> const double * { return G[i]->rk_y; }, none)))
-            return rc;
-        }
-        auto K = [&](int s) { return [&, s](int i) -> const double * { return G[i]->rk_keep[q + s].k; }; };
-        auto acc = [&](int i) { return G[i]->rk_acc; };
-        auto accc = [&](int i) -> const double * { return G[i]->rk_acc; };
-        auto y = [&](int i) { return G[i]->rk_y; };
-        auto yc = [&](int i) -> const double * { return G[i]->rk_y; };
-        if ((rc = lin(acc, 2.0, K(1), 1.0, K(0), none)) || (rc = lin(acc, 2.0, K(2), 1.0, K(3), accc)) ||
-            (rc = lin(y, dt / 6.0, accc, 1.0, yc, none)))
-          return rc;
-        continue;
-      }
-      // one workspace without the memory to keep stage data: the stage states Y1..Y4 only
-      wedg_ws *ws = G[0];
-      double *su[4], *sv[4];
+      const size_t q = base + 4 * (k - k0);
+      for (int i = 0; i < n; ++i)
+        CK(G[i], cudaMemcpyAsync(G[i]->rk_seg[q], y(i), sizeof(double) * nn[i], cudaMemcpyDeviceToDevice, sr));
       for (int s = 0; s < 4; ++s) {
-        su[s] = ws->rk_seg[4 * (k - k0) + s];
-        sv[s] = su[s] + nU[0];
+        for (int i = 0; i < n; ++i) {
+          wedg_ws *ws = G[i];
+          const std::vector<double> &t = ws->rk_t;
+          const double ts[4] = {t[k], t[k] + 0.5 * dt, t[k] + 0.5 * dt, t[k] + dt};
+          wedg_ws::StageData &d = ws->rk_keep[q + s];
+          const double *Y = ws->rk_seg[q + s];
+          S[i] = StageIO{};
+          S[i].xu = Y; S[i].xv = Y + nU[i];
+          stage_factors(ws, ts[s], S[i]);
+          S[i].mode = OUT_RHS;
+          S[i].ut = d.k;
+          S[i].vt = d.k + nU[i];
+          CK(ws, cudaMemsetAsync(d.bin_count, 0, (2 * NBIN + 3) * sizeof(int), sr));   // and d.nmax
+          d.parity = ws->parity;
+          F[i] = kept_fields(ws, d);
+        }
+        int r;
+        if ((r = group_stage(G, S, F))) return r;
+        if (s < 3 && (r = lin_on(sr, [&](int i) { return G[i]->rk_seg[q + s + 1]; }, cs[s],
+                                 [&](int i) -> const double * { return G[i]->rk_keep[q + s].k; }, 1.0, yc, none)))
+          return r;
       }
-      if ((rc = enqueue_rk4(ws, ws->rk_y, ws->rk_y + nU[0], ws->rk_t[k], dt, 1, nullptr, 0, su, sv))) return rc;
+      auto K = [&](int s) { return [&, s](int i) -> const double * { return G[i]->rk_keep[q + s].k; }; };
+      int r;
+      if ((r = lin_on(sr, acc, 2.0, K(1), 1.0, K(0), none)) || (r = lin_on(sr, acc, 2.0, K(2), 1.0, K(3), accc)) ||
+          (r = lin_on(sr, y, dt / 6.0, accc, 1.0, yc, none)))
+        return r;
+    }
+    return WEDG_OK;
+  };
+  // ---- the reverse steps of segment c from the data of set `set` (or, for one workspace without
+  //      room to keep data, the stage states of a recompute and each stage's forward RHS evaluated
+  //      again), on stream st
+  auto reverse = [&](int64_t c, int set) -> int {
+    const int64_t k0 = c * every, k1 = std::min(nsteps, k0 + every);
+    const size_t base = (size_t)set * 4 * seg;
+    int r;
+    on(st);
+    if (!keep) {
+      wedg_ws *ws = G[0];
+      CK(ws, cudaMemcpyAsync(ws->rk_y, ws->rk_chk[c], sizeof(double) * nn[0], cudaMemcpyDeviceToDevice, st));
+      for (int64_t k = k0; k < k1; ++k) {
+        double *su[4], *sv[4];
+        for (int s = 0; s < 4; ++s) {
+          su[s] = ws->rk_seg[4 * (k - k0) + s];
+          sv[s] = su[s] + nU[0];
+        }
+        if ((r = enqueue_rk4(ws, ws->rk_y, ws->rk_y + nU[0], ws->rk_t[k], dt, 1, nullptr, 0, su, sv))) return r;
+      }
     }
     for (int64_t k = k1 - 1; k >= k0; --k) {
       // K̄_s = ca[s] λ + cb[s] Ȳ_{s+1}, Ȳ = Jᵀ K̄ at the stage state: y_{n+1} = y + dt/6 (K1 + 2K2 +
       // 2K3 + K4), Y2 = y + dt/2 K1, Y3 = y + dt/2 K2, Y4 = y + dt K3
-      const size_t q = 4 * (k - k0);
+      const size_t q = base + 4 * (k - k0);
       for (int s = 3; s >= 0; --s) {
-        if ((rc = lin([&](int i) { return G[i]->rk_kbar; }, ca[s],
-                      [&](int i) -> const double * { return G[i]->rk_lam; }, cb[s],
-                      [&](int i) -> const double * { return s == 3 ? nullptr : G[i]->rk_g; }, none)))
-          return rc;
+        if ((r = lin_on(st, [&](int i) { return G[i]->rk_kbar; }, ca[s],
+                        [&](int i) -> const double * { return G[i]->rk_lam; }, cb[s],
+                        [&](int i) -> const double * { return s == 3 ? nullptr : G[i]->rk_g; }, none)))
+          return r;
         for (int i = 0; i < n; ++i) {
           wedg_ws *ws = G[i];
           lu[i] = ws->rk_kbar;
@@ -1116,23 +1174,48 @@ int adjoint_reverse_group(const std::vector<wedg_ws *> &G, const double *const *
             S[i].vt = d.k + nU[i];
             F[i] = kept_fields(ws, d);
           }
-          rc = group_adjoint_core(G, F, S, lu, lv, ggu, ggv, gpar);
+          r = group_adjoint_core(G, F, S, lu, lv, ggu, ggv, gpar);
         } else {
           wedg_ws *ws = G[0];
           const std::vector<double> &t = ws->rk_t;
           const double ts[4] = {t[k], t[k] + 0.5 * dt, t[k] + 0.5 * dt, t[k] + dt};
-          const double *Y = ws->rk_seg[q + s];
-          rc = enqueue_rhs_adjoint(ws, Y, Y + nU[0], ts[s], lu[0], lv[0], ggu[0], ggv[0], gpar[0]);
+          const double *Y = ws->rk_seg[4 * (k - k0) + s];
+          r = enqueue_rhs_adjoint(ws, Y, Y + nU[0], ts[s], lu[0], lv[0], ggu[0], ggv[0], gpar[0]);
         }
-        if (rc) return rc;
-        if ((rc = lin([&](int i) { return G[i]->rk_acc; }, 1.0,
-                      [&](int i) -> const double * { return s == 3 ? G[i]->rk_lam : G[i]->rk_acc; }, 1.0,
-                      [&](int i) -> const double * { return G[i]->rk_g; }, none)))
-          return rc;
+        if (r) return r;
+        if ((r = lin_on(st, [&](int i) { return G[i]->rk_acc; }, 1.0,
+                        [&](int i) -> const double * { return s == 3 ? G[i]->rk_lam : G[i]->rk_acc; }, 1.0,
+                        [&](int i) -> const double * { return G[i]->rk_g; }, none)))
+          return r;
       }
       for (wedg_ws *ws : G) std::swap(ws->rk_lam, ws->rk_acc);
     }
+    return WEDG_OK;
+  };
+  // ---- reverse pass, segment by segment
+  if (pipe) {
+    // set c % 2 holds segment c; the recompute of c - 1 into the other set waits for the reverse
+    // of c + 1 (which read it), the reverse of c for the recompute of c
+    if ((rc = recompute(nchk - 1, (int)((nchk - 1) % 2)))) return rc;
+    CK(G[0], cudaEventRecord(ev_rec[(nchk - 1) % 2], sr));
+    for (int64_t c = nchk - 1; c >= 0; --c) {
+      const int set = (int)(c % 2);
+      if (c >= 1) {
+        CK(G[0], cudaStreamWaitEvent(sr, ev_adj[1 - set], 0));
+        if ((rc = recompute(c - 1, 1 - set))) return rc;
+        CK(G[0], cudaEventRecord(ev_rec[1 - set], sr));
+      }
+      CK(G[0], cudaStreamWaitEvent(st, ev_rec[set], 0));
+      if ((rc = reverse(c, set))) return rc;
+      CK(G[0], cudaEventRecord(ev_adj[set], st));
+    }
+  } else {
+    for (int64_t c = nchk - 1; c >= 0; --c) {
+      if (keep && (rc = recompute(c, 0))) return rc;
+      if ((rc = reverse(c, 0))) return rc;
+    }
   }
+  on(st);
   CK(G[0], cudaGetLastError());
   int first = WEDG_OK;
   const cudaMemcpyKind out = where == WEDG_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
@@ -1359,12 +1442,10 @@ int upload_final_args(wedg_batch *b, double *const *u, double *const *v, const d
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
-  if (!out) return WEDG_ERR_ARGUMENT;
-  *out = nullptr;
-  if (!cfg || !pre) return WEDG_ERR_ARGUMENT;
+// The checks of wedg_create on the configuration (and that a GPU is usable)
+int validate_config(const wedg_config *cfg) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return WEDG_ERR_NO_DEVICE;
   const int N = cfg->N, nu = cfg->qu1, nv = cfg->qv1;
@@ -1374,140 +1455,81 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
   for (int s = 0; s < 4; ++s)
     if (cfg->kind[s] < 0 || cfg->kind[s] > 3) return WEDG_ERR_ARGUMENT;
   if (cfg->mass_solver != WEDG_CHEBYSHEV && cfg->mass_solver != WEDG_CG) return WEDG_ERR_ARGUMENT;
-  const double *need[] = {pre->w, pre->P_u, pre->S_u, pre->Ebl_u, pre->Ebr_u, pre->E1bl_u, pre->E1br_u,
-                          pre->P_h_v, pre->W2d_h, pre->Cw, pre->Aw, pre->hc2, pre->haf, pre->hcf, pre->hbf,
-                          pre->vc2, pre->vaf, pre->vcf, pre->vbf, pre->hc2m, pre->hafm, pre->vc2m, pre->vafm,
-                          pre->hJC, pre->vJC, pre->bcB_sp, pre->bcB_spy, pre->bcT_sp, pre->bcT_spy, pre->bcL_sp,
-                          pre->bcL_spx, pre->bcR_sp, pre->bcR_spx, pre->PiSP, pre->PiBSP2, pre->PiCdiv,
-                          pre->PiDdiv, pre->src_projE, pre->beta_hq};
-  for (const double *p : need)
-    if (!p) return WEDG_ERR_ARGUMENT;
+  return WEDG_OK;
+}
 
+// A new workspace with the configuration's sizes and its 1D operators (with their mirror parities
+// made exact); wedg_create and wedg_create_points then fill the device arrays
+int create_begin(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
   wedg_ws *ws = new wedg_ws();
   ws->cfg = *cfg;
-  ws->N = N;
-  ws->E = N * N;
-  ws->nu = nu;
-  ws->nv = nv;
-  ws->nq = nu;
+  ws->N = cfg->N;
+  ws->E = cfg->N * cfg->N;
+  ws->nu = cfg->qu1;
+  ws->nv = cfg->qv1;
+  ws->nq = cfg->qu1;
   ws->qh = cfg->q_high;
-  const int E = ws->E, nq = nu, qh = ws->qh;
-  const size_t Es = (size_t)E;
-
-  // ---- 1D operators (Julia column-major inputs), with their mirror parities made exact
-  BasisHost &bh = ws->bh;
-  if (build_basis(cfg, pre, bh)) {
+  ws->F.N = ws->N;
+  ws->F.E = ws->E;
+  if (build_basis(cfg, pre, ws->bh)) {
     delete ws;
     return WEDG_ERR_ARGUMENT;
   }
+  *out = ws;
+  return WEDG_OK;
+}
 
-  // ---- constant coefficients per element? Cw = c² W and Aw = α W to 1e-14 (relative)
-  std::vector<double> c2e(E), ae(E), ic2e(E);
-  bool fast = !cfg->general_only;
-  for (int e = 0; e < E && fast; ++e) {
-    const double w00 = bh.w[0] * bh.w[0];
-    const double c2 = pre->Cw[0 + nq * ((size_t)e + Es * 0)] / w00;
-    const double al = pre->Aw[0 + nq * ((size_t)e + Es * 0)] / w00;
-    for (int s = 0; s < nq && fast; ++s)
-      for (int r = 0; r < nq; ++r) {
-        const double W = bh.w[r] * bh.w[s];
-        const double cw = pre->Cw[r + nq * ((size_t)e + Es * s)], aw = pre->Aw[r + nq * ((size_t)e + Es * s)];
-        if (std::fabs(cw - c2 * W) > 1e-14 * std::fabs(cw) || std::fabs(aw - al * W) > 1e-14 * std::fabs(aw) ||
-            !(c2 > 0)) {
-          fast = false;
-          break;
-        }
-      }
-    c2e[e] = c2;
-    ae[e] = al;
-    ic2e[e] = 1.0 / c2;
-  }
+// The kernels of the workspace's degrees and coefficient family, and their 1D operators
+int create_launchers(wedg_ws *ws, bool fast) {
   ws->fast = fast;
-  ws->L = get_launchers(nu, nv, fast);
+  ws->L = get_launchers(ws->nu, ws->nv, fast);
   if (!ws->L.prep) {
-    delete ws;
+    wedg_destroy(ws);
     return WEDG_ERR_ARGUMENT;
   }
   ws->basis.resize(ws->L.basis_size);
-  ws->L.pack(bh, ws->basis.data());
+  ws->L.pack(ws->bh, ws->basis.data());
+  return WEDG_OK;
+}
 
-  int rc = WEDG_OK;
-#define UP(dst, vec)                     \
-  do {                                   \
-    rc = upload(ws, &(dst), vec);        \
-    if (rc) { wedg_destroy(ws); return rc; } \
-  } while (0)
-  Fields &F = ws->F;
-  F.N = N;
-  F.E = E;
-  // ---- element arrays, element index fastest
-  if (fast) {
-    UP(F.c2e, c2e);
-    UP(F.ae, ae);
-    UP(F.ic2e, ic2e);
-  } else {
-    std::vector<double> cw((size_t)nq * nq * E), aw((size_t)nq * nq * E);
-    for (int s = 0; s < nq; ++s)
-      for (int r = 0; r < nq; ++r)
-        for (int e = 0; e < E; ++e) {
-          cw[(r + nq * s) * Es + e] = pre->Cw[r + nq * ((size_t)e + Es * s)];
-          aw[(r + nq * s) * Es + e] = pre->Aw[r + nq * ((size_t)e + Es * s)];
-        }
-    UP(F.Cw, cw);
-    UP(F.Aw, aw);
-    const size_t nt = (size_t)nu * nu * (nu * nu + 1) / 2;
-    if (pre->Ainv_u) {
-      std::vector<double> ai(nt * E);
-      for (int e = 0; e < E; ++e)
-        for (size_t row = 0; row < nt; ++row) ai[row * Es + e] = pre->Ainv_u[row + nt * e];
-      UP(F.Ainv, ai);
-    } else {
-      // the packed inverses of src/solver.jl:528-535, computed on the device from Cw
-      const double *Pu = nullptr, *Su = nullptr;
-      UP(Pu, std::vector<double>(pre->P_u, pre->P_u + (size_t)nq * nu));
-      UP(Su, std::vector<double>(pre->S_u, pre->S_u + (size_t)nq * nu));
-      double *ainv = nullptr;
-      unsigned int *bad = nullptr;
-      if ((rc = dalloc(ws, &ainv, nt * E)) || (rc = dalloc(ws, &bad, 1))) {
-        wedg_destroy(ws);
-        return rc;
-      }
-      const size_t sm = ainv_smem(nu);
-      unsigned int nbad = 0;
-      cudaError_t ce = cudaMemset(bad, 0, sizeof(unsigned int));
-      if (ce == cudaSuccess) ce = cudaFuncSetAttribute(k_ainv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      if (ce == cudaSuccess) {
-        k_ainv<<<E, 128, sm>>>(F.Cw, E, nu, Pu, Su, ainv, bad);
-        ce = cudaGetLastError();
-      }
-      if (ce == cudaSuccess) ce = cudaMemcpy(&nbad, bad, sizeof nbad, cudaMemcpyDeviceToHost);
-      if (ce != cudaSuccess || nbad) {
-        wedg_destroy(ws);
-        return ce != cudaSuccess ? WEDG_ERR_CUDA : WEDG_ERR_ARGUMENT;
-      }
-      F.Ainv = ainv;
-    }
+// The packed inverses of src/solver.jl:528-535 on the device from F.Cw (k_ainv); a stiffness that
+// is not positive definite fails the creation (the workspace is destroyed)
+int device_inverses(wedg_ws *ws, const wedg_pre *pre) {
+  const int nu = ws->nu, nq = ws->nq, E = ws->E;
+  const size_t nt = (size_t)nu * nu * (nu * nu + 1) / 2;
+  const double *Pu = nullptr, *Su = nullptr;
+  int rc;
+  if ((rc = upload(ws, &Pu, std::vector<double>(pre->P_u, pre->P_u + (size_t)nq * nu))) ||
+      (rc = upload(ws, &Su, std::vector<double>(pre->S_u, pre->S_u + (size_t)nq * nu)))) {
+    wedg_destroy(ws);
+    return rc;
   }
-  // ---- face arrays: (nq, N+1, N) -> [jf + (N+1)(k + N i)], (nq, N, N+1) -> [j + N (kf + (N+1) i)]
-  auto hf = [&](const double *a) {
-    std::vector<double> o((size_t)nq * (N + 1) * N);
-    for (int k = 0; k < N; ++k)
-      for (int jf = 0; jf <= N; ++jf)
-        for (int i = 0; i < nq; ++i) o[jf + (size_t)(N + 1) * (k + (size_t)N * i)] = a[i + nq * (jf + (size_t)(N + 1) * k)];
-    return o;
-  };
-  auto vf = [&](const double *a) {
-    std::vector<double> o((size_t)nq * N * (N + 1));
-    for (int kf = 0; kf <= N; ++kf)
-      for (int j = 0; j < N; ++j)
-        for (int i = 0; i < nq; ++i) o[j + (size_t)N * (kf + (size_t)(N + 1) * i)] = a[i + nq * (j + (size_t)N * kf)];
-    return o;
-  };
-  UP(F.hc2, hf(pre->hc2)); UP(F.haf, hf(pre->haf)); UP(F.hcf, hf(pre->hcf)); UP(F.hbf, hf(pre->hbf));
-  UP(F.hc2m, hf(pre->hc2m)); UP(F.hafm, hf(pre->hafm)); UP(F.hJC, hf(pre->hJC));
-  UP(F.vc2, vf(pre->vc2)); UP(F.vaf, vf(pre->vaf)); UP(F.vcf, vf(pre->vcf)); UP(F.vbf, vf(pre->vbf));
-  UP(F.vc2m, vf(pre->vc2m)); UP(F.vafm, vf(pre->vafm)); UP(F.vJC, vf(pre->vJC));
-  // boundary data (nq, N) -> [m + N i]
+  double *ainv = nullptr;
+  unsigned int *bad = nullptr;
+  if ((rc = dalloc(ws, &ainv, nt * E)) || (rc = dalloc(ws, &bad, 1))) {
+    wedg_destroy(ws);
+    return rc;
+  }
+  const size_t sm = ainv_smem(nu);
+  unsigned int nbad = 0;
+  cudaError_t ce = cudaMemset(bad, 0, sizeof(unsigned int));
+  if (ce == cudaSuccess) ce = cudaFuncSetAttribute(k_ainv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (ce == cudaSuccess) {
+    k_ainv<<<E, 128, sm>>>(ws->F.Cw, E, nu, Pu, Su, ainv, bad);
+    ce = cudaGetLastError();
+  }
+  if (ce == cudaSuccess) ce = cudaMemcpy(&nbad, bad, sizeof nbad, cudaMemcpyDeviceToHost);
+  if (ce != cudaSuccess || nbad) {
+    wedg_destroy(ws);
+    return ce != cudaSuccess ? WEDG_ERR_CUDA : WEDG_ERR_ARGUMENT;
+  }
+  ws->F.Ainv = ainv;
+  return WEDG_OK;
+}
+
+// pre's boundary data (nq, N) -> [m + N i]
+int upload_boundary(wedg_ws *ws, const wedg_pre *pre) {
+  const int N = ws->N, nq = ws->nq;
   auto bd = [&](const double *a) {
     std::vector<double> o((size_t)nq * N);
     for (int m = 0; m < N; ++m)
@@ -1517,35 +1539,26 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
   const double *sp[4] = {pre->bcB_sp, pre->bcT_sp, pre->bcL_sp, pre->bcR_sp};
   const double *spn[4] = {pre->bcB_spy, pre->bcT_spy, pre->bcL_spx, pre->bcR_spx};
   for (int s = 0; s < 4; ++s) {
-    UP(F.bsp[s], bd(sp[s]));
-    UP(F.bspn[s], bd(spn[s]));
+    int rc;
+    if ((rc = upload(ws, &ws->F.bsp[s], bd(sp[s]))) || (rc = upload(ws, &ws->F.bspn[s], bd(spn[s])))) {
+      wedg_destroy(ws);
+      return rc;
+    }
   }
-  // projections (nv, nv, N, N) -> [(a + nv b) E + e]
-  auto pj = [&](const double *a) {
-    std::vector<double> o((size_t)nv * nv * E);
-    for (int e = 0; e < E; ++e)
-      for (int l = 0; l < nv * nv; ++l) o[l * Es + e] = a[l + (size_t)nv * nv * e];
-    return o;
-  };
-  if (cfg->mms_on) {
-    UP(F.PiSP, pj(pre->PiSP)); UP(F.PiBSP2, pj(pre->PiBSP2)); UP(F.PiDdiv, pj(pre->PiDdiv));
-  }
-  if (!cfg->src_on) UP(F.PiCdiv, pj(pre->PiCdiv));
-  if (cfg->src_on) UP(F.srcP, pj(pre->src_projE));
-  // β at the high-order points (qh, E, qh) -> [(r + qh s) E + e]
-  {
-    std::vector<double> o((size_t)qh * qh * E);
-    for (int s = 0; s < qh; ++s)
-      for (int e = 0; e < E; ++e)
-        for (int r = 0; r < qh; ++r) o[(r + qh * s) * Es + e] = 2.0 * pre->beta_hq[r + qh * ((size_t)e + Es * s)];
-    UP(F.beta2, o);
-  }
-#undef UP
-  // ---- scratch
+  return WEDG_OK;
+}
+
+// The scratch of the workspace, the kernels' scalars and its stream (the last part of wedg_create)
+int create_finish(wedg_ws *ws) {
+  const wedg_config *cfg = &ws->cfg;
+  const int N = ws->N, E = ws->E, nu = ws->nu, nv = ws->nv, nq = ws->nq, qh = ws->qh;
+  const size_t Es = (size_t)E;
+  Fields &F = ws->F;
+  int rc;
   const size_t nU = (size_t)nu * nu * E, nV = (size_t)nv * nv * E;
   if ((rc = dalloc(ws, &F.tr, (size_t)12 * nq * E)) || (rc = dalloc(ws, &F.G, (size_t)qh * qh * E)) ||
       (rc = dalloc(ws, &F.th, Es)) || (rc = dalloc(ws, &F.de, Es)) || (rc = dalloc(ws, &F.nst, Es)) ||
-      (rc = dalloc(ws, &F.nmax, 1)) || (rc = dalloc(ws, &F.nsum, 1)) || (rc = dalloc(ws, &F.err, 1)) ||
+      (rc = dalloc(ws, &F.nmax, 3)) || (rc = dalloc(ws, &F.nsum, 1)) || (rc = dalloc(ws, &F.err, 1)) ||
       (rc = dalloc(ws, &F.cg_nfail, 1)) ||
       (rc = dalloc(ws, &F.nonfinite, 1)) || (rc = dalloc(ws, &ws->steps_done, 1)) ||
       (rc = dalloc(ws, &ws->d_u, nU)) || (rc = dalloc(ws, &ws->d_v, nV)) || (rc = dalloc(ws, &ws->d_ut, nU)) ||
@@ -1562,7 +1575,6 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
   F.four_hh = 4.0 / (h * h);
   F.mass_tol = cfg->mass_tol;
   F.Lcheb = std::acosh(1.0 / cfg->mass_tol);
-  F.one_sided = cfg->one_sided ? 1 : 0;
   F.mms_on = cfg->mms_on ? 1 : 0;
   F.src_on = cfg->src_on ? 1 : 0;
   F.cg = cfg->mass_solver == WEDG_CG;
@@ -1588,10 +1600,365 @@ int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
     return r;
   }
   ws->stream = ws->own_stream;
-  ws->stats.fast_path = fast ? 1 : 0;
+  ws->stats.fast_path = ws->fast ? 1 : 0;
   ws->stats.device_bytes = (int64_t)ws->bytes;
   cudaDeviceSynchronize();
+  return WEDG_OK;
+}
+
+}  // namespace
+
+
+extern "C" {
+
+int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out) {
+  if (!out) return WEDG_ERR_ARGUMENT;
+  *out = nullptr;
+  if (!cfg || !pre) return WEDG_ERR_ARGUMENT;
+  int rc = validate_config(cfg);
+  if (rc) return rc;
+  const double *need[] = {pre->w, pre->P_u, pre->S_u, pre->Ebl_u, pre->Ebr_u, pre->E1bl_u, pre->E1br_u,
+                          pre->P_h_v, pre->W2d_h, pre->Cw, pre->Aw, pre->hc2, pre->haf, pre->hcf, pre->hbf,
+                          pre->vc2, pre->vaf, pre->vcf, pre->vbf, pre->hc2m, pre->hafm, pre->vc2m, pre->vafm,
+                          pre->hJC, pre->vJC, pre->bcB_sp, pre->bcB_spy, pre->bcT_sp, pre->bcT_spy, pre->bcL_sp,
+                          pre->bcL_spx, pre->bcR_sp, pre->bcR_spx, pre->PiSP, pre->PiBSP2, pre->PiCdiv,
+                          pre->PiDdiv, pre->src_projE, pre->beta_hq};
+  for (const double *p : need)
+    if (!p) return WEDG_ERR_ARGUMENT;
+  wedg_ws *ws = nullptr;
+  if ((rc = create_begin(cfg, pre, &ws))) return rc;
+  const int N = ws->N, E = ws->E, nu = ws->nu, nv = ws->nv, nq = ws->nq, qh = ws->qh;
+  const size_t Es = (size_t)E;
+  BasisHost &bh = ws->bh;
+
+  // ---- constant coefficients per element? Cw = c² W and Aw = α W to 1e-14 (relative)
+  std::vector<double> c2e(E), ae(E), ic2e(E);
+  bool fast = !cfg->general_only;
+  for (int e = 0; e < E && fast; ++e) {
+    const double w00 = bh.w[0] * bh.w[0];
+    const double c2 = pre->Cw[0 + nq * ((size_t)e + Es * 0)] / w00;
+    const double al = pre->Aw[0 + nq * ((size_t)e + Es * 0)] / w00;
+    for (int s = 0; s < nq && fast; ++s)
+      for (int r = 0; r < nq; ++r) {
+        const double W = bh.w[r] * bh.w[s];
+        const double cw = pre->Cw[r + nq * ((size_t)e + Es * s)], aw = pre->Aw[r + nq * ((size_t)e + Es * s)];
+        if (std::fabs(cw - c2 * W) > 1e-14 * std::fabs(cw) || std::fabs(aw - al * W) > 1e-14 * std::fabs(aw) ||
+            !(c2 > 0)) {
+          fast = false;
+          break;
+        }
+      }
+    c2e[e] = c2;
+    ae[e] = al;
+    ic2e[e] = 1.0 / c2;
+  }
+  if ((rc = create_launchers(ws, fast))) return rc;
+
+#define UP(dst, vec)                     \
+  do {                                   \
+    rc = upload(ws, &(dst), vec);        \
+    if (rc) { wedg_destroy(ws); return rc; } \
+  } while (0)
+  Fields &F = ws->F;
+  // ---- element arrays, element index fastest
+  if (fast) {
+    UP(F.c2e, c2e);
+    UP(F.ae, ae);
+    UP(F.ic2e, ic2e);
+  } else {
+    std::vector<double> cw((size_t)nq * nq * E), aw((size_t)nq * nq * E);
+    for (int s = 0; s < nq; ++s)
+      for (int r = 0; r < nq; ++r)
+        for (int e = 0; e < E; ++e) {
+          cw[(r + nq * s) * Es + e] = pre->Cw[r + nq * ((size_t)e + Es * s)];
+          aw[(r + nq * s) * Es + e] = pre->Aw[r + nq * ((size_t)e + Es * s)];
+        }
+    UP(F.Cw, cw);
+    UP(F.Aw, aw);
+    const size_t nt = (size_t)nu * nu * (nu * nu + 1) / 2;
+    if (pre->Ainv_u) {
+      std::vector<double> ai(nt * E);
+      for (int e = 0; e < E; ++e)
+        for (size_t row = 0; row < nt; ++row) ai[row * Es + e] = pre->Ainv_u[row + nt * e];
+      UP(F.Ainv, ai);
+    } else if ((rc = device_inverses(ws, pre))) {
+      return rc;
+    }
+  }
+  // ---- face arrays: (nq, N+1, N) -> [jf + (N+1)(k + N i)], (nq, N, N+1) -> [j + N (kf + (N+1) i)]
+  auto hf = [&](const double *a) {
+    std::vector<double> o((size_t)nq * (N + 1) * N);
+    for (int k = 0; k < N; ++k)
+      for (int jf = 0; jf <= N; ++jf)
+        for (int i = 0; i < nq; ++i) o[jf + (size_t)(N + 1) * (k + (size_t)N * i)] = a[i + nq * (jf + (size_t)(N + 1) * k)];
+    return o;
+  };
+  auto vf = [&](const double *a) {
+    std::vector<double> o((size_t)nq * N * (N + 1));
+    for (int kf = 0; kf <= N; ++kf)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < nq; ++i) o[j + (size_t)N * (kf + (size_t)(N + 1) * i)] = a[i + nq * (j + (size_t)N * kf)];
+    return o;
+  };
+  UP(F.hc2, hf(pre->hc2)); UP(F.haf, hf(pre->haf)); UP(F.hcf, hf(pre->hcf)); UP(F.hbf, hf(pre->hbf));
+  UP(F.hc2m, hf(pre->hc2m)); UP(F.hafm, hf(pre->hafm)); UP(F.hJC, hf(pre->hJC));
+  UP(F.vc2, vf(pre->vc2)); UP(F.vaf, vf(pre->vaf)); UP(F.vcf, vf(pre->vcf)); UP(F.vbf, vf(pre->vbf));
+  UP(F.vc2m, vf(pre->vc2m)); UP(F.vafm, vf(pre->vafm)); UP(F.vJC, vf(pre->vJC));
+  if ((rc = upload_boundary(ws, pre))) return rc;
+  // projections (nv, nv, N, N) -> [(a + nv b) E + e]
+  auto pj = [&](const double *a) {
+    std::vector<double> o((size_t)nv * nv * E);
+    for (int e = 0; e < E; ++e)
+      for (int l = 0; l < nv * nv; ++l) o[l * Es + e] = a[l + (size_t)nv * nv * e];
+    return o;
+  };
+  if (cfg->mms_on) {
+    UP(F.PiSP, pj(pre->PiSP)); UP(F.PiBSP2, pj(pre->PiBSP2)); UP(F.PiDdiv, pj(pre->PiDdiv));
+  }
+  if (!cfg->src_on) UP(F.PiCdiv, pj(pre->PiCdiv));
+  if (cfg->src_on) UP(F.srcP, pj(pre->src_projE));
+  // β at the high-order points (qh, E, qh) -> [(r + qh s) E + e]
+  {
+    std::vector<double> o((size_t)qh * qh * E);
+    for (int s = 0; s < qh; ++s)
+      for (int e = 0; e < E; ++e)
+        for (int r = 0; r < qh; ++r) o[(r + qh * s) * Es + e] = 2.0 * pre->beta_hq[r + qh * ((size_t)e + Es * s)];
+    UP(F.beta2, o);
+  }
+#undef UP
+  F.one_sided = cfg->one_sided ? 1 : 0;
+  if ((rc = create_finish(ws))) return rc;
   *out = ws;
+  return WEDG_OK;
+}
+
+int wedg_create_points(const wedg_config *cfg, const wedg_pre *pre, const wedg_points *pts, char *msg, size_t msg_len,
+                       wedg_ws **out) {
+  if (msg && msg_len) msg[0] = 0;
+  if (!out) return WEDG_ERR_ARGUMENT;
+  *out = nullptr;
+  auto refuse = [&](int status, const char *why) {
+    if (msg && msg_len) snprintf(msg, msg_len, "%s", why);
+    return status;
+  };
+  if (!cfg || !pre || !pts) return refuse(WEDG_ERR_ARGUMENT, "null argument");
+  int rc = validate_config(cfg);
+  if (rc) return refuse(rc, rc == WEDG_ERR_NO_DEVICE ? "no usable CUDA device" : "invalid configuration");
+  const double *need[] = {pre->w, pre->P_u, pre->S_u, pre->Ebl_u, pre->Ebr_u, pre->E1bl_u, pre->E1br_u,
+                          pre->P_h_v, pre->W2d_h, pre->bcB_sp, pre->bcB_spy, pre->bcT_sp, pre->bcT_spy,
+                          pre->bcL_sp, pre->bcL_spx, pre->bcR_sp, pre->bcR_spx};
+  for (const double *p : need)
+    if (!p) return refuse(WEDG_ERR_ARGUMENT, "null 1D operator or boundary data");
+  const wedg_face_values *fam[6] = {&pts->hc, &pts->ha, &pts->hb, &pts->vc, &pts->va, &pts->vb};
+  for (const wedg_face_values *f : fam)
+    if (f->at && (!f->lo || !f->hi)) return refuse(WEDG_ERR_ARGUMENT, "null face values");
+  if (!cfg->src_on && ((pts->hg0.at && (!pts->hg0.lo || !pts->hg0.hi)) || (pts->vg0.at && (!pts->vg0.lo || !pts->vg0.hi)) ||
+                       !pts->cdiv_h || (cfg->mms_on && (!pts->sp_h || !pts->ddiv_h))))
+    return refuse(WEDG_ERR_ARGUMENT, "null initial-data or manufactured-solution arrays");
+  if (cfg->src_on && (!pts->xloc_h || !pts->yloc_h)) return refuse(WEDG_ERR_ARGUMENT, "null high-order points");
+  wedg_ws *ws = nullptr;
+  if ((rc = create_begin(cfg, pre, &ws))) return refuse(rc, "the quadrature rules are not mirror-symmetric");
+  const int N = ws->N, E = ws->E, nv = ws->nv, nq = ws->nq, qh = ws->qh;
+  const size_t nE = (size_t)E * nq * nq, nH = (size_t)E * qh * qh, nF = (size_t)nq * (N + 1) * N;
+  auto cuda_refuse = [&](cudaError_t e) {
+    cuda_fail(ws, e, "wedg_create_points");
+    if (msg && msg_len) snprintf(msg, msg_len, "%s", ws->message.c_str());
+    wedg_destroy(ws);
+    return (int)WEDG_ERR_CUDA;
+  };
+  // ---- the point arrays on the device, freed when this call returns
+  RunBuffers T;
+  double *d_c, *d_a, *d_b, *d_w, *d_Ph, *d_Wh, *d_face[6][3];
+  double *d_g0[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+  double *d_sp = nullptr, *d_cdiv = nullptr, *d_ddiv = nullptr, *d_xh = nullptr, *d_yh = nullptr;
+  unsigned *d_flags;
+  cudaError_t ce;
+  auto put = [&](double **d, const double *h, size_t n) -> cudaError_t {
+    cudaError_t e = T.get(d, n);
+    if (e == cudaSuccess) e = cudaMemcpy(*d, h, n * sizeof(double), cudaMemcpyHostToDevice);
+    return e;
+  };
+  d_c = d_a = d_b = nullptr;
+  if ((pts->c_q && (ce = put(&d_c, pts->c_q, nE)) != cudaSuccess) ||
+      (pts->alpha_q && (ce = put(&d_a, pts->alpha_q, nE)) != cudaSuccess) ||
+      (pts->beta_h && (ce = put(&d_b, pts->beta_h, nH)) != cudaSuccess) || (ce = put(&d_w, pre->w, nq)) != cudaSuccess ||
+      (ce = put(&d_Ph, pre->P_h_v, (size_t)qh * nv)) != cudaSuccess ||
+      (ce = put(&d_Wh, pre->W2d_h, (size_t)qh * qh)) != cudaSuccess || (ce = T.get(&d_flags, 1)) != cudaSuccess ||
+      (ce = cudaMemset(d_flags, 0, sizeof(unsigned))) != cudaSuccess)
+    return cuda_refuse(ce);
+  for (int f = 0; f < 6; ++f) {
+    const double *src[3] = {fam[f]->at, fam[f]->lo, fam[f]->hi};
+    for (int x = 0; x < 3; ++x) {
+      d_face[f][x] = nullptr;
+      if (src[0] && (ce = put(&d_face[f][x], src[x], nF)) != cudaSuccess) return cuda_refuse(ce);
+    }
+  }
+  if (!cfg->src_on) {
+    const wedg_face_values *g[2] = {&pts->hg0, &pts->vg0};
+    for (int f = 0; f < 2; ++f) {
+      const double *src[3] = {g[f]->at, g[f]->lo, g[f]->hi};
+      for (int x = 0; x < 3; ++x)
+        if (src[0] && (ce = put(&d_g0[f][x], src[x], nF)) != cudaSuccess) return cuda_refuse(ce);
+    }
+    if ((ce = put(&d_cdiv, pts->cdiv_h, nH)) != cudaSuccess) return cuda_refuse(ce);
+    if (cfg->mms_on &&
+        ((ce = put(&d_sp, pts->sp_h, nH)) != cudaSuccess || (ce = put(&d_ddiv, pts->ddiv_h, nH)) != cudaSuccess))
+      return cuda_refuse(ce);
+  } else if ((ce = put(&d_xh, pts->xloc_h, (size_t)N * qh)) != cudaSuccess ||
+             (ce = put(&d_yh, pts->yloc_h, (size_t)N * qh)) != cudaSuccess) {
+    return cuda_refuse(ce);
+  }
+  const int tb = 128, eb = (E + tb - 1) / tb;
+  // ---- constant coefficients per element? (the test wedg_create applies to pre's Cw, Aw)
+  unsigned flags = 0;
+  const PtsField fc{d_c, pts->c_value}, fa{d_a, pts->alpha_value}, fb{d_b, pts->beta_value};
+  k_pts_check<<<eb, tb>>>(fc, fa, d_w, nq, E, d_flags);
+  if ((ce = cudaGetLastError()) != cudaSuccess ||
+      (ce = cudaMemcpy(&flags, d_flags, sizeof flags, cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return cuda_refuse(ce);
+  const bool fast = !cfg->general_only && !(flags & PTS_NOT_CONSTANT);
+  if ((rc = create_launchers(ws, fast))) return refuse(rc, "unsupported degrees");
+  Fields &F = ws->F;
+  double *c2e = nullptr, *ae = nullptr, *ic2e = nullptr, *Cw = nullptr, *Aw = nullptr;
+  if (fast) {
+    if (dalloc(ws, &c2e, E) || dalloc(ws, &ae, E) || dalloc(ws, &ic2e, E)) return cuda_refuse(cudaErrorMemoryAllocation);
+    F.c2e = c2e; F.ae = ae; F.ic2e = ic2e;
+  } else {
+    if (dalloc(ws, &Cw, nE) || dalloc(ws, &Aw, nE)) return cuda_refuse(cudaErrorMemoryAllocation);
+    F.Cw = Cw; F.Aw = Aw;
+  }
+  k_pts_elem<<<eb, tb>>>(fc, fa, d_w, nq, E, c2e, ae, ic2e, Cw, Aw);
+  if ((ce = cudaGetLastError()) != cudaSuccess) return cuda_refuse(ce);
+  if (!fast && (rc = device_inverses(ws, pre))) return refuse(rc, "a stiffness matrix is not positive definite");
+  // ---- face arrays, jump terms, one-sided test
+  double *fo[2][7];
+  for (int h = 0; h < 2; ++h)
+    for (int x = 0; x < 7; ++x)
+      if (dalloc(ws, &fo[h][x], nF)) return cuda_refuse(cudaErrorMemoryAllocation);
+  if ((ce = cudaMemset(d_flags, 0, sizeof(unsigned))) != cudaSuccess) return cuda_refuse(ce);
+  for (int h = 0; h < 2; ++h) {
+    const int b = 3 * h;
+    const wedg_face_values &g = h == 0 ? pts->hg0 : pts->vg0;
+    const PtsFace pc{d_face[b][0], d_face[b][1], d_face[b][2], fam[b]->jump_scale, fam[b]->value};
+    const PtsFace pa{d_face[b + 1][0], d_face[b + 1][1], d_face[b + 1][2], fam[b + 1]->jump_scale, fam[b + 1]->value};
+    const PtsFace pb{d_face[b + 2][0], d_face[b + 2][1], d_face[b + 2][2], fam[b + 2]->jump_scale, fam[b + 2]->value};
+    const PtsFace pg{d_g0[h][0], d_g0[h][1], d_g0[h][2], g.jump_scale, cfg->src_on ? 0.0 : g.value};
+    const PtsFaceOut o{fo[h][0], fo[h][1], fo[h][2], fo[h][3], fo[h][4], fo[h][5], fo[h][6]};
+    k_pts_faces<<<(int)std::min<size_t>((nF + 255) / 256, 152 * 16), 256>>>(N, nq, h == 0, pc, pa, pb, pg, o,
+                                                                           d_flags);
+  }
+  if ((ce = cudaGetLastError()) != cudaSuccess ||
+      (ce = cudaMemcpy(&flags, d_flags, sizeof flags, cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return cuda_refuse(ce);
+  F.hc2 = fo[0][0]; F.haf = fo[0][1]; F.hcf = fo[0][2]; F.hbf = fo[0][3]; F.hc2m = fo[0][4]; F.hafm = fo[0][5];
+  F.hJC = fo[0][6];
+  F.vc2 = fo[1][0]; F.vaf = fo[1][1]; F.vcf = fo[1][2]; F.vbf = fo[1][3]; F.vc2m = fo[1][4]; F.vafm = fo[1][5];
+  F.vJC = fo[1][6];
+  if (cfg->mms_on && (flags & PTS_JUMPS)) {
+    wedg_destroy(ws);
+    return refuse(WEDG_ERR_ARGUMENT, "mode = :mms needs c and α continuous across the element faces; "
+                                     "use :initial_value or :source for coefficients that jump");
+  }
+  F.one_sided = (flags & (PTS_JUMPS | PTS_JC)) ? 1 : 0;
+  if ((rc = upload_boundary(ws, pre))) return refuse(rc, "boundary data");
+  // ---- projections and 2β
+  auto proj = [&](double **dst, PtsProj p) -> cudaError_t {
+    if (dalloc(ws, dst, (size_t)nv * nv * E)) return cudaErrorMemoryAllocation;
+    k_pts_proj<<<eb, tb>>>(N, qh, nv, d_Ph, d_Wh, p, *dst);
+    return cudaGetLastError();
+  };
+  double *pisp = nullptr, *pib = nullptr, *pic = nullptr, *pid = nullptr, *psrc = nullptr, *beta2 = nullptr;
+  if (cfg->mms_on) {
+    if ((ce = proj(&pisp, PtsProj{0, d_sp, PtsField{}, nullptr, nullptr, 0, 0, 0, 0})) != cudaSuccess ||
+        (ce = proj(&pib, PtsProj{1, d_sp, fb, nullptr, nullptr, 0, 0, 0, 0})) != cudaSuccess ||
+        (ce = proj(&pid, PtsProj{0, d_ddiv, PtsField{}, nullptr, nullptr, 0, 0, 0, 0})) != cudaSuccess)
+      return cuda_refuse(ce);
+    F.PiSP = pisp; F.PiBSP2 = pib; F.PiDdiv = pid;
+  }
+  if (!cfg->src_on) {
+    if ((ce = proj(&pic, PtsProj{0, d_cdiv, PtsField{}, nullptr, nullptr, 0, 0, 0, 0})) != cudaSuccess)
+      return cuda_refuse(ce);
+    F.PiCdiv = pic;
+  } else {
+    if ((ce = proj(&psrc, PtsProj{2, nullptr, PtsField{}, d_xh, d_yh, pts->src_amp, pts->src_x0, pts->src_y0,
+                                  pts->src_r0})) != cudaSuccess)
+      return cuda_refuse(ce);
+    F.srcP = psrc;
+  }
+  if (dalloc(ws, &beta2, nH)) return cuda_refuse(cudaErrorMemoryAllocation);
+  k_pts_scale<<<(int)std::min<size_t>((nH + 255) / 256, 152 * 16), 256>>>(nH, 2.0, fb, beta2);
+  if ((ce = cudaGetLastError()) != cudaSuccess || (ce = cudaDeviceSynchronize()) != cudaSuccess) return cuda_refuse(ce);
+  F.beta2 = beta2;
+  ws->cfg.one_sided = F.one_sided;
+  if ((rc = create_finish(ws))) return refuse(rc, "scratch");
+  *out = ws;
+  return WEDG_OK;
+}
+
+int wedg_one_sided(const wedg_ws *ws) { return ws ? ws->F.one_sided : -1; }
+
+int wedg_export(const wedg_ws *ws, const char *name, double *out, size_t count) {
+  if (!ws || !name || !out) return WEDG_ERR_ARGUMENT;
+  const Fields &F = ws->F;
+  const int N = ws->N, E = ws->E, nq = ws->nq, nv = ws->nv, qh = ws->qh;
+  const std::string n(name);
+  // the device array, the kind of its layout, its size
+  const double *src = nullptr;
+  int kind = -1;            // 0: h-faces, 1: v-faces, 2: projections, 3: 2β, 4: per element, 5: Cw, Aw
+  const struct {
+    const char *name;
+    const double *p;
+    int kind;
+  } tab[] = {{"hc2", F.hc2, 0},      {"haf", F.haf, 0},       {"hcf", F.hcf, 0},         {"hbf", F.hbf, 0},
+             {"hc2m", F.hc2m, 0},    {"hafm", F.hafm, 0},     {"hJC", F.hJC, 0},         {"vc2", F.vc2, 1},
+             {"vaf", F.vaf, 1},      {"vcf", F.vcf, 1},       {"vbf", F.vbf, 1},         {"vc2m", F.vc2m, 1},
+             {"vafm", F.vafm, 1},    {"vJC", F.vJC, 1},       {"PiSP", F.PiSP, 2},       {"PiBSP2", F.PiBSP2, 2},
+             {"PiCdiv", F.PiCdiv, 2}, {"PiDdiv", F.PiDdiv, 2}, {"src_projE", F.srcP, 2}, {"beta_hq", F.beta2, 3},
+             {"c2e", F.c2e, 4},      {"ae", F.ae, 4},         {"Cw", F.Cw, 5},           {"Aw", F.Aw, 5}};
+  for (const auto &t : tab)
+    if (n == t.name) {
+      src = t.p;
+      kind = t.kind;
+    }
+  if (kind < 0 || !src) return WEDG_ERR_ARGUMENT;
+  const size_t sizes[6] = {(size_t)nq * (N + 1) * N, (size_t)nq * N * (N + 1), (size_t)nv * nv * E,
+                           (size_t)qh * qh * E,      (size_t)E,                 (size_t)nq * nq * E};
+  const size_t len = sizes[kind];
+  if (count != len) return WEDG_ERR_DIMENSION;
+  std::vector<double> d(len);
+  if (cudaMemcpy(d.data(), src, len * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) return WEDG_ERR_CUDA;
+  const size_t Es = (size_t)E;
+  for (size_t t = 0; t < len; ++t) {
+    switch (kind) {
+      case 0: {   // [jf + (N+1)(k + N i)] -> (nq, N+1, N)
+        const size_t jf = t % (N + 1), k = (t / (N + 1)) % N, i = t / ((size_t)(N + 1) * N);
+        out[i + nq * (jf + (size_t)(N + 1) * k)] = d[t];
+        break;
+      }
+      case 1: {   // [j + N (kf + (N+1) i)] -> (nq, N, N+1)
+        const size_t j = t % N, kf = (t / N) % (N + 1), i = t / ((size_t)N * (N + 1));
+        out[i + nq * (j + (size_t)N * kf)] = d[t];
+        break;
+      }
+      case 2: {   // [l E + e] -> (nv, nv, N, N)
+        const size_t e = t % Es, l = t / Es;
+        out[l + (size_t)nv * nv * e] = d[t];
+        break;
+      }
+      case 3: {   // 2β [(r + qh s) E + e] -> β (qh, E, qh)
+        const size_t e = t % Es, rs = t / Es, r = rs % qh, s_ = rs / qh;
+        out[r + qh * (e + Es * s_)] = 0.5 * d[t];
+        break;
+      }
+      case 4:
+        out[t] = d[t];
+        break;
+      default: {  // [(r + nq s) E + e] -> (nq, E, nq)
+        const size_t e = t % Es, rs = t / Es, r = rs % nq, s_ = rs / nq;
+        out[r + nq * (e + Es * s_)] = d[t];
+      }
+    }
+  }
   return WEDG_OK;
 }
 

@@ -99,7 +99,9 @@ struct Fields {
   const double *beta2;        // 2β at the high-order points, [(r + QH s) E + e]
   double *tr, *G, *th, *de;   // G = 2βv at the high-order points
   double *mrhs;               // right-hand side of the mass system, [(a + NV b) E + e]
-  int *nst, *nmax;
+  int *nst;
+  int *nmax;                  // largest Chebyshev count: [parity] of a stage (the common count of
+                              // src/rhs.jl:911-918), [2] of the whole call (statistics)
   int *bins, *bin_count;      // elements by Chebyshev count: bins[b E + i], two count buffers of NBIN
   unsigned long long *nsum;   // Σ of the per-element Chebyshev step counts
   unsigned long long *err;
@@ -356,9 +358,11 @@ __device__ __forceinline__ void prep_body(const Basis<NU, NV> &B, const Fields &
                                           bool first) {
   constexpr int NQ = NU, QH = Basis<NU, NV>::QH;
   const int E = F.E, N = F.N;
-  // the bin counts of the next stage start at zero: all NBIN of them, whatever the element count
+  // the bin counts and the largest count of the next stage start at zero: all NBIN bins, whatever
+  // the element count
   if (first && F.sorted)
     for (int b = threadIdx.x; b < NBIN; b += blockDim.x) F.bin_count[(1 - S.parity) * NBIN + b] = 0;
+  if (first && threadIdx.x == 0) F.nmax[1 - S.parity] = 0;
   if (e >= E) return;
   if (err_word(F) != ERR_NONE) return;
   const int j = e % N, k = e / N;
@@ -451,7 +455,8 @@ __device__ __forceinline__ void prep_body(const Basis<NU, NV> &B, const Fields &
   const unsigned ns = __reduce_add_sync(mask, (unsigned)n);
   const int lane = threadIdx.x & 31;
   if (lane == __ffs(mask) - 1) {
-    atomicMax(F.nmax, nw);
+    atomicMax(&F.nmax[S.parity], nw);
+    atomicMax(&F.nmax[2], nw);
     atomicAdd(F.nsum, (unsigned long long)ns);
   }
   if (F.sorted) {
@@ -1281,7 +1286,7 @@ __device__ __forceinline__ void cheb_body(const Basis<NU, NV> &B, const Fields &
   const int e = mass_element(F, S, g, pref);
   const double th = F.th[e], de = F.de[e];
   const double s1 = th / de;
-  const int n = F.cheb_common ? *F.nmax : F.nst[e];
+  const int n = F.cheb_common ? F.nmax[S.parity] : F.nst[e];
   const double ith = 1.0 / th;
   double rr[J], xx[J], dd[J];
 #pragma unroll

@@ -246,10 +246,10 @@ extern "C" int wedg_rhs_noalloc(const wedg_config *cfg, const wedg_pre *pre, con
   F.mrhs = base + o_mrhs;
   F.bins = reinterpret_cast<int *>(base + o_bins);
   F.bin_count = reinterpret_cast<int *>(base + o_bcnt);
-  double *flags = base + o_flags;   // err (u64), nsum (u64), nmax (int), cg_nfail, nonfinite (u32)
+  double *flags = base + o_flags;   // err (u64), nsum (u64), cg_nfail, nonfinite (u32), nmax (3 ints)
   F.err = reinterpret_cast<unsigned long long *>(flags);
   F.nsum = reinterpret_cast<unsigned long long *>(flags + 1);
-  F.nmax = reinterpret_cast<int *>(flags + 2);
+  F.nmax = reinterpret_cast<int *>(flags + 5);
   F.cg_nfail = reinterpret_cast<unsigned int *>(flags + 3);
   F.nonfinite = reinterpret_cast<unsigned int *>(flags + 4);
   F.theta = cfg->theta; F.tau = cfg->tau; F.lu = cfg->lambda_u; F.lv = cfg->lambda_v;

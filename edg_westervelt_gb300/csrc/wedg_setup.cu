@@ -1,6 +1,8 @@
-// Set-up kernels of wedg_create: the packed inverses of the pinned c²-stiffness of every
-// element (src/solver.jl:528-535), computed on the device from the element's c²W at the
-// u-quadrature points when the caller passes no Ainv_u.
+// Set-up kernels of wedg_create and wedg_create_points: the packed inverses of the pinned
+// c²-stiffness of every element (src/solver.jl:528-535), computed on the device from the
+// element's c²W at the u-quadrature points when the caller passes no Ainv_u; and the arrays of
+// `pre` (element matrices, one-sided face arrays, jump terms, projections) built from the point
+// values of the coefficients and data (src/solver.jl:509-552, 554-602, 647-662, 698-770).
 //
 // One block per element, the n × n matrix (n = (q_u+1)² ≤ 64) in shared memory:
 //   M = Φξᵀ diag(c²W) Φξ + Φηᵀ diag(c²W) Φη, M[0][0] += 1, with Φξ = P_u ⊗ S_u, Φη = S_u ⊗ P_u
@@ -87,6 +89,144 @@ __global__ void k_ainv(const double *Cw, int E, int nu, const double *Pu, const 
 size_t ainv_smem(int nu) {
   const int n = nu * nu, nq = nu;
   return sizeof(double) * (2 * (size_t)n * n + nq * nq + 2 * nq * nu);
+}
+
+// ---------------------------------------------------------------------------------------------
+// The rest of `pre` on the device (wedg_create_points): the arithmetic is the host's (the same
+// products in the same order; __dmul_rn / __dadd_rn where the host rounds a product before a sum,
+// so that no contraction into an FMA changes a comparison)
+// ---------------------------------------------------------------------------------------------
+
+__global__ void k_pts_check(PtsField c_q, PtsField a_q, const double *w, int nq, int E, unsigned *flags) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const size_t Eu = (size_t)E;
+  const double w00 = __dmul_rn(w[0], w[0]);
+  const double c0 = c_q[e], a0 = a_q[e];
+  const double c2 = __dmul_rn(__dmul_rn(c0, c0), w00) / w00, al = __dmul_rn(a0, w00) / w00;
+  bool ok = c2 > 0.0;
+  for (int s = 0; s < nq && ok; ++s)
+    for (int r = 0; r < nq; ++r) {
+      const double W = __dmul_rn(w[r], w[s]);
+      const double c = c_q[e + Eu * (r + nq * s)], a = a_q[e + Eu * (r + nq * s)];
+      const double cw = __dmul_rn(__dmul_rn(c, c), W), aw = __dmul_rn(a, W);
+      if (fabs(cw - __dmul_rn(c2, W)) > __dmul_rn(1e-14, fabs(cw)) ||
+          fabs(aw - __dmul_rn(al, W)) > __dmul_rn(1e-14, fabs(aw))) {
+        ok = false;
+        break;
+      }
+    }
+  if (!ok) atomicOr(flags, (unsigned)PTS_NOT_CONSTANT);
+}
+
+__global__ void k_pts_elem(PtsField c_q, PtsField a_q, const double *w, int nq, int E, double *c2e, double *ae,
+                           double *ic2e, double *Cw, double *Aw) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const size_t Eu = (size_t)E;
+  if (c2e) {
+    const double w00 = __dmul_rn(w[0], w[0]);
+    const double c0 = c_q[e], a0 = a_q[e];
+    const double c2 = __dmul_rn(__dmul_rn(c0, c0), w00) / w00;
+    c2e[e] = c2;
+    ae[e] = __dmul_rn(a0, w00) / w00;
+    ic2e[e] = 1.0 / c2;
+  }
+  if (Cw)
+    for (int s = 0; s < nq; ++s)
+      for (int r = 0; r < nq; ++r) {
+        const size_t l = e + Eu * (r + nq * s);
+        const double W = __dmul_rn(w[r], w[s]);
+        Cw[l] = __dmul_rn(__dmul_rn(c_q[l], c_q[l]), W);
+        Aw[l] = __dmul_rn(a_q[l], W);
+      }
+}
+
+// The value of a family seen from below (lower = true: the "-" side) or above a face point
+// (src/solver.jl:389-392): the plain value where the family is continuous there to the tolerance
+__device__ __forceinline__ double pts_side(const PtsFace &f, size_t i, bool lower) {
+  if (!f.at) return f.value;
+  const double h0 = f.at[i], hm = f.lo[i], hp = f.hi[i];
+  const bool nm = fabs(hm - h0) <= __dadd_rn(__dmul_rn(1e-8, fmax(fabs(hm), fabs(h0))), f.s);
+  const bool np = fabs(hp - h0) <= __dadd_rn(__dmul_rn(1e-8, fmax(fabs(hp), fabs(h0))), f.s);
+  const bool use0 = isfinite(h0) && nm && np;
+  return use0 ? h0 : (lower ? hm : hp);
+}
+
+__global__ void k_pts_faces(int N, int nq, bool hor, PtsFace c, PtsFace a, PtsFace b, PtsFace g0, PtsFaceOut o,
+                            unsigned *flags) {
+  const size_t nf = (size_t)nq * (N + 1) * N;
+  unsigned fl = 0;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nf; t += (size_t)gridDim.x * blockDim.x) {
+    // t walks the output layout: h-faces [jf + (N+1)(k + N i)], v-faces [j + N (kf + (N+1) i)]
+    int f, m, i;                  // f: the face index across (jf or kf), m: the element along it, i: point
+    if (hor) {
+      f = (int)(t % (N + 1));
+      m = (int)((t / (N + 1)) % N);
+      i = (int)(t / ((size_t)(N + 1) * N));
+    } else {
+      m = (int)(t % N);
+      f = (int)((t / N) % (N + 1));
+      i = (int)(t / ((size_t)N * (N + 1)));
+    }
+    const size_t pin = hor ? i + (size_t)nq * (f + (size_t)(N + 1) * m) : i + (size_t)nq * (m + (size_t)N * f);
+    // the "+" array takes the value above face f (inside element f), the last face the one below
+    // it; the "-" array the value below face f, the first face the one above it
+    const bool plus_lower = f == N, minus_lower = f != 0;
+    const double cp = pts_side(c, pin, plus_lower), cm = pts_side(c, pin, minus_lower);
+    const double ap = pts_side(a, pin, plus_lower), am = pts_side(a, pin, minus_lower);
+    const double c2p = __dmul_rn(cp, cp), c2m = __dmul_rn(cm, cm);
+    o.c2[t] = c2p;
+    o.c2m[t] = c2m;
+    o.cf[t] = cp;
+    o.af[t] = ap;
+    o.afm[t] = am;
+    o.bf[t] = pts_side(b, pin, plus_lower);
+    double jc = 0.0;
+    if ((g0.at || g0.value != 0.0) && f != 0 && f != N) {
+      const double gp = pts_side(g0, pin, plus_lower), gm = pts_side(g0, pin, minus_lower);
+      jc = __dmul_rn(c2m, gm) - __dmul_rn(c2p, gp);
+    }
+    o.JC[t] = jc;
+    if (c2m != c2p || am != ap) fl |= PTS_JUMPS;
+    if (jc != 0.0) fl |= PTS_JC;
+  }
+  if (fl) atomicOr(flags, fl);
+}
+
+__global__ void k_pts_proj(int N, int qh, int nv, const double *Ph, const double *Wh, PtsProj p, double *out) {
+  const int E = N * N;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const int j = e % N, k = e / N;
+  const size_t Eu = (size_t)E;
+  double T[12][8];                 // T[r][b] = Σ_s W[r, s] X[r, s] P_h[s, b]  (qh ≤ 12, nv ≤ 8)
+  for (int r = 0; r < qh; ++r) {
+    for (int bb = 0; bb < nv; ++bb) T[r][bb] = 0.0;
+    for (int s = 0; s < qh; ++s) {
+      double x;
+      if (p.kind == 2) {
+        const double dx = p.xh[k + (size_t)N * s] - p.x0, dy = p.yh[j + (size_t)N * r] - p.y0;
+        x = __dmul_rn(p.amp, exp(-__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)) / __dmul_rn(p.r0, p.r0)));
+      } else {
+        x = p.x1[e + Eu * (r + qh * s)];
+        if (p.kind == 1) x = __dmul_rn(p.x2[e + Eu * (r + qh * s)], __dmul_rn(x, x));
+      }
+      const double wx = __dmul_rn(Wh[r + qh * s], x);
+      for (int bb = 0; bb < nv; ++bb) T[r][bb] = fma(wx, Ph[s + qh * bb], T[r][bb]);
+    }
+  }
+  for (int bb = 0; bb < nv; ++bb)
+    for (int a = 0; a < nv; ++a) {
+      double z = 0.0;
+      for (int r = 0; r < qh; ++r) z = fma(Ph[r + qh * a], T[r][bb], z);
+      out[(a + (size_t)nv * bb) * Eu + e] = z;
+    }
+}
+
+__global__ void k_pts_scale(size_t n, double a, PtsField x, double *y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i];
 }
 
 }  // namespace wedg

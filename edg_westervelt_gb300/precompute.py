@@ -15,7 +15,8 @@ import math
 
 import numpy as np
 
-from .coefficients import Coefficients, GaussianSource, _sym, boundary_sides, flux_parameters, paper_coefficients
+from .coefficients import (Coefficients, GaussianSource, _Const, _sym, boundary_sides, flux_parameters,
+                           paper_coefficients)
 from .quadrature import GaussQCofs, GradJacobiP, JacobiP
 
 FACE_SHIFT = 2.0 ** -40   # src/solver.jl:361
@@ -53,6 +54,12 @@ def _sides(H0, HM, HP, s):
 
 
 def _amax(A):
+    """max |A| over the finite entries of A (0 if none)."""
+    if A.size == 0:
+        return 0.0
+    m = float(np.max(np.abs(A)))
+    if math.isfinite(m):
+        return m
     A = A[np.isfinite(A)]
     return float(np.max(np.abs(A))) if A.size else 0.0
 
@@ -140,12 +147,21 @@ def _distinct_rows(a, limit=None):
 
 def precompute(q, N, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, boundary="absorbing_2beta",
                sigma_dirichlet=None, kappa=0.0, phase=(0.0, 0.0), coefficients=None, mode="mms", kx=1, ky=1,
-               source=None, mass_solver="chebyshev", initial_profile=None, inverses="device"):
+               source=None, mass_solver="chebyshev", initial_profile=None, inverses="device", target="host"):
     """Element operators, face coefficients and data arrays of the RHS (``pre``) and the
     quadrature geometry for errors and diagnostics (``geo``); src/solver.jl:428-694.
 
     Keywords as the reference's ``precompute`` (symbols as strings, e.g. flux="upwind").
+    target="device": the large arrays are left to the GPU workspace, which forms them from the
+    coefficient functions' values at the point grids (precompute_points, wedg_create_points).
     """
+    if target == "device":
+        return precompute_points(q, N, mixed=mixed, flux=flux, flux_params=flux_params, sigma=sigma,
+                                 boundary=boundary, sigma_dirichlet=sigma_dirichlet, kappa=kappa, phase=phase,
+                                 coefficients=coefficients, mode=mode, kx=kx, ky=ky, source=source,
+                                 mass_solver=mass_solver, initial_profile=initial_profile)
+    if target != "host":
+        raise ValueError(f"target must be \"host\" or \"device\", not {target!r}")
     mode = _sym(mode)
     mass_solver = _sym(mass_solver)
     flux = _sym(flux)
@@ -424,3 +440,214 @@ def _rhs_data(pre, N):
         W_hq=_F(p["W2d_h"].reshape(qh, 1, qh, order="F")),
         P_h_vT=_F(p["P_h_v"].T), mass_tol=1e-14,
     )
+
+
+def _face_values(f, xloc, yloc, N, h, horizontal=True, vertical=True):
+    """The point values of one family on the faces that side_values reads (src/solver.jl:371-392):
+    per orientation, the value at each face point and δ below (left of) and above (right of) it,
+    the reference's arrays (nq, N+1, N) and (nq, N, N+1) (the δ values outside the domain are the
+    face values, as there), and the family's tolerance term s."""
+    nq = xloc.shape[1]
+    d = FACE_SHIFT
+    out, sh, sv = {}, 0.0, 0.0
+
+    def fortran(a):   # the reference's column-major layout of an (nq, ., .) array evaluated in C order
+        return np.asfortranarray(a)
+    if horizontal:
+        X = np.broadcast_to(xloc.T[:, None, :], (nq, N + 1, N))
+        Yf = np.broadcast_to((np.arange(N + 1) * h)[None, :, None], (nq, N + 1, N))
+        H0 = fortran(evaluate(f, X, Yf))
+        HM, HP = H0.copy(order="F"), H0.copy(order="F")
+        HM[:, 1:, :] = evaluate(f, X[:, 1:, :], Yf[:, 1:, :] - d)
+        HP[:, :N, :] = evaluate(f, X[:, :N, :], Yf[:, :N, :] + d)
+        out["h"] = (H0, HM, HP)
+        sh = max(_amax(HM[:, 1:, :]), _amax(HP[:, :N, :]))
+    if vertical:
+        Xf = np.broadcast_to((np.arange(N + 1) * h)[None, None, :], (nq, N, N + 1))
+        Y = np.broadcast_to(yloc.T[:, :, None], (nq, N, N + 1))
+        V0 = fortran(evaluate(f, Xf, Y))
+        VM, VP = V0.copy(order="F"), V0.copy(order="F")
+        VM[:, :, 1:] = evaluate(f, Xf[:, :, 1:] - d, Y[:, :, 1:])
+        VP[:, :, :N] = evaluate(f, Xf[:, :, :N] + d, Y[:, :, :N])
+        out["v"] = (V0, VM, VP)
+        sv = max(_amax(VM[:, :, 1:]), _amax(VP[:, :, :N]))
+    return out, JUMP_TOL * max(sh, sv)
+
+
+def precompute_points(q, N, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, boundary="absorbing_2beta",
+                      sigma_dirichlet=None, kappa=0.0, phase=(0.0, 0.0), coefficients=None, mode="mms", kx=1, ky=1,
+                      source=None, mass_solver="chebyshev", initial_profile=None):
+    """``precompute`` for a workspace that builds ``pre``'s large arrays on the device
+    (wedg_create_points): the 1D operators, scalars and boundary data of ``pre`` (src/solver.jl:
+    428-490, 604-635, 665-690), and the values of the coefficient functions and data at the point
+    grids, evaluated here (they are the caller's functions) in the memory order the device reads.
+    The element matrices, one-sided face arrays, jump terms, projections and 2β are formed on the
+    device from these values (precompute forms them on the host). Returns (pre, geo) like
+    precompute; pre["points"] holds the point values, and pre has no element or face arrays."""
+    mode = _sym(mode)
+    mass_solver = _sym(mass_solver)
+    if sigma_dirichlet is None:
+        sigma_dirichlet = sigma
+    coefficients = paper_coefficients() if coefficients is None else coefficients
+    source = GaussianSource() if source is None else source
+    if mass_solver not in ("cg", "chebyshev"):
+        raise ValueError(f"unknown mass_solver {mass_solver} (expected :cg or :chebyshev)")
+    if initial_profile is not None and mode != "initial_value":
+        raise ValueError("initial_profile is only available in :initial_value mode")
+    if mode not in ("mms", "initial_value", "source"):
+        raise ValueError(f"unknown mode {mode} (expected :mms, :initial_value or :source)")
+    q_u = int(q)
+    q_v = q_u - 1 if mixed else q_u
+    qu1, qv1 = q_u + 1, q_v + 1
+    h = 1.0 / N
+    omega = 2 * math.pi * math.sqrt(kx ** 2 + ky ** 2)
+    fp = flux_parameters(_sym(flux)) if flux_params is None else {
+        k: float(flux_params[k]) for k in ("theta", "tau", "lambda_u", "lambda_v")}
+    bc = boundary_sides(boundary, sigma, sigma_dirichlet, kappa)
+    legacy = isinstance(boundary, str) and _sym(boundary) in ("absorbing", "dirichlet")
+    gamma_abc = bc["bot"]["gamma_abc"] if legacy else math.nan
+    px, py = phase
+    C = coefficients
+    pi = math.pi
+
+    # ---- 1D bases (solver.jl:462-490), as precompute
+    z, w = GaussQCofs(qu1)
+    W2d = _F(np.outer(w, w))
+    d_idx = range(qu1)
+    P_u = _F(np.stack([JacobiP(z, 0, 0, d) for d in d_idx], axis=1))
+    S_u = _F(np.stack([GradJacobiP(z, 0, 0, d) for d in d_idx], axis=1))
+    Ebl_u = _F([[JacobiP(-1.0, 0, 0, d) for d in d_idx]])
+    Ebr_u = _F([[JacobiP(1.0, 0, 0, d) for d in d_idx]])
+    E1bl_u = _F([[GradJacobiP(-1.0, 0, 0, d) for d in d_idx]])
+    E1br_u = _F([[GradJacobiP(1.0, 0, 0, d) for d in d_idx]])
+    q_high = max(int(math.ceil(3 * q_v / 2) + 1), q_u + 1)
+    z_h, w_h = GaussQCofs(q_high)
+    W2d_h = _F(np.outer(w_h, w_h))
+    P_h_v = _F(np.stack([JacobiP(z_h, 0, 0, d) for d in range(qv1)], axis=1))
+    cells = np.arange(N)
+    xloc = _F((cells[:, None] * h + (cells[:, None] + 1) * h + h * z[None, :]) / 2)
+    xloc_h = _F((cells[:, None] * h + (cells[:, None] + 1) * h + h * z_h[None, :]) / 2)
+    yloc, yloc_h = xloc.copy(order="F"), xloc_h.copy(order="F")
+
+    # ---- point values in the device's order: an (N, N, n, n) array [j, k, r, s] with j fastest is
+    #      the transpose of a C-order (n_s, n_r, N_k, N_j) array, so evaluate on that grid directly
+    def grid(xl, yl):
+        n = xl.shape[1]
+        X = np.broadcast_to(xl.T[:, None, :, None], (n, n, N, N))     # [s, r, k, j] = x_s of column k
+        Y = np.broadcast_to(yl.T[None, :, None, :], (n, n, N, N))     # = y_r of row j
+        return X, Y
+
+    def at(f, XY):
+        return np.ascontiguousarray(evaluate(f, *XY)).T                # (N, N, n, n), Fortran-contiguous
+    XQ, XH = grid(xloc, yloc), grid(xloc_h, yloc_h)
+
+    # a constant coefficient (constant_coefficients, replace_coefficients) is passed as its value:
+    # the device fills it in (its face values are the constant, continuous)
+    def field(f, XY):
+        return (None, f.val) if isinstance(f, _Const) else (at(f, XY), 0.0)
+
+    def face(f):
+        return (None, f.val) if isinstance(f, _Const) else _face_values(f, xloc, yloc, N, h)
+    pts = dict(c_q=field(C.c, XQ), alpha_q=field(C.alpha, XQ), beta_h=field(C.beta, XH),
+               faces={key: face(fun) for key, fun in (("c", C.c), ("a", C.alpha), ("b", C.beta))})
+    src_on = mode == "source"
+    g0 = None
+    if not src_on:
+        if initial_profile is None:
+            def u0_x(x, y):
+                return -2 * pi * kx * np.sin(2 * pi * kx * x + px) * np.sin(2 * pi * ky * y + py)
+
+            def u0_y(x, y):
+                return 2 * pi * ky * np.cos(2 * pi * kx * x + px) * np.cos(2 * pi * ky * y + py)
+        else:
+            u0_x, u0_y = initial_profile["u0_x"], initial_profile["u0_y"]
+        gy, sy = _face_values(u0_y, xloc, yloc, N, h, vertical=False)
+        gx, sx = _face_values(u0_x, xloc, yloc, N, h, horizontal=False)
+        g0 = dict(h=(gy["h"], sy), v=(gx["v"], sx))
+        # data at the high-order points (solver.jl:570-602)
+        XHa, YHa = XH
+        if initial_profile is None:
+            sp = np.cos(2 * pi * kx * XHa + px) * np.sin(2 * pi * ky * YHa + py)
+            sp_x = -2 * pi * kx * np.sin(2 * pi * kx * XHa + px) * np.sin(2 * pi * ky * YHa + py)
+            sp_y = 2 * pi * ky * np.cos(2 * pi * kx * XHa + px) * np.cos(2 * pi * ky * YHa + py)
+            sp_xx = -(2 * pi * kx) ** 2 * sp
+            sp_yy = -(2 * pi * ky) ** 2 * sp
+        else:
+            ip = initial_profile
+            sp, sp_x, sp_y = (evaluate(ip[n], XHa, YHa) for n in ("u0", "u0_x", "u0_y"))
+            sp_xx, sp_yy = evaluate(ip["u0_xx"], XHa, YHa), evaluate(ip["u0_yy"], XHa, YHa)
+        cf = evaluate(C.c, XHa, YHa)
+        c2 = cf ** 2
+        c2x, c2y = 2 * cf * evaluate(C.c_x, XHa, YHa), 2 * cf * evaluate(C.c_y, XHa, YHa)
+        pts["cdiv_h"] = np.ascontiguousarray(c2x * sp_x + c2y * sp_y + c2 * (sp_xx + sp_yy)).T
+        if mode == "mms":
+            af = evaluate(C.alpha, XHa, YHa)
+            ax, ay = evaluate(C.alpha_x, XHa, YHa), evaluate(C.alpha_y, XHa, YHa)
+            pts["sp_h"] = np.ascontiguousarray(sp).T
+            pts["ddiv_h"] = np.ascontiguousarray(ax * sp_x + ay * sp_y + af * (sp_xx + sp_yy)).T
+    pts["g0"] = g0
+
+    # ---- Φ and ∇Φ on the physical boundary (solver.jl:604-635), (nq, N) as _rhs_data lays them out
+    bcd = {}
+    zx = np.zeros_like(xloc)
+    if src_on:
+        for n in ("bc_bot_sp", "bc_bot_spy", "bc_top_sp", "bc_top_spy",
+                  "bc_lft_sp", "bc_lft_spx", "bc_rgt_sp", "bc_rgt_spx"):
+            bcd[n] = np.zeros((N, qu1), order="F")
+    elif initial_profile is None:
+        cx = np.cos(2 * pi * kx * xloc + px)
+        sy_ = np.sin(2 * pi * ky * yloc + py)
+        bcd["bc_bot_sp"] = cx * math.sin(2 * pi * ky * 0 + py)
+        bcd["bc_bot_spy"] = 2 * pi * ky * cx * math.cos(2 * pi * ky * 0 + py)
+        bcd["bc_top_sp"] = cx * math.sin(2 * pi * ky * 1 + py)
+        bcd["bc_top_spy"] = 2 * pi * ky * cx * math.cos(2 * pi * ky * 1 + py)
+        bcd["bc_lft_sp"] = math.cos(2 * pi * kx * 0 + px) * sy_
+        bcd["bc_lft_spx"] = -2 * pi * kx * math.sin(2 * pi * kx * 0 + px) * sy_
+        bcd["bc_rgt_sp"] = math.cos(2 * pi * kx * 1 + px) * sy_
+        bcd["bc_rgt_spx"] = -2 * pi * kx * math.sin(2 * pi * kx * 1 + px) * sy_
+    else:
+        ip = initial_profile
+        bcd["bc_bot_sp"] = evaluate(ip["u0"], xloc, zx)
+        bcd["bc_bot_spy"] = evaluate(ip["u0_y"], xloc, zx)
+        bcd["bc_top_sp"] = evaluate(ip["u0"], xloc, zx + 1.0)
+        bcd["bc_top_spy"] = evaluate(ip["u0_y"], xloc, zx + 1.0)
+        bcd["bc_lft_sp"] = evaluate(ip["u0"], zx, yloc)
+        bcd["bc_lft_spx"] = evaluate(ip["u0_x"], zx, yloc)
+        bcd["bc_rgt_sp"] = evaluate(ip["u0"], zx + 1.0, yloc)
+        bcd["bc_rgt_spx"] = evaluate(ip["u0_x"], zx + 1.0, yloc)
+    names = dict(bcB_sp="bc_bot_sp", bcB_spy="bc_bot_spy", bcT_sp="bc_top_sp", bcT_spy="bc_top_spy",
+                 bcL_sp="bc_lft_sp", bcL_spx="bc_lft_spx", bcR_sp="bc_rgt_sp", bcR_spx="bc_rgt_spx")
+    pts["source"] = dict(xloc_h=xloc_h, yloc_h=yloc_h, amp=float(source.amplitude), x0=float(source.x0[0]),
+                         y0=float(source.x0[1]), r0=float(source.r0))
+
+    pre = dict(
+        N=N, qu1=qu1, qv1=qv1, q_high=q_high, omega=omega, w=w,
+        P_u=P_u, P_v=_F(P_u[:, :qv1]), S_u=S_u, S_v=_F(S_u[:, :qv1]),
+        Ebl_u=Ebl_u, Ebr_u=Ebr_u, E1bl_u=E1bl_u, E1br_u=E1br_u,
+        W2d_h=W2d_h, P_h_v=P_h_v,
+        theta=fp["theta"], tau=fp["tau"], lambda_u=fp["lambda_u"], lambda_v=fp["lambda_v"],
+        gamma_abc=gamma_abc, eta_abc=math.sqrt(1.0 - gamma_abc ** 2) if legacy else math.nan,
+        sigma=bc["bot"]["sigma"] if legacy else math.nan,
+        bc=bc, src_on=src_on, source=source, mms_on=mode == "mms", mass_solver=mass_solver, mass_tol=1e-14,
+        points=pts,
+    )
+    for k, n in names.items():
+        pre[k] = _F(np.asarray(bcd[n]).T)
+    lazy = dict(err_c2=lambda: at(C.c, XQ) ** 2, err_beta=lambda: at(C.beta, XQ))
+    geo = _LazyGeo(lazy, S_u=S_u, W2d=W2d, xloc=xloc, yloc=yloc)
+    return pre, geo
+
+
+class _LazyGeo(dict):
+    """geo of precompute_points: c² and β at the u-points (err_c2, err_beta, only used by the error
+    norms and the source-mode diagnostics) are evaluated on first use."""
+
+    def __init__(self, lazy, **kw):
+        super().__init__(**kw)
+        self._lazy = lazy
+
+    def __missing__(self, key):
+        if key not in self._lazy:
+            raise KeyError(key)
+        self[key] = val = self._lazy[key]()
+        return val

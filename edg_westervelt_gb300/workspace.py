@@ -55,6 +55,46 @@ def _shape(x, nu, N):
     return (ctypes.c_int64 * 4)(*shp)
 
 
+def _points_struct(points, keep):
+    """wedg_points for the point values of precompute_points (arrays kept alive in keep)."""
+    P = L.Points()
+    null = ctypes.POINTER(ctypes.c_double)()
+
+    def arr(a):
+        if a is None:
+            return null
+        a = _f64(a)
+        keep[id(a)] = a
+        return _ptr(a)
+    for name, val in (("c_q", points["c_q"]), ("alpha_q", points["alpha_q"]), ("beta_h", points["beta_h"])):
+        setattr(P, name, arr(val[0]))
+        setattr(P, {"c_q": "c_value", "alpha_q": "alpha_value", "beta_h": "beta_value"}[name], float(val[1]))
+
+    def face(fv, values, scale=None):
+        if values is None:                      # a constant family: (None, value)
+            return
+        fv.at, fv.lo, fv.hi = (arr(x) for x in values)
+        fv.jump_scale = float(scale)
+    for key, (hn, vn) in (("c", ("hc", "vc")), ("a", ("ha", "va")), ("b", ("hb", "vb"))):
+        fam = points["faces"][key]
+        if fam[0] is None:
+            getattr(P, hn).value = getattr(P, vn).value = float(fam[1])
+        else:
+            out, s = fam
+            face(getattr(P, hn), out["h"], s)
+            face(getattr(P, vn), out["v"], s)
+    if points.get("g0") is not None:
+        (hv, hs), (vv, vs) = points["g0"]["h"], points["g0"]["v"]
+        face(P.hg0, hv, hs)
+        face(P.vg0, vv, vs)
+    for name in ("sp_h", "cdiv_h", "ddiv_h"):
+        setattr(P, name, arr(points.get(name)))
+    src = points["source"]
+    P.xloc_h, P.yloc_h = arr(src["xloc_h"]), arr(src["yloc_h"])
+    P.src_amp, P.src_x0, P.src_y0, P.src_r0 = src["amp"], src["x0"], src["y0"], src["r0"]
+    return P
+
+
 def _default_nblocks(pre, N):
     """src/rhs.jl:139-142 (kept for the `nb` attribute; the GPU grid replaces the blocks)."""
     import os
@@ -91,14 +131,15 @@ class Workspace:
         self.fin = True
         # pre of another mesh: the reference's Workspace accepts it and its edg_rhs! refuses it
         # with a DimensionMismatch (src/rhs.jl:500-503); no device workspace is made from it
-        self._mismatch = pre["Cw"].shape[1] != E
+        self._mismatch = (pre["N"] != N) if "points" in pre else pre["Cw"].shape[1] != E
         if self._mismatch:
             return
         cfg = L.Config()
         cfg.N, cfg.qu1, cfg.qv1, cfg.q_high = N, pre["qu1"], pre["qv1"], pre["q_high"]
         cfg.theta, cfg.tau, cfg.lambda_u, cfg.lambda_v = pre["theta"], pre["tau"], pre["lambda_u"], pre["lambda_v"]
         cfg.omega = pre["omega"]
-        cfg.mms_on, cfg.src_on, cfg.one_sided = int(pre["mms_on"]), int(pre["src_on"]), int(pre["one_sided"])
+        cfg.mms_on, cfg.src_on = int(pre["mms_on"]), int(pre["src_on"])
+        cfg.one_sided = int(pre.get("one_sided", False))     # a pre of point values: the device decides
         cfg.mass_solver = 0 if pre["mass_solver"] == "chebyshev" else 1
         cfg.mass_tol = pre["mass_tol"]
         cfg.src_omega, cfg.src_Ts = pre["source"].omega, pre["source"].Ts
@@ -112,22 +153,36 @@ class Workspace:
         self._cfg = cfg
         keep = {}
         p = L.Pre()
+        points = pre.get("points")
         for name in L.PRE_FIELDS:
-            a = pre[name]
-            if name == "Ainv_u" and (a is None or not a.flags.f_contiguous):
-                # NULL: not needed by the constant-coefficient kernels, else computed on the device
+            a = pre.get(name)
+            if a is None or (name == "Ainv_u" and not a.flags.f_contiguous):
+                # NULL: Ainv_u is not needed by the constant-coefficient kernels, else computed on the
+                # device; a pre of point values has no element or face arrays
                 setattr(p, name, ctypes.POINTER(ctypes.c_double)())
                 continue
             a = _f64(np.ascontiguousarray(a) if not a.flags.f_contiguous else a)
             keep[name] = a
             setattr(p, name, _ptr(a))
         h = ctypes.c_void_p()
-        rc = L.lib().wedg_create(ctypes.byref(cfg), ctypes.byref(p), ctypes.byref(h))
+        if points is None:
+            rc = L.lib().wedg_create(ctypes.byref(cfg), ctypes.byref(p), ctypes.byref(h))
+            msg = ""
+        else:
+            pts = _points_struct(points, keep)
+            buf = ctypes.create_string_buffer(512)
+            rc = L.lib().wedg_create_points(ctypes.byref(cfg), ctypes.byref(p), ctypes.byref(pts), buf, 512,
+                                            ctypes.byref(h))
+            msg = buf.value.decode("utf-8")
+            if rc == L.WEDG_ERR_ARGUMENT and msg.startswith("mode = :mms"):
+                raise ValueError(msg)
         if rc == L.WEDG_ERR_NO_DEVICE:
             raise RuntimeError("libwedg: no CUDA device available")
         if rc != L.WEDG_OK:
-            raise RuntimeError(f"wedg_create failed: {L.lib().wedg_status_string(rc).decode()}")
+            raise RuntimeError(f"wedg_create failed: {L.lib().wedg_status_string(rc).decode()}" +
+                               (f": {msg}" if msg else ""))
         self._h = h
+        self.one_sided = bool(L.lib().wedg_one_sided(h))
 
     def __del__(self):
         if getattr(self, "_h", None):

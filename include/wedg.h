@@ -104,6 +104,52 @@ typedef struct wedg_ws wedg_ws;
 int wedg_create(const wedg_config *cfg, const wedg_pre *pre, wedg_ws **out);
 void wedg_destroy(wedg_ws *ws);
 
+/* The same workspace with `pre`'s large arrays built on the device (no counterpart in the reference,
+ * whose precompute, src/solver.jl:428-770, builds them on the host). The caller evaluates the
+ * coefficient functions at the point grids and passes those values; the device then forms what
+ * precompute forms from them: the element matrices c²W, αW (or the constant-coefficient data) and
+ * their packed inverses, the one-sided face values of c, α, β with the reference's jump test
+ * (src/solver.jl:371-408, step δ = 2^-40, tolerance 1e-8 plus jump_scale), the face arrays and jump
+ * terms of _rhs_data (:698-770), the projections Π and the source projection (:647-662, 762-764),
+ * and 2β at the mass points. From `pre` only the 1D operators (w ... W2d_h) and the boundary data
+ * (bcB_sp ... bcR_spx) are read. The one-sided face kernel is chosen from the device's jump test
+ * (wedg_one_sided reports it). On an error, msg (if not NULL) receives the reason, including the
+ * reference's refusal of jumping coefficients in :mms mode (src/solver.jl:745-747). */
+typedef struct wedg_face_values {
+  const double *at, *lo, *hi; /* the value at each face point and δ below (left of) and above (right of) it,
+                                 the reference's array of one face family: horizontal faces (q_u1, N+1, N),
+                                 face row jf at y = jf h; vertical faces (q_u1, N, N+1), face column kf
+                                 at x = kf h. The values δ outside the domain are not read: pass the
+                                 value at the face there, as the reference does. */
+  double jump_scale;          /* the family's s = 1e-8 max|value at ±δ| of src/solver.jl:387 */
+  double value;               /* with at = NULL: the family is this constant everywhere */
+} wedg_face_values;
+typedef struct wedg_points {
+  const double *c_q, *alpha_q;          /* c and α at the u-points, (N, N, q_u1, q_u1): [j, k, r, s] at
+                                           (x_s of column k, y_r of row j) */
+  const double *beta_h;                 /* β at the high-order points, (N, N, q_high, q_high) */
+  double c_value, alpha_value, beta_value; /* a coefficient whose array is NULL is this constant */
+  wedg_face_values hc, ha, hb;          /* c, α, β on the horizontal faces */
+  wedg_face_values vc, va, vb;          /* c, α, β on the vertical faces */
+  wedg_face_values hg0, vg0;            /* ∂u0/∂y on the horizontal and ∂u0/∂x on the vertical faces
+                                           (src/solver.jl:554-568); unused in source mode */
+  const double *sp_h, *cdiv_h, *ddiv_h; /* at the high-order points: Φ and the two divergence terms of the
+                                           manufactured solution (mms), the c²-term alone (initial value);
+                                           unused in source mode */
+  const double *xloc_h, *yloc_h;        /* (N, q_high): the high-order points of the columns and rows
+                                           (source mode) */
+  double src_amp, src_x0, src_y0, src_r0; /* the GaussianSource's profile (source mode) */
+} wedg_points;
+int wedg_create_points(const wedg_config *cfg, const wedg_pre *pre, const wedg_points *pts, char *msg, size_t msg_len,
+                       wedg_ws **out);
+/* 1 if the workspace uses the one-sided face kernel (pre.one_sided), 0 if not. */
+int wedg_one_sided(const wedg_ws *ws);
+/* A device array of the workspace in the reference's layout of the `pre` array of that name (for checks
+ * of the device-built arrays): hc2 haf hcf hbf hc2m hafm hJC and the v-face arrays, PiSP PiBSP2 PiCdiv
+ * PiDdiv src_projE, beta_hq; Cw, Aw (general kernels); c2e, ae (c² and α per element, constant-coefficient
+ * kernels). count must be the array's size; arrays the workspace does not hold are refused. */
+int wedg_export(const wedg_ws *ws, const char *name, double *out, size_t count);
+
 /* edg_rhs!(ws, u, v, t, N, h, pre) of src/rhs.jl:490-550: ut, vt receive the
  * right-hand side. Shapes are checked as src/rhs.jl:500-503 does. */
 int wedg_rhs(wedg_ws *ws, const double *u, const double *v, double t, double *ut, double *vt,

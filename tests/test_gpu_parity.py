@@ -508,3 +508,25 @@ def test_headline_front_state_rk4_step_against_oracle(gpu):
     ow = OracleWorkspace(po)
     ow.rk4_step(u, v, bench.T0, dt)
     assert rel_max((u, v), (ug, vg)) < TOL, rel_max((u, v), (ug, vg))
+
+
+def test_rk4_steps_common_count_against_oracle(gpu):
+    """The reference's Chebyshev policy over RK4 steps: every element of a stage takes that stage's
+    largest count (src/rhs.jl:911-918), which changes from stage to stage as v_h changes. Three RK4
+    steps from a state whose counts differ widely over the elements, against the oracle's."""
+    rng = np.random.default_rng(61)
+    N = 9
+    co = oc.replace_coefficients(oc.paper_coefficients(), beta=8.0)
+    pp, po = _pair(4, N, coefficients=co, mode="source")
+    u = np.asfortranarray(1e-3 * rng.standard_normal((N, N, pp["qu1"], pp["qu1"])))
+    v = np.asfortranarray(1e-4 * rng.standard_normal((N, N, pp["qv1"], pp["qv1"])))
+    v[:, 0:2, 1, 0] = 0.04
+    uo, vo = u.copy(order="F"), v.copy(order="F")
+    ow = OracleWorkspace(po)
+    ws = W.Workspace(pp, N, cheb_steps="common_max")
+    dt = (1.0 / N) / (10 * 16)
+    for k in range(3):
+        ow.rk4_step(uo, vo, 0.1 + k * dt, dt)
+        W.rk4_step_(u, v, 0.1 + k * dt, dt, N, 1.0 / N, pp, ws)
+    assert ws.stats()["cheb_steps_max"] > 20
+    assert rel_max((uo, vo), (u, v)) < TOL, rel_max((uo, vo), (u, v))
