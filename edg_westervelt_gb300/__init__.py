@@ -7,7 +7,7 @@ A GPU (sm_103a, FP64) drop-in for the reference's ``Workspace``,
 names (``edg_rhs_`` / ``rk4_step_`` stand for Julia's ``edg_rhs!`` /
 ``rk4_step!``) and argument meanings.
 """
-from .coefficients import (Coefficients, GaussianSource, constant_coefficients, flux_parameters,
+from .coefficients import (Coefficients, GaussianSource, cell_coefficients, constant_coefficients, flux_parameters,
                            paper_coefficients, replace_coefficients)
 from .precompute import precompute
 from .quadrature import GaussQCofs, GradJacobiP, JacobiP
@@ -19,4 +19,4 @@ __all__ = ["solve", "precompute", "edg_rhs", "edg_rhs_", "rk4_step", "rk4_step_"
            "difference_norms", "flux_parameters", "GaussianSource", "Coefficients", "paper_coefficients",
            "replace_coefficients", "constant_coefficients", "JacobiP", "GradJacobiP", "GaussQCofs",
            "ErrorException", "DimensionMismatch", "misfit", "misfit_gradient", "misfit_gradients",
-           "piecewise_coefficients", "rk4_adjoint_forward_many", "rk4_adjoint_reverse_many"]
+           "piecewise_coefficients", "cell_coefficients", "rk4_adjoint_forward_many", "rk4_adjoint_reverse_many"]

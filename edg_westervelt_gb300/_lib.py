@@ -59,10 +59,17 @@ class FaceValues(ctypes.Structure):
     _fields_ = [("at", _D), ("lo", _D), ("hi", _D), ("jump_scale", ctypes.c_double), ("value", ctypes.c_double)]
 
 
+class CellTable(ctypes.Structure):
+    """wedg_cell_table (include/wedg.h)."""
+    _fields_ = [("values", _D), ("rows", ctypes.c_int32), ("cols", ctypes.c_int32)]
+
+
 class Points(ctypes.Structure):
     """wedg_points (include/wedg.h)."""
     _fields_ = ([("c_q", _D), ("alpha_q", _D), ("beta_h", _D), ("c_value", ctypes.c_double),
-                 ("alpha_value", ctypes.c_double), ("beta_value", ctypes.c_double)]
+                 ("alpha_value", ctypes.c_double), ("beta_value", ctypes.c_double),
+                 ("c_cells", CellTable), ("alpha_cells", CellTable), ("beta_cells", CellTable),
+                 ("xloc", _D), ("yloc", _D)]
                 + [(n, FaceValues) for n in ("hc", "ha", "hb", "vc", "va", "vb", "hg0", "vg0")]
                 + [(n, _D) for n in ("sp_h", "cdiv_h", "ddiv_h", "xloc_h", "yloc_h")]
                 + [(n, ctypes.c_double) for n in ("src_amp", "src_x0", "src_y0", "src_r0")])

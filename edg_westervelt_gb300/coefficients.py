@@ -53,6 +53,28 @@ def _zero(x, y):
     return np.zeros(np.shape(x)) if np.ndim(x) else 0.0
 
 
+class _Cells:
+    """A function constant on the cells of an m × n grid of (0,1)²: tab[row, column], row from y,
+    column from x (the point on a cell boundary belongs to the cell above / right of it)."""
+
+    def __init__(self, tab):
+        self.tab = np.ascontiguousarray(tab, dtype=np.float64)
+        self.m, self.n = self.tab.shape
+
+    def __call__(self, x, y):
+        x = np.asarray(x, dtype=np.float64)
+        y = np.asarray(y, dtype=np.float64)
+        return self.tab[np.clip(np.floor(self.m * y).astype(int), 0, self.m - 1),
+                        np.clip(np.floor(self.n * x).astype(int), 0, self.n - 1)]
+
+
+def cell_coefficients(c, alpha, beta):
+    """Coefficients constant on the cells of an m × n grid of (0,1)²: c, alpha, beta are (m, n)
+    arrays indexed [row (y), column (x)] of c, α and β; the derivatives of c and α vanish inside
+    the cells. A GPU workspace built from point values looks these tables up on the device."""
+    return Coefficients(_Cells(c), _zero, _zero, _Cells(alpha), _zero, _zero, _Cells(beta))
+
+
 def replace_coefficients(coef, c=None, alpha=None, beta=None):
     """Copy of coef with every coefficient given as a number replaced by that
     constant and its derivatives by zero (src/coefficients.jl:66-76)."""

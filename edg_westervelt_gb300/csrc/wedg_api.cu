@@ -1292,7 +1292,8 @@ namespace {
 // (constant per element or not), mass solver and 1D operators -- and share one multi-instance
 // launch per kernel and stage, with the bucket's launch shape: threads per block of k_prep and of
 // the mass solves, and `persist` (0: one block per virtual block; p > 0: a persistent grid of p
-// times the blocks the SMs hold at once)
+// times the blocks the SMs hold at once). With `split` the bucket's instances are launched one by
+// one instead, each on its own stream forked from the bucket's (the single-instance kernels).
 struct BatchBucket {
   std::vector<int> ids;   // instances, largest mesh first
   Launchers L;
@@ -1300,8 +1301,9 @@ struct BatchBucket {
   int nu = 0, nv = 0;
   bool fast = false, cg = false;
   int prep_threads = 128, mass_threads = CHEB_THREADS, persist = 0;
+  bool split = false;
   cudaStream_t st = nullptr;
-  cudaEvent_t join = nullptr;
+  cudaEvent_t join = nullptr, fork = nullptr;
   StepFlags *d_flags = nullptr;   // per instance of the bucket, for k_step_done_m
   FinalArgs *d_final = nullptr;   // per instance, for k_rk4_final_m (CG)
 };
@@ -1328,6 +1330,7 @@ struct wedg_batch {
   std::vector<double *> d_tf;
   double *h_tf = nullptr;                           // pinned: 2 halves × instances × one chunk
   std::vector<void *> dmem;                         // device arrays of the buckets
+  std::vector<cudaEvent_t> ijoin;                   // per instance: the end of its launches (split buckets)
   ~wedg_batch() {
     if (main) cudaStreamSynchronize(main);
     for (BatchBucket &k : buckets)
@@ -1339,8 +1342,10 @@ struct wedg_batch {
     if (h_tf) cudaFreeHost(h_tf);
     for (BatchBucket &k : buckets) {
       if (k.join) cudaEventDestroy(k.join);
+      if (k.fork) cudaEventDestroy(k.fork);
       if (k.st) cudaStreamDestroy(k.st);
     }
+    for (cudaEvent_t e : ijoin) cudaEventDestroy(e);
     for (cudaEvent_t e : half_done)
       if (e) cudaEventDestroy(e);
     if (fork) cudaEventDestroy(fork);
@@ -1367,6 +1372,31 @@ int bucket_grid(const wedg_batch *b, const BatchBucket &k, int total, int reside
 int enqueue_bucket_step(wedg_batch *b, BatchBucket &k, double *const *u, double *const *v, const double *t,
                         const double *dt, int stop_nonfinite, bool tables, long long tf_n) {
   const int n = (int)k.ids.size();
+  if (k.split) {
+    // every instance on its own stream, forked from and joined to the bucket's
+    cudaError_t e = cudaEventRecord(k.fork, k.st);
+    for (int x = 0; x < n && e == cudaSuccess; ++x) {
+      const int i = k.ids[x];
+      wedg_ws *w = b->ws[i];
+      e = cudaStreamWaitEvent(w->stream, k.fork, 0);
+      if (e != cudaSuccess) break;
+      const bool timing = w->timing;
+      w->timing = false;
+      const int pt = w->prep_threads, mt = w->mass_threads;
+      w->prep_threads = k.prep_threads;
+      w->mass_threads = k.mass_threads;
+      const int rc = enqueue_rk4(w, u[i], v[i], tables ? 0.0 : t[i], dt[i], stop_nonfinite,
+                                 tables ? b->d_tf[i] : nullptr, tables ? tf_n : 0);
+      w->prep_threads = pt;
+      w->mass_threads = mt;
+      w->timing = timing;
+      if (rc) return rc;
+      e = cudaEventRecord(b->ijoin[i], w->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(k.st, b->ijoin[i], 0);
+    }
+    if (e != cudaSuccess) return cuda_fail(b->ws[k.ids[0]], e, "split bucket launch");
+    return WEDG_OK;
+  }
   const int BT = stage_threads(k.nu, k.nv, k.fast);
   const int TPW = 32 / (qhigh(k.nu, k.nv) / 2 + (qhigh(k.nu, k.nv) & 1));
   const int mass_tile = (k.mass_threads / 32) * TPW;
@@ -1755,7 +1785,11 @@ int wedg_create_points(const wedg_config *cfg, const wedg_pre *pre, const wedg_p
   if (!cfg->src_on && ((pts->hg0.at && (!pts->hg0.lo || !pts->hg0.hi)) || (pts->vg0.at && (!pts->vg0.lo || !pts->vg0.hi)) ||
                        !pts->cdiv_h || (cfg->mms_on && (!pts->sp_h || !pts->ddiv_h))))
     return refuse(WEDG_ERR_ARGUMENT, "null initial-data or manufactured-solution arrays");
-  if (cfg->src_on && (!pts->xloc_h || !pts->yloc_h)) return refuse(WEDG_ERR_ARGUMENT, "null high-order points");
+  if (!pts->xloc_h || !pts->yloc_h) return refuse(WEDG_ERR_ARGUMENT, "null high-order points");
+  const wedg_cell_table *tabs[3] = {&pts->c_cells, &pts->alpha_cells, &pts->beta_cells};
+  for (const wedg_cell_table *t : tabs)
+    if (t->values && (t->rows < 1 || t->cols < 1 || !pts->xloc || !pts->yloc))
+      return refuse(WEDG_ERR_ARGUMENT, "a cell table needs its sizes and the points xloc, yloc");
   wedg_ws *ws = nullptr;
   if ((rc = create_begin(cfg, pre, &ws))) return refuse(rc, "the quadrature rules are not mirror-symmetric");
   const int N = ws->N, E = ws->E, nv = ws->nv, nq = ws->nq, qh = ws->qh;
@@ -1768,7 +1802,9 @@ int wedg_create_points(const wedg_config *cfg, const wedg_pre *pre, const wedg_p
   };
   // ---- the point arrays on the device, freed when this call returns
   RunBuffers T;
-  double *d_c, *d_a, *d_b, *d_w, *d_Ph, *d_Wh, *d_face[6][3];
+  double *d_c, *d_a, *d_b, *d_w, *d_Ph, *d_Wh, *d_face[6][3], *d_tab[3] = {nullptr, nullptr, nullptr};
+  double *d_xq = nullptr, *d_yq = nullptr;
+  unsigned long long *d_max;
   double *d_g0[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   double *d_sp = nullptr, *d_cdiv = nullptr, *d_ddiv = nullptr, *d_xh = nullptr, *d_yh = nullptr;
   unsigned *d_flags;
@@ -1804,15 +1840,24 @@ int wedg_create_points(const wedg_config *cfg, const wedg_pre *pre, const wedg_p
     if (cfg->mms_on &&
         ((ce = put(&d_sp, pts->sp_h, nH)) != cudaSuccess || (ce = put(&d_ddiv, pts->ddiv_h, nH)) != cudaSuccess))
       return cuda_refuse(ce);
-  } else if ((ce = put(&d_xh, pts->xloc_h, (size_t)N * qh)) != cudaSuccess ||
-             (ce = put(&d_yh, pts->yloc_h, (size_t)N * qh)) != cudaSuccess) {
-    return cuda_refuse(ce);
   }
+  if ((ce = put(&d_xh, pts->xloc_h, (size_t)N * qh)) != cudaSuccess ||
+      (ce = put(&d_yh, pts->yloc_h, (size_t)N * qh)) != cudaSuccess ||
+      (pts->xloc && (ce = put(&d_xq, pts->xloc, (size_t)N * nq)) != cudaSuccess) ||
+      (pts->yloc && (ce = put(&d_yq, pts->yloc, (size_t)N * nq)) != cudaSuccess) ||
+      (ce = T.get(&d_max, 1)) != cudaSuccess)
+    return cuda_refuse(ce);
+  for (int f = 0; f < 3; ++f)
+    if (tabs[f]->values && (ce = put(&d_tab[f], tabs[f]->values, (size_t)tabs[f]->rows * tabs[f]->cols)) != cudaSuccess)
+      return cuda_refuse(ce);
+  const PtsGrid grid{d_xq, d_yq, d_xh, d_yh, N, 1.0 / N};
   const int tb = 128, eb = (E + tb - 1) / tb;
   // ---- constant coefficients per element? (the test wedg_create applies to pre's Cw, Aw)
   unsigned flags = 0;
-  const PtsField fc{d_c, pts->c_value}, fa{d_a, pts->alpha_value}, fb{d_b, pts->beta_value};
-  k_pts_check<<<eb, tb>>>(fc, fa, d_w, nq, E, d_flags);
+  const PtsField fc{d_c, pts->c_value, d_c ? nullptr : d_tab[0], tabs[0]->rows, tabs[0]->cols};
+  const PtsField fa{d_a, pts->alpha_value, d_a ? nullptr : d_tab[1], tabs[1]->rows, tabs[1]->cols};
+  const PtsField fb{d_b, pts->beta_value, d_b ? nullptr : d_tab[2], tabs[2]->rows, tabs[2]->cols};
+  k_pts_check<<<eb, tb>>>(fc, fa, grid, d_w, nq, E, d_flags);
   if ((ce = cudaGetLastError()) != cudaSuccess ||
       (ce = cudaMemcpy(&flags, d_flags, sizeof flags, cudaMemcpyDeviceToHost)) != cudaSuccess)
     return cuda_refuse(ce);
@@ -1827,7 +1872,7 @@ int wedg_create_points(const wedg_config *cfg, const wedg_pre *pre, const wedg_p
     if (dalloc(ws, &Cw, nE) || dalloc(ws, &Aw, nE)) return cuda_refuse(cudaErrorMemoryAllocation);
     F.Cw = Cw; F.Aw = Aw;
   }
-  k_pts_elem<<<eb, tb>>>(fc, fa, d_w, nq, E, c2e, ae, ic2e, Cw, Aw);
+  k_pts_elem<<<eb, tb>>>(fc, fa, grid, d_w, nq, E, c2e, ae, ic2e, Cw, Aw);
   if ((ce = cudaGetLastError()) != cudaSuccess) return cuda_refuse(ce);
   if (!fast && (rc = device_inverses(ws, pre))) return refuse(rc, "a stiffness matrix is not positive definite");
   // ---- face arrays, jump terms, one-sided test
@@ -1836,15 +1881,36 @@ int wedg_create_points(const wedg_config *cfg, const wedg_pre *pre, const wedg_p
     for (int x = 0; x < 7; ++x)
       if (dalloc(ws, &fo[h][x], nF)) return cuda_refuse(cudaErrorMemoryAllocation);
   if ((ce = cudaMemset(d_flags, 0, sizeof(unsigned))) != cudaSuccess) return cuda_refuse(ce);
+  // a family: its arrays, or (no arrays) its table with the tolerance term from the device, or its constant
+  auto family = [&](int f, int h, PtsFace &out) -> cudaError_t {
+    const wedg_face_values *v = fam[3 * h + f];
+    out = PtsFace{d_face[3 * h + f][0], d_face[3 * h + f][1], d_face[3 * h + f][2], v->jump_scale, v->value,
+                  nullptr, 0, 0};
+    if (v->at || !d_tab[f]) return cudaSuccess;
+    out.tab = d_tab[f];
+    out.m = tabs[f]->rows;
+    out.n = tabs[f]->cols;
+    unsigned long long bits = 0;
+    cudaError_t e = cudaMemset(d_max, 0, sizeof bits);
+    if (e == cudaSuccess) {
+      k_pts_face_max<<<(int)std::min<size_t>((2 * nF + 255) / 256, 152 * 16), 256>>>(N, nq, grid, out, d_max);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&bits, d_max, sizeof bits, cudaMemcpyDeviceToHost);
+    double mx;
+    std::memcpy(&mx, &bits, sizeof mx);
+    out.s = 1e-8 * mx;        // JUMP_TOL · max over both orientations (src/solver.jl:387)
+    return e;
+  };
   for (int h = 0; h < 2; ++h) {
-    const int b = 3 * h;
     const wedg_face_values &g = h == 0 ? pts->hg0 : pts->vg0;
-    const PtsFace pc{d_face[b][0], d_face[b][1], d_face[b][2], fam[b]->jump_scale, fam[b]->value};
-    const PtsFace pa{d_face[b + 1][0], d_face[b + 1][1], d_face[b + 1][2], fam[b + 1]->jump_scale, fam[b + 1]->value};
-    const PtsFace pb{d_face[b + 2][0], d_face[b + 2][1], d_face[b + 2][2], fam[b + 2]->jump_scale, fam[b + 2]->value};
-    const PtsFace pg{d_g0[h][0], d_g0[h][1], d_g0[h][2], g.jump_scale, cfg->src_on ? 0.0 : g.value};
+    PtsFace pc, pa, pb;
+    if ((ce = family(0, h, pc)) != cudaSuccess || (ce = family(1, h, pa)) != cudaSuccess ||
+        (ce = family(2, h, pb)) != cudaSuccess)
+      return cuda_refuse(ce);
+    const PtsFace pg{d_g0[h][0], d_g0[h][1], d_g0[h][2], g.jump_scale, cfg->src_on ? 0.0 : g.value, nullptr, 0, 0};
     const PtsFaceOut o{fo[h][0], fo[h][1], fo[h][2], fo[h][3], fo[h][4], fo[h][5], fo[h][6]};
-    k_pts_faces<<<(int)std::min<size_t>((nF + 255) / 256, 152 * 16), 256>>>(N, nq, h == 0, pc, pa, pb, pg, o,
+    k_pts_faces<<<(int)std::min<size_t>((nF + 255) / 256, 152 * 16), 256>>>(N, nq, h == 0, grid, pc, pa, pb, pg, o,
                                                                            d_flags);
   }
   if ((ce = cudaGetLastError()) != cudaSuccess ||
@@ -1864,29 +1930,29 @@ int wedg_create_points(const wedg_config *cfg, const wedg_pre *pre, const wedg_p
   // ---- projections and 2β
   auto proj = [&](double **dst, PtsProj p) -> cudaError_t {
     if (dalloc(ws, dst, (size_t)nv * nv * E)) return cudaErrorMemoryAllocation;
-    k_pts_proj<<<eb, tb>>>(N, qh, nv, d_Ph, d_Wh, p, *dst);
+    k_pts_proj<<<eb, tb>>>(grid, qh, nv, d_Ph, d_Wh, p, *dst);
     return cudaGetLastError();
   };
   double *pisp = nullptr, *pib = nullptr, *pic = nullptr, *pid = nullptr, *psrc = nullptr, *beta2 = nullptr;
   if (cfg->mms_on) {
-    if ((ce = proj(&pisp, PtsProj{0, d_sp, PtsField{}, nullptr, nullptr, 0, 0, 0, 0})) != cudaSuccess ||
-        (ce = proj(&pib, PtsProj{1, d_sp, fb, nullptr, nullptr, 0, 0, 0, 0})) != cudaSuccess ||
-        (ce = proj(&pid, PtsProj{0, d_ddiv, PtsField{}, nullptr, nullptr, 0, 0, 0, 0})) != cudaSuccess)
+    if ((ce = proj(&pisp, PtsProj{0, d_sp, PtsField{}, 0, 0, 0, 0})) != cudaSuccess ||
+        (ce = proj(&pib, PtsProj{1, d_sp, fb, 0, 0, 0, 0})) != cudaSuccess ||
+        (ce = proj(&pid, PtsProj{0, d_ddiv, PtsField{}, 0, 0, 0, 0})) != cudaSuccess)
       return cuda_refuse(ce);
     F.PiSP = pisp; F.PiBSP2 = pib; F.PiDdiv = pid;
   }
   if (!cfg->src_on) {
-    if ((ce = proj(&pic, PtsProj{0, d_cdiv, PtsField{}, nullptr, nullptr, 0, 0, 0, 0})) != cudaSuccess)
+    if ((ce = proj(&pic, PtsProj{0, d_cdiv, PtsField{}, 0, 0, 0, 0})) != cudaSuccess)
       return cuda_refuse(ce);
     F.PiCdiv = pic;
   } else {
-    if ((ce = proj(&psrc, PtsProj{2, nullptr, PtsField{}, d_xh, d_yh, pts->src_amp, pts->src_x0, pts->src_y0,
-                                  pts->src_r0})) != cudaSuccess)
+    if ((ce = proj(&psrc, PtsProj{2, nullptr, PtsField{}, pts->src_amp, pts->src_x0, pts->src_y0, pts->src_r0})) !=
+        cudaSuccess)
       return cuda_refuse(ce);
     F.srcP = psrc;
   }
   if (dalloc(ws, &beta2, nH)) return cuda_refuse(cudaErrorMemoryAllocation);
-  k_pts_scale<<<(int)std::min<size_t>((nH + 255) / 256, 152 * 16), 256>>>(nH, 2.0, fb, beta2);
+  k_pts_beta2<<<(int)std::min<size_t>((nH + 255) / 256, 152 * 16), 256>>>(grid, qh, fb, beta2);
   if ((ce = cudaGetLastError()) != cudaSuccess || (ce = cudaDeviceSynchronize()) != cudaSuccess) return cuda_refuse(ce);
   F.beta2 = beta2;
   ws->cfg.one_sided = F.one_sided;
@@ -2071,8 +2137,11 @@ int wedg_batch_create(int n, wedg_ws *const *instances, wedg_batch **out) {
             cudaMallocHost(&b->h_tf, sizeof(double) * per * n) == cudaSuccess;
   for (int i = 0; i < n && ok; ++i) {
     double *d = nullptr;
+    cudaEvent_t e = nullptr;
     ok = cudaMalloc(&d, sizeof(double) * per) == cudaSuccess;
     if (ok) b->d_tf.push_back(d);
+    ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    if (ok) b->ijoin.push_back(e);
   }
   for (BatchBucket &k : b->buckets) {
     if (!ok) break;
@@ -2082,6 +2151,7 @@ int wedg_batch_create(int n, wedg_ws *const *instances, wedg_batch **out) {
     void *p = nullptr, *q = nullptr;
     ok = cudaStreamCreateWithFlags(&k.st, cudaStreamNonBlocking) == cudaSuccess &&
          cudaEventCreateWithFlags(&k.join, cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&k.fork, cudaEventDisableTiming) == cudaSuccess &&
          cudaMalloc(&p, sizeof(StepFlags) * fl.size()) == cudaSuccess &&
          cudaMalloc(&q, sizeof(FinalArgs) * fl.size()) == cudaSuccess;
     if (p) b->dmem.push_back(p);
@@ -2113,19 +2183,22 @@ int wedg_batch_get_shape(const wedg_batch *b, int bucket, wedg_batch_shape *out)
   out->fast = k.fast ? 1 : 0;
   out->prep_threads = k.prep_threads;
   out->mass_threads = k.mass_threads;
-  out->persist = k.persist;
+  out->persist = k.split ? -1 : k.persist;
   return WEDG_OK;
 }
 
 int wedg_batch_set_shape(wedg_batch *b, int bucket, int prep_threads, int mass_threads, int persist) {
   if (!b || bucket < 0 || bucket >= (int)b->buckets.size()) return WEDG_ERR_ARGUMENT;
   auto ok = [](int t) { return t >= 32 && t <= CHEB_THREADS && t % 32 == 0; };
-  if (!ok(prep_threads) || !ok(mass_threads) || persist < 0 || persist > 8) return WEDG_ERR_ARGUMENT;
+  if (!ok(prep_threads) || !ok(mass_threads) || persist < -1 || persist > 8) return WEDG_ERR_ARGUMENT;
   BatchBucket &k = b->buckets[bucket];
-  if (k.prep_threads != prep_threads || k.mass_threads != mass_threads || k.persist != persist) {
+  const bool split = persist < 0;
+  if (persist < 0) persist = 0;
+  if (k.prep_threads != prep_threads || k.mass_threads != mass_threads || k.persist != persist || k.split != split) {
     k.prep_threads = prep_threads;
     k.mass_threads = mass_threads;
     k.persist = persist;
+    k.split = split;
     ++b->shape_gen;
   }
   return WEDG_OK;
@@ -2305,18 +2378,23 @@ int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_de
   for (int q = 0; q < nb; ++q) {
     def_p[q] = b->buckets[q].prep_threads;
     def_m[q] = b->buckets[q].mass_threads;
-    def_s[q] = b->buckets[q].persist;
+    def_s[q] = b->buckets[q].split ? -1 : b->buckets[q].persist;
   }
   int rc = WEDG_OK;
   // per bucket, alone: one coordinate at a time; a candidate replaces the incumbent only when it is
   // faster in each of kTuneRepeats paired trials and its median is faster by more than 2 %
   for (int q = 0; q < nb && rc == WEDG_OK; ++q) {
     BatchBucket &k = b->buckets[q];
-    for (int c = 0; c < 3 && rc == WEDG_OK; ++c) {
-      for (int x = 0; x < 3 && rc == WEDG_OK; ++x) {
-        const int inc[3] = {k.prep_threads, k.mass_threads, k.persist};
+    // the layout first (one launch per kernel over the bucket, or per-instance launches), then the
+    // threads per block of k_prep and of the mass solves, then persistent grids
+    const int order[3] = {2, 0, 1};
+    for (int oc = 0; oc < 3 && rc == WEDG_OK; ++oc) {
+      const int c = order[oc];
+      for (int x = 0; x < (c == 2 ? 4 : 3) && rc == WEDG_OK; ++x) {
+        const int inc[3] = {k.prep_threads, k.mass_threads, k.split ? -1 : k.persist};
         int cand[3] = {inc[0], inc[1], inc[2]};
-        cand[c] = c < 2 ? kTuneThreads[x] : x;
+        cand[c] = c < 2 ? kTuneThreads[x] : x - 1;                  // persist -1 (split), 0, 1, 2
+        if (c == 2 && inc[2] < 0 && cand[2] > 0) continue;          // persistence is a merged layout's
         if (cand[c] == inc[c]) continue;
         double ti[kTuneRepeats], tc[kTuneRepeats];
         bool wins = true;
@@ -2343,7 +2421,7 @@ int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_de
     for (int q = 0; q < nb; ++q) {
       tp[q] = b->buckets[q].prep_threads;
       tm[q] = b->buckets[q].mass_threads;
-      ts[q] = b->buckets[q].persist;
+      ts[q] = b->buckets[q].split ? -1 : b->buckets[q].persist;
     }
     auto apply = [&](const std::vector<int> &p, const std::vector<int> &m, const std::vector<int> &s_) {
       for (int q = 0; q < nb; ++q) wedg_batch_set_shape(b, q, p[q], m[q], s_[q]);

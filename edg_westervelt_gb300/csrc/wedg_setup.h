@@ -24,23 +24,46 @@ enum { PTS_NOT_CONSTANT = 1, PTS_JUMPS = 2, PTS_JC = 4 };
 
 // The test of src/solver.jl's element matrices for the constant-coefficient kernels, from c and α
 // at the u-points: Cw = c² W, Aw = α W with W = w ⊗ w (wedg_create's test on pre's Cw, Aw)
-// A point array, or the one value of a field that is constant (p null)
+// A coefficient at the points: an array of its values there, a constant (p and tab null), or a
+// table of values on an m × n grid of cells of the unit square, row-major [row (y)][column (x)],
+// looked up as the host's piecewise functions do: row = clip(floor(m y), 0, m-1), column likewise
 struct PtsField {
   const double *p;
   double value;
-  __device__ __forceinline__ double operator[](size_t i) const { return p ? p[i] : value; }
+  const double *tab;
+  int m, n;
+  __device__ __forceinline__ double cell(double x, double y) const {
+    int r = (int)floor((double)m * y), c = (int)floor((double)n * x);
+    r = r < 0 ? 0 : r > m - 1 ? m - 1 : r;
+    c = c < 0 ? 0 : c > n - 1 ? n - 1 : c;
+    return tab[r * n + c];
+  }
+  // at point i of an element array, whose coordinates are (x, y)
+  __device__ __forceinline__ double at(size_t i, double x, double y) const {
+    return p ? p[i] : tab ? cell(x, y) : value;
+  }
 };
-__global__ void k_pts_check(PtsField c_q, PtsField a_q, const double *w, int nq, int E, unsigned *flags);
+// The coordinates of the points: the u-points of the columns (xq) and rows (yq), (N, nq), and the
+// high-order points (xh, yh), (N, qh), column-major; h = 1/N
+struct PtsGrid {
+  const double *xq, *yq, *xh, *yh;
+  int N;
+  double h;
+};
+__global__ void k_pts_check(PtsField c_q, PtsField a_q, PtsGrid g, const double *w, int nq, int E, unsigned *flags);
 // c² and α per element (and 1/c²) for the constant-coefficient kernels, or Cw, Aw in the device
 // layout [(r + nq s) E + e] for the general kernels (null outputs are skipped)
-__global__ void k_pts_elem(PtsField c_q, PtsField a_q, const double *w, int nq, int E, double *c2e, double *ae,
-                           double *ic2e, double *Cw, double *Aw);
+__global__ void k_pts_elem(PtsField c_q, PtsField a_q, PtsGrid g, const double *w, int nq, int E, double *c2e,
+                           double *ae, double *ic2e, double *Cw, double *Aw);
 
 // One family of face values (src/solver.jl:371-408): the value at the face point and δ on either
-// side, and the tolerance term s of the family; a constant family (at null) is `value` everywhere
+// side, and the tolerance term s of the family; a constant family (at and tab null) is `value`
+// everywhere; a table family (tab) is looked up at the face points and δ on either side
 struct PtsFace {
   const double *at, *lo, *hi;
   double s, value;
+  const double *tab;
+  int m, n;
 };
 // The face arrays of `pre` in the kernels' layouts from the one-sided values of c, α, β and of the
 // data derivative g0 (src/solver.jl:538-568, 716-770); horizontal when hor (face row jf, column k),
@@ -48,8 +71,11 @@ struct PtsFace {
 struct PtsFaceOut {
   double *c2, *af, *cf, *bf, *c2m, *afm, *JC;
 };
-__global__ void k_pts_faces(int N, int nq, bool hor, PtsFace c, PtsFace a, PtsFace b, PtsFace g0, PtsFaceOut o,
-                            unsigned *flags);
+__global__ void k_pts_faces(int N, int nq, bool hor, PtsGrid g, PtsFace c, PtsFace a, PtsFace b, PtsFace g0,
+                            PtsFaceOut o, unsigned *flags);
+// max |value| of a table family at the points δ off the faces inside the domain (the values
+// side_values takes the tolerance term from), as the bits of the non-negative double, atomicMax
+__global__ void k_pts_face_max(int N, int nq, PtsGrid g, PtsFace f, unsigned long long *out);
 
 // The projections Π(X)[a, b] = Σ_r Σ_s P_h[r, a] W[r, s] X[r, s] P_h[s, b] of the element data
 // at the high-order points (src/solver.jl:704-764), into [(a + nv b) E + e]: kind 0 X = x1,
@@ -59,12 +85,11 @@ struct PtsProj {
   int kind;
   const double *x1;
   PtsField x2;
-  const double *xh, *yh;
   double amp, x0, y0, r0;
 };
-__global__ void k_pts_proj(int N, int qh, int nv, const double *Ph, const double *Wh, PtsProj p, double *out);
+__global__ void k_pts_proj(PtsGrid g, int qh, int nv, const double *Ph, const double *Wh, PtsProj p, double *out);
 
-// y = a x elementwise
-__global__ void k_pts_scale(size_t n, double a, PtsField x, double *y);
+// 2β at the high-order points, [(r + qh s) E + e]
+__global__ void k_pts_beta2(PtsGrid g, int qh, PtsField b, double *out);
 
 }  // namespace wedg

@@ -15,7 +15,7 @@ import math
 
 import numpy as np
 
-from .coefficients import (Coefficients, GaussianSource, _Const, _sym, boundary_sides, flux_parameters,
+from .coefficients import (Coefficients, GaussianSource, _Cells, _Const, _sym, boundary_sides, flux_parameters,
                            paper_coefficients)
 from .quadrature import GaussQCofs, GradJacobiP, JacobiP
 
@@ -541,13 +541,19 @@ def precompute_points(q, N, *, mixed=True, flux="upwind", flux_params=None, sigm
         return np.ascontiguousarray(evaluate(f, *XY)).T                # (N, N, n, n), Fortran-contiguous
     XQ, XH = grid(xloc, yloc), grid(xloc_h, yloc_h)
 
-    # a constant coefficient (constant_coefficients, replace_coefficients) is passed as its value:
-    # the device fills it in (its face values are the constant, continuous)
+    # a constant coefficient (constant_coefficients, replace_coefficients) is passed as its value and
+    # a table of cells (cell_coefficients) as the table: the device evaluates both at every point
     def field(f, XY):
-        return (None, f.val) if isinstance(f, _Const) else (at(f, XY), 0.0)
+        if isinstance(f, _Const):
+            return dict(value=f.val)
+        if isinstance(f, _Cells):
+            return dict(table=f.tab)
+        return dict(array=at(f, XY))
 
     def face(f):
-        return (None, f.val) if isinstance(f, _Const) else _face_values(f, xloc, yloc, N, h)
+        if isinstance(f, (_Const, _Cells)):
+            return None
+        return _face_values(f, xloc, yloc, N, h)
     pts = dict(c_q=field(C.c, XQ), alpha_q=field(C.alpha, XQ), beta_h=field(C.beta, XH),
                faces={key: face(fun) for key, fun in (("c", C.c), ("a", C.alpha), ("b", C.beta))})
     src_on = mode == "source"
@@ -617,8 +623,9 @@ def precompute_points(q, N, *, mixed=True, flux="upwind", flux_params=None, sigm
         bcd["bc_rgt_spx"] = evaluate(ip["u0_x"], zx + 1.0, yloc)
     names = dict(bcB_sp="bc_bot_sp", bcB_spy="bc_bot_spy", bcT_sp="bc_top_sp", bcT_spy="bc_top_spy",
                  bcL_sp="bc_lft_sp", bcL_spx="bc_lft_spx", bcR_sp="bc_rgt_sp", bcR_spx="bc_rgt_spx")
-    pts["source"] = dict(xloc_h=xloc_h, yloc_h=yloc_h, amp=float(source.amplitude), x0=float(source.x0[0]),
-                         y0=float(source.x0[1]), r0=float(source.r0))
+    pts["source"] = dict(amp=float(source.amplitude), x0=float(source.x0[0]), y0=float(source.x0[1]),
+                         r0=float(source.r0))
+    pts["grid"] = dict(xloc=xloc, yloc=yloc, xloc_h=xloc_h, yloc_h=yloc_h)
 
     pre = dict(
         N=N, qu1=qu1, qv1=qv1, q_high=q_high, omega=omega, w=w,

@@ -156,20 +156,9 @@ def piecewise_coefficients(c2, alpha, beta):
     """Coefficients constant on the cells of an m × n grid of (0,1)²: c2, alpha, beta are (m, n)
     arrays indexed [row (y), column (x)] of c², α and β (the parameter fields of the misfit
     gradient). The derivatives of c and α vanish inside the cells."""
-    from .coefficients import Coefficients
+    from .coefficients import cell_coefficients
     c2, alpha, beta = (np.asarray(a, dtype=np.float64) for a in (c2, alpha, beta))
-    m, n = c2.shape
-
-    def cell(tab):
-        def f(x, y):
-            x = np.asarray(x, dtype=np.float64)
-            y = np.asarray(y, dtype=np.float64)
-            return tab[np.clip(np.floor(m * y).astype(int), 0, m - 1), np.clip(np.floor(n * x).astype(int), 0, n - 1)]
-        return f
-
-    def zero(x, y):
-        return np.zeros(np.broadcast(np.asarray(x), np.asarray(y)).shape)
-    return Coefficients(cell(np.sqrt(c2)), zero, zero, cell(alpha), zero, zero, cell(beta))
+    return cell_coefficients(np.sqrt(c2), alpha, beta)
 
 
 def _misfit_problem(q, N, T, c2, alpha, beta, dt_fac, kw):
@@ -178,7 +167,8 @@ def _misfit_problem(q, N, T, c2, alpha, beta, dt_fac, kw):
     m, n = c2.shape
     if N % m or N % n:
         raise ErrorException(f"the {m} × {n} parameter cells must be unions of elements (N = {N})")
-    pre, _ = precompute(q, N, mode="source", coefficients=piecewise_coefficients(c2, alpha, beta), **kw)
+    pre, _ = precompute(q, N, mode="source", coefficients=piecewise_coefficients(c2, alpha, beta), target="device",
+                        **kw)
     dt = (1.0 / N) / (dt_fac * q ** 2)
     nsteps = int(round(T / dt))
     return pre, Workspace(pre, N), T / nsteps, nsteps, (m, n)

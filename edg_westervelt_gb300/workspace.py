@@ -66,19 +66,26 @@ def _points_struct(points, keep):
         a = _f64(a)
         keep[id(a)] = a
         return _ptr(a)
-    for name, val in (("c_q", points["c_q"]), ("alpha_q", points["alpha_q"]), ("beta_h", points["beta_h"])):
-        setattr(P, name, arr(val[0]))
-        setattr(P, {"c_q": "c_value", "alpha_q": "alpha_value", "beta_h": "beta_value"}[name], float(val[1]))
+    for name, value, cells in (("c_q", "c_value", "c_cells"), ("alpha_q", "alpha_value", "alpha_cells"),
+                               ("beta_h", "beta_value", "beta_cells")):
+        f = points[name]
+        setattr(P, name, arr(f.get("array")))
+        setattr(P, value, float(f.get("value", 0.0)))
+        if "table" in f:
+            t = getattr(P, cells)
+            t.values = arr(np.asfortranarray(f["table"].T))       # row-major (m, n) bytes
+            t.rows, t.cols = f["table"].shape
 
     def face(fv, values, scale=None):
         if values is None:                      # a constant family: (None, value)
             return
         fv.at, fv.lo, fv.hi = (arr(x) for x in values)
         fv.jump_scale = float(scale)
-    for key, (hn, vn) in (("c", ("hc", "vc")), ("a", ("ha", "va")), ("b", ("hb", "vb"))):
+    for key, fld, (hn, vn) in (("c", "c_q", ("hc", "vc")), ("a", "alpha_q", ("ha", "va")),
+                               ("b", "beta_h", ("hb", "vb"))):
         fam = points["faces"][key]
-        if fam[0] is None:
-            getattr(P, hn).value = getattr(P, vn).value = float(fam[1])
+        if fam is None:                         # a constant (its value) or a table (looked up on the device)
+            getattr(P, hn).value = getattr(P, vn).value = float(points[fld].get("value", 0.0))
         else:
             out, s = fam
             face(getattr(P, hn), out["h"], s)
@@ -89,8 +96,9 @@ def _points_struct(points, keep):
         face(P.vg0, vv, vs)
     for name in ("sp_h", "cdiv_h", "ddiv_h"):
         setattr(P, name, arr(points.get(name)))
-    src = points["source"]
-    P.xloc_h, P.yloc_h = arr(src["xloc_h"]), arr(src["yloc_h"])
+    src, grid = points["source"], points["grid"]
+    P.xloc, P.yloc = arr(grid["xloc"]), arr(grid["yloc"])
+    P.xloc_h, P.yloc_h = arr(grid["xloc_h"]), arr(grid["yloc_h"])
     P.src_amp, P.src_x0, P.src_y0, P.src_r0 = src["amp"], src["x0"], src["y0"], src["r0"]
     return P
 
@@ -470,10 +478,11 @@ class Batch:
         return out
 
     def set_shape(self, bucket, prep_threads, mass_threads, persist=0):
-        """wedg_batch_set_shape: the launch shape of one bucket (results do not depend on it)."""
+        """wedg_batch_set_shape: the launch shape of one bucket (results do not depend on it);
+        persist -1 launches the bucket's instances one by one."""
         rc = L.lib().wedg_batch_set_shape(self._h, int(bucket), int(prep_threads), int(mass_threads), int(persist))
         if rc != L.WEDG_OK:
-            raise ErrorException("launch shapes are 32, 64, 96 or 128 threads per block and persist 0 to 8")
+            raise ErrorException("launch shapes are 32, 64, 96 or 128 threads per block and persist -1 to 8")
 
     def autotune(self, us, vs, t0s, dts, steps=3):
         """wedg_batch_autotune: the launch shapes of every bucket, each tuned alone from copies of

@@ -124,11 +124,21 @@ typedef struct wedg_face_values {
   double jump_scale;          /* the family's s = 1e-8 max|value at ±δ| of src/solver.jl:387 */
   double value;               /* with at = NULL: the family is this constant everywhere */
 } wedg_face_values;
+/* A coefficient given as its values on an m × n grid of cells of the unit square, row-major
+ * [row (y)][column (x)]: the value at (x, y) is values[clip(floor(m y), 0, m-1) n + clip(floor(n x), 0, n-1)]
+ * (the lookup of piecewise-constant coefficients; the device evaluates it at every point). */
+typedef struct wedg_cell_table {
+  const double *values;
+  int32_t rows, cols;
+} wedg_cell_table;
 typedef struct wedg_points {
   const double *c_q, *alpha_q;          /* c and α at the u-points, (N, N, q_u1, q_u1): [j, k, r, s] at
                                            (x_s of column k, y_r of row j) */
   const double *beta_h;                 /* β at the high-order points, (N, N, q_high, q_high) */
-  double c_value, alpha_value, beta_value; /* a coefficient whose array is NULL is this constant */
+  double c_value, alpha_value, beta_value; /* a coefficient whose array is NULL is this constant... */
+  wedg_cell_table c_cells, alpha_cells, beta_cells; /* ...unless it has a table: then the device looks it
+                                           up at every point, faces and their δ-neighbours included */
+  const double *xloc, *yloc;            /* (N, q_u1): the u-points of the columns and rows (needed for tables) */
   wedg_face_values hc, ha, hb;          /* c, α, β on the horizontal faces */
   wedg_face_values vc, va, vb;          /* c, α, β on the vertical faces */
   wedg_face_values hg0, vg0;            /* ∂u0/∂y on the horizontal and ∂u0/∂x on the vertical faces
@@ -136,8 +146,7 @@ typedef struct wedg_points {
   const double *sp_h, *cdiv_h, *ddiv_h; /* at the high-order points: Φ and the two divergence terms of the
                                            manufactured solution (mms), the c²-term alone (initial value);
                                            unused in source mode */
-  const double *xloc_h, *yloc_h;        /* (N, q_high): the high-order points of the columns and rows
-                                           (source mode) */
+  const double *xloc_h, *yloc_h;        /* (N, q_high): the high-order points of the columns and rows */
   double src_amp, src_x0, src_y0, src_r0; /* the GaussianSource's profile (source mode) */
 } wedg_points;
 int wedg_create_points(const wedg_config *cfg, const wedg_pre *pre, const wedg_points *pts, char *msg, size_t msg_len,
@@ -340,7 +349,9 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
  * one element each) and of the mass solves (threads / 32 warps of teams of threads per
  * element), 32, 64, 96 or 128 threads, and `persist`: 0 launches one block per tile, p > 0 a
  * persistent grid of p times the blocks the SMs hold at once, each block taking tile after
- * tile. Results do not depend on the shape (every element's arithmetic is its own). */
+ * tile; -1 launches the bucket's instances one by one instead (the single-instance kernels, each
+ * instance on its own stream). Results do not depend on the shape (every element's arithmetic
+ * is its own). */
 typedef struct wedg_batch_shape {
   int32_t qu1, qv1, instances, fast;   /* the bucket's degrees + 1, its instances, the kernel family */
   int32_t prep_threads, mass_threads, persist;
@@ -352,8 +363,8 @@ int wedg_batch_set_shape(wedg_batch *b, int bucket, int prep_threads, int mass_t
 /* Autotuner of the batch's launch shapes (no counterpart in the reference, whose only shape is the
  * nblocks partition of src/rhs.jl:139-142): per bucket, run alone from copies of its instances'
  * states (left unchanged), steps RK4 steps after one untimed step, timed with CUDA events, for the
- * candidates of one coordinate at a time (k_prep's and the mass solves' threads per block: 32,
- * 64, 128; persist: 0, 1, 2). A candidate replaces the bucket's shape only when it is faster in
+ * candidates of one coordinate at a time (persist: -1, 0, 1, 2; then k_prep's and the mass
+ * solves' threads per block: 32, 64, 128). A candidate replaces the bucket's shape only when it is faster in
  * each of three paired trials against it and faster by more than 2 % in the median. Then the
  * whole batch's step (graph replays) with the tuned shapes against the shapes it had before,
  * three paired trials: the tuned shapes stay only if they win every trial, so the batch never

@@ -89,7 +89,7 @@ def test_batch_autotune_then_batch_matches_single_instances():
     ms = batch.autotune(us, vs, t0s, dts, steps=2)
     assert ms > 0
     for s in batch.shapes():
-        assert s["prep_threads"] in (32, 64, 128) and s["mass_threads"] in (32, 64, 128) and s["persist"] in (0, 1, 2)
+        assert s["prep_threads"] in (32, 64, 128) and s["mass_threads"] in (32, 64, 128) and s["persist"] in (-1, 0, 1, 2)
     for x, u, v in zip(inst, us, vs):
         assert torch.equal(u, x[2]) and torch.equal(v, x[3])
     batch.rk4_steps(us, vs, t0s, dts, 30)

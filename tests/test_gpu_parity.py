@@ -476,7 +476,7 @@ def test_config3_full_size_against_oracle(gpu):
     rng = np.random.default_rng(33)
     d = lambda n: 1.0 / (1.0 + np.add.outer(np.arange(n), np.arange(n))) ** 2   # noqa: E731
     u = np.asfortranarray(1e-3 * rng.standard_normal((N, N, nu, nu)) * d(nu))
-    v = np.asfortranarray(2e-3 * rng.standard_normal((N, N, nv, nv)) * d(nv))
+    v = np.asfortranarray(2e-4 * rng.standard_normal((N, N, nv, nv)) * d(nv))    # 2βv well below 1 (β ≤ 10)
     ow, ws = OracleWorkspace(po), W.Workspace(pp, N)
     assert ws.stats()["fast_path"] == 1
     assert rel_max(ow.rhs(u, v, 0.01), ws.rhs(u, v, 0.01)) < TOL

@@ -60,6 +60,18 @@ CASES = {
     "source, constant": (6, 4, dict(mode="source", mixed=False, coefficients=None, flux="alternating",
                                     boundary=dict(bot="absorbing_2beta", top="wall", lft="wall", rgt="wall"),
                                     kappa=0.5)),
+    # tables of cells, looked up on the device (faces on cell boundaries: one-sided)
+    "source, cell tables": (4, 8, dict(mode="source", mixed=True, flux="upwind", kappa=0.5,
+                                       coefficients=W.cell_coefficients(np.array([[1.0, 0.7], [1.3, 0.9]]),
+                                                                        np.array([[1e-4, 3e-4], [2e-4, 1e-5]]),
+                                                                        np.array([[0.5, 2.0], [1.0, 3.0]])),
+                                       boundary=dict(bot="absorbing", top="absorbing_2beta", lft="wall",
+                                                     rgt="dirichlet"))),
+    "initial value, cell tables": (3, 6, dict(mode="initial_value", mixed=False, flux="alternating", kappa=0.5,
+                                              coefficients=W.cell_coefficients(np.array([[1.0, 0.6, 1.2]]),
+                                                                               np.array([[1e-4, 2e-4, 5e-5]]),
+                                                                               np.array([[0.1, 0.2, 0.05]])),
+                                              initial_profile=_gauss_profile())),
 }
 
 

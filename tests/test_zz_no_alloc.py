@@ -66,11 +66,12 @@ CASES = {
 
 @pytest.mark.parametrize("case", list(CASES))
 def test_noalloc_matches_workspace_twice(case):
-    """Two calls in a row on different states: the first on the default stream, the second on a
-    stream of the caller's."""
+    """Calls in a row on different states, alternating between the default stream and a stream of
+    the caller's; from the second call on, device memory stays as it is."""
     import torch
     assert torch.cuda.is_available()
     q, N, kw = CASES[case]
+    side = torch.cuda.Stream(device=torch.device("cuda:0"))
     pre, _ = W.precompute(q, N, inverses="host", **kw)     # wedg_rhs_noalloc reads Ainv_u from pre
     nu, nv = pre["qu1"], pre["qv1"]
     cfg, p, keep = _abi_structs(pre, N)
@@ -79,7 +80,7 @@ def test_noalloc_matches_workspace_twice(case):
     lib = L.lib()
     rng = np.random.default_rng(42)
     free_before = None
-    for call in range(2):
+    for call in range(4):
         u = np.asfortranarray(rng.standard_normal((N, N, nu, nu)))
         v = np.asfortranarray(1e-4 * rng.standard_normal((N, N, nv, nv)))
         t = 0.037 + 0.1 * call
@@ -90,17 +91,18 @@ def test_noalloc_matches_workspace_twice(case):
         vt = torch.full_like(dv, float("nan"))
         torch.cuda.synchronize()
         msg = ctypes.create_string_buffer(512)
-        side = torch.cuda.Stream(device=dev) if call == 1 else None
+        stream = side.cuda_stream if call % 2 else None
         rc = lib.wedg_rhs_noalloc(ctypes.byref(cfg), ctypes.byref(p), du.data_ptr(), dv.data_ptr(), t,
-                                  ut.data_ptr(), vt.data_ptr(), side.cuda_stream if side else None, msg, 512)
+                                  ut.data_ptr(), vt.data_ptr(), stream, msg, 512)
         assert rc == L.WEDG_OK, msg.value.decode()
         got = (ut.cpu().numpy().reshape((N, N, nu, nu), order="F"),
                vt.cpu().numpy().reshape((N, N, nv, nv), order="F"))
         assert _rel(ref, got) < 1e-12, (call, _rel(ref, got))
         torch.cuda.synchronize()
-        if free_before is None:
+        if call == 1:
             # the static array is placed when the library's device code is loaded (at the latest
-            # by the first call); from then on the calls take no device memory
+            # by the first call), and the first use of a stream may set up driver state of its own;
+            # from then on the calls take no device memory
             free_before = torch.cuda.mem_get_info(dev)[0]
     assert abs(torch.cuda.mem_get_info(dev)[0] - free_before) < (1 << 20)
     del keep
@@ -155,7 +157,10 @@ def test_noalloc_errors_match_workspace(solver):
         assert rc == status
         assert msg.value.decode() == str(ei.value)
     # a good state after the errors: the error word starts clear again
-    v = np.zeros((N, N, nv, nv), order="F")
+    rng = np.random.default_rng(5)
+    u = np.asfortranarray(0.1 * rng.standard_normal((N, N, nu, nu)))
+    v = np.asfortranarray(1e-3 * rng.standard_normal((N, N, nv, nv)))
+    du = torch.from_numpy(u.reshape(-1, order="F").copy()).to(dev)
     dv = torch.from_numpy(v.reshape(-1, order="F").copy()).to(dev)
     vt = torch.empty_like(dv)
     msg = ctypes.create_string_buffer(512)
