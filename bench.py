@@ -299,7 +299,8 @@ def run_ours(args):
         print(json.dumps({"batched": run_batched(torch, dev, args.steps, args.warmup)}), flush=True)
         return
     if args.adjoint:
-        print(json.dumps({"adjoint": run_adjoint(torch, args.adjoint_T)}), flush=True)
+        print(json.dumps({"adjoint": run_adjoint(torch, args.adjoint_T, args.adjoint_every, args.adjoint_batch,
+                                                 args.adjoint_batch_T)}), flush=True)
         return
     if args.general_only:
         print(json.dumps({"general": run_general(torch, dev, args.steps, args.warmup)}), flush=True)
@@ -413,7 +414,7 @@ def run_ours(args):
         config3 = run_config3(torch, dev, args.steps, args.warmup)
         general = run_general(torch, dev, args.steps, args.warmup)
     if world == 1 and not args.no_adjoint:
-        adjoint = run_adjoint(torch, args.adjoint_T)
+        adjoint = run_adjoint(torch, args.adjoint_T, args.adjoint_every, args.adjoint_batch, args.adjoint_batch_T)
 
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
@@ -838,6 +839,9 @@ def main():
     ap.add_argument("--adjoint", action="store_true", help="only the adjoint-form measurement (one gradient)")
     ap.add_argument("--adjoint-T", type=float, default=0.5, help="final time of the adjoint-form workload")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-form measurement")
+    ap.add_argument("--adjoint-batch", type=int, default=16, help="gradients of the adjoint-form batch")
+    ap.add_argument("--adjoint-batch-T", type=float, default=0.125, help="final time of the adjoint-form batch")
+    ap.add_argument("--adjoint-every", type=int, default=32, help="checkpoint interval of the adjoint form")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

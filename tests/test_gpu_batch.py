@@ -99,10 +99,10 @@ def _many(seed=12):
         kw = dict(flux=str(rng.choice(["upwind", "central", "alternating"])), mixed=True, mode=mode, kappa=0.5,
                   boundary=dict(bot=kinds[0], top=kinds[1], lft=kinds[2], rgt=kinds[3]))
         if mode != "mms":
-            # β small enough that 1 - 2βv stays positive under the initial data Φ (|v| grows to ~2)
+            # β small enough that 1 - 2βv stays positive under the initial data Φ (|v| grows to ~15)
             kw["coefficients"] = W.constant_coefficients(c=float(rng.uniform(0.6, 1.5)),
                                                          alpha=float(10 ** rng.uniform(-5, -3)),
-                                                         beta=float(rng.uniform(0.0, 0.05)))
+                                                         beta=0.3 * float(rng.uniform(0.0, 0.05)))
         pre, _ = W.precompute(q, N, **kw)
         out.append((pre, N, q, 0.0 if mode == "mms" else 0.013))
     return out

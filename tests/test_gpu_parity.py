@@ -122,7 +122,8 @@ def test_chebyshev_step_policies_and_cg(gpu):
     N = 9
     co = oc.replace_coefficients(oc.paper_coefficients(), beta=8.0)
     pp, po = _pair(4, N, coefficients=co, mode="source")
-    u = np.asfortranarray(1e-3 * rng.standard_normal((N, N, pp["qu1"], pp["qu1"])))
+    # u small enough that c²Δu does not push 2βv past 1 within the three steps (β = 8)
+    u = np.asfortranarray(1e-4 * rng.standard_normal((N, N, pp["qu1"], pp["qu1"])))
     v = np.asfortranarray(1e-4 * rng.standard_normal((N, N, pp["qv1"], pp["qv1"])))
     v[:, 0:2, 1, 0] = 0.04
     ow = OracleWorkspace(po)
@@ -475,8 +476,10 @@ def test_config3_full_size_against_oracle(gpu):
     nu, nv = pp["qu1"], pp["qv1"]
     rng = np.random.default_rng(33)
     d = lambda n: 1.0 / (1.0 + np.add.outer(np.arange(n), np.arange(n))) ** 2   # noqa: E731
-    u = np.asfortranarray(1e-3 * rng.standard_normal((N, N, nu, nu)) * d(nu))
-    v = np.asfortranarray(2e-4 * rng.standard_normal((N, N, nv, nv)) * d(nv))    # 2βv well below 1 (β ≤ 10)
+    # rough random data: at 1e-4 the stages already drive 2βv past 1 somewhere (β ≤ 10); at 1e-5 |v| stays
+    # near 2e-3
+    u = np.asfortranarray(1e-5 * rng.standard_normal((N, N, nu, nu)) * d(nu))
+    v = np.asfortranarray(2e-6 * rng.standard_normal((N, N, nv, nv)) * d(nv))
     ow, ws = OracleWorkspace(po), W.Workspace(pp, N)
     assert ws.stats()["fast_path"] == 1
     assert rel_max(ow.rhs(u, v, 0.01), ws.rhs(u, v, 0.01)) < TOL
@@ -518,7 +521,8 @@ def test_rk4_steps_common_count_against_oracle(gpu):
     N = 9
     co = oc.replace_coefficients(oc.paper_coefficients(), beta=8.0)
     pp, po = _pair(4, N, coefficients=co, mode="source")
-    u = np.asfortranarray(1e-3 * rng.standard_normal((N, N, pp["qu1"], pp["qu1"])))
+    # u small enough that c²Δu does not push 2βv past 1 within the three steps (β = 8)
+    u = np.asfortranarray(1e-4 * rng.standard_normal((N, N, pp["qu1"], pp["qu1"])))
     v = np.asfortranarray(1e-4 * rng.standard_normal((N, N, pp["qv1"], pp["qv1"])))
     v[:, 0:2, 1, 0] = 0.04
     uo, vo = u.copy(order="F"), v.copy(order="F")
