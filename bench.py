@@ -598,8 +598,10 @@ def run_batched(torch, dev, steps, warmup):
                                  "(Batch.autotune, paired trials); value and ms_per_step are the faster of the "
                                  "default-shape and the tuned-shape runs"},
             "timing": "host clock around each call (each call returns synchronised); states resident on the GPU",
-            "batched": "Batch.rk4_steps: per stage, one launch of each stage kernel per bucket of instances with the "
-                       "same kernels; one CUDA graph of one RK4 step of every instance, replayed per step",
+            "batched": "Batch.rk4_steps: buckets of instances with the same kernels side by side, each bucket's "
+                       "instances on their own streams (the default) or one multi-instance launch per stage kernel "
+                       "(the tuner's choice per bucket); CUDA graphs of one and of four RK4 steps of every instance, "
+                       "replayed",
             "plain_loop": "Workspace.rk4_steps for each instance in turn"}
 
 

@@ -105,10 +105,9 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_hats(const __grid_constant_
 template <int NU, int NV>
 __global__ void __launch_bounds__(ADJ_THREADS) k_adj_hats_m(const __grid_constant__ Basis<NU, NV> B,
                                                      const __grid_constant__ MultiAdj P) {
-  __shared__ AdjArgs sa;
   for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
-    const int inst = multi_begin(P, vb, sa);
-    adj_hats_body<NU, NV>(B, sa.F, sa.A, (vb - P.first[inst]) * P.tile + (int)threadIdx.x);
+    const int inst = multi_begin(P, vb);
+    adj_hats_body<NU, NV>(B, P.a[inst].F, P.a[inst].A, (vb - P.first[inst]) * P.tile + (int)threadIdx.x);
   }
 }
 
@@ -205,10 +204,9 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
 template <int NU, int NV>
 __global__ void __launch_bounds__(CHEB_THREADS, 3)
     k_adj_mass_m(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ MultiAdj P) {
-  __shared__ AdjArgs sa;
   for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
-    const int inst = multi_begin(P, vb, sa);
-    adj_mass_body<NU, NV>(B, sa.F, sa.A, (vb - P.first[inst]) * P.tile);
+    const int inst = multi_begin(P, vb);
+    adj_mass_body<NU, NV>(B, P.a[inst].F, P.a[inst].A, (vb - P.first[inst]) * P.tile);
   }
 }
 
@@ -556,10 +554,10 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_face(const __grid_constant_
 template <int NU, int NV, bool PARAMS>
 __global__ void __launch_bounds__(ADJ_THREADS) k_adj_face_m(const __grid_constant__ Basis<NU, NV> B,
                                                      const __grid_constant__ MultiAdj P) {
-  __shared__ AdjArgs sa;
   for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
-    const int inst = multi_begin(P, vb, sa);
-    adj_face_body<NU, NV, PARAMS>(B, sa.F, sa.S, sa.A, sa.gc2, sa.gal, sa.gbe,
+    const int inst = multi_begin(P, vb);
+    const AdjArgs &a = P.a[inst];
+    adj_face_body<NU, NV, PARAMS>(B, a.F, a.S, a.A, a.gc2, a.gal, a.gbe,
                                   (vb - P.first[inst]) * P.tile + (int)threadIdx.x);
   }
 }

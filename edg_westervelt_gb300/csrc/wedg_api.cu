@@ -110,6 +110,10 @@ __global__ void k_step_done_p(const __grid_constant__ StepMulti P) {
 const int kTuneThreads[3] = {32, 64, 128};
 constexpr double kTuneGain = 0.98;
 constexpr int kTuneRepeats = 3;   // paired trials of the batch autotuner
+// RK4 steps of the batch's larger graph: within it an instance starts its next step as soon as its
+// own step is done (the table chunk, WEDG_BATCH_CHUNK steps, is a multiple of it)
+constexpr int kBatchGraphSteps = 4;
+static_assert(WEDG_BATCH_CHUNK % kBatchGraphSteps == 0, "a table chunk holds whole multi-step graphs");
 
 Launchers get_launchers(int nu, int nv, bool fast) {
   switch (nu) {
@@ -137,6 +141,9 @@ struct wedg_ws {
   std::vector<char> basis;
   Fields F{};
   cudaStream_t own_stream = nullptr, stream = nullptr;
+  // host-state calls: copies beside the workspace's stream (created on first use)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_copy[2] = {nullptr, nullptr};
   std::vector<void *> allocs;
   size_t bytes = 0;
   // state buffers
@@ -302,6 +309,15 @@ int reset_flags(wedg_ws *ws) {
   return WEDG_OK;
 }
 
+// The copy stream and its two events of host-state calls (created on first use)
+int copy_stream_ready(wedg_ws *ws) {
+  if (ws->copy_stream) return WEDG_OK;
+  CK(ws, cudaEventCreateWithFlags(&ws->ev_copy[0], cudaEventDisableTiming));
+  CK(ws, cudaEventCreateWithFlags(&ws->ev_copy[1], cudaEventDisableTiming));
+  CK(ws, cudaStreamCreateWithFlags(&ws->copy_stream, cudaStreamNonBlocking));
+  return WEDG_OK;
+}
+
 cudaEvent_t take_event(wedg_ws *ws) {
   if (!ws->ev_pool.empty()) {
     cudaEvent_t e = ws->ev_pool.back();
@@ -328,8 +344,9 @@ void drain_events(wedg_ws *ws) {
   ws->ev_pending.clear();
 }
 
-// enqueue the three kernels of one stage (on the workspace's Fields, or on Fo)
-int enqueue_stage(wedg_ws *ws, const StageIO &S, const Fields *Fo = nullptr) {
+// enqueue the three kernels of one stage (on the workspace's Fields, or on Fo); after_stage, when
+// given, is recorded on the stream after the stage kernel
+int enqueue_stage(wedg_ws *ws, const StageIO &S, const Fields *Fo = nullptr, cudaEvent_t after_stage = nullptr) {
   const Fields &F = Fo ? *Fo : ws->F;
   const int tp = ws->prep_threads, bp = (ws->E + tp - 1) / tp;
   const int ts = stage_threads(ws->nu, ws->nv, ws->fast), bs = (ws->E + ts - 1) / ts;
@@ -345,6 +362,7 @@ int enqueue_stage(wedg_ws *ws, const StageIO &S, const Fields *Fo = nullptr) {
   CK(ws, ws->L.prep(ws->basis.data(), F, Sp, bp, tp, ws->stream));
   if (ws->timing) cudaEventRecord(e1, ws->stream);
   CK(ws, ws->L.stage(ws->basis.data(), F, Sp, bs, ts, ws->stream));
+  if (after_stage) CK(ws, cudaEventRecord(after_stage, ws->stream));
   if (ws->timing) cudaEventRecord(e2, ws->stream);
   CK(ws, ws->L.mass(ws->basis.data(), F, Sp, bm, ws->mass_threads, ws->stream));
   if (ws->timing) {
@@ -410,10 +428,12 @@ StageIO rk4_stage_io(const wedg_ws *ws, double *u, double *v, int s, double t, d
 
 // One RK4 step on the workspace stream. With tf != nullptr the stage kernels take their time
 // factors from the device table tf (tf_n steps, indexed by the device step counter), so that the
-// launches can be captured once into a CUDA graph and replayed for every step.
+// launches can be captured once into a CUDA graph and replayed for every step. u_final, when
+// given (Chebyshev mass solves only), is recorded once the last stage's k_stage has written the
+// step's u: nothing of the step writes u after it.
 int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop_nonfinite,
                 const double *tf = nullptr, long long tf_n = 0, double *const *stage_u = nullptr,
-                double *const *stage_v = nullptr) {
+                double *const *stage_v = nullptr, cudaEvent_t u_final = nullptr) {
   // with stage_u, stage_v (four buffers each) the stage states Y1..Y4 of the step are kept there
   const bool cg = ws->cfg.mass_solver == WEDG_CG;
   if (stage_u) {
@@ -422,7 +442,8 @@ int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop
     CK(ws, cudaMemcpyAsync(stage_v[0], v, bV, cudaMemcpyDeviceToDevice, ws->stream));
   }
   for (int s = 0; s < 4; ++s) {
-    int rc = enqueue_stage(ws, rk4_stage_io(ws, u, v, s, t, dt, tf, tf_n, stage_u, stage_v));
+    int rc = enqueue_stage(ws, rk4_stage_io(ws, u, v, s, t, dt, tf, tf_n, stage_u, stage_v), nullptr,
+                           s == 3 && !cg ? u_final : nullptr);
     if (rc) return rc;
   }
   if (cg) {
@@ -528,21 +549,10 @@ size_t stage_data_bytes(const wedg_ws *ws) {
          sizeof(int) * (E * (1 + NBIN) + 2 * NBIN + 4);
 }
 
-int collect(wedg_ws *ws) {
-  unsigned long long err;
-  unsigned int cgf, nonf;
-  int nmax;
-  long long done;
-  unsigned long long nsum;
-  CK(ws, cudaStreamSynchronize(ws->stream));
-  drain_events(ws);
-  CK(ws, cudaMemcpy(&nsum, ws->F.nsum, sizeof nsum, cudaMemcpyDeviceToHost));
+// The status and statistics of a call from the workspace's flags (read back after the call)
+int apply_flags(wedg_ws *ws, unsigned long long err, unsigned int cgf, unsigned int nonf, int nmax, long long done,
+                unsigned long long nsum) {
   ws->stats.cheb_steps_sum = (int64_t)nsum;
-  CK(ws, cudaMemcpy(&err, ws->F.err, sizeof err, cudaMemcpyDeviceToHost));
-  CK(ws, cudaMemcpy(&cgf, ws->F.cg_nfail, sizeof cgf, cudaMemcpyDeviceToHost));
-  CK(ws, cudaMemcpy(&nonf, ws->F.nonfinite, sizeof nonf, cudaMemcpyDeviceToHost));
-  CK(ws, cudaMemcpy(&nmax, ws->F.nmax + 2, sizeof nmax, cudaMemcpyDeviceToHost));
-  CK(ws, cudaMemcpy(&done, ws->steps_done, sizeof done, cudaMemcpyDeviceToHost));
   ws->stats.cg_not_converged = (int32_t)cgf;
   ws->stats.finite = nonf ? 0 : 1;
   ws->stats.cheb_steps_max = nmax;
@@ -582,6 +592,60 @@ int collect(wedg_ws *ws) {
                   julia_float(ws->cfg.mass_tol);
   }
   return ws->status;
+}
+
+int collect(wedg_ws *ws) {
+  unsigned long long err;
+  unsigned int cgf, nonf;
+  int nmax;
+  long long done;
+  unsigned long long nsum;
+  CK(ws, cudaStreamSynchronize(ws->stream));
+  drain_events(ws);
+  CK(ws, cudaMemcpy(&nsum, ws->F.nsum, sizeof nsum, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(&err, ws->F.err, sizeof err, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(&cgf, ws->F.cg_nfail, sizeof cgf, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(&nonf, ws->F.nonfinite, sizeof nonf, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(&nmax, ws->F.nmax + 2, sizeof nmax, cudaMemcpyDeviceToHost));
+  CK(ws, cudaMemcpy(&done, ws->steps_done, sizeof done, cudaMemcpyDeviceToHost));
+  return apply_flags(ws, err, cgf, nonf, nmax, done, nsum);
+}
+
+// The flags of every instance of a batch, reset and read back by one launch each
+struct BatchFlagPtrs {
+  unsigned long long *err, *nsum;
+  unsigned int *cg_nfail, *nonfinite;
+  int *nmax, *bin_count;
+  long long *steps_done;
+};
+struct BatchFlagVals {
+  unsigned long long err, nsum;
+  long long done;
+  unsigned int cgf, nonf;
+  int nmax, pad;
+};
+
+// reset_flags of instance blockIdx.x
+__global__ void k_batch_reset(const BatchFlagPtrs *p, int n) {
+  if ((int)blockIdx.x >= n) return;
+  const BatchFlagPtrs f = p[blockIdx.x];
+  for (int t = threadIdx.x; t < 2 * NBIN; t += blockDim.x) f.bin_count[t] = 0;
+  if (threadIdx.x == 0) {
+    *f.err = ERR_NONE;
+    *f.nsum = 0;
+    *f.cg_nfail = 0;
+    *f.nonfinite = 0;
+    f.nmax[0] = f.nmax[1] = f.nmax[2] = 0;
+    *f.steps_done = 0;
+  }
+}
+
+// the flags collect reads, of every instance
+__global__ void k_batch_read(const BatchFlagPtrs *p, int n, BatchFlagVals *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const BatchFlagPtrs f = p[i];
+  out[i] = BatchFlagVals{*f.err, *f.nsum, *f.steps_done, *f.cg_nfail, *f.nonfinite, f.nmax[2], 0};
 }
 
 int argument_error(wedg_ws *ws, const std::string &msg) {
@@ -1301,7 +1365,7 @@ struct BatchBucket {
   int nu = 0, nv = 0;
   bool fast = false, cg = false;
   int prep_threads = 128, mass_threads = CHEB_THREADS, persist = 0;
-  bool split = false;
+  bool split = true;   // the default: faster than the merged launches on the mixed batches measured
   cudaStream_t st = nullptr;
   cudaEvent_t join = nullptr, fork = nullptr;
   StepFlags *d_flags = nullptr;   // per instance of the bucket, for k_step_done_m
@@ -1319,11 +1383,17 @@ struct wedg_batch {
   cudaStream_t main = nullptr;
   cudaEvent_t fork = nullptr;
   cudaEvent_t half_done[2] = {nullptr, nullptr};   // the host half of the tables may be refilled
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  // what the captured graph was made for
+  // graph[0]: one RK4 step of every instance; graph[1]: kBatchGraphSteps steps, in which each
+  // instance (or merged bucket) goes on to its next step without waiting for the others
+  cudaGraph_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  // what the captured graphs were made for
   std::vector<double *> gu, gv;
   std::vector<double> gdt;
+  std::vector<int64_t> step_launches;               // per instance: its kernel launches in one step
+  BatchFlagPtrs *d_flagp = nullptr;                 // per instance: its flags (k_batch_reset, k_batch_read)
+  BatchFlagVals *d_flagv = nullptr, *h_flagv = nullptr;   // their values after a call (h_flagv pinned)
+  double *d_tf_all = nullptr;                       // the instances' factor tables, instance after instance
   int gstop = -1;
   int64_t shape_gen = 0, gshape = -1;              // changes of the buckets' launch shapes
   // per instance: device factor table of 2 chunks (the kernels index it by step mod 2 chunks)
@@ -1335,9 +1405,14 @@ struct wedg_batch {
     if (main) cudaStreamSynchronize(main);
     for (BatchBucket &k : buckets)
       if (k.st) cudaStreamSynchronize(k.st);
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-    for (double *p : d_tf) cudaFree(p);
+    for (int g = 0; g < 2; ++g) {
+      if (exec[g]) cudaGraphExecDestroy(exec[g]);
+      if (graph[g]) cudaGraphDestroy(graph[g]);
+    }
+    if (d_tf_all) cudaFree(d_tf_all);
+    if (d_flagp) cudaFree(d_flagp);
+    if (d_flagv) cudaFree(d_flagv);
+    if (h_flagv) cudaFreeHost(h_flagv);
     for (void *p : dmem) cudaFree(p);
     if (h_tf) cudaFreeHost(h_tf);
     for (BatchBucket &k : buckets) {
@@ -1364,13 +1439,18 @@ int bucket_grid(const wedg_batch *b, const BatchBucket &k, int total, int reside
   return std::min(total, std::max(cap, 1));
 }
 
-// Enqueue one RK4 step of every instance of bucket k on its stream: per stage, k_prep, k_stage
-// and the mass solve as multi-instance launches (chunks of up to MultiStage::cap instances), then
-// the last update of CG instances and the step bookkeeping. u, v, t, dt are indexed by instance
-// (t is ignored with tables: the stage kernels then read their time factors from the instances'
-// device tables d_tf, tf_n steps). Advances each instance's bin parity as enqueue_stage does.
+int enqueue_merged_step(wedg_batch *b, BatchBucket &k, double *const *u, double *const *v, const double *t,
+                        const double *dt, int stop_nonfinite, bool tables, long long tf_n);
+
+// Enqueue `steps` RK4 steps of every instance of bucket k on its stream: per stage, k_prep,
+// k_stage and the mass solve as multi-instance launches (chunks of up to MultiStage::cap
+// instances), then the last update of CG instances and the step bookkeeping. u, v, t, dt are
+// indexed by instance (t is ignored with tables: the stage kernels then read their time factors
+// from the instances' device tables d_tf, tf_n steps, at the instance's device step counter; without
+// tables `steps` is 1). Advances each instance's bin parity as enqueue_stage does. A split bucket's
+// instances run their steps one after another on their own streams, with no join between steps.
 int enqueue_bucket_step(wedg_batch *b, BatchBucket &k, double *const *u, double *const *v, const double *t,
-                        const double *dt, int stop_nonfinite, bool tables, long long tf_n) {
+                        const double *dt, int stop_nonfinite, bool tables, long long tf_n, int steps = 1) {
   const int n = (int)k.ids.size();
   if (k.split) {
     // every instance on its own stream, forked from and joined to the bucket's
@@ -1385,8 +1465,10 @@ int enqueue_bucket_step(wedg_batch *b, BatchBucket &k, double *const *u, double 
       const int pt = w->prep_threads, mt = w->mass_threads;
       w->prep_threads = k.prep_threads;
       w->mass_threads = k.mass_threads;
-      const int rc = enqueue_rk4(w, u[i], v[i], tables ? 0.0 : t[i], dt[i], stop_nonfinite,
-                                 tables ? b->d_tf[i] : nullptr, tables ? tf_n : 0);
+      int rc = WEDG_OK;
+      for (int it = 0; it < steps && rc == WEDG_OK; ++it)
+        rc = enqueue_rk4(w, u[i], v[i], tables ? 0.0 : t[i], dt[i], stop_nonfinite, tables ? b->d_tf[i] : nullptr,
+                         tables ? tf_n : 0);
       w->prep_threads = pt;
       w->mass_threads = mt;
       w->timing = timing;
@@ -1397,6 +1479,17 @@ int enqueue_bucket_step(wedg_batch *b, BatchBucket &k, double *const *u, double 
     if (e != cudaSuccess) return cuda_fail(b->ws[k.ids[0]], e, "split bucket launch");
     return WEDG_OK;
   }
+  for (int it = 0; it < steps; ++it) {
+    const int rc = enqueue_merged_step(b, k, u, v, t, dt, stop_nonfinite, tables, tf_n);
+    if (rc) return rc;
+  }
+  return WEDG_OK;
+}
+
+// One RK4 step of a merged bucket (see enqueue_bucket_step)
+int enqueue_merged_step(wedg_batch *b, BatchBucket &k, double *const *u, double *const *v, const double *t,
+                        const double *dt, int stop_nonfinite, bool tables, long long tf_n) {
+  const int n = (int)k.ids.size();
   const int BT = stage_threads(k.nu, k.nv, k.fast);
   const int TPW = 32 / (qhigh(k.nu, k.nv) / 2 + (qhigh(k.nu, k.nv) & 1));
   const int mass_tile = (k.mass_threads / 32) * TPW;
@@ -2034,8 +2127,12 @@ void wedg_destroy(wedg_ws *ws) {
   if (ws->stream) cudaStreamSynchronize(ws->stream);
   drain_events(ws);
   for (cudaEvent_t e : ws->ev_pool) cudaEventDestroy(e);
+  if (ws->copy_stream) cudaStreamSynchronize(ws->copy_stream);
   for (void *p : ws->allocs) cudaFree(p);
   if (ws->own_stream) cudaStreamDestroy(ws->own_stream);
+  if (ws->copy_stream) cudaStreamDestroy(ws->copy_stream);
+  for (cudaEvent_t e : ws->ev_copy)
+    if (e) cudaEventDestroy(e);
   delete ws;
 }
 
@@ -2080,24 +2177,42 @@ int wedg_rk4_steps(wedg_ws *ws, double *u, double *v, double t0, double dt, int6
   if (nsteps < 0) return argument_error(ws, "nsteps must be ≥ 0");
   const size_t bU = sizeof(double) * ws->E * ws->nu * ws->nu, bV = sizeof(double) * ws->E * ws->nv * ws->nv;
   double *du = u, *dv = v;
-  if (where == WEDG_HOST) {
+  const bool host = where == WEDG_HOST;
+  // with host state: v is copied in on the copy stream beside u on the workspace's stream, and the
+  // final u is copied out while the last stage's mass solve runs (Chebyshev)
+  const bool u_early = host && nsteps > 0 && ws->cfg.mass_solver != WEDG_CG;
+  if (host) {
+    if ((rc = copy_stream_ready(ws))) return rc;
+    CK(ws, cudaEventRecord(ws->ev_copy[0], ws->stream));           // after the stream's earlier work
+    CK(ws, cudaStreamWaitEvent(ws->copy_stream, ws->ev_copy[0], 0));
+    CK(ws, cudaMemcpyAsync(ws->d_v, v, bV, cudaMemcpyHostToDevice, ws->copy_stream));
     CK(ws, cudaMemcpyAsync(ws->d_u, u, bU, cudaMemcpyHostToDevice, ws->stream));
-    CK(ws, cudaMemcpyAsync(ws->d_v, v, bV, cudaMemcpyHostToDevice, ws->stream));
+    CK(ws, cudaEventRecord(ws->ev_copy[1], ws->copy_stream));
+    CK(ws, cudaStreamWaitEvent(ws->stream, ws->ev_copy[1], 0));
     du = ws->d_u; dv = ws->d_v;
   }
   if ((rc = reset_flags(ws))) return rc;
   double t = t0;
   for (int64_t it = 0; it < nsteps; ++it) {
-    if ((rc = enqueue_rk4(ws, du, dv, t, dt, stop_nonfinite))) return rc;
+    if ((rc = enqueue_rk4(ws, du, dv, t, dt, stop_nonfinite, nullptr, 0, nullptr, nullptr,
+                          u_early && it == nsteps - 1 ? ws->ev_copy[0] : nullptr)))
+      return rc;
     t += dt;
+  }
+  if (host) {
+    if (u_early) {
+      CK(ws, cudaStreamWaitEvent(ws->copy_stream, ws->ev_copy[0], 0));
+      CK(ws, cudaMemcpyAsync(u, ws->d_u, bU, cudaMemcpyDeviceToHost, ws->copy_stream));
+      CK(ws, cudaEventRecord(ws->ev_copy[1], ws->copy_stream));
+    } else {
+      CK(ws, cudaMemcpyAsync(u, ws->d_u, bU, cudaMemcpyDeviceToHost, ws->stream));
+    }
+    CK(ws, cudaMemcpyAsync(v, ws->d_v, bV, cudaMemcpyDeviceToHost, ws->stream));
+    if (u_early) CK(ws, cudaStreamWaitEvent(ws->stream, ws->ev_copy[1], 0));   // collect's sync covers it
   }
   rc = collect(ws);
   if (steps_done) *steps_done = ws->stats.steps_done;
   if (finite) *finite = ws->stats.finite;
-  if (where == WEDG_HOST) {
-    CK(ws, cudaMemcpy(u, ws->d_u, bU, cudaMemcpyDeviceToHost));
-    CK(ws, cudaMemcpy(v, ws->d_v, bV, cudaMemcpyDeviceToHost));
-  }
   return rc;
 }
 
@@ -2135,13 +2250,23 @@ int wedg_batch_create(int n, wedg_ws *const *instances, wedg_batch **out) {
             cudaEventCreateWithFlags(&b->half_done[0], cudaEventDisableTiming) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->half_done[1], cudaEventDisableTiming) == cudaSuccess &&
             cudaMallocHost(&b->h_tf, sizeof(double) * per * n) == cudaSuccess;
+  ok = ok && cudaMalloc(&b->d_tf_all, sizeof(double) * per * n) == cudaSuccess &&
+       cudaMalloc(&b->d_flagp, sizeof(BatchFlagPtrs) * n) == cudaSuccess &&
+       cudaMalloc(&b->d_flagv, sizeof(BatchFlagVals) * n) == cudaSuccess &&
+       cudaMallocHost(&b->h_flagv, sizeof(BatchFlagVals) * n) == cudaSuccess;
   for (int i = 0; i < n && ok; ++i) {
-    double *d = nullptr;
     cudaEvent_t e = nullptr;
-    ok = cudaMalloc(&d, sizeof(double) * per) == cudaSuccess;
-    if (ok) b->d_tf.push_back(d);
-    ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    b->d_tf.push_back(b->d_tf_all + per * i);
+    ok = cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
     if (ok) b->ijoin.push_back(e);
+  }
+  if (ok) {
+    std::vector<BatchFlagPtrs> fp(n);
+    for (int i = 0; i < n; ++i) {
+      const Fields &F = b->ws[i]->F;
+      fp[i] = BatchFlagPtrs{F.err, F.nsum, F.cg_nfail, F.nonfinite, F.nmax, F.bin_count, b->ws[i]->steps_done};
+    }
+    ok = cudaMemcpy(b->d_flagp, fp.data(), sizeof(BatchFlagPtrs) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   }
   for (BatchBucket &k : b->buckets) {
     if (!ok) break;
@@ -2225,44 +2350,53 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
   for (int i = 0; i < n; ++i) {
     wedg_ws *w = b->ws[i];
     w->stats.kernel_launches = 0;
+    w->parity = 0;
+    w->stats.element_stages = 0;
     BK(cudaEventRecord(b->fork, w->stream));
     BK(cudaStreamWaitEvent(b->main, b->fork, 0));
-    cudaStream_t own = w->stream;
-    w->stream = b->main;
-    const int rc = reset_flags(w);
-    w->stream = own;
-    if (rc) return rc;
   }
-  // ---- the graph of one step of every instance, captured again when its key changed
-  bool same = b->exec && b->gstop == (stop_nonfinite ? 1 : 0) && b->gshape == b->shape_gen;
+  k_batch_reset<<<n, 128, 0, b->main>>>(b->d_flagp, n);
+  BK(cudaGetLastError());
+  // ---- the graphs of one and of kBatchGraphSteps steps of every instance, captured again when
+  //      their key changed
+  bool same = b->exec[0] && b->gstop == (stop_nonfinite ? 1 : 0) && b->gshape == b->shape_gen;
   for (int i = 0; i < n && same; ++i) same = b->gu[i] == u_dev[i] && b->gv[i] == v_dev[i] && b->gdt[i] == dt[i];
   if (!same) {
-    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
-    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    for (int g = 0; g < 2; ++g) {
+      if (b->exec[g]) { cudaGraphExecDestroy(b->exec[g]); b->exec[g] = nullptr; }
+      if (b->graph[g]) { cudaGraphDestroy(b->graph[g]); b->graph[g] = nullptr; }
+    }
     int rc = upload_final_args(b, u_dev, v_dev, dt);
     if (rc) return rc;
-    BK(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
-    cudaError_t ce = cudaEventRecord(b->fork, b->main);
-    for (size_t q = 0; q < b->buckets.size() && ce == cudaSuccess && rc == WEDG_OK; ++q) {
-      BatchBucket &k = b->buckets[q];
-      ce = cudaStreamWaitEvent(k.st, b->fork, 0);
-      if (ce != cudaSuccess) break;
-      rc = enqueue_bucket_step(b, k, u_dev, v_dev, nullptr, dt, stop_nonfinite ? 1 : 0, true, 2 * C);
-      if (rc == WEDG_OK) ce = cudaEventRecord(k.join, k.st);
-      if (ce == cudaSuccess && rc == WEDG_OK) ce = cudaStreamWaitEvent(b->main, k.join, 0);
+    b->step_launches.assign(n, 0);
+    for (int g = 0; g < 2; ++g) {
+      BK(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
+      cudaError_t ce = cudaEventRecord(b->fork, b->main);
+      for (size_t q = 0; q < b->buckets.size() && ce == cudaSuccess && rc == WEDG_OK; ++q) {
+        BatchBucket &k = b->buckets[q];
+        ce = cudaStreamWaitEvent(k.st, b->fork, 0);
+        if (ce != cudaSuccess) break;
+        for (int i : k.ids) b->ws[i]->stats.kernel_launches = 0;
+        rc = enqueue_bucket_step(b, k, u_dev, v_dev, nullptr, dt, stop_nonfinite ? 1 : 0, true, 2 * C,
+                                 g == 0 ? 1 : kBatchGraphSteps);
+        if (g == 0)
+          for (int i : k.ids) b->step_launches[i] = b->ws[i]->stats.kernel_launches;
+        if (rc == WEDG_OK) ce = cudaEventRecord(k.join, k.st);
+        if (ce == cudaSuccess && rc == WEDG_OK) ce = cudaStreamWaitEvent(b->main, k.join, 0);
+      }
+      cudaGraph_t gr = nullptr;
+      const cudaError_t ce2 = cudaStreamEndCapture(b->main, &gr);
+      if (rc != WEDG_OK) {
+        if (gr) cudaGraphDestroy(gr);
+        return rc;
+      }
+      if (ce != cudaSuccess || ce2 != cudaSuccess) {
+        if (gr) cudaGraphDestroy(gr);
+        return cuda_err(ce != cudaSuccess ? ce : ce2);
+      }
+      b->graph[g] = gr;
+      BK(cudaGraphInstantiate(&b->exec[g], gr, 0));
     }
-    cudaGraph_t g = nullptr;
-    const cudaError_t ce2 = cudaStreamEndCapture(b->main, &g);
-    if (rc != WEDG_OK) {
-      if (g) cudaGraphDestroy(g);
-      return rc;
-    }
-    if (ce != cudaSuccess || ce2 != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      return cuda_err(ce != cudaSuccess ? ce : ce2);
-    }
-    b->graph = g;
-    BK(cudaGraphInstantiate(&b->exec, g, 0));
     b->gu.assign(u_dev, u_dev + n);
     b->gv.assign(v_dev, v_dev + n);
     b->gdt.assign(dt, dt + n);
@@ -2281,20 +2415,27 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
       factor_table(b->ws[i], t[i], dt[i], cnt, h + (size_t)i * chunk);
       for (int64_t it = 0; it < cnt; ++it) t[i] += dt[i];
     }
-    for (int i = 0; i < n; ++i)
-      BK(cudaMemcpyAsync(b->d_tf[i] + (size_t)half * chunk, h + (size_t)i * chunk, sizeof(double) * cnt * 32,
-                         cudaMemcpyHostToDevice, b->main));
+    // instance i's rows from h + i chunk to d_tf[i] + half chunk, d_tf[i] = d_tf_all + i per
+    BK(cudaMemcpy2DAsync(b->d_tf_all + (size_t)half * chunk, sizeof(double) * 2 * chunk, h, sizeof(double) * chunk,
+                         sizeof(double) * cnt * 32, n, cudaMemcpyHostToDevice, b->main));
     BK(cudaEventRecord(b->half_done[half], b->main));
-    for (int64_t it = 0; it < cnt; ++it) BK(cudaGraphLaunch(b->exec, b->main));
+    for (int64_t it = 0; it < cnt;) {
+      const bool many = cnt - it >= kBatchGraphSteps;
+      BK(cudaGraphLaunch(b->exec[many ? 1 : 0], b->main));
+      it += many ? kBatchGraphSteps : 1;
+    }
   }
+  k_batch_read<<<(n + 127) / 128, 128, 0, b->main>>>(b->d_flagp, n, b->d_flagv);
+  BK(cudaGetLastError());
+  BK(cudaMemcpyAsync(b->h_flagv, b->d_flagv, sizeof(BatchFlagVals) * n, cudaMemcpyDeviceToHost, b->main));
   BK(cudaStreamSynchronize(b->main));
 #undef BK
   int first = WEDG_OK;
   for (int i = 0; i < n; ++i) {
     wedg_ws *w = b->ws[i];
-    const int64_t launches = w->stats.kernel_launches;
-    const int rc = collect(w);
-    w->stats.kernel_launches = launches;
+    const BatchFlagVals &f = b->h_flagv[i];
+    const int rc = apply_flags(w, f.err, f.cgf, f.nonf, f.nmax, f.done, f.nsum);
+    w->stats.kernel_launches = b->step_launches[i] * nsteps;   // the instance's share of the launches run
     if (steps_done) steps_done[i] = w->stats.steps_done;
     if (finite) finite[i] = w->stats.finite;
     if (status) status[i] = rc;
@@ -2367,9 +2508,11 @@ int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_de
     }
     int rc = wedg_batch_rk4_steps(b, su.data(), sv.data(), t0, dt, 1, 0, nullptr, nullptr, nullptr);
     if (rc != WEDG_OK && rc != WEDG_WARN_CG_NOT_CONVERGED) return rc;
+    // at least two of the larger graphs, so that the call's fixed costs weigh little
+    const int64_t ns = std::max<int64_t>(steps, 2 * kBatchGraphSteps);
     const auto c0 = std::chrono::steady_clock::now();
-    rc = wedg_batch_rk4_steps(b, su.data(), sv.data(), t1.data(), dt, steps, 0, nullptr, nullptr, nullptr);
-    ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c0).count() / steps;
+    rc = wedg_batch_rk4_steps(b, su.data(), sv.data(), t1.data(), dt, ns, 0, nullptr, nullptr, nullptr);
+    ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c0).count() / ns;
     return (rc == WEDG_WARN_CG_NOT_CONVERGED) ? WEDG_OK : rc;
   };
   auto median3 = [](double a, double x, double c) { return std::max(std::min(a, x), std::min(std::max(a, x), c)); };

@@ -183,17 +183,14 @@ struct Multi {
 // CAP is what fits the kernel parameter limit (32 764 bytes) beside the largest Basis
 using MultiStage = Multi<StageArgs, 32>;
 
-// The instance of virtual block vb, its arguments copied into sa (all threads of the block call
-// this together: it synchronises before overwriting sa and after filling it)
+// The instance of virtual block vb. The kernels read that instance's arguments where they lie, in
+// the parameter block: the index is the same for the whole block, so the reads are uniform
+// constant-bank loads. The barrier keeps a persistent block's next virtual block from reusing
+// shared memory that threads of the previous one still read.
 template <class Args, int CAP>
-__device__ __forceinline__ int multi_begin(const Multi<Args, CAP> &P, int vb, Args &sa) {
-  static_assert(sizeof(Args) % 8 == 0, "instance arguments are copied as 8-byte words");
+__device__ __forceinline__ int multi_begin(const Multi<Args, CAP> &P, int vb) {
   int inst = 0;
   while (inst + 1 < P.n && vb >= P.first[inst + 1]) ++inst;
-  __syncthreads();
-  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&P.a[inst]);
-  unsigned long long *dst = reinterpret_cast<unsigned long long *>(&sa);
-  for (int i = threadIdx.x; i < (int)(sizeof(Args) / 8); i += blockDim.x) dst[i] = src[i];
   __syncthreads();
   return inst;
 }
@@ -299,49 +296,48 @@ __device__ __forceinline__ void ph_row_mid(const double (&Ph)[QH][NV], const X &
 //   oL[i] = Σ_b P[i,b] Σ_a El[a] X[b][a],  oR with Er,
 // where El, Er are the values (DER false) or the derivatives (DER true) of the modes at the
 // two ends: Er[a] = ±(-1)^a El[a], so both ends come from the even and odd parts of one sum.
-// With SCALE, every output is multiplied by sc.
-template <int NQ, int NU, int n, bool DER, bool SCALE = false>
-__device__ __forceinline__ void trace4(const double (&X)[n][n], const double (&P)[NQ][NU], const double *El,
-                                       double *tr, int fam, int E, int e, double sc = 1.0) {
-  double sB[n], sT[n], sL[n], sR[n];
+// The bottom/top pair (AXIS 0) and the left/right pair (AXIS 1) are separate passes, so that
+// only one pair's end sums are live at a time. With SCALE, every output is multiplied by sc.
+template <int NQ, int NU, int n, bool DER, int AXIS, bool SCALE>
+__device__ __forceinline__ void trace2(const double (&X)[n][n], const double (&P)[NQ][NU], const double *El,
+                                       double *tr, int fam, int E, int e, double sc) {
+  double sA[n], sZ[n];   // the end sums at the low (B or L) and the high (T or R) end
 #pragma unroll
   for (int b = 0; b < n; ++b) {
-    double xe = 0, xo = 0, ye = 0, yo = 0;
+    double xe = 0, xo = 0;
 #pragma unroll
-    for (int a = 0; a < n; a += 2) { xe = fma(El[a], X[a][b], xe); ye = fma(El[a], X[b][a], ye); }
+    for (int a = 0; a < n; a += 2) xe = fma(El[a], AXIS == 0 ? X[a][b] : X[b][a], xe);
 #pragma unroll
-    for (int a = 1; a < n; a += 2) { xo = fma(El[a], X[a][b], xo); yo = fma(El[a], X[b][a], yo); }
-    sB[b] = xe + xo; sL[b] = ye + yo;
-    sT[b] = DER ? xo - xe : xe - xo;
-    sR[b] = DER ? yo - ye : ye - yo;
+    for (int a = 1; a < n; a += 2) xo = fma(El[a], AXIS == 0 ? X[a][b] : X[b][a], xo);
+    sA[b] = xe + xo;
+    sZ[b] = DER ? xo - xe : xe - xo;
   }
-  auto put = [&](int i, double oB, double oT, double oL, double oR) {
-    if constexpr (SCALE) { oB *= sc; oT *= sc; oL *= sc; oR *= sc; }
-    tr[((fam * 4 + 0) * NQ + i) * (size_t)E + e] = oB;
-    tr[((fam * 4 + 1) * NQ + i) * (size_t)E + e] = oT;
-    tr[((fam * 4 + 2) * NQ + i) * (size_t)E + e] = oL;
-    tr[((fam * 4 + 3) * NQ + i) * (size_t)E + e] = oR;
+  auto put = [&](int i, double oA, double oZ) {
+    if constexpr (SCALE) { oA *= sc; oZ *= sc; }
+    tr[((fam * 4 + 2 * AXIS) * NQ + i) * (size_t)E + e] = oA;
+    tr[((fam * 4 + 2 * AXIS + 1) * NQ + i) * (size_t)E + e] = oZ;
   };
 #pragma unroll
   for (int i = 0; i < (NQ + 1) / 2; ++i) {
-    double eB = 0, eT = 0, eL = 0, eR = 0, oB = 0, oT = 0, oL = 0, oR = 0;
+    double eA = 0, eZ = 0, oA = 0, oZ = 0;
 #pragma unroll
-    for (int b = 0; b < n; b += 2) {
-      eB = fma(P[i][b], sB[b], eB); eT = fma(P[i][b], sT[b], eT);
-      eL = fma(P[i][b], sL[b], eL); eR = fma(P[i][b], sR[b], eR);
-    }
+    for (int b = 0; b < n; b += 2) { eA = fma(P[i][b], sA[b], eA); eZ = fma(P[i][b], sZ[b], eZ); }
     if (2 * i + 1 == NQ) {      // the middle point: the odd modes vanish there
-      put(i, eB, eT, eL, eR);
+      put(i, eA, eZ);
       continue;
     }
 #pragma unroll
-    for (int b = 1; b < n; b += 2) {
-      oB = fma(P[i][b], sB[b], oB); oT = fma(P[i][b], sT[b], oT);
-      oL = fma(P[i][b], sL[b], oL); oR = fma(P[i][b], sR[b], oR);
-    }
-    put(i, eB + oB, eT + oT, eL + oL, eR + oR);
-    put(NQ - 1 - i, eB - oB, eT - oT, eL - oL, eR - oR);
+    for (int b = 1; b < n; b += 2) { oA = fma(P[i][b], sA[b], oA); oZ = fma(P[i][b], sZ[b], oZ); }
+    put(i, eA + oA, eZ + oZ);
+    put(NQ - 1 - i, eA - oA, eZ - oZ);
   }
+}
+
+template <int NQ, int NU, int n, bool DER, bool SCALE = false>
+__device__ __forceinline__ void trace4(const double (&X)[n][n], const double (&P)[NQ][NU], const double *El,
+                                       double *tr, int fam, int E, int e, double sc = 1.0) {
+  trace2<NQ, NU, n, DER, 0, SCALE>(X, P, El, tr, fam, E, e, sc);
+  trace2<NQ, NU, n, DER, 1, SCALE>(X, P, El, tr, fam, E, e, sc);
 }
 
 template <int n>
@@ -409,19 +405,33 @@ __device__ __forceinline__ void prep_body(const Basis<NU, NV> &B, const Fields &
   long long kmin = LLONG_MAX, kmax = LLONG_MIN;
   bool nan = false;
   auto vx = [&](int a, int b) { return V[a][b]; };
+  auto point = [&](double y, int r, int s2) {
+    const size_t gi = (r + QH * s2) * (size_t)E + e;
+    const double g = y * F.beta2[gi];
+    F.G[gi] = g;
+    const long long bits = __double_as_longlong(g);
+    nan |= (bits & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+    const long long key = bits ^ ((bits >> 63) & 0x7fffffffffffffffLL);
+    kmin = min(kmin, key);
+    kmax = max(kmax, key);
+  };
+  // the points of row r: v_q = Σ_b T[b] Ph[s2][b], mirrored columns s2 and QH-1-s2 together
   auto points = [&](const double (&T)[NV], int r) {
-    double Y[QH];
-    ph_to_points<QH, NV>(B.Ph, T, Y);
 #pragma unroll
-    for (int s2 = 0; s2 < QH; ++s2) {
-      const size_t gi = (r + QH * s2) * (size_t)E + e;
-      const double g = Y[s2] * F.beta2[gi];
-      F.G[gi] = g;
-      const long long bits = __double_as_longlong(g);
-      nan |= (bits & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
-      const long long key = bits ^ ((bits >> 63) & 0x7fffffffffffffffLL);
-      kmin = min(kmin, key);
-      kmax = max(kmax, key);
+    for (int s2 = 0; s2 < QH / 2; ++s2) {
+      double ev = 0.0, od = 0.0;
+#pragma unroll
+      for (int b = 0; b < NV; b += 2) ev = fma(T[b], B.Ph[s2][b], ev);
+#pragma unroll
+      for (int b = 1; b < NV; b += 2) od = fma(T[b], B.Ph[s2][b], od);
+      point(ev + od, r, s2);
+      point(ev - od, r, QH - 1 - s2);
+    }
+    if constexpr ((QH & 1) != 0) {
+      double ev = 0.0;
+#pragma unroll
+      for (int b = 0; b < NV; b += 2) ev = fma(T[b], B.Ph[QH / 2][b], ev);
+      point(ev, r, QH / 2);
     }
   };
 #pragma unroll 1
@@ -482,11 +492,10 @@ __global__ void __launch_bounds__(128, 3) k_prep(const __grid_constant__ Basis<N
 template <int NU, int NV>
 __global__ void __launch_bounds__(128, 3) k_prep_m(const __grid_constant__ Basis<NU, NV> B,
                                                 const __grid_constant__ MultiStage P) {
-  __shared__ StageArgs sa;
   for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
-    const int inst = multi_begin(P, vb, sa);
+    const int inst = multi_begin(P, vb);
     const int e0 = (vb - P.first[inst]) * P.tile;
-    prep_body<NU, NV>(B, sa.F, sa.S, e0 + (int)threadIdx.x, e0 == 0);
+    prep_body<NU, NV>(B, P.a[inst].F, P.a[inst].S, e0 + (int)threadIdx.x, e0 == 0);
   }
 }
 
@@ -1101,14 +1110,19 @@ __global__ void __launch_bounds__(stage_threads(NU, NV, FAST), 2)
   stage_body<NU, NV, FAST>(B, F, S, blockIdx.x * BT + (int)threadIdx.x, threadIdx.x);
 }
 
+// Blocks per SM asked of the multi-instance k_stage: the residency the single-instance kernel
+// reaches with its registers at low degrees (the instance arguments in shared memory otherwise
+// take registers of their own and halve it)
+__host__ __device__ constexpr int stage_m_blocks(int nu) { return nu <= 2 ? 5 : nu == 3 ? 4 : nu == 4 ? 3 : 2; }
+
 // tile = stage_threads(NU, NV, FAST) elements per virtual block
 template <int NU, int NV, bool FAST>
-__global__ void __launch_bounds__(stage_threads(NU, NV, FAST), 2)
+__global__ void __launch_bounds__(stage_threads(NU, NV, FAST), stage_m_blocks(NU))
     k_stage_m(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ MultiStage P) {
-  __shared__ StageArgs sa;
   for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
-    const int inst = multi_begin(P, vb, sa);
-    stage_body<NU, NV, FAST>(B, sa.F, sa.S, (vb - P.first[inst]) * P.tile + (int)threadIdx.x, threadIdx.x);
+    const int inst = multi_begin(P, vb);
+    stage_body<NU, NV, FAST>(B, P.a[inst].F, P.a[inst].S, (vb - P.first[inst]) * P.tile + (int)threadIdx.x,
+                             threadIdx.x);
   }
 }
 
@@ -1459,12 +1473,11 @@ __global__ void __launch_bounds__(CHEB_THREADS, 3)
 template <int NU, int NV, bool CG>
 __global__ void __launch_bounds__(CHEB_THREADS, 3)
     k_mass_m(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ MultiStage P) {
-  __shared__ StageArgs sa;
   for (int vb = blockIdx.x; vb < P.first[P.n]; vb += gridDim.x) {
-    const int inst = multi_begin(P, vb, sa);
+    const int inst = multi_begin(P, vb);
     const int g0 = (vb - P.first[inst]) * P.tile;
-    if constexpr (CG) cg_body<NU, NV>(B, sa.F, sa.S, g0);
-    else cheb_body<NU, NV>(B, sa.F, sa.S, g0);
+    if constexpr (CG) cg_body<NU, NV>(B, P.a[inst].F, P.a[inst].S, g0);
+    else cheb_body<NU, NV>(B, P.a[inst].F, P.a[inst].S, g0);
   }
 }
 

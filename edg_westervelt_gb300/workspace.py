@@ -419,8 +419,9 @@ class Workspace:
 class Batch:
     """Many independent instances advanced together (wedg_batch_*): each a Workspace of its own
     N, degrees, flux, boundary kinds and coefficients. Instances that run the same kernels form a
-    bucket, and every stage kernel runs once per bucket over all of its instances; one RK4 step
-    of all of them is one replay of a CUDA graph. No counterpart in the reference (there,
+    bucket, whose instances run their own launches on their own streams (the default) or every
+    stage kernel once over all of them (set_shape, autotune); the steps are replays of CUDA graphs
+    of one and of four RK4 steps of all instances. No counterpart in the reference (there,
     batching is a loop over solves)."""
 
     def __init__(self, workspaces):
@@ -479,7 +480,8 @@ class Batch:
 
     def set_shape(self, bucket, prep_threads, mass_threads, persist=0):
         """wedg_batch_set_shape: the launch shape of one bucket (results do not depend on it);
-        persist -1 launches the bucket's instances one by one."""
+        persist -1 launches the bucket's instances one by one (the default), 0 runs each stage
+        kernel once over them, p > 0 the same on a persistent grid."""
         rc = L.lib().wedg_batch_set_shape(self._h, int(bucket), int(prep_threads), int(mass_threads), int(persist))
         if rc != L.WEDG_OK:
             raise ErrorException("launch shapes are 32, 64, 96 or 128 threads per block and persist -1 to 8")

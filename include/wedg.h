@@ -322,15 +322,18 @@ int wedg_set_adjoint_memory(wedg_ws *ws, int64_t bytes);
  * the reference, whose batching is the caller's loop over instances (the element blocks of
  * src/rhs.jl:130-180, 227-252 split one instance). The instances are grouped into buckets that
  * run the same kernels (the same degrees, coefficient kernels, mass solver and 1D operators;
- * any mesh sizes). Per stage of an RK4 step, each bucket runs k_prep, k_stage and its mass
- * solve as one launch each over all of its instances (up to 32 instances per launch; larger
- * buckets take several), whose blocks each take a tile of one instance's elements, so an
- * element's arithmetic is the one of a launch of its instance alone. The buckets run side by
- * side on their own streams; one RK4 step of the whole batch is captured once into a CUDA graph
- * and replayed for every step. The stage kernels of a replay take their time factors from
- * per-instance tables that the host refills every WEDG_BATCH_CHUNK steps (the factors are the
- * ones the single-instance calls compute). The graph is captured again when the state
- * pointers, the steps dt, stop_nonfinite or a bucket's launch shape change. */
+ * any mesh sizes). A bucket runs in one of two layouts (wedg_batch_set_shape): its instances'
+ * own launches, each instance on its own stream (the default, the faster on the mixed batches
+ * measured), or per stage of an RK4 step k_prep, k_stage and its mass solve as one launch each
+ * over all of its instances (up to 32 instances per launch; larger buckets take several), whose
+ * blocks each take a tile of one instance's elements. Either way an element's arithmetic is the
+ * one of a launch of its instance alone. The buckets run side by side on their own streams. One
+ * RK4 step of the whole batch, and four steps in which each instance (or merged bucket) goes on
+ * to its next step without waiting for the others, are captured once into CUDA graphs and
+ * replayed. The stage kernels of a replay take their time factors from per-instance tables that
+ * the host refills every WEDG_BATCH_CHUNK steps (the factors are the ones the single-instance
+ * calls compute), at the instance's device step counter. The graphs are captured again when the
+ * state pointers, the steps dt, stop_nonfinite or a bucket's launch shape change. */
 #define WEDG_BATCH_CHUNK 256
 typedef struct wedg_batch wedg_batch;
 int wedg_batch_create(int n, wedg_ws *const *instances, wedg_batch **out);
@@ -349,9 +352,9 @@ int wedg_batch_rk4_steps(wedg_batch *b, double *const *u_dev, double *const *v_d
  * one element each) and of the mass solves (threads / 32 warps of teams of threads per
  * element), 32, 64, 96 or 128 threads, and `persist`: 0 launches one block per tile, p > 0 a
  * persistent grid of p times the blocks the SMs hold at once, each block taking tile after
- * tile; -1 launches the bucket's instances one by one instead (the single-instance kernels, each
- * instance on its own stream). Results do not depend on the shape (every element's arithmetic
- * is its own). */
+ * tile; -1 (the default) launches the bucket's instances one by one instead (the single-instance
+ * kernels, each instance on its own stream). Results do not depend on the shape (every element's
+ * arithmetic is its own). */
 typedef struct wedg_batch_shape {
   int32_t qu1, qv1, instances, fast;   /* the bucket's degrees + 1, its instances, the kernel family */
   int32_t prep_threads, mass_threads, persist;
@@ -366,10 +369,10 @@ int wedg_batch_set_shape(wedg_batch *b, int bucket, int prep_threads, int mass_t
  * candidates of one coordinate at a time (persist: -1, 0, 1, 2; then k_prep's and the mass
  * solves' threads per block: 32, 64, 128). A candidate replaces the bucket's shape only when it is faster in
  * each of three paired trials against it and faster by more than 2 % in the median. Then the
- * whole batch's step (graph replays) with the tuned shapes against the shapes it had before,
- * three paired trials: the tuned shapes stay only if they win every trial, so the batch never
- * ends up slower than before tuning. *best_ms (may be NULL) receives the median milliseconds per
- * step of the shapes kept. */
+ * whole batch's step (graph replays over at least 8 steps) with the tuned shapes against the
+ * shapes it had before, three paired trials: the tuned shapes stay only if they win every trial,
+ * so the batch never ends up slower than before tuning. *best_ms (may be NULL) receives the
+ * median milliseconds per step of the shapes kept. */
 int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_dev, const double *t0,
                         const double *dt, int64_t steps, double *best_ms);
 

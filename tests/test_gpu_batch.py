@@ -42,10 +42,12 @@ def _setup():
 
 
 def test_batch_matches_single_instances():
+    """602 steps: two table chunks of 256 and a third of 90, run as graphs of four steps and, for
+    the last two, of one step; then 3 more steps (graphs of one step)."""
     import torch
     dev = torch.device("cuda:0")
     inst = _setup()
-    nsteps = 600
+    nsteps = 602
     ref = []
     for pre, N, u, v, dt, t0 in inst:
         ws = W.Workspace(pre, N)
