@@ -39,7 +39,7 @@ class Config(ctypes.Structure):
                 + [(n, ctypes.c_double) for n in ("mass_tol", "src_omega", "src_Ts")]
                 + [("kind", ctypes.c_int32 * 4)]
                 + [(n, ctypes.c_double * 4) for n in ("gamma_abc", "eta_abc", "sigma", "kb", "kappa")]
-                + [("cheb_steps", ctypes.c_int32), ("general_only", ctypes.c_int32)])
+                + [("cheb_steps", ctypes.c_int32), ("general_only", ctypes.c_int32), ("point_traces", ctypes.c_int32)])
 
 
 class Pre(ctypes.Structure):
@@ -51,7 +51,7 @@ class Stats(ctypes.Structure):
                 ("finite", ctypes.c_int32), ("fast_path", ctypes.c_int32),
                 ("steps_done", ctypes.c_int64), ("kernel_launches", ctypes.c_int64),
                 ("device_bytes", ctypes.c_int64), ("cheb_steps_sum", ctypes.c_int64),
-                ("element_stages", ctypes.c_int64)]
+                ("element_stages", ctypes.c_int64), ("modal_traces", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class FaceValues(ctypes.Structure):

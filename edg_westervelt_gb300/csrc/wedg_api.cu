@@ -140,6 +140,7 @@ struct wedg_ws {
   BasisHost bh;
   std::vector<char> basis;
   Fields F{};
+  bool modal_ok = false;   // the traces may be kept as modal end sums (Fields::modal)
   cudaStream_t own_stream = nullptr, stream = nullptr;
   // host-state calls: copies beside the workspace's stream (created on first use)
   cudaStream_t copy_stream = nullptr;
@@ -195,6 +196,18 @@ struct wedg_ws {
 };
 
 namespace {
+
+// The point traces of the adjoint calls: the adjoint kernels read the traces at the face points,
+// so the forward kernels these calls run keep point traces while the guard lives
+struct PointTraces {
+  std::vector<wedg_ws *> G;
+  explicit PointTraces(const std::vector<wedg_ws *> &g) : G(g) {
+    for (wedg_ws *w : G) w->F.modal = 0;
+  }
+  ~PointTraces() {
+    for (wedg_ws *w : G) w->F.modal = w->modal_ok ? 1 : 0;
+  }
+};
 
 int cuda_fail(wedg_ws *ws, cudaError_t e, const char *what) {
   if (ws) {
@@ -913,6 +926,7 @@ namespace {
 int adjoint_forward_group(const std::vector<wedg_ws *> &G, const double *const *u0, const double *const *v0,
                           double t0, double dt, int64_t nsteps, int64_t every, double *const *uT, double *const *vT,
                           int where) {
+  PointTraces point_traces(G);
   const int n = (int)G.size();
   if (nsteps < 0 || every < 1) return argument_error(G[0], "nsteps must be ≥ 0 and the checkpoint interval ≥ 1");
   const int64_t nchk = nsteps ? (nsteps + every - 1) / every : 0;
@@ -997,6 +1011,7 @@ int adjoint_forward_group(const std::vector<wedg_ws *> &G, const double *const *
 int adjoint_reverse_group(const std::vector<wedg_ws *> &G, const double *const *lam_u, const double *const *lam_v,
                           double *const *gu, double *const *gv, double *const *g_c2, double *const *g_alpha,
                           double *const *g_beta, int where) {
+  PointTraces point_traces(G);
   const int n = (int)G.size();
   for (wedg_ws *ws : G) ws->stats.kernel_launches = 0;
   const bool params = g_c2[0] || g_alpha[0] || g_beta[0];
@@ -1671,6 +1686,38 @@ int upload_boundary(wedg_ws *ws, const wedg_pre *pre) {
   return WEDG_OK;
 }
 
+// Whether the traces can be kept as modal end sums (Fields::modal): sets *flag when an interior
+// face's coefficient values differ along the face or, with one-sided faces, its jump term is not
+// zero. One thread per interior face: the horizontal faces (jf, k), jf = 1..N-1, then the vertical
+// faces (j, kf), kf = 1..N-1, in the device layouts [jf + (N+1)(k + N i)] and [j + N(kf + (N+1) i)].
+__global__ void k_modal_check(const Fields F, int nq, unsigned *flag) {
+  const int N = F.N;
+  const int nh = (N - 1) * N;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * nh) return;
+  const bool hor = t < nh;
+  const int r = hor ? t : t - nh;
+  size_t f0;
+  const size_t stride = (size_t)(N + 1) * N;
+  const double *c2, *af, *c2m, *afm, *jc;
+  if (hor) {
+    f0 = (size_t)(1 + r % (N - 1)) + (size_t)(N + 1) * (r / (N - 1));
+    c2 = F.hc2; af = F.haf; c2m = F.hc2m; afm = F.hafm; jc = F.hJC;
+  } else {
+    f0 = (size_t)(r % N) + (size_t)N * (1 + r / N);
+    c2 = F.vc2; af = F.vaf; c2m = F.vc2m; afm = F.vafm; jc = F.vJC;
+  }
+  bool ok = true;
+  for (int i = 1; i < nq; ++i) {
+    const size_t fi = f0 + stride * i;
+    ok = ok && c2[fi] == c2[f0] && af[fi] == af[f0];
+    if (F.one_sided) ok = ok && c2m[fi] == c2m[f0] && afm[fi] == afm[f0];
+  }
+  if (F.one_sided)
+    for (int i = 0; i < nq; ++i) ok = ok && jc[f0 + stride * i] == 0.0;
+  if (!ok) atomicOr(flag, 1u);
+}
+
 // The scratch of the workspace, the kernels' scalars and its stream (the last part of wedg_create)
 int create_finish(wedg_ws *ws) {
   const wedg_config *cfg = &ws->cfg;
@@ -1723,6 +1770,31 @@ int create_finish(wedg_ws *ws) {
     return r;
   }
   ws->stream = ws->own_stream;
+  // traces as modal end sums when every interior face's coefficients are one value along it (after
+  // the face arrays' uploads or set-up kernels on any stream)
+  const int nface = 2 * (N - 1) * N;
+  unsigned flag = cfg->point_traces ? 1u : 0u;
+  if (nface > 0 && !flag) {
+    unsigned *d = nullptr;
+    ce = cudaDeviceSynchronize();
+    if (ce == cudaSuccess) ce = cudaMalloc(&d, sizeof(unsigned));
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(d, 0, sizeof(unsigned), ws->stream);
+    if (ce == cudaSuccess) {
+      k_modal_check<<<(nface + 255) / 256, 256, 0, ws->stream>>>(F, nq, d);
+      ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&flag, d, sizeof(unsigned), cudaMemcpyDeviceToHost, ws->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(ws->stream);
+    if (d) cudaFree(d);
+    if (ce != cudaSuccess) {
+      int r = cuda_fail(ws, ce, "wedg_create");
+      wedg_destroy(ws);
+      return r;
+    }
+  }
+  ws->modal_ok = flag == 0;
+  F.modal = ws->modal_ok ? 1 : 0;
+  ws->stats.modal_traces = F.modal;
   ws->stats.fast_path = ws->fast ? 1 : 0;
   ws->stats.device_bytes = (int64_t)ws->bytes;
   cudaDeviceSynchronize();
@@ -2063,7 +2135,7 @@ int wedg_export(const wedg_ws *ws, const char *name, double *out, size_t count) 
   const std::string n(name);
   // the device array, the kind of its layout, its size
   const double *src = nullptr;
-  int kind = -1;            // 0: h-faces, 1: v-faces, 2: projections, 3: 2β, 4: per element, 5: Cw, Aw
+  int kind = -1;            // 0: h-faces, 1: v-faces, 2: projections, 3: 2β, 4: per element, 5: Cw, Aw, 6: traces
   const struct {
     const char *name;
     const double *p;
@@ -2073,15 +2145,17 @@ int wedg_export(const wedg_ws *ws, const char *name, double *out, size_t count) 
              {"vaf", F.vaf, 1},      {"vcf", F.vcf, 1},       {"vbf", F.vbf, 1},         {"vc2m", F.vc2m, 1},
              {"vafm", F.vafm, 1},    {"vJC", F.vJC, 1},       {"PiSP", F.PiSP, 2},       {"PiBSP2", F.PiBSP2, 2},
              {"PiCdiv", F.PiCdiv, 2}, {"PiDdiv", F.PiDdiv, 2}, {"src_projE", F.srcP, 2}, {"beta_hq", F.beta2, 3},
-             {"c2e", F.c2e, 4},      {"ae", F.ae, 4},         {"Cw", F.Cw, 5},           {"Aw", F.Aw, 5}};
+             {"c2e", F.c2e, 4},      {"ae", F.ae, 4},         {"Cw", F.Cw, 5},           {"Aw", F.Aw, 5},
+             {"tr", F.tr, 6}};
   for (const auto &t : tab)
     if (n == t.name) {
       src = t.p;
       kind = t.kind;
     }
   if (kind < 0 || !src) return WEDG_ERR_ARGUMENT;
-  const size_t sizes[6] = {(size_t)nq * (N + 1) * N, (size_t)nq * N * (N + 1), (size_t)nv * nv * E,
-                           (size_t)qh * qh * E,      (size_t)E,                 (size_t)nq * nq * E};
+  const size_t sizes[7] = {(size_t)nq * (N + 1) * N, (size_t)nq * N * (N + 1), (size_t)nv * nv * E,
+                           (size_t)qh * qh * E,      (size_t)E,                 (size_t)nq * nq * E,
+                           (size_t)12 * nq * E};
   const size_t len = sizes[kind];
   if (count != len) return WEDG_ERR_DIMENSION;
   std::vector<double> d(len);
@@ -2089,6 +2163,9 @@ int wedg_export(const wedg_ws *ws, const char *name, double *out, size_t count) 
   const size_t Es = (size_t)E;
   for (size_t t = 0; t < len; ++t) {
     switch (kind) {
+      case 6:     // the traces of the last evaluation, in the device layout [((fam 4 + side) nq + i) E + e]
+        out[t] = d[t];
+        break;
       case 0: {   // [jf + (N+1)(k + N i)] -> (nq, N+1, N)
         const size_t jf = t % (N + 1), k = (t / (N + 1)) % N, i = t / ((size_t)(N + 1) * N);
         out[i + nq * (jf + (size_t)(N + 1) * k)] = d[t];
@@ -2739,7 +2816,10 @@ int wedg_rhs_adjoint(wedg_ws *ws, const double *u, const double *v, double t, co
     dgu = ws->d_ut; dgv = ws->d_vt;
   }
   if ((rc = reset_flags(ws))) return rc;
-  if ((rc = enqueue_rhs_adjoint(ws, du, dv, t, dlu, dlv, dgu, dgv))) return rc;
+  {
+    PointTraces point_traces({ws});
+    if ((rc = enqueue_rhs_adjoint(ws, du, dv, t, dlu, dlv, dgu, dgv))) return rc;
+  }
   rc = collect(ws);
   if (where == WEDG_HOST) {
     CK(ws, cudaMemcpy(gu, ws->d_ut, bU, cudaMemcpyDeviceToHost));

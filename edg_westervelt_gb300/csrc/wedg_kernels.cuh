@@ -108,6 +108,10 @@ struct Fields {
   unsigned int *cg_nfail, *nonfinite;
   double theta, tau, lu, lv, omega, two_h, four_hh, mass_tol, Lcheb;
   int one_sided, mms_on, src_on, cg, cheb_common, sorted;
+  // modal traces: tr holds each side's modal end sums (index b < n in place of point i), and the
+  // interior slots are projected in that form (every interior face's coefficients are one value
+  // along the face and its jump term vanishes; the adjoint kernels read point traces)
+  int modal;
   int kind[4];
   double gam[4], eta[4], sig[4], kb[4], kap[4];
 };
@@ -181,7 +185,7 @@ struct Multi {
 };
 
 // CAP is what fits the kernel parameter limit (32 764 bytes) beside the largest Basis
-using MultiStage = Multi<StageArgs, 32>;
+using MultiStage = Multi<StageArgs, 31>;
 
 // The instance of virtual block vb. The kernels read that instance's arguments where they lie, in
 // the parameter block: the index is the same for the whole block, so the reads are uniform
@@ -300,7 +304,7 @@ __device__ __forceinline__ void ph_row_mid(const double (&Ph)[QH][NV], const X &
 // only one pair's end sums are live at a time. With SCALE, every output is multiplied by sc.
 template <int NQ, int NU, int n, bool DER, int AXIS, bool SCALE>
 __device__ __forceinline__ void trace2(const double (&X)[n][n], const double (&P)[NQ][NU], const double *El,
-                                       double *tr, int fam, int E, int e, double sc) {
+                                       double *tr, int fam, int E, int e, double sc, bool modal) {
   double sA[n], sZ[n];   // the end sums at the low (B or L) and the high (T or R) end
 #pragma unroll
   for (int b = 0; b < n; ++b) {
@@ -317,6 +321,11 @@ __device__ __forceinline__ void trace2(const double (&X)[n][n], const double (&P
     tr[((fam * 4 + 2 * AXIS) * NQ + i) * (size_t)E + e] = oA;
     tr[((fam * 4 + 2 * AXIS + 1) * NQ + i) * (size_t)E + e] = oZ;
   };
+  if (modal) {            // the end sums themselves, mode b in the slot of point b
+#pragma unroll
+    for (int b = 0; b < n; ++b) put(b, sA[b], sZ[b]);
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < (NQ + 1) / 2; ++i) {
     double eA = 0, eZ = 0, oA = 0, oZ = 0;
@@ -335,9 +344,20 @@ __device__ __forceinline__ void trace2(const double (&X)[n][n], const double (&P
 
 template <int NQ, int NU, int n, bool DER, bool SCALE = false>
 __device__ __forceinline__ void trace4(const double (&X)[n][n], const double (&P)[NQ][NU], const double *El,
-                                       double *tr, int fam, int E, int e, double sc = 1.0) {
-  trace2<NQ, NU, n, DER, 0, SCALE>(X, P, El, tr, fam, E, e, sc);
-  trace2<NQ, NU, n, DER, 1, SCALE>(X, P, El, tr, fam, E, e, sc);
+                                       double *tr, int fam, int E, int e, double sc = 1.0, bool modal = false) {
+  trace2<NQ, NU, n, DER, 0, SCALE>(X, P, El, tr, fam, E, e, sc, modal);
+  trace2<NQ, NU, n, DER, 1, SCALE>(X, P, El, tr, fam, E, e, sc, modal);
+}
+
+// The value at face point i of side `side` of trace family fam of element e held as modal end sums
+// (Fields::modal): Σ_b P[i][b] t[b] over the family's n modes
+template <int NQ, int NU, int n>
+__device__ __forceinline__ double modal_at(const double (&P)[NQ][NU], const double *tr, int fam, int side, int i,
+                                           size_t E, int e) {
+  double x = 0.0;
+#pragma unroll
+  for (int b = 0; b < n; ++b) x = fma(P[i][b], tr[((fam * 4 + side) * NQ + b) * E + e], x);
+  return x;
 }
 
 template <int n>
@@ -362,15 +382,16 @@ __device__ __forceinline__ void prep_body(const Basis<NU, NV> &B, const Fields &
   if (e >= E) return;
   if (err_word(F) != ERR_NONE) return;
   const int j = e % N, k = e / N;
+  const bool modal = F.modal != 0;
   {
     double U[NU][NU];
     load_regs<NU>(U, S.xu, E, e);
-    trace4<NQ, NU, NU, true>(U, B.P, B.E1l, F.tr, 0, E, e);
+    trace4<NQ, NU, NU, true>(U, B.P, B.E1l, F.tr, 0, E, e, 1.0, modal);
   }
   double V[NV][NV];
   load_regs<NV>(V, S.xv, E, e);
-  trace4<NQ, NU, NV, false>(V, B.P, B.El, F.tr, 1, E, e);
-  trace4<NQ, NU, NV, true>(V, B.P, B.E1l, F.tr, 2, E, e);
+  trace4<NQ, NU, NV, false>(V, B.P, B.El, F.tr, 1, E, e, 1.0, modal);
+  trace4<NQ, NU, NV, true>(V, B.P, B.E1l, F.tr, 2, E, e, 1.0, modal);
 
   const TimeF tf = time_factors(S);
   // weight check 1 - kβv > 0 for the trace and the data on physical sides
@@ -385,7 +406,8 @@ __device__ __forceinline__ void prep_body(const Basis<NU, NV> &B, const Fields &
     for (int i = 0; i < NQ; ++i) {
       const double bf = s < 2 ? F.hbf[(s == 0 ? 0 : N) + (size_t)(N + 1) * (k + (size_t)N * i)]
                               : F.vbf[j + (size_t)N * ((s == 2 ? 0 : N) + (size_t)(N + 1) * i)];
-      const double v_fp = F.tr[((1 * 4 + s) * NQ + i) * (size_t)E + e];
+      const double v_fp = modal ? modal_at<NQ, NU, NV>(B.P, F.tr, 1, s, i, E, e)
+                                : F.tr[((1 * 4 + s) * NQ + i) * (size_t)E + e];
       const double v_ex = -F.omega * tf.st * F.bsp[s][m + (size_t)N * i];
       const int check = (1.0 - F.kb[s] * bf * v_fp <= 0.0) ? 1 : (1.0 - F.kb[s] * bf * v_ex <= 0.0) ? 2 : 0;
       if (check) {
@@ -569,9 +591,10 @@ __device__ __forceinline__ void side_point(const Basis<NU, NV> &B, const Fields 
     if (s < 2) { fi = (s == 0 ? 0 : N) + (size_t)(N + 1) * (k + (size_t)N * i); c2a = F.hc2; afa = F.haf; cfa = F.hcf; bfa = F.hbf; }
     else { fi = j + (size_t)N * ((s == 2 ? 0 : N) + (size_t)(N + 1) * i); c2a = F.vc2; afa = F.vaf; cfa = F.vcf; bfa = F.vbf; }
     const double c2f = c2a[fi], af = afa[fi], cf = cfa[fi];
-    const double v_fp = T(1, s, e);
-    const double gun = sgn * (F.two_h * T(0, s, e));
-    const double gvn = sgn * (F.two_h * T(2, s, e));
+    const bool modal = F.modal != 0;
+    const double v_fp = modal ? modal_at<NQ, NU, NV>(B.P, tr, 1, s, i, E, e) : T(1, s, e);
+    const double gun = sgn * (F.two_h * (modal ? modal_at<NQ, NU, NU>(B.P, tr, 0, s, i, E, e) : T(0, s, e)));
+    const double gvn = sgn * (F.two_h * (modal ? modal_at<NQ, NU, NV>(B.P, tr, 2, s, i, E, e) : T(2, s, e)));
     const double spn = F.bspn[s][m + (size_t)N * i], sp = F.bsp[s][m + (size_t)N * i];
     const double gu_ex = sgn * (S.ct * spn - spn);
     const double gv_ex = sgn * (-F.omega * S.st * spn);
@@ -616,6 +639,52 @@ __device__ __forceinline__ void side_point(const Basis<NU, NV> &B, const Fields 
   const double dvm = T(2, sm, em), dvp = T(2, spp, ep);
   const FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);
   interior_flux(F, cf, plus, dum, dup, vm, vp, dvm, dvp, A, D, Fs);
+}
+
+// The projections Y_A, Y_D (b < NV) and Y_F (b < NU) of the flux slots of interior side s, with
+// the traces held as modal end sums (Fields::modal). The face coefficients are one value along the
+// face and the jump term vanishes, so every slot is a linear combination of the six traces with
+// the same weights at every point, and its projection Σ_i w_i P[i][b] (.)_i is that combination of
+// the traces' modes b: the face rule integrates the product of two modes exactly and the modes
+// are orthonormal. The same results as the point form of side_point and the projections, to
+// rounding.
+template <int NU, int NV>
+__device__ __forceinline__ void modal_side(const Fields &F, int s, int j, int k, int e, double (&YA)[NV],
+                                           double (&YD)[NV], double (&YF)[NU]) {
+  constexpr int NQ = NU;
+  const int N = F.N;
+  const size_t E = F.E;
+  const bool plus = (s == 0 || s == 2);
+  const int nb = s == 0 ? e - 1 : s == 1 ? e + 1 : s == 2 ? e - N : e + N;
+  const int sm = s < 2 ? 1 : 3, spp = s < 2 ? 0 : 2;      // trace sides of the "-" and "+" elements
+  const int em = plus ? nb : e, ep = plus ? e : nb;
+  size_t fi;
+  const double *c2p_a, *afp_a, *c2m_a, *afm_a, *jc_a;
+  if (s < 2) {
+    fi = (s == 0 ? j : j + 1) + (size_t)(N + 1) * k;
+    c2p_a = F.hc2; afp_a = F.haf; c2m_a = F.hc2m; afm_a = F.hafm; jc_a = F.hJC;
+  } else {
+    fi = j + (size_t)N * (s == 2 ? k : k + 1);
+    c2p_a = F.vc2; afp_a = F.vaf; c2m_a = F.vc2m; afm_a = F.vafm; jc_a = F.vJC;
+  }
+  FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);   // point 0 of the face
+  cf.K = 0.0;
+  const double *tr = F.tr;
+  // mode b of trace family fam on side `side` of element el
+  auto T = [&](int fam, int side, int el, int b) { return tr[((fam * 4 + side) * NQ + b) * E + el]; };
+#pragma unroll
+  for (int b = 0; b < NU; ++b) {
+    const double dum = T(0, sm, em, b), dup = T(0, spp, ep, b);
+    double vm = 0.0, vp = 0.0, dvm = 0.0, dvp = 0.0;
+    if (b < NV) {
+      vm = T(1, sm, em, b); vp = T(1, spp, ep, b);
+      dvm = T(2, sm, em, b); dvp = T(2, spp, ep, b);
+    }
+    double A, D, Fs;
+    interior_flux(F, cf, plus, dum, dup, vm, vp, dvm, dvp, A, D, Fs);
+    if (b < NV) { YA[b] = A; YD[b] = D; }
+    YF[b] = Fs;
+  }
 }
 
 // ----------------------------------------------------------------------------
@@ -665,33 +734,37 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
         if (b < NV) { YA[b] = 0.0; YD[b] = 0.0; }
         YF[b] = 0.0;
       }
+      if (F.modal && !boundary) {
+        modal_side<NU, NV>(F, s, j, k, e, YA, YD, YF);
+      } else {
 #pragma unroll 1
-      for (int i = 0; i < NQ / 2; ++i) {
-        double A1, D1, F1, A2, D2, F2;
-        side_point<NU, NV>(B, F, tf, s, boundary, j, k, e, i, A1, D1, F1);
-        side_point<NU, NV>(B, F, tf, s, boundary, j, k, e, NQ - 1 - i, A2, D2, F2);
-        const double as = A1 + A2, ad = A1 - A2, ds = D1 + D2, dd = D1 - D2, fs = F1 + F2, fd = F1 - F2;
+        for (int i = 0; i < NQ / 2; ++i) {
+          double A1, D1, F1, A2, D2, F2;
+          side_point<NU, NV>(B, F, tf, s, boundary, j, k, e, i, A1, D1, F1);
+          side_point<NU, NV>(B, F, tf, s, boundary, j, k, e, NQ - 1 - i, A2, D2, F2);
+          const double as = A1 + A2, ad = A1 - A2, ds = D1 + D2, dd = D1 - D2, fs = F1 + F2, fd = F1 - F2;
 #pragma unroll
-        for (int b = 0; b < NU; ++b) {
-          const double p = B.Pw[i][b];
-          if (b < NV) {
-            YA[b] = fma(p, (b & 1) ? ad : as, YA[b]);
-            YD[b] = fma(p, (b & 1) ? dd : ds, YD[b]);
+          for (int b = 0; b < NU; ++b) {
+            const double p = B.Pw[i][b];
+            if (b < NV) {
+              YA[b] = fma(p, (b & 1) ? ad : as, YA[b]);
+              YD[b] = fma(p, (b & 1) ? dd : ds, YD[b]);
+            }
+            YF[b] = fma(p, (b & 1) ? fd : fs, YF[b]);
           }
-          YF[b] = fma(p, (b & 1) ? fd : fs, YF[b]);
         }
-      }
-      if constexpr ((NQ & 1) != 0) {         // the middle point: the odd modes vanish there
-        double A1, D1, F1;
-        side_point<NU, NV>(B, F, tf, s, boundary, j, k, e, NQ / 2, A1, D1, F1);
+        if constexpr ((NQ & 1) != 0) {         // the middle point: the odd modes vanish there
+          double A1, D1, F1;
+          side_point<NU, NV>(B, F, tf, s, boundary, j, k, e, NQ / 2, A1, D1, F1);
 #pragma unroll
-        for (int b = 0; b < NU; b += 2) {
-          const double p = B.Pw[NQ / 2][b];
-          if (b < NV) {
-            YA[b] = fma(p, A1, YA[b]);
-            YD[b] = fma(p, D1, YD[b]);
+          for (int b = 0; b < NU; b += 2) {
+            const double p = B.Pw[NQ / 2][b];
+            if (b < NV) {
+              YA[b] = fma(p, A1, YA[b]);
+              YD[b] = fma(p, D1, YD[b]);
+            }
+            YF[b] = fma(p, F1, YF[b]);
           }
-          YF[b] = fma(p, F1, YF[b]);
         }
       }
       if (t == 0) {

@@ -121,9 +121,12 @@ class Workspace:
     cheb_steps: "per_element" (default; every element takes the Chebyshev step
     count its own spectral interval needs, each to the same tolerance) or
     "common_max" (all elements take the largest count, as src/rhs.jl:911-918).
+    fast_path=False keeps the quadrature form of the volume terms and the stored
+    inverses; modal_traces=False keeps the traces at the face points (the interior
+    flux slots are then evaluated point by point, as src/rhs.jl:589-700 does).
     """
 
-    def __init__(self, pre, N, nblocks=None, cheb_steps="per_element", fast_path=True):
+    def __init__(self, pre, N, nblocks=None, cheb_steps="per_element", fast_path=True, modal_traces=True):
         if nblocks is None:
             nblocks = _default_nblocks(pre, N)
         if not nblocks >= 1:
@@ -158,6 +161,7 @@ class Workspace:
             cfg.kb[i], cfg.kappa[i] = bs["kb"], bs["kappa"]
         cfg.cheb_steps = {"per_element": 0, "common_max": 1}[cheb_steps]
         cfg.general_only = 0 if fast_path else 1
+        cfg.point_traces = 0 if modal_traces else 1
         self._cfg = cfg
         keep = {}
         p = L.Pre()

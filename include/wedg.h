@@ -63,6 +63,9 @@ typedef struct wedg_config {
   int32_t cheb_steps;                    /* wedg_cheb_steps: per-element count (default) or the
                                             reference's common maximum (src/rhs.jl:911-918) */
   int32_t general_only;                  /* 1: never use the constant-coefficient kernels */
+  int32_t point_traces;                  /* 1: keep the traces at the face points; 0: as modal end sums
+                                            where every interior face's coefficients are one value along
+                                            it and no jump term is present (wedg_stats.modal_traces) */
 } wedg_config;
 
 /* Host pointers to the arrays of `pre`, each in the reference's layout
@@ -94,6 +97,11 @@ typedef struct wedg_stats {
   int64_t device_bytes;        /* device memory held by the workspace */
   int64_t cheb_steps_sum;      /* Σ over elements and stages of the Chebyshev step counts */
   int64_t element_stages;      /* elements × stages evaluated by the last call */
+  int32_t modal_traces;        /* 1 if the traces are kept as modal end sums and the interior flux
+                                  slots projected in that form (every interior face's coefficients
+                                  one value along the face, no jump term); the adjoint calls use
+                                  point traces */
+  int32_t reserved;
 } wedg_stats;
 
 typedef struct wedg_ws wedg_ws;
@@ -156,7 +164,9 @@ int wedg_one_sided(const wedg_ws *ws);
 /* A device array of the workspace in the reference's layout of the `pre` array of that name (for checks
  * of the device-built arrays): hc2 haf hcf hbf hc2m hafm hJC and the v-face arrays, PiSP PiBSP2 PiCdiv
  * PiDdiv src_projE, beta_hq; Cw, Aw (general kernels); c2e, ae (c² and α per element, constant-coefficient
- * kernels). count must be the array's size; arrays the workspace does not hold are refused. */
+ * kernels); tr, the traces of the last evaluation in the device layout [((fam 4 + side) q_u1 + i) E + e]
+ * (fam du, v, dv; side B, T, L, R; i a face point, or a mode with wedg_stats.modal_traces). count must be
+ * the array's size; arrays the workspace does not hold are refused. */
 int wedg_export(const wedg_ws *ws, const char *name, double *out, size_t count);
 
 /* edg_rhs!(ws, u, v, t, N, h, pre) of src/rhs.jl:490-550: ut, vt receive the
@@ -325,7 +335,7 @@ int wedg_set_adjoint_memory(wedg_ws *ws, int64_t bytes);
  * any mesh sizes). A bucket runs in one of two layouts (wedg_batch_set_shape): its instances'
  * own launches, each instance on its own stream (the default, the faster on the mixed batches
  * measured), or per stage of an RK4 step k_prep, k_stage and its mass solve as one launch each
- * over all of its instances (up to 32 instances per launch; larger buckets take several), whose
+ * over all of its instances (up to 31 instances per launch; larger buckets take several), whose
  * blocks each take a tile of one instance's elements. Either way an element's arithmetic is the
  * one of a launch of its instance alone. The buckets run side by side on their own streams. One
  * RK4 step of the whole batch, and four steps in which each instance (or merged bucket) goes on

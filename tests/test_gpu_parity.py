@@ -534,3 +534,73 @@ def test_rk4_steps_common_count_against_oracle(gpu):
         W.rk4_step_(u, v, 0.1 + k * dt, dt, N, 1.0 / N, pp, ws)
     assert ws.stats()["cheb_steps_max"] > 20
     assert rel_max((uo, vo), (u, v)) < TOL, rel_max((uo, vo), (u, v))
+
+
+def test_modal_traces_against_oracle(gpu):
+    """The traces kept as modal end sums (interior faces with one coefficient value along them and
+    no jump term: constant coefficients, and coefficients constant on cells of the mesh in source
+    mode, whose one-sided faces carry no jump term), against the oracle's point form: one RHS and
+    two RK4 steps over the fluxes, side kinds, pairings and degrees; and the point form where a
+    face's coefficients vary along it (paper coefficients) or a jump term is present (initial
+    data across jumping coefficients)."""
+    rng = np.random.default_rng(23)
+    worst = 0.0
+    kinds = (dict(bot="absorbing_2beta", top="dirichlet", lft="wall", rgt="absorbing"),
+             dict(bot="wall", top="absorbing", lft="dirichlet", rgt="absorbing_2beta"), "absorbing_2beta")
+    cells = W.cell_coefficients(np.array([[1.0, 0.7], [1.3, 0.9]]), np.array([[1e-4, 3e-4], [2e-4, 1e-5]]),
+                                np.array([[0.05, 0.2], [0.1, 0.3]]))   # β small enough for the source's v
+    for q in (1, 3, 6):
+        for N in (3, 4):
+            for mixed in (True, False):
+                for flux in ("upwind", "central", "alternating"):
+                    for bd in kinds:
+                        for co in ("constant", "cells"):
+                            if co == "cells" and N % 2:
+                                continue
+                            kw = dict(flux=flux, mixed=mixed, mode="source", boundary=bd, sigma=0.3,
+                                      sigma_dirichlet=0.6, kappa=0.7)
+                            if co == "constant":
+                                pp = W.precompute(q, N, coefficients=W.constant_coefficients(c=1.2, alpha=3e-4,
+                                                                                              beta=0.5), **kw)[0]
+                                po = opre(q, N, coefficients=oc.constant_coefficients(c=1.2, alpha=3e-4, beta=0.5),
+                                          **kw)[0]
+                            else:
+                                pp, po = _pair(q, N, coefficients=cells, **kw)
+                                assert pp["one_sided"]
+                            ws = W.Workspace(pp, N)
+                            assert ws.stats()["modal_traces"] == 1, (q, N, co)
+                            u, v = _state(rng, pp, N, 1e-3, 1e-4)
+                            ow = OracleWorkspace(po)
+                            worst = max(worst, rel_max(ow.rhs(u, v, 0.037), ws.rhs(u, v, 0.037)))
+                            if q == 3 and flux == "alternating":
+                                uo, vo = u.copy(order="F"), v.copy(order="F")
+                                dt = (1.0 / N) / (10 * q * q)
+                                for k in range(2):
+                                    ow.rk4_step(uo, vo, 0.02 + k * dt, dt)
+                                    W.rk4_step_(u, v, 0.02 + k * dt, dt, N, 1.0 / N, pp, ws)
+                                worst = max(worst, rel_max((uo, vo), (u, v)))
+    assert worst < TOL, worst
+    pp = W.precompute(3, 4, mode="source")[0]                                        # paper coefficients
+    assert W.Workspace(pp, 4).stats()["modal_traces"] == 0
+    pp = W.precompute(3, 4, mode="initial_value", coefficients=quadrant_coefficients(0.5, 0.5, smooth=False))[0]
+    assert np.any(pp["hJC"] != 0) or np.any(pp["vJC"] != 0)
+    assert W.Workspace(pp, 4).stats()["modal_traces"] == 0
+
+
+def test_modal_and_point_traces_agree(gpu):
+    """The same workspace with modal traces and with point traces (modal_traces=False): the RHS and
+    ten RK4 steps agree to rounding, for the constant-coefficient and the general kernels."""
+    rng = np.random.default_rng(29)
+    for q, N, fast in ((6, 6, True), (3, 5, True), (4, 4, False)):
+        kw = dict(flux="alternating", mixed=False, mode="source", kappa=0.5,
+                  boundary=dict(bot="absorbing_2beta", top="wall", lft="wall", rgt="wall"))
+        pp = W.precompute(q, N, coefficients=W.constant_coefficients(c=1.0, alpha=1e-4, beta=2.0), **kw)[0]
+        wm = W.Workspace(pp, N, fast_path=fast)
+        wp = W.Workspace(pp, N, fast_path=fast, modal_traces=False)
+        assert wm.stats()["modal_traces"] == 1 and wp.stats()["modal_traces"] == 0
+        u, v = _state(rng, pp, N, 1e-6, 1e-7)      # rough data: small, so that 1 - 2βv stays positive
+        assert rel_max(wm.rhs(u, v, 0.2), wp.rhs(u, v, 0.2)) < 1e-13
+        um, vm = u.copy(order="F"), v.copy(order="F")
+        dt = (1.0 / N) / (10 * q * q)
+        assert wm.rk4_steps(um, vm, 0.2, dt, 10) == 10 and wp.rk4_steps(u, v, 0.2, dt, 10) == 10
+        assert rel_max((um, vm), (u, v)) < 1e-13
