@@ -1686,10 +1686,11 @@ int upload_boundary(wedg_ws *ws, const wedg_pre *pre) {
   return WEDG_OK;
 }
 
-// Whether the traces can be kept as modal end sums (Fields::modal): sets *flag when an interior
-// face's coefficient values differ along the face or, with one-sided faces, its jump term is not
-// zero. One thread per interior face: the horizontal faces (jf, k), jf = 1..N-1, then the vertical
-// faces (j, kf), kf = 1..N-1, in the device layouts [jf + (N+1)(k + N i)] and [j + N(kf + (N+1) i)].
+// Whether the traces can be kept as modal end sums (Fields::modal): sets bit 0 of *flag when an
+// interior face's coefficient values differ along the face, bit 1 when, with one-sided faces, its
+// jump term is not zero (its projections are then needed). One thread per interior face: the
+// horizontal faces (jf, k), jf = 1..N-1, then the vertical faces (j, kf), kf = 1..N-1, in the
+// device layouts [jf + (N+1)(k + N i)] and [j + N(kf + (N+1) i)].
 __global__ void k_modal_check(const Fields F, int nq, unsigned *flag) {
   const int N = F.N;
   const int nh = (N - 1) * N;
@@ -1707,15 +1708,34 @@ __global__ void k_modal_check(const Fields F, int nq, unsigned *flag) {
     f0 = (size_t)(r % N) + (size_t)N * (1 + r / N);
     c2 = F.vc2; af = F.vaf; c2m = F.vc2m; afm = F.vafm; jc = F.vJC;
   }
-  bool ok = true;
+  bool ok = true, jump = false;
   for (int i = 1; i < nq; ++i) {
     const size_t fi = f0 + stride * i;
     ok = ok && c2[fi] == c2[f0] && af[fi] == af[f0];
     if (F.one_sided) ok = ok && c2m[fi] == c2m[f0] && afm[fi] == afm[f0];
   }
   if (F.one_sided)
-    for (int i = 0; i < nq; ++i) ok = ok && jc[f0 + stride * i] == 0.0;
+    for (int i = 0; i < nq; ++i) jump = jump || jc[f0 + stride * i] != 0.0;
   if (!ok) atomicOr(flag, 1u);
+  if (jump) atomicOr(flag, 2u);
+}
+
+// The face weights w_i P[i][b] of the projections on the face modes (a kernel parameter)
+struct FaceProj {
+  double Pw[MAXN][MAXN];
+};
+
+// The projections Km[b] = Σ_i w_i P[i][b] K_i of the jump terms K of every face on its nq modes,
+// in the face array's layout with mode b in the slot of point b (stride (N+1) N): one thread per
+// face of a family of nf faces
+__global__ void k_jc_project(const double *jc, int nf, int nq, size_t stride, const FaceProj fp, double *out) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  for (int b = 0; b < nq; ++b) {
+    double x = 0.0;
+    for (int i = 0; i < nq; ++i) x = fma(fp.Pw[i][b], jc[f + stride * i], x);
+    out[f + stride * b] = x;
+  }
 }
 
 // The scratch of the workspace, the kernels' scalars and its stream (the last part of wedg_create)
@@ -1792,7 +1812,32 @@ int create_finish(wedg_ws *ws) {
       return r;
     }
   }
-  ws->modal_ok = flag == 0;
+  ws->modal_ok = (flag & 1u) == 0;
+  if (ws->modal_ok && (flag & 2u)) {
+    // the jump terms' projections on the face modes
+    FaceProj fp{};
+    for (int i = 0; i < nq; ++i)
+      for (int b = 0; b < nq; ++b) fp.Pw[i][b] = ws->bh.Pw[i][b];
+    const size_t nf = (size_t)(N + 1) * N;
+    double *hm = nullptr, *vm = nullptr;
+    int rc = dalloc(ws, &hm, nf * nq);
+    if (!rc) rc = dalloc(ws, &vm, nf * nq);
+    if (rc) {
+      wedg_destroy(ws);
+      return rc;
+    }
+    k_jc_project<<<(int)((nf + 255) / 256), 256, 0, ws->stream>>>(F.hJC, (int)nf, nq, nf, fp, hm);
+    k_jc_project<<<(int)((nf + 255) / 256), 256, 0, ws->stream>>>(F.vJC, (int)nf, nq, nf, fp, vm);
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(ws->stream);
+    if (ce != cudaSuccess) {
+      int r = cuda_fail(ws, ce, "wedg_create");
+      wedg_destroy(ws);
+      return r;
+    }
+    F.hJCm = hm;
+    F.vJCm = vm;
+  }
   F.modal = ws->modal_ok ? 1 : 0;
   ws->stats.modal_traces = F.modal;
   ws->stats.fast_path = ws->fast ? 1 : 0;

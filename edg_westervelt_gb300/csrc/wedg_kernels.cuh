@@ -94,6 +94,9 @@ struct Fields {
   const double *Cw, *Aw, *Ainv, *ic2e, *c2e, *ae;
   const double *hc2, *haf, *hcf, *hbf, *hc2m, *hafm, *hJC;
   const double *vc2, *vaf, *vcf, *vbf, *vc2m, *vafm, *vJC;
+  // with modal traces and one-sided faces: the jump terms' projections Σ_i w_i P[i][b] JC_i on the
+  // face modes b, in the layouts of hJC, vJC with mode b in the slot of point b (null: no jump term)
+  const double *hJCm, *vJCm;
   const double *bsp[4], *bspn[4];
   const double *PiSP, *PiBSP2, *PiCdiv, *PiDdiv, *srcP;
   const double *beta2;        // 2β at the high-order points, [(r + QH s) E + e]
@@ -110,7 +113,7 @@ struct Fields {
   int one_sided, mms_on, src_on, cg, cheb_common, sorted;
   // modal traces: tr holds each side's modal end sums (index b < n in place of point i), and the
   // interior slots are projected in that form (every interior face's coefficients are one value
-  // along the face and its jump term vanishes; the adjoint kernels read point traces)
+  // along the face; the adjoint kernels read point traces)
   int modal;
   int kind[4];
   double gam[4], eta[4], sig[4], kb[4], kap[4];
@@ -643,11 +646,11 @@ __device__ __forceinline__ void side_point(const Basis<NU, NV> &B, const Fields 
 
 // The projections Y_A, Y_D (b < NV) and Y_F (b < NU) of the flux slots of interior side s, with
 // the traces held as modal end sums (Fields::modal). The face coefficients are one value along the
-// face and the jump term vanishes, so every slot is a linear combination of the six traces with
-// the same weights at every point, and its projection Σ_i w_i P[i][b] (.)_i is that combination of
-// the traces' modes b: the face rule integrates the product of two modes exactly and the modes
-// are orthonormal. The same results as the point form of side_point and the projections, to
-// rounding.
+// face, so every slot is a linear combination of the six traces and the jump term K with the same
+// weights at every point, and its projection Σ_i w_i P[i][b] (.)_i is that combination of the
+// traces' modes b and of K's projection on mode b (hJCm, vJCm): the face rule integrates the
+// product of two modes exactly and the modes are orthonormal. The same results as the point form
+// of side_point and the projections, to rounding.
 template <int NU, int NV>
 __device__ __forceinline__ void modal_side(const Fields &F, int s, int j, int k, int e, double (&YA)[NV],
                                            double (&YD)[NV], double (&YF)[NU]) {
@@ -659,16 +662,16 @@ __device__ __forceinline__ void modal_side(const Fields &F, int s, int j, int k,
   const int sm = s < 2 ? 1 : 3, spp = s < 2 ? 0 : 2;      // trace sides of the "-" and "+" elements
   const int em = plus ? nb : e, ep = plus ? e : nb;
   size_t fi;
-  const double *c2p_a, *afp_a, *c2m_a, *afm_a, *jc_a;
+  const double *c2p_a, *afp_a, *c2m_a, *afm_a, *jc_a, *jcm;
   if (s < 2) {
     fi = (s == 0 ? j : j + 1) + (size_t)(N + 1) * k;
-    c2p_a = F.hc2; afp_a = F.haf; c2m_a = F.hc2m; afm_a = F.hafm; jc_a = F.hJC;
+    c2p_a = F.hc2; afp_a = F.haf; c2m_a = F.hc2m; afm_a = F.hafm; jc_a = F.hJC; jcm = F.hJCm;
   } else {
     fi = j + (size_t)N * (s == 2 ? k : k + 1);
-    c2p_a = F.vc2; afp_a = F.vaf; c2m_a = F.vc2m; afm_a = F.vafm; jc_a = F.vJC;
+    c2p_a = F.vc2; afp_a = F.vaf; c2m_a = F.vc2m; afm_a = F.vafm; jc_a = F.vJC; jcm = F.vJCm;
   }
   FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);   // point 0 of the face
-  cf.K = 0.0;
+  const size_t fstride = (size_t)(N + 1) * N;                         // from point (mode) b to b + 1
   const double *tr = F.tr;
   // mode b of trace family fam on side `side` of element el
   auto T = [&](int fam, int side, int el, int b) { return tr[((fam * 4 + side) * NQ + b) * E + el]; };
@@ -680,6 +683,7 @@ __device__ __forceinline__ void modal_side(const Fields &F, int s, int j, int k,
       vm = T(1, sm, em, b); vp = T(1, spp, ep, b);
       dvm = T(2, sm, em, b); dvp = T(2, spp, ep, b);
     }
+    cf.K = jcm ? jcm[fi + fstride * b] : 0.0;
     double A, D, Fs;
     interior_flux(F, cf, plus, dum, dup, vm, vp, dvm, dvp, A, D, Fs);
     if (b < NV) { YA[b] = A; YD[b] = D; }

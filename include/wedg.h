@@ -65,7 +65,7 @@ typedef struct wedg_config {
   int32_t general_only;                  /* 1: never use the constant-coefficient kernels */
   int32_t point_traces;                  /* 1: keep the traces at the face points; 0: as modal end sums
                                             where every interior face's coefficients are one value along
-                                            it and no jump term is present (wedg_stats.modal_traces) */
+                                            it (wedg_stats.modal_traces) */
 } wedg_config;
 
 /* Host pointers to the arrays of `pre`, each in the reference's layout
@@ -99,8 +99,8 @@ typedef struct wedg_stats {
   int64_t element_stages;      /* elements × stages evaluated by the last call */
   int32_t modal_traces;        /* 1 if the traces are kept as modal end sums and the interior flux
                                   slots projected in that form (every interior face's coefficients
-                                  one value along the face, no jump term); the adjoint calls use
-                                  point traces */
+                                  one value along the face; jump terms projected on the face modes
+                                  once); the adjoint calls use point traces */
   int32_t reserved;
 } wedg_stats;
 

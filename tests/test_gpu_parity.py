@@ -537,12 +537,11 @@ def test_rk4_steps_common_count_against_oracle(gpu):
 
 
 def test_modal_traces_against_oracle(gpu):
-    """The traces kept as modal end sums (interior faces with one coefficient value along them and
-    no jump term: constant coefficients, and coefficients constant on cells of the mesh in source
-    mode, whose one-sided faces carry no jump term), against the oracle's point form: one RHS and
-    two RK4 steps over the fluxes, side kinds, pairings and degrees; and the point form where a
-    face's coefficients vary along it (paper coefficients) or a jump term is present (initial
-    data across jumping coefficients)."""
+    """The traces kept as modal end sums (interior faces with one coefficient value along them:
+    constant coefficients, and coefficients constant on cells of the mesh, whose one-sided faces
+    carry jump terms in initial-value mode), against the oracle's point form: one RHS and two RK4
+    steps over the fluxes, side kinds, pairings and degrees, and the RHS with jump terms; the point
+    form where a face's coefficients vary along it (paper coefficients)."""
     rng = np.random.default_rng(23)
     worst = 0.0
     kinds = (dict(bot="absorbing_2beta", top="dirichlet", lft="wall", rgt="absorbing"),
@@ -582,9 +581,15 @@ def test_modal_traces_against_oracle(gpu):
     assert worst < TOL, worst
     pp = W.precompute(3, 4, mode="source")[0]                                        # paper coefficients
     assert W.Workspace(pp, 4).stats()["modal_traces"] == 0
-    pp = W.precompute(3, 4, mode="initial_value", coefficients=quadrant_coefficients(0.5, 0.5, smooth=False))[0]
-    assert np.any(pp["hJC"] != 0) or np.any(pp["vJC"] != 0)
-    assert W.Workspace(pp, 4).stats()["modal_traces"] == 0
+    # jump terms from the initial data across jumping coefficients: projected on the face modes
+    for q, N, flux in ((3, 4, "central"), (5, 4, "upwind"), (2, 6, "alternating")):
+        pp, po = _pair(q, N, mode="initial_value", flux=flux, boundary="dirichlet", sigma=0.3,
+                       coefficients=quadrant_coefficients(0.5, 0.5, smooth=False))
+        assert pp["one_sided"] and (np.any(pp["hJC"] != 0) or np.any(pp["vJC"] != 0))
+        ws = W.Workspace(pp, N)
+        assert ws.stats()["modal_traces"] == 1
+        u, v = _state(rng, pp, N, 1e-3, 1e-4)
+        assert rel_max(OracleWorkspace(po).rhs(u, v, 0.037), ws.rhs(u, v, 0.037)) < TOL
 
 
 def test_modal_and_point_traces_agree(gpu):
