@@ -670,24 +670,45 @@ __device__ __forceinline__ void modal_side(const Fields &F, int s, int j, int k,
     fi = j + (size_t)N * (s == 2 ? k : k + 1);
     c2p_a = F.vc2; afp_a = F.vaf; c2m_a = F.vc2m; afm_a = F.vafm; jc_a = F.vJC; jcm = F.vJCm;
   }
-  FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);   // point 0 of the face
-  const size_t fstride = (size_t)(N + 1) * N;                         // from point (mode) b to b + 1
+  const FaceCoef cf = face_coef(F, c2p_a, afp_a, c2m_a, afm_a, jc_a, fi);   // point 0 of the face
+  // the slots of interior_flux as linear forms with the face's weights (continuous faces: the
+  // one-sided form with equal values on both sides): G = Σ g·traces, J = Σ j·traces + K,
+  // s = v⁻ - v⁺; "+": A = pen s - G - (1-θ)K, w = θ s - τJ, D = -α⁺ w, F = c²⁺ w;
+  // "-": A = G - pen s - θK, w = -(1-θ) s - τJ, D = α⁻ w, F = -c²⁻ w
+  const double th = F.theta, tau = F.tau, two_h = F.two_h;
+  const double c2m = F.one_sided ? cf.c2m : cf.c2p, afm = F.one_sided ? cf.afm : cf.afp;
+  const double c2p = cf.c2p, afp = cf.afp;
+  const double g_um = two_h * ((1 - th) * c2m), g_up = two_h * (th * c2p);
+  const double g_vm = two_h * ((1 - th) * afm), g_vp = two_h * (th * afp);
+  const double j_um = two_h * c2m, j_up = -(two_h * c2p), j_vm = two_h * afm, j_vp = -(two_h * afp);
+  const double pen = (0.5 * (c2m + c2p)) * F.lu + (0.5 * (afm + afp)) * F.lv;
+  const double sw = plus ? th : -(1 - th);                 // w = sw s - τJ
+  const double kA = plus ? -(1 - th) : -th;                // A = ±(pen s - G) + kA K
+  const double dD = plus ? -afp : afm, dF = plus ? c2p : -c2m;
+  const size_t fstride = (size_t)(N + 1) * N;              // from point (mode) b to b + 1
   const double *tr = F.tr;
   // mode b of trace family fam on side `side` of element el
   auto T = [&](int fam, int side, int el, int b) { return tr[((fam * 4 + side) * NQ + b) * E + el]; };
 #pragma unroll
   for (int b = 0; b < NU; ++b) {
     const double dum = T(0, sm, em, b), dup = T(0, spp, ep, b);
-    double vm = 0.0, vp = 0.0, dvm = 0.0, dvp = 0.0;
+    double G = fma(g_um, dum, g_up * dup), J = fma(j_um, dum, j_up * dup), sj = 0.0;
     if (b < NV) {
-      vm = T(1, sm, em, b); vp = T(1, spp, ep, b);
-      dvm = T(2, sm, em, b); dvp = T(2, spp, ep, b);
+      const double vm = T(1, sm, em, b), vp = T(1, spp, ep, b);
+      const double dvm = T(2, sm, em, b), dvp = T(2, spp, ep, b);
+      G = fma(g_vp, dvp, fma(g_vm, dvm, G));
+      J = fma(j_vp, dvp, fma(j_vm, dvm, J));
+      sj = vm - vp;
     }
-    cf.K = jcm ? jcm[fi + fstride * b] : 0.0;
-    double A, D, Fs;
-    interior_flux(F, cf, plus, dum, dup, vm, vp, dvm, dvp, A, D, Fs);
-    if (b < NV) { YA[b] = A; YD[b] = D; }
-    YF[b] = Fs;
+    const double K = jcm ? jcm[fi + fstride * b] : 0.0;
+    J += K;
+    const double w = fma(sw, sj, -tau * J);
+    if (b < NV) {
+      const double a = fma(pen, sj, -G);
+      YA[b] = fma(kA, K, plus ? a : -a);
+      YD[b] = dD * w;
+    }
+    YF[b] = dF * w;
   }
 }
 
