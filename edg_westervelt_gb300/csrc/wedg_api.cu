@@ -2704,7 +2704,7 @@ int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_de
     }
     if (rc == WEDG_OK) {
       const double md = median3(td[0], td[1], td[2]), mt = median3(tt[0], tt[1], tt[2]);
-      if (wins && mt < md) {
+      if (wins && mt < kTuneGain * md) {
         apply(tp, tm, ts);
         best = mt;
       } else {

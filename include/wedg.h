@@ -380,8 +380,8 @@ int wedg_batch_set_shape(wedg_batch *b, int bucket, int prep_threads, int mass_t
  * solves' threads per block: 32, 64, 128). A candidate replaces the bucket's shape only when it is faster in
  * each of three paired trials against it and faster by more than 2 % in the median. Then the
  * whole batch's step (graph replays over at least 8 steps) with the tuned shapes against the
- * shapes it had before, three paired trials: the tuned shapes stay only if they win every trial,
- * so the batch never ends up slower than before tuning. *best_ms (may be NULL) receives the
+ * shapes it had before, three paired trials: the tuned shapes stay only if they win every trial
+ * and gain more than 2 % in the median, so the batch does not end up slower than before tuning. *best_ms (may be NULL) receives the
  * median milliseconds per step of the shapes kept. */
 int wedg_batch_autotune(wedg_batch *b, double *const *u_dev, double *const *v_dev, const double *t0,
                         const double *dt, int64_t steps, double *best_ms);
