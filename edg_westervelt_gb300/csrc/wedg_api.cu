@@ -113,6 +113,9 @@ constexpr int kTuneRepeats = 3;   // paired trials of the batch autotuner
 // RK4 steps of the batch's larger graph: within it an instance starts its next step as soon as its
 // own step is done (the table chunk, WEDG_BATCH_CHUNK steps, is a multiple of it)
 constexpr int kBatchGraphSteps = 4;
+// element ranges in which a host state is copied in while the first k_prep runs on the ranges that
+// have arrived
+constexpr int kCopyChunks = 4;
 static_assert(WEDG_BATCH_CHUNK % kBatchGraphSteps == 0, "a table chunk holds whole multi-step graphs");
 
 Launchers get_launchers(int nu, int nv, bool fast) {
@@ -145,6 +148,7 @@ struct wedg_ws {
   // host-state calls: copies beside the workspace's stream (created on first use)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_copy[2] = {nullptr, nullptr};
+  cudaEvent_t ev_chunk[kCopyChunks] = {};
   std::vector<void *> allocs;
   size_t bytes = 0;
   // state buffers
@@ -327,6 +331,7 @@ int copy_stream_ready(wedg_ws *ws) {
   if (ws->copy_stream) return WEDG_OK;
   CK(ws, cudaEventCreateWithFlags(&ws->ev_copy[0], cudaEventDisableTiming));
   CK(ws, cudaEventCreateWithFlags(&ws->ev_copy[1], cudaEventDisableTiming));
+  for (cudaEvent_t &e : ws->ev_chunk) CK(ws, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   CK(ws, cudaStreamCreateWithFlags(&ws->copy_stream, cudaStreamNonBlocking));
   return WEDG_OK;
 }
@@ -358,8 +363,10 @@ void drain_events(wedg_ws *ws) {
 }
 
 // enqueue the three kernels of one stage (on the workspace's Fields, or on Fo); after_stage, when
-// given, is recorded on the stream after the stage kernel
-int enqueue_stage(wedg_ws *ws, const StageIO &S, const Fields *Fo = nullptr, cudaEvent_t after_stage = nullptr) {
+// given, is recorded on the stream after the stage kernel; with prep_done the stage's k_prep has
+// been enqueued already (by ranges of elements, with this stage's bin parity)
+int enqueue_stage(wedg_ws *ws, const StageIO &S, const Fields *Fo = nullptr, cudaEvent_t after_stage = nullptr,
+                  bool prep_done = false) {
   const Fields &F = Fo ? *Fo : ws->F;
   const int tp = ws->prep_threads, bp = (ws->E + tp - 1) / tp;
   const int ts = stage_threads(ws->nu, ws->nv, ws->fast), bs = (ws->E + ts - 1) / ts;
@@ -372,7 +379,7 @@ int enqueue_stage(wedg_ws *ws, const StageIO &S, const Fields *Fo = nullptr, cud
     e0 = take_event(ws); e1 = take_event(ws); e2 = take_event(ws); e3 = take_event(ws);
     cudaEventRecord(e0, ws->stream);
   }
-  CK(ws, ws->L.prep(ws->basis.data(), F, Sp, bp, tp, ws->stream));
+  if (!prep_done) CK(ws, ws->L.prep(ws->basis.data(), F, Sp, bp, tp, ws->stream, 0));
   if (ws->timing) cudaEventRecord(e1, ws->stream);
   CK(ws, ws->L.stage(ws->basis.data(), F, Sp, bs, ts, ws->stream));
   if (after_stage) CK(ws, cudaEventRecord(after_stage, ws->stream));
@@ -382,7 +389,7 @@ int enqueue_stage(wedg_ws *ws, const StageIO &S, const Fields *Fo = nullptr, cud
     cudaEventRecord(e3, ws->stream);
     ws->ev_pending.push_back({e0, e1, e2, e3});
   }
-  ws->stats.kernel_launches += 3;
+  ws->stats.kernel_launches += prep_done ? 2 : 3;
   ws->stats.element_stages += ws->E;
   CK(ws, cudaGetLastError());
   return WEDG_OK;
@@ -446,7 +453,7 @@ StageIO rk4_stage_io(const wedg_ws *ws, double *u, double *v, int s, double t, d
 // step's u: nothing of the step writes u after it.
 int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop_nonfinite,
                 const double *tf = nullptr, long long tf_n = 0, double *const *stage_u = nullptr,
-                double *const *stage_v = nullptr, cudaEvent_t u_final = nullptr) {
+                double *const *stage_v = nullptr, cudaEvent_t u_final = nullptr, bool first_prep_done = false) {
   // with stage_u, stage_v (four buffers each) the stage states Y1..Y4 of the step are kept there
   const bool cg = ws->cfg.mass_solver == WEDG_CG;
   if (stage_u) {
@@ -456,7 +463,7 @@ int enqueue_rk4(wedg_ws *ws, double *u, double *v, double t, double dt, int stop
   }
   for (int s = 0; s < 4; ++s) {
     int rc = enqueue_stage(ws, rk4_stage_io(ws, u, v, s, t, dt, tf, tf_n, stage_u, stage_v), nullptr,
-                           s == 3 && !cg ? u_final : nullptr);
+                           s == 3 && !cg ? u_final : nullptr, s == 0 && first_prep_done);
     if (rc) return rc;
   }
   if (cg) {
@@ -2255,6 +2262,8 @@ void wedg_destroy(wedg_ws *ws) {
   if (ws->copy_stream) cudaStreamDestroy(ws->copy_stream);
   for (cudaEvent_t e : ws->ev_copy)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : ws->ev_chunk)
+    if (e) cudaEventDestroy(e);
   delete ws;
 }
 
@@ -2303,21 +2312,49 @@ int wedg_rk4_steps(wedg_ws *ws, double *u, double *v, double t0, double dt, int6
   // with host state: v is copied in on the copy stream beside u on the workspace's stream, and the
   // final u is copied out while the last stage's mass solve runs (Chebyshev)
   const bool u_early = host && nsteps > 0 && ws->cfg.mass_solver != WEDG_CG;
+  // with host state and a step to take, the state comes in by ranges of elements on the copy stream
+  // and the first stage's k_prep runs on each range as it arrives (k_prep reads only its own
+  // element's state)
+  const int tp = ws->prep_threads;
+  const int nchunk = host && nsteps > 0 && !ws->timing && ws->E >= kCopyChunks * 4 * tp ? kCopyChunks : 0;
+  if ((rc = reset_flags(ws))) return rc;
   if (host) {
     if ((rc = copy_stream_ready(ws))) return rc;
     CK(ws, cudaEventRecord(ws->ev_copy[0], ws->stream));           // after the stream's earlier work
     CK(ws, cudaStreamWaitEvent(ws->copy_stream, ws->ev_copy[0], 0));
-    CK(ws, cudaMemcpyAsync(ws->d_v, v, bV, cudaMemcpyHostToDevice, ws->copy_stream));
-    CK(ws, cudaMemcpyAsync(ws->d_u, u, bU, cudaMemcpyHostToDevice, ws->stream));
-    CK(ws, cudaEventRecord(ws->ev_copy[1], ws->copy_stream));
-    CK(ws, cudaStreamWaitEvent(ws->stream, ws->ev_copy[1], 0));
     du = ws->d_u; dv = ws->d_v;
+    if (nchunk) {
+      // element ranges of whole k_prep blocks; the state's rows (one per mode) are E doubles apart
+      const StageIO S0 = rk4_stage_io(ws, du, dv, 0, t0, dt, nullptr, 0, nullptr, nullptr);
+      StageIO Sp = S0;
+      Sp.parity = ws->parity;
+      const int nb = (ws->E + tp - 1) / tp, per = (nb + nchunk - 1) / nchunk;
+      const size_t row = sizeof(double) * ws->E;
+      for (int c = 0; c < nchunk; ++c) {
+        const int b0 = c * per, b1 = std::min(nb, b0 + per);
+        if (b0 >= b1) break;
+        const int e0 = b0 * tp, e1 = std::min(ws->E, b1 * tp);
+        const size_t w = sizeof(double) * (size_t)(e1 - e0);
+        CK(ws, cudaMemcpy2DAsync(ws->d_u + e0, row, u + e0, row, w, (size_t)ws->nu * ws->nu, cudaMemcpyHostToDevice,
+                                 ws->copy_stream));
+        CK(ws, cudaMemcpy2DAsync(ws->d_v + e0, row, v + e0, row, w, (size_t)ws->nv * ws->nv, cudaMemcpyHostToDevice,
+                                 ws->copy_stream));
+        CK(ws, cudaEventRecord(ws->ev_chunk[c], ws->copy_stream));
+        CK(ws, cudaStreamWaitEvent(ws->stream, ws->ev_chunk[c], 0));
+        CK(ws, ws->L.prep(ws->basis.data(), ws->F, Sp, b1 - b0, tp, ws->stream, e0));
+        ws->stats.kernel_launches += 1;
+      }
+    } else {
+      CK(ws, cudaMemcpyAsync(ws->d_v, v, bV, cudaMemcpyHostToDevice, ws->copy_stream));
+      CK(ws, cudaMemcpyAsync(ws->d_u, u, bU, cudaMemcpyHostToDevice, ws->stream));
+      CK(ws, cudaEventRecord(ws->ev_copy[1], ws->copy_stream));
+      CK(ws, cudaStreamWaitEvent(ws->stream, ws->ev_copy[1], 0));
+    }
   }
-  if ((rc = reset_flags(ws))) return rc;
   double t = t0;
   for (int64_t it = 0; it < nsteps; ++it) {
     if ((rc = enqueue_rk4(ws, du, dv, t, dt, stop_nonfinite, nullptr, 0, nullptr, nullptr,
-                          u_early && it == nsteps - 1 ? ws->ev_copy[0] : nullptr)))
+                          u_early && it == nsteps - 1 ? ws->ev_copy[0] : nullptr, it == 0 && nchunk > 0)))
       return rc;
     t += dt;
   }

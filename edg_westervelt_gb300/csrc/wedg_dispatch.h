@@ -45,8 +45,13 @@ typedef cudaError_t (*multi_fn)(const void *basis, const MultiStage &P, int grid
                                 cudaStream_t st);
 typedef cudaError_t (*multi_adj_fn)(const void *basis, const MultiAdj &P, int grid, cudaStream_t st);
 
+// k_prep over the elements [e0, e0 + blocks × threads) (clipped to the mesh)
+typedef cudaError_t (*prep_fn)(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads,
+                               cudaStream_t st, int e0);
+
 struct Launchers {
-  launch_fn prep = nullptr, stage = nullptr, mass = nullptr;
+  prep_fn prep = nullptr;
+  launch_fn stage = nullptr, mass = nullptr;
   adj_fn adj_hats = nullptr, adj_mass = nullptr;
   adj_face_fn adj_face = nullptr;
   multi_fn prep_m = nullptr, stage_m = nullptr, mass_m = nullptr;
@@ -82,8 +87,8 @@ void pack_basis(const BasisHost &h, void *out) {
 
 template <int NU, int NV>
 cudaError_t launch_prep(const void *basis, const Fields &F, const StageIO &S, int blocks, int threads,
-                        cudaStream_t st) {
-  k_prep<NU, NV><<<blocks, threads, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S);
+                        cudaStream_t st, int e0) {
+  k_prep<NU, NV><<<blocks, threads, 0, st>>>(*static_cast<const Basis<NU, NV> *>(basis), F, S, e0);
   return cudaSuccess;
 }
 

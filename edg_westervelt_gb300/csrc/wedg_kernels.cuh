@@ -510,8 +510,10 @@ __device__ __forceinline__ void prep_body(const Basis<NU, NV> &B, const Fields &
 template <int NU, int NV>
 __global__ void __launch_bounds__(128, 3) k_prep(const __grid_constant__ Basis<NU, NV> B,
                                               const __grid_constant__ Fields F,
-                                              const __grid_constant__ StageIO S) {
-  prep_body<NU, NV>(B, F, S, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.x == 0);
+                                              const __grid_constant__ StageIO S, int e0) {
+  // elements e0 + (block, thread): a launch may cover a range of the elements (the first range
+  // clears the next stage's counts)
+  prep_body<NU, NV>(B, F, S, e0 + (int)(blockIdx.x * blockDim.x + threadIdx.x), blockIdx.x == 0 && e0 == 0);
 }
 
 template <int NU, int NV>

@@ -301,7 +301,7 @@ extern "C" int wedg_rhs_noalloc(const wedg_config *cfg, const wedg_pre *pre, con
   const int tp = 128, ts = stage_threads(nu, nv, fast);
   unsigned long long err = 0;
   unsigned int cgf = 0;
-  if ((ce = Lch.prep(basis, F, S, (iE + tp - 1) / tp, tp, st)) != cudaSuccess ||
+  if ((ce = Lch.prep(basis, F, S, (iE + tp - 1) / tp, tp, st, 0)) != cudaSuccess ||
       (ce = Lch.stage(basis, F, S, (iE + ts - 1) / ts, ts, st)) != cudaSuccess ||
       (ce = Lch.mass(basis, F, S, 1, CHEB_THREADS, st)) != cudaSuccess ||
       (ce = cudaGetLastError()) != cudaSuccess ||

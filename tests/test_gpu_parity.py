@@ -609,3 +609,26 @@ def test_modal_and_point_traces_agree(gpu):
         dt = (1.0 / N) / (10 * q * q)
         assert wm.rk4_steps(um, vm, 0.2, dt, 10) == 10 and wp.rk4_steps(u, v, 0.2, dt, 10) == 10
         assert rel_max((um, vm), (u, v)) < 1e-13
+
+
+@pytest.mark.parametrize("solver", ["chebyshev", "cg"])
+def test_host_state_steps_match_device_state(gpu, solver):
+    """rk4_steps on a host state -- copied in by ranges of elements while the first stage's k_prep
+    runs on the ranges that have arrived, the final u copied out beside the last mass solve --
+    against the same steps on a device state: bit for bit (N = 64, every range boundary inside the
+    mesh)."""
+    import torch
+    N, q = 64, 3
+    pp = W.precompute(q, N, flux="upwind", mixed=True, mode="source", mass_solver=solver, kappa=0.5,
+                      coefficients=W.constant_coefficients(c=1.1, alpha=1e-4, beta=2.0))[0]
+    rng = np.random.default_rng(37)
+    u, v = _state(rng, pp, N, 1e-6, 1e-7)
+    dt = (1.0 / N) / (10 * q * q)
+    wh, wd = W.Workspace(pp, N), W.Workspace(pp, N)
+    uh, vh = u.copy(order="F"), v.copy(order="F")
+    assert wh.rk4_steps(uh, vh, 0.05, dt, 3) == 3
+    ud = torch.from_numpy(u.reshape(-1, order="F").copy()).cuda()
+    vd = torch.from_numpy(v.reshape(-1, order="F").copy()).cuda()
+    assert wd.rk4_steps(ud, vd, 0.05, dt, 3) == 3
+    assert np.array_equal(uh.reshape(-1, order="F"), ud.cpu().numpy())
+    assert np.array_equal(vh.reshape(-1, order="F"), vd.cpu().numpy())
