@@ -135,6 +135,47 @@ Launchers get_launchers(int nu, int nv, bool fast) {
 
 using namespace wedg;
 
+namespace {
+
+// The flags of a workspace (or of every instance of a batch), reset and read back by one launch each
+struct BatchFlagPtrs {
+  unsigned long long *err, *nsum;
+  unsigned int *cg_nfail, *nonfinite;
+  int *nmax, *bin_count;
+  long long *steps_done;
+};
+struct BatchFlagVals {
+  unsigned long long err, nsum;
+  long long done;
+  unsigned int cgf, nonf;
+  int nmax, pad;
+};
+
+// reset_flags of instance blockIdx.x
+__global__ void k_batch_reset(const BatchFlagPtrs *p, int n) {
+  if ((int)blockIdx.x >= n) return;
+  const BatchFlagPtrs f = p[blockIdx.x];
+  for (int t = threadIdx.x; t < 2 * NBIN; t += blockDim.x) f.bin_count[t] = 0;
+  if (threadIdx.x == 0) {
+    *f.err = ERR_NONE;
+    *f.nsum = 0;
+    *f.cg_nfail = 0;
+    *f.nonfinite = 0;
+    f.nmax[0] = f.nmax[1] = f.nmax[2] = 0;
+    *f.steps_done = 0;
+  }
+}
+
+// the flags collect reads, of every instance
+__global__ void k_batch_read(const BatchFlagPtrs *p, int n, BatchFlagVals *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const BatchFlagPtrs f = p[i];
+  out[i] = BatchFlagVals{*f.err, *f.nsum, *f.steps_done, *f.cg_nfail, *f.nonfinite, f.nmax[2], 0};
+}
+
+}  // namespace
+
 struct wedg_ws {
   wedg_config cfg;
   int N = 0, E = 0, nu = 0, nv = 0, nq = 0, qh = 0;
@@ -144,6 +185,9 @@ struct wedg_ws {
   std::vector<char> basis;
   Fields F{};
   bool modal_ok = false;   // the traces may be kept as modal end sums (Fields::modal)
+  // the flags' pointers and their values after a call (h_flagv pinned): one reset and one read
+  BatchFlagPtrs *d_flagp = nullptr;
+  BatchFlagVals *d_flagv = nullptr, *h_flagv = nullptr;
   cudaStream_t own_stream = nullptr, stream = nullptr;
   // host-state calls: copies beside the workspace's stream (created on first use)
   cudaStream_t copy_stream = nullptr;
@@ -314,15 +358,10 @@ void stage_factors(const wedg_ws *ws, double t, StageIO &S) {
 }
 
 int reset_flags(wedg_ws *ws) {
-  CK(ws, cudaMemsetAsync(ws->F.err, 0xFF, sizeof(unsigned long long), ws->stream));
-  CK(ws, cudaMemsetAsync(ws->F.cg_nfail, 0, sizeof(unsigned int), ws->stream));
-  CK(ws, cudaMemsetAsync(ws->F.nonfinite, 0, sizeof(unsigned int), ws->stream));
-  CK(ws, cudaMemsetAsync(ws->F.nmax, 0, 3 * sizeof(int), ws->stream));
-  CK(ws, cudaMemsetAsync(ws->F.nsum, 0, sizeof(unsigned long long), ws->stream));
-  CK(ws, cudaMemsetAsync(ws->F.bin_count, 0, 2 * NBIN * sizeof(int), ws->stream));
+  k_batch_reset<<<1, 128, 0, ws->stream>>>(ws->d_flagp, 1);
+  CK(ws, cudaGetLastError());
   ws->parity = 0;
   ws->stats.element_stages = 0;
-  CK(ws, cudaMemsetAsync(ws->steps_done, 0, sizeof(long long), ws->stream));
   return WEDG_OK;
 }
 
@@ -615,58 +654,15 @@ int apply_flags(wedg_ws *ws, unsigned long long err, unsigned int cgf, unsigned 
 }
 
 int collect(wedg_ws *ws) {
-  unsigned long long err;
-  unsigned int cgf, nonf;
-  int nmax;
-  long long done;
-  unsigned long long nsum;
+  k_batch_read<<<1, 32, 0, ws->stream>>>(ws->d_flagp, 1, ws->d_flagv);
+  CK(ws, cudaGetLastError());
+  CK(ws, cudaMemcpyAsync(ws->h_flagv, ws->d_flagv, sizeof(BatchFlagVals), cudaMemcpyDeviceToHost, ws->stream));
   CK(ws, cudaStreamSynchronize(ws->stream));
   drain_events(ws);
-  CK(ws, cudaMemcpy(&nsum, ws->F.nsum, sizeof nsum, cudaMemcpyDeviceToHost));
-  CK(ws, cudaMemcpy(&err, ws->F.err, sizeof err, cudaMemcpyDeviceToHost));
-  CK(ws, cudaMemcpy(&cgf, ws->F.cg_nfail, sizeof cgf, cudaMemcpyDeviceToHost));
-  CK(ws, cudaMemcpy(&nonf, ws->F.nonfinite, sizeof nonf, cudaMemcpyDeviceToHost));
-  CK(ws, cudaMemcpy(&nmax, ws->F.nmax + 2, sizeof nmax, cudaMemcpyDeviceToHost));
-  CK(ws, cudaMemcpy(&done, ws->steps_done, sizeof done, cudaMemcpyDeviceToHost));
-  return apply_flags(ws, err, cgf, nonf, nmax, done, nsum);
+  const BatchFlagVals &f = *ws->h_flagv;
+  return apply_flags(ws, f.err, f.cgf, f.nonf, f.nmax, f.done, f.nsum);
 }
 
-// The flags of every instance of a batch, reset and read back by one launch each
-struct BatchFlagPtrs {
-  unsigned long long *err, *nsum;
-  unsigned int *cg_nfail, *nonfinite;
-  int *nmax, *bin_count;
-  long long *steps_done;
-};
-struct BatchFlagVals {
-  unsigned long long err, nsum;
-  long long done;
-  unsigned int cgf, nonf;
-  int nmax, pad;
-};
-
-// reset_flags of instance blockIdx.x
-__global__ void k_batch_reset(const BatchFlagPtrs *p, int n) {
-  if ((int)blockIdx.x >= n) return;
-  const BatchFlagPtrs f = p[blockIdx.x];
-  for (int t = threadIdx.x; t < 2 * NBIN; t += blockDim.x) f.bin_count[t] = 0;
-  if (threadIdx.x == 0) {
-    *f.err = ERR_NONE;
-    *f.nsum = 0;
-    *f.cg_nfail = 0;
-    *f.nonfinite = 0;
-    f.nmax[0] = f.nmax[1] = f.nmax[2] = 0;
-    *f.steps_done = 0;
-  }
-}
-
-// the flags collect reads, of every instance
-__global__ void k_batch_read(const BatchFlagPtrs *p, int n, BatchFlagVals *out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const BatchFlagPtrs f = p[i];
-  out[i] = BatchFlagVals{*f.err, *f.nsum, *f.steps_done, *f.cg_nfail, *f.nonfinite, f.nmax[2], 0};
-}
 
 int argument_error(wedg_ws *ws, const std::string &msg) {
   if (ws) {
@@ -1761,9 +1757,20 @@ int create_finish(wedg_ws *ws) {
       (rc = dalloc(ws, &ws->d_u, nU)) || (rc = dalloc(ws, &ws->d_v, nV)) || (rc = dalloc(ws, &ws->d_ut, nU)) ||
       (rc = dalloc(ws, &ws->d_vt, nV)) || (rc = dalloc(ws, &ws->su, nU)) || (rc = dalloc(ws, &ws->sv, nV)) ||
       (rc = dalloc(ws, &ws->accu, nU)) || (rc = dalloc(ws, &ws->accv, nV)) || (rc = dalloc(ws, &F.mrhs, nV)) ||
-      (rc = dalloc(ws, &F.bins, (size_t)NBIN * E)) || (rc = dalloc(ws, &F.bin_count, (size_t)2 * NBIN))) {
+      (rc = dalloc(ws, &F.bins, (size_t)NBIN * E)) || (rc = dalloc(ws, &F.bin_count, (size_t)2 * NBIN)) ||
+      (rc = dalloc(ws, &ws->d_flagp, 1)) || (rc = dalloc(ws, &ws->d_flagv, 1))) {
     wedg_destroy(ws);
     return rc;
+  }
+  {
+    const BatchFlagPtrs fp{F.err, F.nsum, F.cg_nfail, F.nonfinite, F.nmax, F.bin_count, ws->steps_done};
+    cudaError_t e = cudaMallocHost(&ws->h_flagv, sizeof(BatchFlagVals));
+    if (e == cudaSuccess) e = cudaMemcpy(ws->d_flagp, &fp, sizeof fp, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      int r = cuda_fail(ws, e, "wedg_create");
+      wedg_destroy(ws);
+      return r;
+    }
   }
   F.theta = cfg->theta; F.tau = cfg->tau; F.lu = cfg->lambda_u; F.lv = cfg->lambda_v;
   F.omega = cfg->omega;
@@ -2258,6 +2265,7 @@ void wedg_destroy(wedg_ws *ws) {
   for (cudaEvent_t e : ws->ev_pool) cudaEventDestroy(e);
   if (ws->copy_stream) cudaStreamSynchronize(ws->copy_stream);
   for (void *p : ws->allocs) cudaFree(p);
+  if (ws->h_flagv) cudaFreeHost(ws->h_flagv);
   if (ws->own_stream) cudaStreamDestroy(ws->own_stream);
   if (ws->copy_stream) cudaStreamDestroy(ws->copy_stream);
   for (cudaEvent_t e : ws->ev_copy)
