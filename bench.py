@@ -564,6 +564,7 @@ def run_batched(torch, dev, steps, warmup):
     advance(steps)
     assert all(d == steps for d in done) and all(fin)
     # the autotuner: launch shapes per bucket, on copies of the present states
+    shapes_default = [dict(s) for s in batch.shapes()]
     t0 = time.perf_counter()
     ms_tuner = batch.autotune(us, vs, t, dts, steps=2)
     t_tune = time.perf_counter() - t0
@@ -594,9 +595,12 @@ def run_batched(torch, dev, steps, warmup):
             "setup_s": t_setup,
             "autotune": {"default_ms_per_step": tb_default / steps * 1e3, "tuned_ms_per_step": tb / steps * 1e3,
                          "tuner_median_ms_per_step": ms_tuner, "tune_s": t_tune, "shapes": shapes,
-                         "note": "per bucket: threads per block of k_prep and of the mass solves and persistent grids "
-                                 "(Batch.autotune, paired trials); value and ms_per_step are the faster of the "
-                                 "default-shape and the tuned-shape runs"},
+                         "kept_default_shapes": shapes == shapes_default,
+                         "note": "per bucket: the layout (persist -1: the instances' own launches; 0: one launch per "
+                                 "stage kernel over the bucket; > 0: persistent grids) and the threads per block of "
+                                 "k_prep and of the mass solves (Batch.autotune, paired trials; kept only on a 2 % "
+                                 "gain of the whole batch); value and ms_per_step are the faster of the default-shape "
+                                 "and the tuned-shape runs (the same shapes when kept_default_shapes)"},
             "timing": "host clock around each call (each call returns synchronised); states resident on the GPU",
             "batched": "Batch.rk4_steps: buckets of instances with the same kernels side by side, each bucket's "
                        "instances on their own streams (the default) or one multi-instance launch per stage kernel "
