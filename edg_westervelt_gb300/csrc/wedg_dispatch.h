@@ -79,6 +79,11 @@ void pack_basis(const BasisHost &h, void *out) {
     b.E1F[d] = h.E1F[d];
     for (int c = 0; c < NU; ++c) { b.K1[d][c] = h.K1[d][c]; b.Q[d][c] = h.Q[d][c]; b.ilam2[d][c] = h.ilam2[d][c]; }
   }
+  for (int i = 0; i < NU; ++i) {
+    double x = 0.0;
+    for (int a = 0; a < NU; ++a) x += h.Q[a][i] * h.E1F[a];
+    b.QE[i] = x;
+  }
   for (int r = 0; r < QH; ++r) {
     b.wh[r] = h.wh[r];
     for (int d = 0; d < NV; ++d) { b.Ph[r][d] = h.Ph[r][d]; b.PhW[r][d] = h.PhW[r][d]; }

@@ -87,6 +87,7 @@ struct Basis {
   double K1[NU][NU];             // 1D stiffness S^T diag(w) S
   double Q[NU][NU];              // its eigenvectors, Q[row][col]; Q[.][0] = e_0
   double ilam2[NU][NU];          // 1 / (λ_i + λ_j), and 1 at (0, 0)
+  double QE[NU];                 // Q^T E1F: the u-slots' lift factor in the eigenbasis of K1
 };
 
 struct Fields {
@@ -748,6 +749,10 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
 #pragma unroll
     for (int b = 0; b < NU; ++b) bb(a, b) = S.mode == OUT_ADJ_USOLVE ? S.xu[e + (size_t)E * (a + NU * b)] : 0.0;
   const bool adjoint = S.mode >= OUT_ADJ_USOLVE;
+  // the forward modes of the constant-coefficient kernels with q_u = q_v build the u-equation's
+  // right-hand side in the eigenbasis of K1 (the adjoint's volume mode needs the plain basis)
+  constexpr bool EIG = FAST && NU == NV;
+  const bool eig = EIG && !adjoint;
 #pragma unroll 1
   for (int ax = 0; ax < 2 && !adjoint; ++ax) {
     double A0[NV], D0[NV], F0[NU];          // the projections of the axis' first side (B or L)
@@ -815,6 +820,21 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
       const double fp = F0[b] + YF[b], fm = F0[b] - YF[b];
       F0[b] = fm; YF[b] = fp;
     }
+    if (eig) {
+      // the u-slots' lifts straight into the eigenbasis of K1: Q^T (E1F_even ⊗ F_0 + E1F_odd ⊗ F_1) Q
+      // = QE_even ⊗ Q^T F_0 + QE_odd ⊗ Q^T F_1 (QE = Q^T E1F keeps the parity of its index)
+      double t0[NU], t1[NU];
+#pragma unroll
+      for (int i = 0; i < NU; ++i) { t0[i] = 0.0; t1[i] = 0.0; }
+#pragma unroll
+      for (int a = 0; a < NU; ++a)
+#pragma unroll
+        for (int i = 0; i < NU; ++i)
+          if (qnz(a, i)) { t0[i] = fma(B.Q[a][i], F0[a], t0[i]); t1[i] = fma(B.Q[a][i], YF[a], t1[i]); }
+#pragma unroll
+      for (int i = 0; i < NU; ++i) { F0[i] = t0[i]; YF[i] = t1[i]; }
+    }
+    const double *LF = eig ? B.QE : B.E1F;
     if (ax == 0) {
 #pragma unroll 1
       for (int a = 0; a < NV; ++a) {
@@ -826,7 +846,7 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
       }
 #pragma unroll 1
       for (int a = 0; a < NU; ++a) {
-        const double ce = B.E1F[a];
+        const double ce = LF[a];
         const bool od = a & 1;
 #pragma unroll
         for (int b = 0; b < NU; ++b) bb(a, b) = fma(ce, od ? YF[b] : F0[b], bb(a, b));
@@ -841,7 +861,7 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
 #pragma unroll
       for (int a = 0; a < NU; ++a) {
 #pragma unroll
-        for (int b = 0; b < NU; ++b) bb(a, b) = fma(B.E1F[b], (b & 1) ? YF[a] : F0[a], bb(a, b));
+        for (int b = 0; b < NU; ++b) bb(a, b) = fma(LF[b], (b & 1) ? YF[a] : F0[a], bb(a, b));
       }
     }
   }
@@ -887,10 +907,12 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
           for (int c = 2 - (a & 1); c < NU; c += 2) acc = fma(B.K1[a][c], w[c], acc);
           Rv(a, b) = acc;
         }
-        double acc = bb(a, b);
+        if (!eig) {
+          double acc = bb(a, b);
 #pragma unroll
-        for (int c = 2 - (a & 1); c < NV; c += 2) acc = fma(B.K1[a][c], vc[c], acc);
-        bb(a, b) = acc;
+          for (int c = 2 - (a & 1); c < NV; c += 2) acc = fma(B.K1[a][c], vc[c], acc);
+          bb(a, b) = acc;
+        }
       }
     }
 #pragma unroll 1
@@ -915,10 +937,12 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
           for (int c = 2 - (b & 1); c < NU; c += 2) acc = fma(w[c], B.K1[c][b], acc);
           Rv(a, b) = acc;
         }
-        double acc = bb(a, b);
+        if (!eig) {
+          double acc = bb(a, b);
 #pragma unroll
-        for (int c = 2 - (b & 1); c < NV; c += 2) acc = fma(vr[c], B.K1[c][b], acc);
-        bb(a, b) = acc;
+          for (int c = 2 - (b & 1); c < NV; c += 2) acc = fma(vr[c], B.K1[c][b], acc);
+          bb(a, b) = acc;
+        }
       }
     }
   } else {
@@ -1074,6 +1098,44 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
     // terms at compile time. The four products run in place: a product with Q from the left
     // changes each column on its own, one from the right each row.
     const double ic2 = F.ic2e[e];
+    if (eig) {
+      // b is in the eigenbasis except for its volume part c²(K1 V + V K1), whose transform
+      // c²(Λ Ṽ + Ṽ Λ), Ṽ = Q^T V Q, divided by c²(λ_i + λ_j) is Ṽ itself (zero at (0, 0)):
+      // X = Ṽ + (Q^T b' Q) ∘ L. T1 = Q^T V by columns into the space of R_v (written out above),
+      // then X = T1 Q + b' ∘ L by rows.
+      Blk<NV, BT> T1 = Rv;
+#pragma unroll 1
+      for (int c = 0; c < NU; ++c) {
+        double t[NU], x[NU];
+#pragma unroll
+        for (int a = 0; a < NU; ++a) x[a] = S.xv[e + Eu * (a + NU * c)];
+#pragma unroll
+        for (int i = 0; i < NU; ++i) t[i] = 0;
+#pragma unroll
+        for (int a = 0; a < NU; ++a)
+#pragma unroll
+          for (int i = 0; i < NU; ++i)
+            if (qnz(a, i)) t[i] = fma(B.Q[a][i], x[a], t[i]);
+#pragma unroll
+        for (int i = 0; i < NU; ++i) T1(i, c) = t[i];
+      }
+#pragma unroll 1
+      for (int i = 0; i < NU; ++i) {
+        double t[NU];
+#pragma unroll
+        for (int jj = 0; jj < NU; ++jj) t[jj] = 0;
+#pragma unroll
+        for (int c = 0; c < NU; ++c) {
+          const double x = T1(i, c);
+#pragma unroll
+          for (int jj = 0; jj < NU; ++jj)
+            if (qnz(c, jj)) t[jj] = fma(x, B.Q[c][jj], t[jj]);
+        }
+#pragma unroll
+        for (int jj = 0; jj < NU; ++jj)
+          bb(i, jj) = (i == 0 && jj == 0) ? bb(0, 0) : fma(bb(i, jj), B.ilam2[i][jj] * ic2, t[jj]);
+      }
+    } else {
 #pragma unroll 1
     for (int c = 0; c < NU; ++c) {                 // T1 = Q^T b, by columns
       double t[NU];
@@ -1103,6 +1165,7 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
       }
 #pragma unroll
       for (int jj = 0; jj < NU; ++jj) bb(i, jj) = (i == 0 && jj == 0) ? t[jj] : t[jj] * (B.ilam2[i][jj] * ic2);
+    }
     }
 #pragma unroll 1
     for (int jj = 0; jj < NU; ++jj) {              // T3 = Q T2, by columns
@@ -1202,18 +1265,19 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
   if (S.mode == OUT_RK4_LAST && !fin) atomicOr(F.nonfinite, 1u);
 }
 
+// Blocks per SM asked of k_stage: at low degrees the registers allow more than two blocks of
+// 128 elements (the shared memory does), and the compiler keeps the kernel within them without
+// spilling; from q_u = 4 on, two
+__host__ __device__ constexpr int stage_m_blocks(int nu) { return nu <= 2 ? 5 : nu == 3 ? 4 : nu == 4 ? 3 : 2; }
+
 template <int NU, int NV, bool FAST>
-__global__ void __launch_bounds__(stage_threads(NU, NV, FAST), 2)
+__global__ void __launch_bounds__(stage_threads(NU, NV, FAST), stage_m_blocks(NU))
     k_stage(const __grid_constant__ Basis<NU, NV> B, const __grid_constant__ Fields F,
             const __grid_constant__ StageIO S) {
   constexpr int BT = stage_threads(NU, NV, FAST);
   stage_body<NU, NV, FAST>(B, F, S, blockIdx.x * BT + (int)threadIdx.x, threadIdx.x);
 }
 
-// Blocks per SM asked of the multi-instance k_stage: the residency the single-instance kernel
-// reaches with its registers at low degrees (the instance arguments in shared memory otherwise
-// take registers of their own and halve it)
-__host__ __device__ constexpr int stage_m_blocks(int nu) { return nu <= 2 ? 5 : nu == 3 ? 4 : nu == 4 ? 3 : 2; }
 
 // tile = stage_threads(NU, NV, FAST) elements per virtual block
 template <int NU, int NV, bool FAST>
