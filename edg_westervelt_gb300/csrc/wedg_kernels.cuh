@@ -749,10 +749,9 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
 #pragma unroll
     for (int b = 0; b < NU; ++b) bb(a, b) = S.mode == OUT_ADJ_USOLVE ? S.xu[e + (size_t)E * (a + NU * b)] : 0.0;
   const bool adjoint = S.mode >= OUT_ADJ_USOLVE;
-  // the forward modes of the constant-coefficient kernels with q_u = q_v build the u-equation's
-  // right-hand side in the eigenbasis of K1 (the adjoint's volume mode needs the plain basis)
-  constexpr bool EIG = FAST && NU == NV;
-  const bool eig = EIG && !adjoint;
+  // the forward modes of the constant-coefficient kernels build the u-equation's right-hand side
+  // in the eigenbasis of K1 (the adjoint's volume mode needs the plain basis)
+  const bool eig = FAST && !adjoint;
 #pragma unroll 1
   for (int ax = 0; ax < 2 && !adjoint; ++ax) {
     double A0[NV], D0[NV], F0[NU];          // the projections of the axis' first side (B or L)
@@ -1099,6 +1098,33 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
     // changes each column on its own, one from the right each row.
     const double ic2 = F.ic2e[e];
     if (eig) {
+      if constexpr (NU != NV) {
+      // as below, Ṽ accumulated column by column of V (padded with zeros to NU × NU): with
+      // t = Q^T V[:, c], X += t ⊗ Q[c, :] (R_v's space is too small for Q^T V here)
+#pragma unroll 1
+      for (int i = 0; i < NU; ++i)
+#pragma unroll
+        for (int jj = 0; jj < NU; ++jj)
+          if (i != 0 || jj != 0) bb(i, jj) = bb(i, jj) * (B.ilam2[i][jj] * ic2);
+#pragma unroll 1
+      for (int c = 0; c < NV; ++c) {
+        double t[NU], x[NV];
+#pragma unroll
+        for (int a = 0; a < NV; ++a) x[a] = S.xv[e + Eu * (a + NV * c)];
+#pragma unroll
+        for (int i = 0; i < NU; ++i) t[i] = 0;
+#pragma unroll
+        for (int a = 0; a < NV; ++a)
+#pragma unroll
+          for (int i = 0; i < NU; ++i)
+            if (qnz(a, i)) t[i] = fma(B.Q[a][i], x[a], t[i]);
+#pragma unroll
+        for (int i = 0; i < NU; ++i)
+#pragma unroll
+          for (int jj = 0; jj < NU; ++jj)
+            if (qnz(c, jj) && (i != 0 || jj != 0)) bb(i, jj) = fma(t[i], B.Q[c][jj], bb(i, jj));
+      }
+      } else {
       // b is in the eigenbasis except for its volume part c²(K1 V + V K1), whose transform
       // c²(Λ Ṽ + Ṽ Λ), Ṽ = Q^T V Q, divided by c²(λ_i + λ_j) is Ṽ itself (zero at (0, 0)):
       // X = Ṽ + (Q^T b' Q) ∘ L. T1 = Q^T V by columns into the space of R_v (written out above),
@@ -1134,6 +1160,7 @@ __device__ __forceinline__ void stage_body(const Basis<NU, NV> &B, const Fields 
 #pragma unroll
         for (int jj = 0; jj < NU; ++jj)
           bb(i, jj) = (i == 0 && jj == 0) ? bb(0, 0) : fma(bb(i, jj), B.ilam2[i][jj] * ic2, t[jj]);
+      }
       }
     } else {
 #pragma unroll 1
