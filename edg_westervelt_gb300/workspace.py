@@ -482,7 +482,7 @@ class Batch:
             out.append({f: int(getattr(s, f)) for f, _ in s._fields_})
         return out
 
-    def set_shape(self, bucket, prep_threads, mass_threads, persist=0):
+    def set_shape(self, bucket, prep_threads, mass_threads, persist=-1):
         """wedg_batch_set_shape: the launch shape of one bucket (results do not depend on it);
         persist -1 launches the bucket's instances one by one (the default), 0 runs each stage
         kernel once over them, p > 0 the same on a persistent grid."""
