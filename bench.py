@@ -6,9 +6,10 @@ coefficients c = 1, α = 1e-6, β = 8, Gaussian source, bottom :absorbing_2beta
 and three :wall sides with κ = 0.5, alternating flux, Chebyshev mass solver,
 dt = h / (10 q²) — the GPU-scale configuration of the reference's plain method.
 The state is synthetic and seeded (the reference measures on no dataset): a
-steepened-wave state whose 1 - 2βv_h spans about [0.42, 1.58] on every element
-(about 30 Chebyshev steps, the regime of data/steepening/nl), and, reported
-beside it, the zero state (one Chebyshev step).
+steep circular front across which 1 - 2βv_h spans about [0.42, 1.58] (the
+regime of data/steepening/nl; up to about 30 Chebyshev steps at the front, one
+or two elsewhere), and, reported beside it, a short-wave state where every
+element spans that range and the zero state (one Chebyshev step).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -385,6 +386,30 @@ def run_ours(args):
     ms_step = main["ms"] / args.steps
     value = replica_value(dof, world, args.steps, main["ms"])
 
+    # one edg_rhs! per call (wedg_rhs on device-resident state, each call returning synchronised
+    # with its error word read): the per-evaluation time of the RHS alone, at the front state
+    # advanced by `warmup` RK4 steps (the exact initial projection has nearly constant v on the
+    # elements away from the front, one Chebyshev step each; a few steps give them the counts
+    # they keep along the run)
+    ur, vr = device_state(args.state, seed=0)
+    utr, vtr = torch.empty_like(ur), torch.empty_like(vr)
+    t_r = T0 + max(args.warmup, 1) * dt
+    if ws.rk4_steps(ur, vr, T0, dt, max(args.warmup, 1)) != max(args.warmup, 1):
+        raise RuntimeError("the RK4 steps before the edg_rhs! timing did not complete")
+    for _ in range(args.warmup):
+        ws.rhs(ur, vr, t_r, utr, vtr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ws.rhs(ur, vr, t_r, utr, vtr)
+    t_rhs = (time.perf_counter() - t0) / args.steps
+    rhs_call = {"ms_per_call": t_rhs * 1e3, "value": world * dof / t_rhs, "unit": "DOF·stage/s",
+                "calls": args.steps, "cheb_steps_max": ws.stats()["cheb_steps_max"],
+                "cheb_steps_mean": ws.stats()["cheb_steps_sum"] / max(ws.stats()["element_stages"], 1),
+                "timing": "host clock around each call (wedg_rhs with device pointers: three kernels, the "
+                          "error word read back, synchronised); the front state after the warm-up's RK4 steps"}
+    del ur, vr, utr, vtr
+
     # end to end through the public API: pinned host state in, result out, every step
     e2e = None
     if rank == 0 or world > 1:
@@ -481,6 +506,7 @@ def run_ours(args):
                        "stage_ms": common["prep_ms"] + common["stage_ms"] + common["mass_ms"],
                        "note": "the same workload and state with the reference's Chebyshev policy: every element "
                                "takes the stage's largest count (src/rhs.jl:911-918), as the reference arm does"},
+        "rhs_call": rhs_call,
         "roofline": roofline, "fp64_pipe": fp64_pipe, "reference_op_rate": reference_ops,
         "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clocks.summary(), "gpu_launches": main["launches"],

@@ -634,3 +634,26 @@ def test_host_state_steps_match_device_state(gpu, solver):
     assert wd.rk4_steps(ud, vd, 0.05, dt, 3) == 3
     assert np.array_equal(uh.reshape(-1, order="F"), ud.cpu().numpy())
     assert np.array_equal(vh.reshape(-1, order="F"), vd.cpu().numpy())
+
+
+@pytest.mark.parametrize("solver", ["chebyshev", "cg"])
+def test_rhs_on_device_state_matches_host_state(gpu, solver):
+    """edg_rhs! with device pointers (wedg_rhs, WEDG_DEVICE: no copies) against the host-state call
+    on the same inputs, bit for bit, and against the oracle; twice in a row on different states."""
+    import torch
+    N, q = 6, 4
+    kw = dict(flux="alternating", mixed=True, mode="mms", mass_solver=solver,
+              boundary=dict(bot="absorbing_2beta", top="dirichlet", lft="wall", rgt="absorbing"))
+    pp, po = _pair(q, N, **kw)
+    ws = W.Workspace(pp, N)
+    rng = np.random.default_rng(41)
+    for t in (0.037, 0.11):
+        u, v = _state(rng, pp, N)
+        host = tuple(x.copy() for x in ws.rhs(u, v, t))
+        ud = torch.from_numpy(u.reshape(-1, order="F").copy()).to(gpu)
+        vd = torch.from_numpy(v.reshape(-1, order="F").copy()).to(gpu)
+        utd, vtd = torch.full_like(ud, float("nan")), torch.full_like(vd, float("nan"))
+        ws.rhs(ud, vd, t, utd, vtd)
+        dev = (utd.cpu().numpy().reshape(u.shape, order="F"), vtd.cpu().numpy().reshape(v.shape, order="F"))
+        assert np.array_equal(host[0], dev[0]) and np.array_equal(host[1], dev[1])
+        assert rel_max(OracleWorkspace(po).rhs(u, v, t), dev) < TOL
