@@ -657,3 +657,70 @@ def test_rhs_on_device_state_matches_host_state(gpu, solver):
         dev = (utd.cpu().numpy().reshape(u.shape, order="F"), vtd.cpu().numpy().reshape(v.shape, order="F"))
         assert np.array_equal(host[0], dev[0]) and np.array_equal(host[1], dev[1])
         assert rel_max(OracleWorkspace(po).rhs(u, v, t), dev) < TOL
+
+
+@pytest.mark.parametrize("solver", ["chebyshev", "cg"])
+def test_mass_solves_against_the_dense_reference(gpu, solver):
+    """The mass systems at max 2β|v_q| of 1e-3, 0.5 and 0.9 (test/runtests.jl:418-441): the RHS of the
+    GPU (both mass solvers; up to 45 Chebyshev steps at q = 6) against the dense restatement of
+    test/reference_rhs.jl, whose mass solve is an LU factorisation of each element matrix. Walls
+    (no boundary weight) so that only the mass matrices bound v."""
+    from oracle.reference_rhs import dense_volume, edg_rhs_reference, reference_pre
+    rng = np.random.default_rng(7)
+    worst = 0.0
+    for q, mixed, N in ((1, True, 3), (3, True, 4), (4, False, 3), (6, True, 2)):
+        pp, po = _pair(q, N, mixed=mixed, mass_solver=solver, boundary="wall", kappa=0.5)
+        nv, E = pp["qv1"], N * N
+        V0 = rng.standard_normal((N, N, nv, nv))
+        U = np.asfortranarray(rng.standard_normal((N, N, pp["qu1"], pp["qu1"])))
+        vq = np.einsum("ra,eab,sb->ers", po["P_h_v"], V0.reshape(E, nv, nv, order="F"), po["P_h_v"])
+        g0 = np.max(np.abs(2 * np.transpose(po["beta_hq"], (1, 0, 2)) * vq))
+        dense = dense_volume(reference_pre(po))
+        ws = W.Workspace(pp, N)
+        for gmax in (1e-3, 0.5, 0.9):
+            V = np.asfortranarray(V0 * (gmax / g0))
+            a = edg_rhs_reference(U, V, 0.037, N, 1.0 / N, dense)
+            worst = max(worst, rel_max(a, ws.rhs(U, V, 0.037)))
+    assert worst < TOL, worst
+
+
+@pytest.mark.parametrize("solver", ["chebyshev", "cg"])
+@pytest.mark.parametrize("q", [1, 2, 3, 6])
+def test_nblocks_bitwise_rhs_and_rk4(gpu, solver, q):
+    """test/runtests.jl:468-500: every nblocks gives the same RHS and RK4 steps bit for bit (N = 7,
+    both pairings, every mode, two mixed side layouts, the paper's coefficients and jumping ones on
+    the mesh lines x = 3/7, y = 4/7). Here nblocks is accepted and recorded (ws.nb); each workspace
+    is a separate allocation, so this also checks that runs are reproducible bit for bit although
+    k_prep lists the elements by Chebyshev count with atomics."""
+    N, h = 7, 1.0 / 7
+    mixed2 = dict(bot="wall", top="absorbing", lft="dirichlet", rgt="absorbing_2beta")
+    mixed1 = dict(bot="absorbing_2beta", top="dirichlet", lft="wall", rgt="absorbing")
+    pw7 = quadrant_coefficients(3 / 7, 4 / 7, alpha=(1e-5, 4e-6, 2e-5, 1e-6), smooth=True)
+    for mixed in (True, False):
+        for mode in ("mms", "initial_value", "source"):
+            for boundary in (mixed1, mixed2):
+                for coef in (None, pw7):
+                    if mode == "mms" and coef is not None:
+                        continue
+                    kw = dict(mixed=mixed, mode=mode, boundary=boundary, mass_solver=solver, sigma=0.3,
+                              sigma_dirichlet=0.6, kappa=0.7, phase=(0.4, 0.3))
+                    if coef is not None:
+                        kw["coefficients"] = coef
+                    pre = W.precompute(q, N, **kw)[0]
+                    assert bool(pre["one_sided"]) == (coef is not None)
+                    rng = np.random.default_rng(q)
+                    u, v = _state(rng, pre, N, 1e-2, 0.05)
+                    ws1 = W.Workspace(pre, N, nblocks=1)
+                    r1 = tuple(x.copy() for x in ws1.rhs(u, v, 0.037))
+                    s1 = (u.copy(order="F"), v.copy(order="F"))
+                    for k in (1, 2):
+                        W.rk4_step_(*s1, 0.01 * k, 1e-4, N, h, pre, ws1)
+                    for nb in (3, 5, 8):
+                        ws = W.Workspace(pre, N, nblocks=nb)
+                        assert ws.nb == nb
+                        r = ws.rhs(u, v, 0.037)
+                        assert np.array_equal(r[0], r1[0]) and np.array_equal(r[1], r1[1])
+                        s = (u.copy(order="F"), v.copy(order="F"))
+                        for k in (1, 2):
+                            W.rk4_step_(*s, 0.01 * k, 1e-4, N, h, pre, ws)
+                        assert np.array_equal(s[0], s1[0]) and np.array_equal(s[1], s1[1])
