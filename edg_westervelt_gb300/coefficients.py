@@ -10,6 +10,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
+from .errors import ArgumentErrorException
+
 
 @dataclass
 class Coefficients:
@@ -114,7 +116,7 @@ def flux_parameters(flux):
         return dict(theta=1.0, tau=0.0, lambda_u=0.0, lambda_v=0.0)
     if flux == "central":
         return dict(theta=0.5, tau=0.0, lambda_u=0.0, lambda_v=0.0)
-    raise ValueError(f"unknown flux {flux} (expected :upwind, :alternating or :central)")
+    raise ArgumentErrorException(f"unknown flux {flux} (expected :upwind, :alternating or :central)")
 
 
 BOUNDARY_KINDS = ("absorbing_2beta", "absorbing", "dirichlet", "wall")
@@ -144,15 +146,15 @@ def boundary_sides(boundary, sigma, sigma_dirichlet, kappa):
         kinds = (_sym(boundary),) * 4
     else:
         if not (len(boundary) == 4 and set(boundary) == set(SIDES)):
-            raise ValueError("boundary must be a kind or a NamedTuple with the keys bot, top, lft, rgt")
+            raise ArgumentErrorException("boundary must be a kind or a NamedTuple with the keys bot, top, lft, rgt")
         kinds = tuple(_sym(boundary[s]) for s in SIDES)
     for k in kinds:
         if k not in BOUNDARY_KINDS:
-            raise ValueError(f"unknown boundary {k} (expected one of {BOUNDARY_KINDS})")
+            raise ArgumentErrorException(f"unknown boundary {k} (expected one of {BOUNDARY_KINDS})")
     if any(k in ("absorbing", "absorbing_2beta") for k in kinds) and not (-1.0 <= sigma <= 1.0):
-        raise ValueError(f"absorbing sides need -1 ≤ sigma ≤ 1 (got {sigma})")
+        raise ArgumentErrorException(f"absorbing sides need -1 ≤ sigma ≤ 1 (got {sigma})")
     if "dirichlet" in kinds and not (sigma_dirichlet >= 0.0):
-        raise ValueError(f"Dirichlet sides need sigma_dirichlet ≥ 0 (got {sigma_dirichlet}; it defaults to sigma)")
+        raise ArgumentErrorException(f"Dirichlet sides need sigma_dirichlet ≥ 0 (got {sigma_dirichlet}; it defaults to sigma)")
     if not kappa >= 0.0:
-        raise ValueError(f"kappa must be ≥ 0 (got {kappa})")
+        raise ArgumentErrorException(f"kappa must be ≥ 0 (got {kappa})")
     return {s: boundary_side(k, sigma, sigma_dirichlet, kappa) for s, k in zip(SIDES, kinds)}

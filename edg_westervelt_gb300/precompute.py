@@ -17,6 +17,7 @@ import numpy as np
 
 from .coefficients import (Coefficients, GaussianSource, _Cells, _Const, _sym, boundary_sides, flux_parameters,
                            paper_coefficients)
+from .errors import ArgumentErrorException
 from .quadrature import GaussQCofs, GradJacobiP, JacobiP
 
 FACE_SHIFT = 2.0 ** -40   # src/solver.jl:361
@@ -161,7 +162,7 @@ def precompute(q, N, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, 
                                  coefficients=coefficients, mode=mode, kx=kx, ky=ky, source=source,
                                  mass_solver=mass_solver, initial_profile=initial_profile)
     if target != "host":
-        raise ValueError(f"target must be \"host\" or \"device\", not {target!r}")
+        raise ArgumentErrorException(f"target must be \"host\" or \"device\", not {target!r}")
     mode = _sym(mode)
     mass_solver = _sym(mass_solver)
     flux = _sym(flux)
@@ -170,11 +171,11 @@ def precompute(q, N, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, 
     coefficients = paper_coefficients() if coefficients is None else coefficients
     source = GaussianSource() if source is None else source
     if mass_solver not in ("cg", "chebyshev"):
-        raise ValueError(f"unknown mass_solver {mass_solver} (expected :cg or :chebyshev)")
+        raise ArgumentErrorException(f"unknown mass_solver {mass_solver} (expected :cg or :chebyshev)")
     if initial_profile is not None and mode != "initial_value":
-        raise ValueError("initial_profile is only available in :initial_value mode")
+        raise ArgumentErrorException("initial_profile is only available in :initial_value mode")
     if mode not in ("mms", "initial_value", "source"):
-        raise ValueError(f"unknown mode {mode} (expected :mms, :initial_value or :source)")
+        raise ArgumentErrorException(f"unknown mode {mode} (expected :mms, :initial_value or :source)")
     q_u = int(q)
     q_v = q_u - 1 if mixed else q_u
     qu1, qv1 = q_u + 1, q_v + 1
@@ -231,7 +232,7 @@ def precompute(q, N, *, mixed=True, flux="upwind", flux_params=None, sigma=0.0, 
     Aw = _F(np.transpose(aw_e, (1, 0, 2)))
     cw_cols = np.transpose(cw_e, (0, 2, 1)).reshape(E, qu1 * qu1)      # vec in column-major (r fastest)
     if inverses not in ("device", "host"):
-        raise ValueError(f"inverses must be \"device\" or \"host\", not {inverses!r}")
+        raise ArgumentErrorException(f"inverses must be \"device\" or \"host\", not {inverses!r}")
     uniq, inv = _distinct_rows(cw_cols, limit=64 if inverses == "device" else None)
     if inverses == "device" and uniq is None:
         Ainv_u = None                         # computed by the GPU workspace from Cw
@@ -411,7 +412,7 @@ def _rhs_data(pre, N):
     jumps = not (np.array_equal(hc2m, hc2) and np.array_equal(hafm, haf)
                  and np.array_equal(vc2m, vc2) and np.array_equal(vafm, vaf))
     if p["mms_on"] and jumps:
-        raise ValueError("mode = :mms needs c and α continuous across the element faces; "
+        raise ArgumentErrorException("mode = :mms needs c and α continuous across the element faces; "
                          "use :initial_value or :source for coefficients that jump")
     hJC = _F(hc2m * hg0m - hc2 * hg0)
     vJC = _F(vc2m * vg0m - vc2 * vg0)
@@ -491,11 +492,11 @@ def precompute_points(q, N, *, mixed=True, flux="upwind", flux_params=None, sigm
     coefficients = paper_coefficients() if coefficients is None else coefficients
     source = GaussianSource() if source is None else source
     if mass_solver not in ("cg", "chebyshev"):
-        raise ValueError(f"unknown mass_solver {mass_solver} (expected :cg or :chebyshev)")
+        raise ArgumentErrorException(f"unknown mass_solver {mass_solver} (expected :cg or :chebyshev)")
     if initial_profile is not None and mode != "initial_value":
-        raise ValueError("initial_profile is only available in :initial_value mode")
+        raise ArgumentErrorException("initial_profile is only available in :initial_value mode")
     if mode not in ("mms", "initial_value", "source"):
-        raise ValueError(f"unknown mode {mode} (expected :mms, :initial_value or :source)")
+        raise ArgumentErrorException(f"unknown mode {mode} (expected :mms, :initial_value or :source)")
     q_u = int(q)
     q_v = q_u - 1 if mixed else q_u
     qu1, qv1 = q_u + 1, q_v + 1

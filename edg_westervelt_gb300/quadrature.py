@@ -9,6 +9,8 @@ import math
 
 import numpy as np
 
+from .errors import ArgumentErrorException
+
 
 def JacobiP(x, alpha, beta, n):
     """Orthonormal Jacobi polynomial P_n^(alpha,beta) at x (src/quadrature.jl:11-35).
@@ -61,7 +63,7 @@ def GaussQCofs(q):
     """Nodes and weights of the q-point Gauss-Legendre rule on [-1, 1], ascending
     (src/quadrature.jl:57-66 computes the same rule by Golub-Welsch)."""
     if q < 1:
-        raise ValueError("GaussQCofs needs q ≥ 1")
+        raise ArgumentErrorException("GaussQCofs needs q ≥ 1")
     k = np.arange(1, q + 1, dtype=np.float64)
     x = -np.cos(np.pi * (k - 0.25) / (q + 0.5))      # initial guesses, ascending
     for _ in range(100):

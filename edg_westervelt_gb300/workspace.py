@@ -16,14 +16,7 @@ import warnings
 import numpy as np
 
 from . import _lib as L
-
-
-class ErrorException(RuntimeError):
-    """The reference's ErrorException (its own error messages, e.g. src/rhs.jl:114-115, 845, 916)."""
-
-
-class DimensionMismatch(ValueError):
-    """The reference's DimensionMismatch (src/rhs.jl:500-503)."""
+from .errors import ArgumentErrorException, DimensionMismatch, ErrorException
 
 
 def _f64(a):
@@ -187,7 +180,7 @@ class Workspace:
                                             ctypes.byref(h))
             msg = buf.value.decode("utf-8")
             if rc == L.WEDG_ERR_ARGUMENT and msg.startswith("mode = :mms"):
-                raise ValueError(msg)
+                raise ArgumentErrorException(msg)   # the device-side form of src/solver.jl:744-747
         if rc == L.WEDG_ERR_NO_DEVICE:
             raise RuntimeError("libwedg: no CUDA device available")
         if rc != L.WEDG_OK:

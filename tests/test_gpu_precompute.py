@@ -121,7 +121,7 @@ def test_device_built_pre_against_the_oracle(gpu, case):
 def test_device_built_pre_refuses_jumps_in_mms_mode(gpu):
     """src/solver.jl:745-747: the manufactured solution needs c and α continuous across faces."""
     pd, _ = W.precompute(2, 4, target="device", mode="mms", coefficients=quadrant_coefficients(0.5, 0.5, smooth=False))
-    with pytest.raises(ValueError, match="mode = :mms needs c and α continuous"):
+    with pytest.raises(W.ErrorException, match="mode = :mms needs c and α continuous"):
         W.Workspace(pd, 4)
 
 

@@ -80,7 +80,7 @@ def test_precompute_initial_profile_default_equivalent():
     b, _ = ppre(3, 6, mode="initial_value", initial_profile=prof)
     for k in ("PiCdiv", "bcB_sp", "bcL_spx", "hJC", "vJC"):
         assert np.max(np.abs(a[k] - b[k])) <= 1e-12 * max(1.0, np.max(np.abs(a[k]))), k
-    with pytest.raises(ValueError):
+    with pytest.raises(W.ErrorException, match="initial_profile is only available"):
         ppre(2, 2, initial_profile=prof)
 
 
@@ -91,9 +91,12 @@ def test_argument_checks():
                dict(boundary=dict(bot="wall", top="wall", lft="wall")),
                dict(boundary=dict(bot="wall", top="wall", lft="wall", rgt="foo")), dict(mass_solver="lu"),
                dict(mode="nope")):
+        # the reference's error(...) (an ErrorException); a ValueError for Python callers as well
+        with pytest.raises(W.ErrorException):
+            ppre(2, 2, **kw)
         with pytest.raises(ValueError):
             ppre(2, 2, **kw)
-    with pytest.raises(ValueError):
+    with pytest.raises(W.ErrorException, match="unknown flux downwind"):
         W.flux_parameters("downwind")
     bc = ppre(2, 2, boundary=dict(bot="absorbing_2beta", top="dirichlet", lft="wall", rgt="absorbing"), sigma=0.3,
               sigma_dirichlet=0.6, kappa=0.7)[0]["bc"]
@@ -161,7 +164,7 @@ def test_face_values_and_jumps():
         assert np.all(np.isfinite(pre["vc2m"])) and np.all(np.isfinite(pre["vcf"])) and pre["one_sided"]
     # jumps of c or α are refused in :mms mode; β alone is not a jump
     co = quadrant_coefficients(0.5, 0.5, c=(1.0, 1.0, 1.0, 1.0), alpha=(1e-3, 1e-3, 2e-3, 2e-3))
-    with pytest.raises(ValueError):
+    with pytest.raises(W.ErrorException, match="mode = :mms needs c and α continuous"):
         ppre(2, 6, coefficients=co)
     cb = quadrant_coefficients(0.5, 0.5, c=(1.0, 1.0, 1.0, 1.0), alpha=(1e-3, 1e-3, 1e-3, 1e-3))
     assert not ppre(2, 6, coefficients=cb)[0]["one_sided"]
