@@ -11,7 +11,8 @@ source-mode diagnostics and the error norms on the GPU).
 - with c, α, β jumping on mesh lines and absorbing sides the energy decays after the source
   stops (test/runtests.jl:838-848);
 - the interface terms of an initial profile u₀ (test/runtests.jl:760-784);
-- the semi-discrete energy identity with jumping coefficients (test/runtests.jl:734-761).
+- the semi-discrete energy identity with jumping coefficients (test/runtests.jl:734-761);
+- the convergence of a two-layer standing mode across a jump of c (test/runtests.jl:816-823).
 """
 import math
 
@@ -243,3 +244,52 @@ def test_energy_identity_with_jumping_coefficients(gpu):
                 rise = max(rise, et["dEdt"] / et["scale"])
     assert worst < 1e-12, worst
     assert rise < 1e-12, rise
+
+
+def two_layer_error(solve, Coefficients, q, N, T, flux, direction):
+    """test/runtests.jl:125-152: the energy-norm error at T of the exact standing mode of a two-layer
+    medium (c = 1 below s = ½, c = ½ above, s = x or y, four walls), started from its profile
+    in :initial_value mode; `solve` and `Coefficients` are those of the package under test."""
+    om, A = 2 * math.atan(math.sqrt(2.0)), -math.sqrt(3.0)
+    phi = lambda s: np.where(s < 0.5, np.cos(om * s), A * np.cos(2 * om * (1 - s)))                    # noqa: E731
+    dphi = lambda s: np.where(s < 0.5, -om * np.sin(om * s), 2 * om * A * np.sin(2 * om * (1 - s)))    # noqa: E731
+    d2phi = lambda s: np.where(s < 0.5, -om ** 2 * np.cos(om * s), -(2 * om) ** 2 * A * np.cos(2 * om * (1 - s)))  # noqa: E731
+    cs = lambda s: 1.0 if s < 0.5 else 0.5   # noqa: E731
+    z0 = lambda x, y: 0.0   # noqa: E731
+    f = lambda g: (lambda x, y: float(g(np.float64(x if direction == "x" else y))))   # noqa: E731
+    co = Coefficients(lambda x, y: cs(x if direction == "x" else y), z0, z0, z0, z0, z0, z0)
+    ip = dict(u0=f(phi), u0_x=f(dphi) if direction == "x" else z0, u0_y=z0 if direction == "x" else f(dphi),
+              u0_xx=f(d2phi) if direction == "x" else z0, u0_yy=z0 if direction == "x" else f(d2phi))
+    st = solve(q, N, T, mode="initial_value", initial_profile=ip, coefficients=co, boundary="wall", flux=flux,
+               return_state=True)
+    fu, fv = math.cos(om * T) - 1.0, -om * math.sin(om * T)      # ũ = u - Φ and v at T, times Φ
+    h = st["h"]
+    z, _ = W.GaussQCofs(q + 1)
+    e = 0.0
+    for j in range(N):
+        for k in range(N):
+            if direction == "x":
+                S = np.tile(((k + 0.5) * h + h * z / 2)[None, :], (q + 1, 1))
+            else:
+                S = np.tile(((j + 0.5) * h + h * z / 2)[:, None], (1, q + 1))
+            U, V = st["u"][j, k], st["v"][j, k]
+            ux = (2 / h) * (st["P_u"] @ U @ st["S_u"].T)
+            uy = (2 / h) * (st["S_u"] @ U @ st["P_u"].T)
+            g = fu * dphi(S)
+            gx, gy = (g, np.zeros_like(S)) if direction == "x" else (np.zeros_like(S), g)
+            e += np.sum(st["W2d"] * (0.5 * st["err_c2"][j, k] * ((gx - ux) ** 2 + (gy - uy) ** 2)
+                                     + 0.5 * (fv * phi(S) - st["P_v"] @ V @ st["P_v"].T) ** 2))
+    return h / 2 * math.sqrt(e)
+
+
+def test_convergence_at_a_coefficient_jump(gpu):
+    """test/runtests.jl:816-823: the two-layer standing mode converges at about q_u in the energy
+    norm for the upwind flux and about 1 for the central flux (q_u = 2, meshes 8 → 16), and the
+    interface along y gives the same error as along x."""
+    e8 = two_layer_error(W.solve, W.Coefficients, 2, 8, 0.5, "upwind", "x")
+    e16 = two_layer_error(W.solve, W.Coefficients, 2, 16, 0.5, "upwind", "x")
+    assert math.log2(e8 / e16) > 1.8
+    assert two_layer_error(W.solve, W.Coefficients, 2, 16, 0.5, "upwind", "y") == pytest.approx(e16, rel=1e-10)
+    c8 = two_layer_error(W.solve, W.Coefficients, 2, 8, 0.5, "central", "x")
+    c16 = two_layer_error(W.solve, W.Coefficients, 2, 16, 0.5, "central", "x")
+    assert math.log2(c8 / c16) > 0.9
