@@ -173,3 +173,68 @@ def test_oracle_error_messages(oracle_lib):
     with pytest.raises(RuntimeError) as ei:
         OracleWorkspace(pre).rhs(z, zv, 0.07)
     assert str(ei.value) == "boundary weight 1 - βg ≤ 0 for the boundary data g (absorbing side)"
+
+
+# ---- the reference's whole-scheme properties, on the oracle (the same helpers the GPU tests apply
+#      to the product: tests/reference_properties.py)
+
+def test_oracle_energy_identity(oracle_lib):
+    """test/runtests.jl:734-761 on the oracle: dE/dt = -Σ∫α|∇v_h|² - D_I to 1e-12 with c, α, β
+    jumping on x = ½ and y = ½, four walls with κ = 0, q = 1..4, six flux parameter sets."""
+    import math
+
+    from oracle.rhs import edg_rhs
+    from reference_properties import ENERGY_FLUXES, energy_terms
+    co = quadrant_coefficients(0.5, 0.5, beta=(0.0, 0.3, 0.1, 0.2))
+    N, worst, rise = 4, 0.0, -math.inf
+    for q in (1, 2, 3, 4):
+        for mixed in (True, False):
+            for fp in ENERGY_FLUXES:
+                pre, _ = precompute(q, N, flux_params=fp, mixed=mixed, mode="source", boundary="wall", kappa=0.0,
+                                    coefficients=co, source=oc.GaussianSource(amplitude=0.0))
+                rng = np.random.default_rng(10 * q + mixed)
+                u = np.asfortranarray(rng.standard_normal((N, N, pre["qu1"], pre["qu1"])))
+                v = np.asfortranarray(0.05 * rng.standard_normal((N, N, pre["qv1"], pre["qv1"])))
+                ut, vt = edg_rhs(u, v, 0.3, N, 1.0 / N, pre)
+                et = energy_terms(u, v, ut, vt, pre, co, N)
+                if fp["tau"] == 0 and fp["lambda_u"] == 0 and fp["lambda_v"] == 0:
+                    assert et["DI"] == 0
+                worst = max(worst, abs(et["dEdt"] + et["Dv"] + et["DI"]) / et["scale"])
+                rise = max(rise, et["dEdt"] / et["scale"])
+    assert worst < 1e-12 and rise < 1e-12, (worst, rise)
+
+
+def test_oracle_interface_terms_of_the_initial_profile(oracle_lib):
+    """test/runtests.jl:760-784 on the oracle (see the GPU test of the same name)."""
+    from oracle.rhs import edg_rhs
+    from reference_properties import lin_profile, project_u
+    from test_host import Step
+    z0 = lambda x, y: 0.0   # noqa: E731
+    N, h = 8, 1.0 / 8
+    for c1, c2, ip in ((1.0, 0.5, lin_profile(0.0, 1.0)), (0.8, 0.8, lin_profile(1.0, 0.0))):
+        coef = oc.Coefficients(Step(1, 0.5, c1, c2), z0, z0, Step(1, 0.5, 1e-3 * c1 ** 2, 1e-3 * c2 ** 2), z0, z0, z0)
+        for flux in ("upwind", "central", "alternating"):
+            for q in (1, 3):
+                kw = dict(coefficients=coef, boundary="wall", flux=flux)
+                pI, _ = precompute(q, N, mode="initial_value", initial_profile=ip, **kw)
+                pS, _ = precompute(q, N, mode="source", source=oc.GaussianSource(amplitude=0.0), **kw)
+                assert pI["one_sided"]
+                zv = np.zeros((N, N, pI["qv1"], pI["qv1"]), order="F")
+                rI = edg_rhs(np.zeros((N, N, pI["qu1"], pI["qu1"]), order="F"), zv, 0.3, N, h, pI)
+                rS = edg_rhs(project_u(ip["u0"], pS, N), zv, 0.3, N, h, pS)
+                assert np.max(np.abs(rI[1] - rS[1])) <= 1e-11 * np.max(np.abs(rS[1]))
+                assert np.max(np.abs(rI[0] - rS[0])) <= 1e-11
+
+
+def test_oracle_two_layer_convergence(oracle_lib):
+    """test/runtests.jl:816-823 on the oracle (see the GPU test of the same name)."""
+    import math
+
+    from reference_properties import two_layer_error
+    e8 = two_layer_error(solve, oc.Coefficients, 2, 8, 0.5, "upwind", "x")
+    e16 = two_layer_error(solve, oc.Coefficients, 2, 16, 0.5, "upwind", "x")
+    assert math.log2(e8 / e16) > 1.8
+    assert two_layer_error(solve, oc.Coefficients, 2, 16, 0.5, "upwind", "y") == pytest.approx(e16, rel=1e-10)
+    c8 = two_layer_error(solve, oc.Coefficients, 2, 8, 0.5, "central", "x")
+    c16 = two_layer_error(solve, oc.Coefficients, 2, 16, 0.5, "central", "x")
+    assert math.log2(c8 / c16) > 0.9
