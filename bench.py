@@ -782,7 +782,7 @@ def adjoint_problem(seed=5, m=16):
 
 
 def run_adjoint(torch, T, every=32, batch=16, batch_T=0.125):
-    """The adjoint form (config 5): the gradient of J = ½ Σ_r (u_h(x_r, T) - u_obs_r)² with respect to
+    """The adjoint form (N = 128, q = 4): the gradient of J = ½ Σ_r (u_h(x_r, T) - u_obs_r)² with respect to
     the 3 × 16 × 16 cell values (adjoint_problem), u_obs from the forward solver on the field
     perturbed by ±10 %, checkpoints every 32 steps. Timed: one forward solve (Workspace.rk4_steps),
     one gradient (misfit_gradient: forward with checkpoints, misfit, reverse sweep with the parameter

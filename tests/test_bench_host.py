@@ -4,9 +4,9 @@ The algorithmic bytes and FP64 operations per element and RK4 stage follow the r
 data model (packed inverse stiffnesses, element coefficient blocks, β at the mass points, face
 coefficients, the source or manufactured-solution projections and 4.25 state-sized transfers per
 stage; the volume, u-equation, trace, lift, face, Chebyshev set-up and RK4 operations plus the
-per-step cost of the Chebyshev iteration). Their values at the four single-instance
-configurations are pinned here: config 1 (N = 10, q_u = 3, q_v = 2, mms), config 2 (the bench's
-N = 512, q = 6, source mode), config 3 (q_u = 5, q_v = 4, one-sided faces) and config 5 (q = 4).
+per-step cost of the Chebyshev iteration). Their values are pinned here for four workloads:
+the manufactured-solution run (q_u = 3, q_v = 2), the bench's source-mode run (q = 6), the
+jumping-coefficient run (q_u = 5, q_v = 4, one-sided faces) and the adjoint's forward run (q = 4).
 """
 import json
 
@@ -16,10 +16,10 @@ import bench
 
 
 @pytest.mark.parametrize("nu, nv, qh, one_sided, s_mode, bytes_, flops1, per_step", [
-    (4, 3, 4, False, 4, 2866, 3850, 426),          # config 1: mms (four Π arrays)
-    (7, 7, 10, False, 1, 15556, 23478, 5250),      # config 2: source mode (the bench)
-    (6, 5, 7, True, 1, 9242, 12922, 1930),         # config 3: initial-value mode, one-sided faces
-    (5, 5, 7, False, 1, 5612, 8890, 1930),         # config 5: source mode
+    (4, 3, 4, False, 4, 2866, 3850, 426),          # mms, q_u = 3, q_v = 2 (four Π arrays)
+    (7, 7, 10, False, 1, 15556, 23478, 5250),      # source mode, q = 6 (the bench)
+    (6, 5, 7, True, 1, 9242, 12922, 1930),         # initial-value mode, q_u = 5, q_v = 4, one-sided faces
+    (5, 5, 7, False, 1, 5612, 8890, 1930),         # source mode, q = 4 (the adjoint's forward run)
 ])
 def test_algorithmic_bytes_and_flops(nu, nv, qh, one_sided, s_mode, bytes_, flops1, per_step):
     assert bench.alg_bytes_per_element_stage(nu, nv, qh, one_sided=one_sided, s_mode_nv2=s_mode) == bytes_
