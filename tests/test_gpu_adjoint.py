@@ -242,7 +242,7 @@ def test_misfit_gradient_against_oracle_differences(gpu):
         assert abs(fd - ad) <= 1e-5 * abs(fd), (name, fd, ad)
 
 
-def test_misfit_gradient_config5_shape_twenty_directions(gpu):
+def test_misfit_gradient_n128_q4_twenty_directions(gpu):
     """The adjoint form at the shape of its workload: N = 128, q_u = q_v = 4, c², α, β constant on
     16 × 16 cells (c ~ U[0.8, 1.25], α log-uniform on [1e-6, 1e-5], β ~ U[0, 4]), a 32 × 32 receiver
     grid whose observations come from the forward solver on the fields perturbed by ±10 %,

@@ -449,8 +449,8 @@ def test_rk4_many_steps_on_a_mesh_with_fewer_elements_than_bins(gpu):
     assert rel_max((u, v), (uo, vo)) < TOL, rel_max((u, v), (uo, vo))
 
 
-def test_config1_per_evaluation_rhs_seeds(gpu):
-    """Config 1, solve(3, 10, 0.1; flux=:upwind, mixed=true) with its defaults (paper
+def test_mms_n10_per_evaluation_rhs_seeds(gpu):
+    """The manufactured-solution run solve(3, 10, 0.1; flux=:upwind, mixed=true) with its defaults (paper
     coefficients, absorbing_2beta on every side, σ = 0): the per-evaluation RHS against the
     oracle's on the seeded states u ~ N(0, 1), v ~ 0.05 N(0, 1) of test/runtests.jl:273, seeds 0 to 9,
     at t = 0.037, one workspace for all ten calls."""
@@ -464,8 +464,8 @@ def test_config1_per_evaluation_rhs_seeds(gpu):
     assert worst < TOL, worst
 
 
-def test_config3_full_size_against_oracle(gpu):
-    """Config 3 at its size: N = 256, q_u = 5, q_v = 4, initial-value mode, c, α, β constant on 4 × 4
+def test_jumping_coefficients_n256_against_oracle(gpu):
+    """The jumping-coefficient workload at its size: N = 256, q_u = 5, q_v = 4, initial-value mode, c, α, β constant on 4 × 4
     subsquares (the bench's default_rng(3) draw), dirichlet / absorbing / absorbing_2beta / wall
     sides, central flux, one-sided faces. One RHS and two RK4 steps on a seeded state against the
     oracle on the same pre (src/rhs.jl:490-550, src/solver.jl:289-321)."""
