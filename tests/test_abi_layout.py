@@ -1,0 +1,50 @@
+"""The Python mirror's ctypes structures against the C ABI of include/wedg.h, on the CPU.
+
+A field whose offset or size differs between include/wedg.h and edg_westervelt_gb300/_lib.py
+would make every call that passes the structure read the wrong bytes without an error. A small C
+program compiled with gcc against the header prints sizeof and offsetof of every field of every
+structure the Python side builds; they must equal ctypes' figures field by field.
+"""
+import ctypes
+import os
+import subprocess
+
+import pytest
+
+from edg_westervelt_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+STRUCTS = {"wedg_config": L.Config, "wedg_pre": L.Pre, "wedg_stats": L.Stats, "wedg_face_values": L.FaceValues,
+           "wedg_cell_table": L.CellTable, "wedg_points": L.Points, "wedg_batch_shape": L.BatchShape,
+           "wedg_source_run": L.SourceRun, "wedg_norm_args": L.NormArgs}
+
+
+def _c_layout(tmp_path):
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "wedg.h"', "int main(void) {"]
+    for cname, py in STRUCTS.items():
+        lines.append(f'  printf("{cname} . %zu\\n", sizeof({cname}));')
+        for field, _ in py._fields_:
+            lines.append(f'  printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["  return 0;", "}"]
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines) + "\n")
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), "-o", str(exe), str(src)],
+                   check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    layout = {}
+    for line in out.splitlines():
+        cname, field, value = line.split()
+        layout[(cname, field)] = int(value)
+    return layout
+
+
+def test_ctypes_structures_match_the_header(tmp_path):
+    try:
+        layout = _c_layout(tmp_path)
+    except (OSError, subprocess.CalledProcessError) as e:   # no gcc, or the header does not compile as C
+        pytest.fail(f"the layout probe did not build or run: {e}")
+    for cname, py in STRUCTS.items():
+        assert ctypes.sizeof(py) == layout[(cname, ".")], cname
+        for field, _ in py._fields_:
+            assert getattr(py, field).offset == layout[(cname, field)], (cname, field)
