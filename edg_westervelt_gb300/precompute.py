@@ -15,7 +15,7 @@ import math
 
 import numpy as np
 
-from .coefficients import (Coefficients, GaussianSource, _Cells, _Const, _sym, boundary_sides, flux_parameters,
+from .coefficients import (GaussianSource, _Cells, _Const, _sym, boundary_sides, flux_parameters,
                            paper_coefficients)
 from .errors import ArgumentErrorException
 from .quadrature import GaussQCofs, GradJacobiP, JacobiP
